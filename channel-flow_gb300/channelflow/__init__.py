@@ -1,0 +1,9 @@
+"""GB300 (sm_103a) RK3-substep library for the staggered finite-difference
+channel solver of Adrian-Lozano/channel-flow: Python host mirror of the
+reference's time-integration interface over the C ABI of libchannel_gpu.so."""
+from . import grids
+from .lib import (PREC_FP64, PREC_SPLIT, Channel, CfError, CfParams, default_params, header_functions, load,
+                  read_input_parameters, read_snapshot, write_snapshot)
+
+__all__ = ["grids", "Channel", "CfError", "CfParams", "default_params", "header_functions", "load",
+           "read_input_parameters", "read_snapshot", "write_snapshot", "PREC_FP64", "PREC_SPLIT"]

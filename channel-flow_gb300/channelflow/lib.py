@@ -1,0 +1,350 @@
+"""ctypes binding of libchannel_gpu.so and a host mirror of the reference's
+time-integration interface (time_integration.f90).
+
+``Channel`` exposes the subroutines that ``compute_time_step_RK3`` calls under
+their Fortran names (``compute_eddy_viscosity``, ``compute_rhs_u``, ...,
+``compute_projection_step``) plus the device fast path ``time_step_rk3``.
+Every call goes through the C ABI declared in include/channel_gpu.h; there is
+no CPU fallback: a missing or unloadable library raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import grids
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(HERE)
+ROOT = os.path.dirname(PKG)
+LIB_PATH = os.path.join(PKG, "libchannel_gpu.so")
+HEADER = os.path.join(ROOT, "include", "channel_gpu.h")
+
+PREC_FP64, PREC_SPLIT = 0, 1
+
+
+class CfParams(C.Structure):
+    _fields_ = [
+        ("nu", C.c_double), ("CFL", C.c_double), ("dPdx", C.c_double), ("dPdz", C.c_double),
+        ("Rossby_plus", C.c_double), ("freq_mult", C.c_double),
+        ("Retau_int", C.c_int), ("x_mass_cte", C.c_int), ("y_mass_cte", C.c_int),
+        ("LES_model", C.c_int), ("iwall_model", C.c_int), ("Dirichlet_nu_t", C.c_int), ("jref_eqwm", C.c_int),
+        ("precision", C.c_int), ("eqwm_ncv", C.c_int), ("eqwm_stretch", C.c_double), ("sgs_recompute", C.c_int),
+    ]
+
+
+class CfError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def header_functions() -> list[str]:
+    """Names of the functions declared in include/channel_gpu.h."""
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(cf_[a-z0-9_]+)\s*\(", src)))
+
+
+def load(build_if_missing: bool = True):
+    """Loads the library (building it in-tree when it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise CfError(f"{LIB_PATH} not built")
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("build_lib", os.path.join(PKG, "build_lib.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    L = C.CDLL(LIB_PATH)
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    L.cf_default_params.argtypes = [C.POINTER(CfParams)]
+    L.cf_default_params.restype = None
+    L.cf_create.argtypes = [C.c_int, C.c_int, C.c_int, dp, dp, dp, C.POINTER(CfParams), C.c_int, C.POINTER(vp)]
+    L.cf_last_error.argtypes = [vp]
+    L.cf_last_error.restype = C.c_char_p
+    L.cf_destroy.argtypes = [vp]
+    L.cf_upload_fields.argtypes = [vp, dp, dp, dp]
+    L.cf_download_fields.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.cf_download_wall.argtypes = [vp, dp, dp, dp]
+    L.cf_upload_wall.argtypes = [vp, dp, dp, dp]
+    L.cf_set_scalars.argtypes = [vp, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double]
+    L.cf_get_scalars.argtypes = [vp, dp, dp, ip, dp, dp]
+    L.cf_init_mass_flow.argtypes = [vp, dp]
+    L.cf_compute_dt.argtypes = [vp, dp]
+    for n in ["cf_compute_eddy_viscosity", "cf_compute_wall_model", "cf_apply_boundary_conditions",
+              "cf_compute_projection_step", "cf_save_old_state", "cf_synchronize", "cf_launches_per_step"]:
+        getattr(L, n).argtypes = [vp]
+    for n in ["cf_compute_rhs_u", "cf_compute_rhs_v", "cf_compute_rhs_w", "cf_rk_update", "cf_set_fixed_dt"]:
+        getattr(L, n).argtypes = [vp, C.c_int]
+    L.cf_set_fixed_dt.argtypes = [vp, C.c_double]
+    for n in ["cf_compute_dPx_for_constant_mass_flow", "cf_compute_dPy_for_constant_mass_flow",
+              "cf_compute_dPx_for_constant_Ucenterline"]:
+        getattr(L, n).argtypes = [vp, dp]
+    L.cf_check_divergence.argtypes = [vp, dp, dp]
+    L.cf_apply_mass_flow_correction.argtypes = [vp, C.c_int, C.c_double]
+    L.cf_download_rhs.argtypes = [vp, C.c_int, C.c_int, dp]
+    L.cf_download_avg_nu_t.argtypes = [vp, dp]
+    L.cf_get_eqwm_counters.argtypes = [vp, ip, ip]
+    L.cf_time_step_rk3.argtypes = [vp, C.c_int, C.c_int]
+    L.cf_get_stream.argtypes = [vp]
+    L.cf_get_stream.restype = vp
+    L.cf_compute_statistics.argtypes = [vp, dp]
+    L.cf_read_input_parameters.argtypes = [C.c_char_p, C.POINTER(CfParams), ip, C.c_char_p, C.c_char_p, ip, ip]
+    L.cf_read_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp]
+    L.cf_write_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
+    _lib = L
+    return L
+
+
+def _dp(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def default_params(**kw) -> CfParams:
+    p = CfParams()
+    load().cf_default_params(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise KeyError(k)
+        setattr(p, k, v)
+    return p
+
+
+class Channel:
+    """One channel on one GPU, arrays in the reference's Fortran layout."""
+
+    def __init__(self, x, y, z, params: CfParams | None = None, device: int = 0, **kw):
+        self.L = load()
+        self.x = np.ascontiguousarray(x, dtype=np.float64)
+        self.y = np.ascontiguousarray(y, dtype=np.float64)
+        self.z = np.ascontiguousarray(z, dtype=np.float64)
+        self.nx, self.ny, self.nz = len(self.x), len(self.y), len(self.z)
+        self.params = params if params is not None else default_params(**kw)
+        h = C.c_void_p()
+        rc = self.L.cf_create(self.nx, self.ny, self.nz, _dp(self.x), _dp(self.y), _dp(self.z),
+                              C.byref(self.params), device, C.byref(h))
+        if rc != 0:
+            msg = self.L.cf_last_error(h).decode() if h.value else f"cf_create failed ({rc})"
+            if h.value:
+                self.L.cf_destroy(h)
+            raise CfError(msg)
+        self.h = h
+        self.shapes = grids.field_shapes(self.nx, self.ny, self.nz)
+
+    # ---------------------------------------------------------------- utils
+    def _check(self, rc):
+        if rc != 0:
+            raise CfError(self.L.cf_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.cf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---------------------------------------------------------- transfers
+    def upload(self, U, V, W):
+        U = np.asfortranarray(U, dtype=np.float64)
+        V = np.asfortranarray(V, dtype=np.float64)
+        W = np.asfortranarray(W, dtype=np.float64)
+        for n, a in (("U", U), ("V", V), ("W", W)):
+            if a.shape != self.shapes[n]:
+                raise ValueError(f"{n} has shape {a.shape}, expected {self.shapes[n]}")
+        self._check(self.L.cf_upload_fields(self.h, _dp(U), _dp(V), _dp(W)))
+
+    def download(self):
+        out = {k: np.zeros(self.shapes[k], order="F") for k in ("U", "V", "W", "P", "nu_t")}
+        self._check(self.L.cf_download_fields(self.h, *[_dp(out[k]) for k in ("U", "V", "W", "P", "nu_t")]))
+        return out
+
+    def download_wall(self):
+        nx, nz = self.nx, self.nz
+        ax = np.zeros((nx, 2, nz + 1), order="F")
+        az = np.zeros((nx + 1, 2, nz), order="F")
+        tau = np.zeros((nx, 2, nz + 1), order="F")
+        self._check(self.L.cf_download_wall(self.h, _dp(ax), _dp(az), _dp(tau)))
+        return dict(alpha_x=ax, alpha_z=az, tau_eqwm_initial=tau)
+
+    def download_rhs(self, comp: int, slot: int):
+        shp = [self.shapes["U"], self.shapes["V"], self.shapes["W"]][comp]
+        a = np.zeros(shp, order="F")
+        self._check(self.L.cf_download_rhs(self.h, comp, slot, _dp(a)))
+        return a
+
+    def avg_nu_t(self):
+        a = np.zeros(self.ny + 1)
+        self._check(self.L.cf_download_avg_nu_t(self.h, _dp(a)))
+        return a
+
+    def set_scalars(self, t=0.0, dt=0.0, rk_step=1, dPdx=None, dPdy=0.0):
+        if dPdx is None:
+            dPdx = self.scalars()["dPdx"]
+        self._check(self.L.cf_set_scalars(self.h, t, dt, rk_step, dPdx, dPdy))
+
+    def scalars(self):
+        t, dt, dpx, dpy = C.c_double(), C.c_double(), C.c_double(), C.c_double()
+        rk = C.c_int()
+        self._check(self.L.cf_get_scalars(self.h, C.byref(t), C.byref(dt), C.byref(rk), C.byref(dpx), C.byref(dpy)))
+        return dict(t=t.value, dt=dt.value, rk_step=rk.value, dPdx=dpx.value, dPdy=dpy.value)
+
+    # ---------------------------------------------- reference subroutines
+    def init_mass_flow(self):
+        q = C.c_double()
+        self._check(self.L.cf_init_mass_flow(self.h, C.byref(q)))
+        return q.value
+
+    def compute_dt(self):
+        v = C.c_double()
+        self._check(self.L.cf_compute_dt(self.h, C.byref(v)))
+        return v.value
+
+    def compute_eddy_viscosity(self):
+        self._check(self.L.cf_compute_eddy_viscosity(self.h))
+
+    def compute_wall_model(self):
+        self._check(self.L.cf_compute_wall_model(self.h))
+
+    def compute_rhs_u(self, slot):
+        self._check(self.L.cf_compute_rhs_u(self.h, slot))
+
+    def compute_rhs_v(self, slot):
+        self._check(self.L.cf_compute_rhs_v(self.h, slot))
+
+    def compute_rhs_w(self, slot):
+        self._check(self.L.cf_compute_rhs_w(self.h, slot))
+
+    def save_old_state(self):
+        self._check(self.L.cf_save_old_state(self.h))
+
+    def rk_update(self, substep):
+        self._check(self.L.cf_rk_update(self.h, substep))
+
+    def apply_boundary_conditions(self):
+        self._check(self.L.cf_apply_boundary_conditions(self.h))
+
+    def compute_projection_step(self):
+        self._check(self.L.cf_compute_projection_step(self.h))
+
+    def compute_dPx_for_constant_mass_flow(self):
+        v = C.c_double()
+        self._check(self.L.cf_compute_dPx_for_constant_mass_flow(self.h, C.byref(v)))
+        return v.value
+
+    def apply_mass_flow_correction(self, comp, value):
+        self._check(self.L.cf_apply_mass_flow_correction(self.h, comp, value))
+
+    def check_divergence(self):
+        a, b = C.c_double(), C.c_double()
+        self._check(self.L.cf_check_divergence(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def eqwm_counters(self):
+        a, b = C.c_int(), C.c_int()
+        self._check(self.L.cf_get_eqwm_counters(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def statistics(self):
+        out = np.zeros(9 * self.ny + 8)
+        self._check(self.L.cf_compute_statistics(self.h, _dp(out)))
+        return out
+
+    # ------------------------------------------------------------ fast path
+    def time_step_rk3(self, nsteps: int = 1, sync: bool = True):
+        self._check(self.L.cf_time_step_rk3(self.h, nsteps, 1 if sync else 0))
+
+    def set_fixed_dt(self, dt: float):
+        self._check(self.L.cf_set_fixed_dt(self.h, dt))
+
+    def synchronize(self):
+        self._check(self.L.cf_synchronize(self.h))
+
+    def stream(self) -> int:
+        return self.L.cf_get_stream(self.h)
+
+    def launches_per_step(self) -> int:
+        return self.L.cf_launches_per_step(self.h)
+
+    def compute_time_step_rk3_mirror(self):
+        """The reference's compute_time_step_RK3 (time_integration.f90:89-173)
+        driven call by call through the fine-grained ABI."""
+        sc = self.scalars()
+        to, dt = sc["t"], sc["dt"]
+        rk_t = [8.0 / 15.0, 2.0 / 3.0, 1.0]
+        self.save_old_state()
+        p = self.params
+        for s in (1, 2, 3):
+            self.set_scalars(t=self.scalars()["t"], dt=dt, rk_step=s)
+            self.compute_eddy_viscosity()
+            if s == 1:
+                self.compute_wall_model()
+                self.compute_eddy_viscosity()
+            self.compute_rhs_u(s)
+            self.compute_rhs_v(s)
+            self.compute_rhs_w(s)
+            self.rk_update(s)
+            self.set_scalars(t=to + rk_t[s - 1] * dt, dt=dt, rk_step=s)
+            self.apply_boundary_conditions()
+            self.compute_projection_step()
+            self.apply_boundary_conditions()
+        if p.x_mass_cte == 1:
+            d = self.compute_dPx_for_constant_mass_flow()
+            self.apply_mass_flow_correction(0, d)
+            self.apply_boundary_conditions()
+
+
+def read_input_parameters(path: str):
+    """Parses an input_parameters file (input_output.f90:21-133)."""
+    L = load()
+    p = CfParams()
+    grid = (C.c_int * 3)()
+    fi, fo = C.create_string_buffer(200), C.create_string_buffer(200)
+    ints, ints2 = (C.c_int * 4)(), (C.c_int * 2)()
+    rc = L.cf_read_input_parameters(path.encode(), C.byref(p), grid, fi, fo, ints, ints2)
+    if rc != 0:
+        raise CfError(f"cannot parse {path} ({rc})")
+    return dict(params=p, grid=tuple(grid), filein=fi.value.decode(), fileout=fo.value.decode(),
+                nsteps=ints[0], nsave=ints[1], nstats=ints[2], nmonitor=ints[3], nstep_init=ints2[0],
+                random_init=ints2[1])
+
+
+def read_snapshot(path: str, nx: int, ny: int, nz: int):
+    L = load()
+    x, y, z = np.zeros(nx), np.zeros(ny), np.zeros(nz)
+    s = grids.field_shapes(nx, ny, nz)
+    U, V, W = (np.zeros(s[k], order="F") for k in ("U", "V", "W"))
+    rc = L.cf_read_snapshot(path.encode(), nx, ny, nz, _dp(x), _dp(y), _dp(z), _dp(U), _dp(V), _dp(W))
+    if rc != 0:
+        raise CfError(f"cannot read snapshot {path} ({rc})")
+    return x, y, z, U, V, W
+
+
+def write_snapshot(path: str, x, y, z, U, V, W, P=None, nu_t=None):
+    L = load()
+    f = lambda a: None if a is None else np.asfortranarray(a, dtype=np.float64)
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+    U, V, W, P, nu_t = f(U), f(V), f(W), f(P), f(nu_t)
+    rc = L.cf_write_snapshot(path.encode(), len(x), len(y), len(z), _dp(x), _dp(y), _dp(z), _dp(U), _dp(V), _dp(W),
+                             _dp(P), _dp(nu_t))
+    if rc != 0:
+        raise CfError(f"cannot write snapshot {path} ({rc})")

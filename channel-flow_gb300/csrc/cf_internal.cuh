@@ -1,0 +1,164 @@
+// cf_internal.cuh -- shared definitions of the channel RK3-substep library.
+//
+// Device layout: every field keeps the reference's Fortran extents and order
+// (initialization.f90:121-152), 1-based indices, x fastest:
+//   U (nx,nyg,nzg)  V (nxg,ny,nzg)  W (nxg,nyg,nz)  P, nu_t (nxg,nyg,nzg)
+// with nxg = nx+1 etc.  Ghost layers and the periodic duplicate planes are
+// stored, so a kernel reads exactly the values the reference reads.
+// Quantities the reference only keeps periodic copies of (the eddy-viscosity
+// intermediates, the pseudo-pressure) live in a compact "canonical" layout of
+// the nxp x nym x nzp unique cells (i = 2..nx-1, j = 2..nyg-1, k = 2..nz-1),
+// read through the periodic wrap  i -> 2 + (i-2) mod nxp.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "channel_gpu.h"
+
+#define CF_CUDA(call)                                                                  \
+    do {                                                                               \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            return cf_fail(ctx, CF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+        }                                                                              \
+    } while (0)
+
+// Fortran-layout 3-D field view with 1-based indices.
+template <typename T>
+struct Fld {
+    T *p;
+    int sy, sz, off;  // off = 1 + sy + sz
+    __host__ __device__ __forceinline__ T &operator()(int i, int j, int k) const {
+        return p[i + sy * j + sz * k - off];
+    }
+    __host__ __device__ __forceinline__ int idx(int i, int j, int k) const { return i + sy * j + sz * k - off; }
+};
+
+template <typename T>
+static inline Fld<T> make_fld(void *p, int n1, int n2) {
+    Fld<T> f;
+    f.p = (T *)p;
+    f.sy = n1;
+    f.sz = n1 * n2;
+    f.off = 1 + f.sy + f.sz;
+    return f;
+}
+
+// Grid geometry (device pointers, 1-based: x[1..nx]); T = double or float.
+template <typename T>
+struct GeoT {
+    int nx, ny, nz, nxg, nyg, nzg, nxp, nym, nzp, nxh;
+    const T *x, *y, *z, *xg, *yg, *zg, *w0, *w1;
+};
+typedef GeoT<double> Geo;
+
+// Device-resident scalars (module globals of global.f90 touched per step).
+struct DevScal {
+    double dt, t, dPdx, dPdy, dPdz;
+    double Qflow_x_0, Qflow_y_0, Ucenterline_x, tau_mean_eqwm;
+    double lmax[3];        // compute_dt maxima (bit patterns ordered as int64)
+    double mass_sum;       // mass-flow integral
+    double fixed_dt;       // > 0: dt forced (CFL < 0 rule)
+    int rk_step, n_nan, n_iter, pad;
+};
+
+__host__ __device__ __forceinline__ int wrapc(int i, int np) {
+    // canonical index of a periodic index (faces or centres): 2 + (i-2) mod np
+    int r = (i - 2) % np;
+    if (r < 0) r += np;
+    return 2 + r;
+}
+
+static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+struct cf_ctx {
+    int dev = 0;
+    cf_params prm;
+    int nx, ny, nz, nxg, nyg, nzg, nxp, nym, nzp, nxh;
+    size_t nU, nV, nW, nC, nCan, nSpec;
+    cudaStream_t st = nullptr;
+    std::string err;
+
+    // host geometry (1-based vectors)
+    std::vector<double> hx, hy, hz, hxg, hyg, hzg, hw0, hw1, hkxx, hkzz;
+    std::vector<double> Dd, Dl, Du;  // tridiagonal rows of Dyy (2..nyg-1)
+    double dxmin, dymin, dzmin, Lx, Ly, Lz, mass_norm, omega_z;
+    double *d_geo = nullptr;
+    float *d_geo_f = nullptr;
+    Geo geo;
+    GeoT<float> geof;
+    double mass_norm_vv = 1.0;
+
+    // state (element type: double for FP64, float for the split path)
+    int esz = 8;                       // bytes per state element
+    void *U[3] = {}, *V[3] = {}, *W[3] = {};
+    void *Ulo[3] = {}, *Vlo[3] = {}, *Wlo[3] = {};  // split path: low words
+    int cur = 0, old = 0;              // current state and Uo buffers
+    void *nut = nullptr, *P = nullptr;
+    void *F[3][3] = {};                // [slot 0..2][comp]
+    // eddy viscosity
+    void *dsm_q = nullptr;             // 16 canonical arrays
+    void *dsm_lf = nullptr;            // 12 canonical arrays (L and hat(|S|Sij))
+    void *Uf = nullptr, *Vf = nullptr, *Wf = nullptr;
+    double *dsm_part = nullptr;        // plane partial sums
+    double *avg_nu_t = nullptr;        // (nyg) device
+    int dsm_nblk = 0;
+    // pressure
+    void *phi = nullptr;               // canonical real
+    void *spec = nullptr;              // complex spectrum (nxh, nym, nzp)
+    double *d_tri = nullptr;           // Dd, Dl, Du (nym each), kxx (nxp), kzz (nzp)
+    double *d_tw = nullptr;            // twiddles: x fwd, x bwd, z fwd, z bwd
+    int radx[8], nradx, radz[8], nradz;
+    // wall model
+    double *alpha_x = nullptr, *alpha_z = nullptr, *alpha_zt = nullptr, *tau0 = nullptr;
+    double *wtemp1 = nullptr, *wtemp2 = nullptr;   // W at jref: z-interp (nxg,2,nzg), x-interp (nx,2,nzg)
+    double *eq_grid = nullptr;                      // y_cv(1..ncv), y_fa(1..ncv+1)
+    int *eq_zst = nullptr, *eq_xst = nullptr;       // stencil indices
+    double *eq_zw = nullptr, *eq_xw = nullptr;      // stencil weights
+    int n_nan = 0, n_iter = 0;
+    // scalars
+    DevScal hs;
+    DevScal *ds = nullptr;
+    double *d_red = nullptr;           // reduction scratch
+    int red_n = 0;
+    // staging for transfers
+    double *stage = nullptr;
+    size_t stage_n = 0;
+    // one captured step graph per starting state buffer (the three state
+    // buffers rotate with period three)
+    cudaGraphExec_t graphs[3] = {};
+    int next_buf[3] = {};
+    int step_launches = 0;
+    int launches = 0;
+    bool counting = false;
+};
+
+int cf_fail(cf_ctx *ctx, int code, const std::string &msg);
+
+// ---- launchers (kernels in the .cu files), all enqueue on ctx->st -------
+template <typename T> int launch_bc(cf_ctx *ctx, int buf);                 // apply_boundary_conditions
+template <typename T> int launch_rhs(cf_ctx *ctx, int comp, int slot);     // store F slot
+template <typename T> int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst);  // fused RHS + RK update
+template <typename T> int launch_rk_update(cf_ctx *ctx, int s);            // from stored F slots
+template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // eddy viscosity
+template <typename T> int launch_nut_zero(cf_ctx *ctx);
+template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p);
+template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
+template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode);  // 1: x mass flow, 2: centre-line, 3: y
+template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only
+template <typename T> int launch_mass_apply(cf_ctx *ctx, int buf, int mode); // add ds->lmax[2], dPdx = it/dt
+template <typename T> int launch_dt(cf_ctx *ctx, int buf);
+template <typename T> int launch_eqwm(cf_ctx *ctx, int buf);
+template <typename T> int launch_copy_state(cf_ctx *ctx, int src, int dst);
+template <typename T> int launch_stats(cf_ctx *ctx, int buf, double *d_out);
+
+static inline void count_launch(cf_ctx *ctx) {
+    if (ctx->counting) ctx->launches++;
+}
+
+template <typename T> static inline GeoT<T> geo_of(cf_ctx *ctx);
+template <> inline GeoT<double> geo_of<double>(cf_ctx *ctx) { return ctx->geo; }
+template <> inline GeoT<float> geo_of<float>(cf_ctx *ctx) { return ctx->geof; }

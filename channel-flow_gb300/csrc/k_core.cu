@@ -1,0 +1,684 @@
+// k_core.cu -- boundary conditions, momentum right-hand sides, RK3 update,
+// mass-flow forcing, time-step and divergence reductions.
+#include "cf_internal.cuh"
+
+// ---------------------------------------------------------------------------
+// apply_boundary_conditions (boundary_conditions.f90:20-75).
+// One thread per ghost element.  The reference first copies the x-periodic
+// planes, then the z-periodic planes (including x ghosts), then overwrites the
+// two wall rows for every (i,k); the composed result at a ghost element is
+// therefore a copy from the canonical position (wrap(i), j, wrap(k)), and the
+// wall rows are built from row 2 / row nyg-1 at (wrap(i), wrap(k)).
+// ---------------------------------------------------------------------------
+// ybc: 0 = Dirichlet at centres (ghost = -interior), 1 = zero at faces,
+//      2 = nonzero Neumann at centres (ghost = interior - dy*alpha(i,wall,k))
+template <typename T>
+__global__ void k_bc(Fld<T> F, Fld<T> Flo, int n1, int n2, int n3, int xc, int zc, int nxp, int nzp, int ybc,
+                     const double *alpha, double dyb, double dyt) {
+    const int gx = xc ? 3 : 2, gz = zc ? 3 : 2;
+    const long nY = 2L * n1 * n3;
+    const long nX = (long)gx * (n2 - 2) * n3;
+    const long nZ = (long)gz * (n2 - 2) * (n1 - gx);
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    int i, j, k;
+    if (t < nY) {
+        i = (int)(t % n1) + 1;
+        long r = t / n1;
+        k = (int)(r % n3) + 1;
+        j = (r / n3) == 0 ? 1 : n2;
+        int is = wrapc(i, nxp), ks = wrapc(k, nzp);
+        if (ybc == 1) {
+            F(i, j, k) = T(0);
+            if (Flo.p) Flo(i, j, k) = T(0);
+        } else {
+            int jsrc = (j == 1) ? 2 : n2 - 1;
+            T v = F(is, jsrc, ks);
+            if (ybc == 0) {
+                F(i, j, k) = -v;
+                if (Flo.p) Flo(i, j, k) = -Flo(is, jsrc, ks);
+            } else {
+                int w = (j == 1) ? 0 : 1;
+                double a = alpha[(i - 1) + (long)n1 * (w + 2L * (k - 1))];
+                double dy = (j == 1) ? dyb : dyt;
+                if (Flo.p) {
+                    double hv = (double)v + (double)Flo(is, jsrc, ks) - dy * a;
+                    T hi = (T)hv;
+                    F(i, j, k) = hi;
+                    Flo(i, j, k) = (T)(hv - (double)hi);
+                } else {
+                    F(i, j, k) = (T)((double)v - dy * a);
+                }
+            }
+        }
+        return;
+    }
+    t -= nY;
+    if (t < nX) {
+        int g = (int)(t % gx);
+        long r = t / gx;
+        j = (int)(r % (n2 - 2)) + 2;
+        k = (int)(r / (n2 - 2)) + 1;
+        i = (g == 0) ? 1 : (xc ? (g == 1 ? n1 - 1 : n1) : n1);
+    } else {
+        t -= nX;
+        if (t >= nZ) return;
+        int g = (int)(t % gz);
+        long r = t / gz;
+        j = (int)(r % (n2 - 2)) + 2;
+        i = (int)(r / (n2 - 2)) + 2;  // non-ghost x: 2 .. n1-gx+1
+        k = (g == 0) ? 1 : (zc ? (g == 1 ? n3 - 1 : n3) : n3);
+    }
+    int is = wrapc(i, nxp), ks = wrapc(k, nzp);
+    F(i, j, k) = F(is, j, ks);
+    if (Flo.p) Flo(i, j, k) = Flo(is, j, ks);
+}
+
+template <typename T>
+static int bc_field(cf_ctx *ctx, void *p, void *plo, int n1, int n2, int n3, int xc, int zc, int ybc,
+                    const double *alpha) {
+    int gx = xc ? 3 : 2, gz = zc ? 3 : 2;
+    long tot = 2L * n1 * n3 + (long)gx * (n2 - 2) * n3 + (long)gz * (n2 - 2) * (n1 - gx);
+    Fld<T> F = make_fld<T>(p, n1, n2);
+    Fld<T> L = make_fld<T>(plo, n1, n2);
+    double dyb = ctx->hyg[2] - ctx->hyg[1], dyt = ctx->hyg[ctx->nyg] - ctx->hyg[ctx->nyg - 1];
+    k_bc<T><<<cdiv(tot, 256), 256, 0, ctx->st>>>(F, L, n1, n2, n3, xc, zc, ctx->nxp, ctx->nzp, ybc, alpha, dyb, dyt);
+    count_launch(ctx);
+    return 0;
+}
+
+template <typename T>
+int launch_bc(cf_ctx *ctx, int b) {
+    int wm = ctx->prm.iwall_model;
+    // U: x faces, y centres, z centres
+    bc_field<T>(ctx, ctx->U[b], ctx->Ulo[b], ctx->nx, ctx->nyg, ctx->nzg, 0, 1, wm == 3 ? 2 : 0, ctx->alpha_x);
+    // V: x centres, y faces, z centres
+    bc_field<T>(ctx, ctx->V[b], ctx->Vlo[b], ctx->nxg, ctx->ny, ctx->nzg, 1, 1, 1, nullptr);
+    // W: x centres, y centres, z faces
+    bc_field<T>(ctx, ctx->W[b], ctx->Wlo[b], ctx->nxg, ctx->nyg, ctx->nz, 1, 0, wm == 3 ? 2 : 0, ctx->alpha_z);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Momentum right-hand sides, equations.f90:24-498, one thread per point.
+// ---------------------------------------------------------------------------
+struct RkCoef {
+    double c[4][4];
+};
+
+template <typename T>
+__device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W,
+                                         const Fld<T> &nt, T nu, T dPdx, T Om, int i, int j, int k) {
+    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
+    const T h = T(0.5), q = T(0.25);
+    // 1) -du^2/dx  (equations.f90:43-57)
+    T a = h * (U(i, j, k) + U(i + 1, j, k));
+    T b = h * (U(i - 1, j, k) + U(i, j, k));
+    T r = -(a * a - b * b) / (xg[i + 1] - xg[i]);
+    // 2) -duv/dy   (:62-79)
+    T uy1 = w0[j] * U(i, j, k) + w1[j] * U(i, j + 1, k);
+    T uy0 = w0[j - 1] * U(i, j - 1, k) + w1[j - 1] * U(i, j, k);
+    T vx1 = h * (V(i, j, k) + V(i + 1, j, k));
+    T vx0 = h * (V(i, j - 1, k) + V(i + 1, j - 1, k));
+    r += -(uy1 * vx1 - uy0 * vx0) / (y[j] - y[j - 1]);
+    // 3) -duw/dz   (:84-101)
+    T uz1 = h * (U(i, j, k) + U(i, j, k + 1));
+    T uz0 = h * (U(i, j, k - 1) + U(i, j, k));
+    T wx1 = h * (W(i, j, k) + W(i + 1, j, k));
+    T wx0 = h * (W(i, j, k - 1) + W(i + 1, j, k - 1));
+    r += -(uz1 * wx1 - uz0 * wx0) / (z[k] - z[k - 1]);
+    // 4) viscous   (:108-163)
+    T dx_1 = x[i] - x[i - 1], dx_2 = x[i + 1] - x[i], dx_3 = xg[i + 1] - xg[i];
+    T dy_3 = y[j] - y[j - 1];
+    T dz_1 = zg[k] - zg[k - 1], dz_2 = zg[k + 1] - zg[k], dz_3 = z[k] - z[k - 1];
+    T t2j = (U(i, j + 1, k) - U(i, j, k)) / (yg[j + 1] - yg[j]);
+    T t2jm = (U(i, j, k) - U(i, j - 1, k)) / (yg[j] - yg[j - 1]);
+    T nu_x1 = nu + nt(i, j, k);
+    T nu_x2 = nu + nt(i + 1, j, k);
+    T nu_y1 = nu + h * (w0[j - 1] * nt(i, j - 1, k) + w1[j - 1] * nt(i, j, k) + w0[j - 1] * nt(i + 1, j - 1, k) +
+                        w1[j - 1] * nt(i + 1, j, k));
+    T nu_y2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i + 1, j, k) + w1[j] * nt(i + 1, j + 1, k));
+    T nu_z1 = nu + q * (nt(i, j, k) + nt(i, j, k - 1) + nt(i + 1, j, k) + nt(i + 1, j, k - 1));
+    T nu_z2 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i + 1, j, k) + nt(i + 1, j, k + 1));
+    T visc = T(2) / dx_3 * (nu_x2 * (U(i + 1, j, k) - U(i, j, k)) / dx_2 - nu_x1 * (U(i, j, k) - U(i - 1, j, k)) / dx_1) +
+             T(1) / dy_3 * (nu_y2 * (t2j + (V(i + 1, j, k) - V(i, j, k)) / dx_2) -
+                            nu_y1 * (t2jm + (V(i + 1, j - 1, k) - V(i, j - 1, k)) / dx_1)) +
+             T(1) / dz_3 * (nu_z2 * ((U(i, j, k + 1) - U(i, j, k)) / dz_2 + (W(i + 1, j, k) - W(i, j, k)) / dx_2) -
+                            nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) / dz_1 + (W(i + 1, j, k - 1) - W(i, j, k - 1)) / dx_1));
+    r += visc;
+    r += dPdx;  // :166
+    if (fabs((double)Om) > 1e-6) {  // :169-177
+        T tv0 = h * (V(i, j - 1, k) + V(i, j, k));
+        T tv1 = h * (V(i + 1, j - 1, k) + V(i + 1, j, k));
+        r += T(2) * Om * (h * (tv0 + tv1));
+    }
+    return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W,
+                                         const Fld<T> &nt, T nu, T Om, int i, int j, int k) {
+    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
+    const T h = T(0.5);
+    // 1) -dv^2/dy (equations.f90:205-223)
+    T a = h * (V(i, j, k) + V(i, j + 1, k));
+    T b = h * (V(i, j - 1, k) + V(i, j, k));
+    T r = -(a * a - b * b) / (yg[j + 1] - yg[j]);
+    // 2) -duv/dx (:228-245)
+    T uy1 = w0[j] * U(i, j, k) + w1[j] * U(i, j + 1, k);
+    T uy0 = w0[j] * U(i - 1, j, k) + w1[j] * U(i - 1, j + 1, k);
+    T vx1 = h * (V(i, j, k) + V(i + 1, j, k));
+    T vx0 = h * (V(i - 1, j, k) + V(i, j, k));
+    r += -(uy1 * vx1 - uy0 * vx0) / (x[i] - x[i - 1]);
+    // 3) -dvw/dz (:250-267)
+    T vz1 = h * (V(i, j, k) + V(i, j, k + 1));
+    T vz0 = h * (V(i, j, k - 1) + V(i, j, k));
+    T wy1 = w0[j] * W(i, j, k) + w1[j] * W(i, j + 1, k);
+    T wy0 = w0[j] * W(i, j, k - 1) + w1[j] * W(i, j + 1, k - 1);
+    r += -(vz1 * wy1 - vz0 * wy0) / (z[k] - z[k - 1]);
+    // 4) viscous (:276-331)
+    T dx_1 = xg[i] - xg[i - 1], dx_2 = xg[i + 1] - xg[i], dx_3 = x[i] - x[i - 1];
+    T dy_1 = y[j] - y[j - 1], dy_2 = y[j + 1] - y[j], dy_3 = yg[j + 1] - yg[j];
+    T dz_1 = zg[k] - zg[k - 1], dz_2 = zg[k + 1] - zg[k], dz_3 = z[k] - z[k - 1];
+    T nu_x1 = nu + h * (w0[j] * nt(i - 1, j, k) + w1[j] * nt(i - 1, j + 1, k) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
+    T nu_x2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i + 1, j, k) + w1[j] * nt(i + 1, j + 1, k));
+    T nu_y1 = nu + nt(i, j, k);
+    T nu_y2 = nu + nt(i, j + 1, k);
+    T nu_z1 = nu + h * (w0[j] * nt(i, j, k - 1) + w1[j] * nt(i, j + 1, k - 1) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
+    T nu_z2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i, j, k + 1) + w1[j] * nt(i, j + 1, k + 1));
+    T visc = T(1) / dx_3 * (nu_x2 * ((V(i + 1, j, k) - V(i, j, k)) / dx_2 + (U(i, j + 1, k) - U(i, j, k)) / dy_3) -
+                            nu_x1 * ((V(i, j, k) - V(i - 1, j, k)) / dx_1 + (U(i - 1, j + 1, k) - U(i - 1, j, k)) / dy_3)) +
+             T(2) / dy_3 * (nu_y2 * (V(i, j + 1, k) - V(i, j, k)) / dy_2 - nu_y1 * (V(i, j, k) - V(i, j - 1, k)) / dy_1) +
+             T(1) / dz_3 * (nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) / dz_2 + (W(i, j + 1, k) - W(i, j, k)) / dy_3) -
+                            nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) / dz_1 + (W(i, j + 1, k - 1) - W(i, j, k - 1)) / dy_3));
+    r += visc;
+    if (fabs((double)Om) > 1e-6) {  // :334-342
+        T tu0 = h * (U(i - 1, j, k) + U(i, j, k));
+        T tu1 = h * (U(i - 1, j + 1, k) + U(i, j + 1, k));
+        r -= T(2) * Om * (w0[j] * tu0 + w1[j] * tu1);
+    }
+    return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W,
+                                         const Fld<T> &nt, T nu, T dPdz, int i, int j, int k) {
+    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
+    const T h = T(0.5), q = T(0.25);
+    // 1) -dw^2/dz (equations.f90:370-384)
+    T a = h * (W(i, j, k) + W(i, j, k + 1));
+    T b = h * (W(i, j, k - 1) + W(i, j, k));
+    T r = -(a * a - b * b) / (zg[k + 1] - zg[k]);
+    // 2) -duw/dx (:389-406)
+    T uz1 = h * (U(i, j, k) + U(i, j, k + 1));
+    T uz0 = h * (U(i - 1, j, k) + U(i - 1, j, k + 1));
+    T wx1 = h * (W(i, j, k) + W(i + 1, j, k));
+    T wx0 = h * (W(i - 1, j, k) + W(i, j, k));
+    r += -(uz1 * wx1 - uz0 * wx0) / (x[i] - x[i - 1]);
+    // 3) -dvw/dy (:411-428)
+    T vz1 = h * (V(i, j, k) + V(i, j, k + 1));
+    T vz0 = h * (V(i, j - 1, k) + V(i, j - 1, k + 1));
+    T wy1 = w0[j] * W(i, j, k) + w1[j] * W(i, j + 1, k);
+    T wy0 = w0[j - 1] * W(i, j - 1, k) + w1[j - 1] * W(i, j, k);
+    r += -(vz1 * wy1 - vz0 * wy0) / (y[j] - y[j - 1]);
+    // 4) viscous (:435-493)
+    T dx_1 = xg[i] - xg[i - 1], dx_2 = xg[i + 1] - xg[i], dx_3 = x[i] - x[i - 1];
+    T dy_3 = y[j] - y[j - 1];
+    T dz_1 = z[k] - z[k - 1], dz_2 = z[k + 1] - z[k], dz_3 = zg[k + 1] - zg[k];
+    T t2j = (W(i, j + 1, k) - W(i, j, k)) / (yg[j + 1] - yg[j]);
+    T t2jm = (W(i, j, k) - W(i, j - 1, k)) / (yg[j] - yg[j - 1]);
+    T nu_x1 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i - 1, j, k) + nt(i - 1, j, k + 1));
+    T nu_x2 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i + 1, j, k) + nt(i + 1, j, k + 1));
+    T nu_y1 = nu + h * (w0[j - 1] * nt(i, j - 1, k) + w1[j - 1] * nt(i, j, k) + w0[j - 1] * nt(i, j - 1, k + 1) +
+                        w1[j - 1] * nt(i, j, k + 1));
+    T nu_y2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i, j, k + 1) + w1[j] * nt(i, j + 1, k + 1));
+    T nu_z1 = nu + nt(i, j, k);
+    T nu_z2 = nu + nt(i, j, k + 1);
+    T visc = T(1) / dx_3 * (nu_x2 * ((W(i + 1, j, k) - W(i, j, k)) / dx_2 + (U(i, j, k + 1) - U(i, j, k)) / dz_2) -
+                            nu_x1 * ((W(i, j, k) - W(i - 1, j, k)) / dx_1 + (U(i - 1, j, k + 1) - U(i - 1, j, k)) / dz_1)) +
+             T(1) / dy_3 * (nu_y2 * (t2j + (V(i, j, k + 1) - V(i, j, k)) / dz_2) -
+                            nu_y1 * (t2jm + (V(i, j - 1, k + 1) - V(i, j - 1, k)) / dz_1)) +
+             T(2) / dz_3 * (nu_z2 * (W(i, j, k + 1) - W(i, j, k)) / dz_2 - nu_z1 * (W(i, j, k) - W(i, j, k - 1)) / dz_1);
+    r += visc;
+    r += dPdz;  // :496
+    return r;
+}
+
+// mode: 0 = store F(slot); 1 = fused update from Uo with F1 (s = 1 stores F1)
+template <typename T, int COMP>
+__global__ void k_rhs(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds, T nu, T Om,
+                      Fld<T> out, Fld<T> F1, Fld<T> Uo, Fld<T> Uolo, Fld<T> Unlo, int mode, int s, RkCoef rk,
+                      int i1, int j1, int k1) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    int k = blockIdx.z + 2;
+    if (i > i1 || j > j1 || k > k1) return;
+    T r;
+    if (COMP == 0) r = rhs_u_point<T>(g, U, V, W, nt, nu, (T)ds->dPdx, Om, i, j, k);
+    else if (COMP == 1) r = rhs_v_point<T>(g, U, V, W, nt, nu, Om, i, j, k);
+    else r = rhs_w_point<T>(g, U, V, W, nt, nu, (T)ds->dPdz, i, j, k);
+    if (mode == 0) {
+        out(i, j, k) = r;
+        return;
+    }
+    // time_integration.f90:108-110 / 124-126 / 140-145 with F2 never reused
+    // (rk_coef(3,2) = 0, initialization.f90:416)
+    const double dt = ds->dt;
+    double inc;
+    if (s == 1) {
+        F1(i, j, k) = r;
+        inc = dt * rk.c[1][1] * (double)r;
+    } else if (s == 2) {
+        inc = dt * (rk.c[2][1] * (double)F1(i, j, k) + rk.c[2][2] * (double)r);
+    } else {
+        inc = dt * (rk.c[3][1] * (double)F1(i, j, k) + rk.c[3][3] * (double)r);
+    }
+    if (Uolo.p) {
+        // split precision: u^n kept as hi + lo; the new state keeps a low word
+        double v = (double)Uo(i, j, k) + (double)Uolo(i, j, k) + inc;
+        T hi = (T)v;
+        out(i, j, k) = hi;
+        if (Unlo.p) Unlo(i, j, k) = (T)(v - (double)hi);
+    } else {
+        out(i, j, k) = (T)((double)Uo(i, j, k) + inc);
+    }
+}
+
+
+static RkCoef rk_coefs() {
+    RkCoef c = {};
+    c.c[1][1] = 8.0 / 15.0;
+    c.c[2][1] = 1.0 / 4.0;
+    c.c[2][2] = 5.0 / 12.0;
+    c.c[3][1] = 1.0 / 4.0;
+    c.c[3][2] = 0.0;
+    c.c[3][3] = 3.0 / 4.0;
+    return c;
+}
+
+template <typename T>
+static int rhs_launch(cf_ctx *ctx, int comp, int src, int mode, int s, int slot, int dst) {
+    GeoT<T> g = geo_of<T>(ctx);
+    Fld<T> U = make_fld<T>(ctx->U[src], ctx->nx, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[src], ctx->nxg, ctx->ny);
+    Fld<T> W = make_fld<T>(ctx->W[src], ctx->nxg, ctx->nyg);
+    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+    int i1, j1, k1, n1, n2;
+    void *outp, *uo, *uolo = nullptr, *unlo = nullptr;
+    if (comp == 0) { i1 = ctx->nx - 1; j1 = ctx->nyg - 1; k1 = ctx->nzg - 1; n1 = ctx->nx; n2 = ctx->nyg; }
+    else if (comp == 1) { i1 = ctx->nxg - 1; j1 = ctx->ny - 1; k1 = ctx->nzg - 1; n1 = ctx->nxg; n2 = ctx->ny; }
+    else { i1 = ctx->nxg - 1; j1 = ctx->nyg - 1; k1 = ctx->nz - 1; n1 = ctx->nxg; n2 = ctx->nyg; }
+    void **cur = comp == 0 ? ctx->U : comp == 1 ? ctx->V : ctx->W;
+    void **lo = comp == 0 ? ctx->Ulo : comp == 1 ? ctx->Vlo : ctx->Wlo;
+    if (mode == 0) {
+        outp = ctx->F[slot][comp];
+        uo = nullptr;
+    } else {
+        outp = cur[dst];
+        uo = cur[ctx->old];
+        if (lo[ctx->old]) {
+            uolo = lo[ctx->old];
+            if (s == 3) unlo = lo[dst];
+        }
+    }
+    // F arrays use the full field extents (interior written)
+    Fld<T> out = make_fld<T>(outp, n1, n2);
+    Fld<T> F1 = make_fld<T>(ctx->F[0][comp], n1, n2);
+    Fld<T> Uo = make_fld<T>(uo, n1, n2);
+    Fld<T> Uolo = make_fld<T>(uolo, n1, n2);
+    Fld<T> Unlo = make_fld<T>(unlo, n1, n2);
+    dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
+    T nu = (T)ctx->prm.nu, Om = (T)ctx->omega_z;
+    RkCoef rk = rk_coefs();
+    if (comp == 0) k_rhs<T, 0><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    else if (comp == 1) k_rhs<T, 1><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    else k_rhs<T, 2><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+int launch_rhs(cf_ctx *ctx, int comp, int slot) {
+    return rhs_launch<T>(ctx, comp, ctx->cur, 0, 0, slot, 0);
+}
+
+template <typename T>
+int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst) {
+    for (int c = 0; c < 3; c++) {
+        int rc = rhs_launch<T>(ctx, c, src, 1, s, 0, dst);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
+// RK update from stored slots (time_integration.f90:108-146), U = Uo + dt*sum
+template <typename T>
+__global__ void k_rk_update(Fld<T> U, Fld<T> Uo, Fld<T> F1, Fld<T> F2, Fld<T> F3, const DevScal *ds, int s, RkCoef rk,
+                            int i1, int j1, int k1) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    int k = blockIdx.z + 2;
+    if (i > i1 || j > j1 || k > k1) return;
+    double dt = ds->dt, f;
+    if (s == 1) f = dt * rk.c[1][1] * (double)F1(i, j, k);
+    else if (s == 2) f = dt * (rk.c[2][1] * (double)F1(i, j, k) + rk.c[2][2] * (double)F2(i, j, k));
+    else f = dt * (rk.c[3][1] * (double)F1(i, j, k) + rk.c[3][2] * (double)F2(i, j, k) + rk.c[3][3] * (double)F3(i, j, k));
+    U(i, j, k) = (T)((double)Uo(i, j, k) + f);
+}
+
+template <typename T>
+int launch_rk_update(cf_ctx *ctx, int s) {
+    RkCoef rk = rk_coefs();
+    for (int comp = 0; comp < 3; comp++) {
+        int i1, j1, k1, n1, n2;
+        if (comp == 0) { i1 = ctx->nx - 1; j1 = ctx->nyg - 1; k1 = ctx->nzg - 1; n1 = ctx->nx; n2 = ctx->nyg; }
+        else if (comp == 1) { i1 = ctx->nxg - 1; j1 = ctx->ny - 1; k1 = ctx->nzg - 1; n1 = ctx->nxg; n2 = ctx->ny; }
+        else { i1 = ctx->nxg - 1; j1 = ctx->nyg - 1; k1 = ctx->nz - 1; n1 = ctx->nxg; n2 = ctx->nyg; }
+        void **cur = comp == 0 ? ctx->U : comp == 1 ? ctx->V : ctx->W;
+        Fld<T> U = make_fld<T>(cur[ctx->cur], n1, n2), Uo = make_fld<T>(cur[ctx->old], n1, n2);
+        Fld<T> F1 = make_fld<T>(ctx->F[0][comp], n1, n2), F2 = make_fld<T>(ctx->F[1][comp], n1, n2),
+               F3 = make_fld<T>(ctx->F[2][comp], n1, n2);
+        dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
+        k_rk_update<T><<<grd, blk, 0, ctx->st>>>(U, Uo, F1, F2, F3, ctx->ds, s, rk, i1, j1, k1);
+        count_launch(ctx);
+    }
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+__global__ void k_copy(const T *a, T *b, long n) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) b[t] = a[t];
+}
+
+template <typename T>
+int launch_copy_state(cf_ctx *ctx, int src, int dst) {
+    size_t n[3] = {ctx->nU, ctx->nV, ctx->nW};
+    void **f[3] = {ctx->U, ctx->V, ctx->W};
+    void **lo[3] = {ctx->Ulo, ctx->Vlo, ctx->Wlo};
+    for (int c = 0; c < 3; c++) {
+        CF_CUDA(cudaMemcpyAsync(f[c][dst], f[c][src], n[c] * sizeof(T), cudaMemcpyDeviceToDevice, ctx->st));
+        if (lo[c][src] && lo[c][dst])
+            CF_CUDA(cudaMemcpyAsync(lo[c][dst], lo[c][src], n[c] * sizeof(T), cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Mass flow, mass_flow.f90.  Block partial sums + a fixed-order final sum so
+// the result does not depend on scheduling.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffff, v, o);
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) sh[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) r += sh[q];
+    __syncthreads();
+    return r;
+}
+
+// mode 1: trapezoid of U (mass_flow.f90:116-123), one block per k plane
+template <typename T>
+__global__ void k_mass_partial(Fld<T> U, const double *yg, int nx, int nyg, double *part) {
+    __shared__ double sh[32];
+    int k = blockIdx.x + 2;
+    double s = 0.0;
+    int ni = nx - 2, nj = nyg - 3;
+    for (int t = threadIdx.x; t < ni * nj; t += blockDim.x) {
+        int i = t % ni + 2, j = t / ni + 3;
+        s += ((double)U(i, j, k) + (double)U(i, j - 1, k)) * 0.5 * (yg[j] - yg[j - 1]);
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// mode 2: centre-line sum (mass_flow.f90:203-204), planes k = 1..nzg-2
+template <typename T>
+__global__ void k_ucl_partial(Fld<T> U, int nx, int jc, double *part) {
+    __shared__ double sh[32];
+    int k = blockIdx.x + 1;
+    double s = 0.0;
+    for (int i = threadIdx.x + 1; i <= nx - 2; i += blockDim.x) s += (double)U(i, jc, k);
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// mode 3: trapezoid of V (mass_flow.f90:160-167)
+template <typename T>
+__global__ void k_massv_partial(Fld<T> V, const double *y, int nxg, int ny, double *part) {
+    __shared__ double sh[32];
+    int k = blockIdx.x + 2;
+    double s = 0.0;
+    int ni = nxg - 2, nj = ny - 1;
+    for (int t = threadIdx.x; t < ni * nj; t += blockDim.x) {
+        int i = t % ni + 2, j = t / ni + 2;
+        s += ((double)V(i, j, k) + (double)V(i, j - 1, k)) * 0.5 * (y[j] - y[j - 1]);
+    }
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// final: the correction into ds (mass_flow.f90:130, 174, 209)
+__global__ void k_mass_final(const double *part, int n, DevScal *ds, int mode, double norm) {
+    if (threadIdx.x != 0) return;
+    double s = 0.0;
+    for (int q = 0; q < n; q++) s += part[q];
+    ds->mass_sum = s;
+    double corr;
+    if (mode == 1) corr = ds->Qflow_x_0 - s / norm;
+    else if (mode == 2) corr = ds->Ucenterline_x - s / norm;
+    else corr = ds->Qflow_y_0 - s / norm;
+    ds->lmax[2] = corr;  // scratch slot: correction before division by dt
+}
+
+// add the correction to the interior and store dPdx = corr/dt
+// (time_integration.f90:154-156, 159-161, 167-169)
+template <typename T>
+__global__ void k_mass_apply(Fld<T> F, Fld<T> Flo, DevScal *ds, int i1, int j1, int k1, int mode) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    int k = blockIdx.z + 2;
+    double corr = ds->lmax[2];
+    if (i == 2 && j == 2 && k == 2) {
+        if (mode == 3) ds->dPdy = corr / ds->dt;
+        else ds->dPdx = corr / ds->dt;
+    }
+    if (i > i1 || j > j1 || k > k1) return;
+    if (Flo.p) {
+        double v = (double)F(i, j, k) + (double)Flo(i, j, k) + corr;
+        T hi = (T)v;
+        F(i, j, k) = hi;
+        Flo(i, j, k) = (T)(v - (double)hi);
+    } else {
+        F(i, j, k) = (T)((double)F(i, j, k) + corr);
+    }
+}
+
+template <typename T>
+static int mass_partial(cf_ctx *ctx, int b, int mode) {
+    double *part = ctx->d_red;
+    int nb = ctx->nzg - 2;
+    double norm;
+    if (mode == 1) {
+        k_mass_partial<T><<<nb, 256, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), ctx->geo.yg, ctx->nx,
+                                                    ctx->nyg, part);
+        norm = ctx->mass_norm;
+    } else if (mode == 2) {
+        int jc = ctx->ny / 2 + 1;
+        k_ucl_partial<T><<<nb, 256, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), ctx->nx, jc, part);
+        norm = (double)(ctx->nx - 2) * (double)(ctx->nzg - 2);
+    } else {
+        k_massv_partial<T><<<nb, 256, 0, ctx->st>>>(make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny), ctx->geo.y, ctx->nxg,
+                                                     ctx->ny, part);
+        norm = ctx->mass_norm_vv;
+    }
+    count_launch(ctx);
+    k_mass_final<<<1, 32, 0, ctx->st>>>(part, nb, ctx->ds, mode, norm);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+int launch_mass_value(cf_ctx *ctx, int b, int mode) {
+    return mass_partial<T>(ctx, b, mode);
+}
+
+template <typename T>
+int launch_mass_flow(cf_ctx *ctx, int b, int mode) {
+    int rc = mass_partial<T>(ctx, b, mode);
+    if (rc) return rc;
+    return launch_mass_apply<T>(ctx, b, mode);
+}
+
+template <typename T>
+int launch_mass_apply(cf_ctx *ctx, int b, int mode) {
+    if (mode == 3) {
+        int i1 = ctx->nxg - 1, j1 = ctx->ny - 1, k1 = ctx->nzg - 1;
+        dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
+        k_mass_apply<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
+                                                  make_fld<T>(ctx->Vlo[b], ctx->nxg, ctx->ny), ctx->ds, i1, j1, k1, mode);
+    } else {
+        int i1 = ctx->nx - 1, j1 = ctx->nyg - 1, k1 = ctx->nzg - 1;
+        dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
+        k_mass_apply<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg),
+                                                  make_fld<T>(ctx->Ulo[b], ctx->nx, ctx->nyg), ctx->ds, i1, j1, k1, mode);
+    }
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// compute_dt, time_integration.f90:179-227.  max over (i,j,k) of dx_i/|U| is
+// dx_i / min_{j,k}|U| exactly (division by a positive number is monotone), so
+// the kernel reduces min|U| per x index, min|V| per y index, min|W| per z
+// index and a second kernel forms the maxima.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void atomic_min_pos(double *a, double v) {
+    // non-negative doubles order like their bit patterns
+    atomicMin((unsigned long long *)a, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__global__ void k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, double *mu, double *mv, double *mw) {
+    int k = blockIdx.x + 2;
+    double wmin = INFINITY;
+    for (int j = 2; j <= nyg - 1; j++) {
+        double vmin = INFINITY;
+        for (int i = threadIdx.x + 2; i <= nxg - 1; i += blockDim.x) {
+            double u = fabs((double)U(i, j, k)), v = fabs((double)V(i, j, k)), w = fabs((double)W(i, j, k));
+            atomic_min_pos(&mu[i], u);
+            vmin = fmin(vmin, v);
+            wmin = fmin(wmin, w);
+        }
+        for (int o = 16; o > 0; o >>= 1) vmin = fmin(vmin, __shfl_down_sync(0xffffffff, vmin, o));
+        if ((threadIdx.x & 31) == 0) atomic_min_pos(&mv[j], vmin);
+    }
+    for (int o = 16; o > 0; o >>= 1) wmin = fmin(wmin, __shfl_down_sync(0xffffffff, wmin, o));
+    if ((threadIdx.x & 31) == 0) atomic_min_pos(&mw[k], wmin);
+}
+
+__global__ void k_dt_init(double *m, int n) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) m[t] = INFINITY;
+}
+
+__global__ void k_dt_final(const double *mu, const double *mv, const double *mw, Geo g, DevScal *ds, double CFL,
+                           double dt_vis) {
+    if (threadIdx.x != 0) return;
+    double lU = 0.0, lV = 0.0, lW = 0.0;
+    for (int i = 2; i <= g.nxg - 1; i++) lU = fmax(lU, (g.xg[i + 1] - g.xg[i]) / mu[i]);
+    for (int j = 2; j <= g.nyg - 1; j++) lV = fmax(lV, (g.yg[j + 1] - g.yg[j]) / mv[j]);
+    for (int k = 2; k <= g.nzg - 1; k++) lW = fmax(lW, (g.zg[k + 1] - g.zg[k]) / mw[k]);
+    double du = CFL * lU, dv = CFL * lV, dw = CFL * lW;
+    double dt_conv = fmin(du, fmin(dv, dw));
+    double dt = fmin(dt_conv, dt_vis);
+    dt = fmin(dt, 5e-3);
+    if (CFL < 0) dt = -CFL;
+    if (ds->fixed_dt > 0) dt = ds->fixed_dt;
+    ds->dt = dt;
+    ds->lmax[0] = lU;
+    ds->lmax[1] = lV;
+}
+
+template <typename T>
+int launch_dt(cf_ctx *ctx, int b) {
+    double *mu = ctx->d_red, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
+    int n = ctx->nxg + ctx->nyg + ctx->nzg + 6;
+    k_dt_init<<<cdiv(n, 256), 256, 0, ctx->st>>>(mu, n);
+    count_launch(ctx);
+    k_dt_min<T><<<ctx->nzg - 2, 128, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg),
+                                                   make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
+                                                   make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->nxg, ctx->nyg,
+                                                   ctx->nzg, mu, mv, mw);
+    count_launch(ctx);
+    double CFL = ctx->prm.CFL;
+    double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
+           vw = CFL * pow(ctx->dzmin, 2.0) / ctx->prm.nu;
+    double dt_vis = fmin(vu, fmin(vv, vw));
+    k_dt_final<<<1, 32, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// check_divergence, projection.f90:234-256 (signed max from 0, and max |div|)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void atomic_max_pos(double *a, double v) {
+    atomicMax((unsigned long long *)a, (unsigned long long)__double_as_longlong(v));
+}
+
+template <typename T>
+__global__ void k_div(Fld<T> U, Fld<T> V, Fld<T> W, Geo g, double *out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    int k = blockIdx.z + 2;
+    double d = 0.0, a = 0.0;
+    if (i <= g.nxg - 1 && j <= g.nyg - 1) {
+        d = ((double)U(i, j, k) - (double)U(i - 1, j, k)) / (g.x[i] - g.x[i - 1]) +
+            ((double)V(i, j, k) - (double)V(i, j - 1, k)) / (g.y[j] - g.y[j - 1]) +
+            ((double)W(i, j, k) - (double)W(i, j, k - 1)) / (g.z[k] - g.z[k - 1]);
+        a = fabs(d);
+        d = fmax(d, 0.0);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        d = fmax(d, __shfl_down_sync(0xffffffff, d, o));
+        a = fmax(a, __shfl_down_sync(0xffffffff, a, o));
+    }
+    if (((threadIdx.x + threadIdx.y * blockDim.x) & 31) == 0) {
+        atomic_max_pos(&out[0], d);
+        atomic_max_pos(&out[1], a);
+    }
+}
+
+template <typename T>
+int launch_div_check(cf_ctx *ctx, int b, double *d_out) {
+    CF_CUDA(cudaMemsetAsync(d_out, 0, 2 * sizeof(double), ctx->st));
+    dim3 blk(32, 4, 1), grd(cdiv(ctx->nxg - 2, 32), cdiv(ctx->nyg - 2, 4), ctx->nzg - 2);
+    k_div<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
+                                       make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->geo, d_out);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+#define INST(T)                                                      \
+    template int launch_bc<T>(cf_ctx *, int);                        \
+    template int launch_rhs<T>(cf_ctx *, int, int);                  \
+    template int launch_rhs_update<T>(cf_ctx *, int, int, int);      \
+    template int launch_rk_update<T>(cf_ctx *, int);                 \
+    template int launch_copy_state<T>(cf_ctx *, int, int);           \
+    template int launch_mass_flow<T>(cf_ctx *, int, int);            \
+    template int launch_mass_value<T>(cf_ctx *, int, int);           \
+    template int launch_mass_apply<T>(cf_ctx *, int, int);           \
+    template int launch_dt<T>(cf_ctx *, int);                        \
+    template int launch_div_check<T>(cf_ctx *, int, double *);
+INST(double)
+INST(float)

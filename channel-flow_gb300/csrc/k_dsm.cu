@@ -1,0 +1,296 @@
+// k_dsm.cu -- dynamic Smagorinsky eddy viscosity, subgrid.f90:376-538.
+//
+// Quantities the reference keeps only as periodic copies are computed at the
+// canonical cells (i = 2..nx-1, j = 2..nyg-1, k = 2..nz-1) and read through
+// the periodic wrap; U, V, W are always read at their actual indices, because
+// with the equilibrium wall model their wall ghost rows are not periodic at
+// the duplicate planes.  Plane sums (subgrid.f90:497-513) run over
+// i = 2..nxg-1, k = 2..nzg-1 like the reference, i.e. the duplicate column
+// i = nxg-1 and row k = nzg-1 (copies of i = 2, k = 2) are counted twice;
+// here that is a weight 2 on the canonical column/row 2.
+#include "cf_internal.cuh"
+
+enum { Q_UC = 0, Q_VC, Q_WC, Q_UU, Q_VV, Q_WW, Q_UV, Q_UW, Q_VW, Q_SS1, Q_SS2, Q_SS3, Q_SS4, Q_SS5, Q_SS6, Q_S, NQ };
+enum { L_1 = 0, L_6 = 5, FSS_1 = 6, NLF = 12 };
+
+struct Can {
+    int nxp, nym, nzp;
+    long n;
+    __device__ __forceinline__ long operator()(int i, int j, int k) const {
+        return (long)(i - 2) + (long)nxp * ((j - 2) + (long)nym * (k - 2));
+    }
+};
+
+// compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual indices.
+template <typename T>
+__device__ __forceinline__ void sij_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W, int i,
+                                          int j, int k, T s[6], T &S) {
+    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg;
+    const T h = T(0.5), q = T(0.25);
+    s[0] = (U(i, j, k) - U(i - 1, j, k)) / (x[i] - x[i - 1]);
+    s[1] = (V(i, j, k) - V(i, j - 1, k)) / (y[j] - y[j - 1]);
+    s[2] = (W(i, j, k) - W(i, j, k - 1)) / (z[k] - z[k - 1]);
+    T e4[2][2], e5[2][2], e6[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            int ii = i + a, jj = j + b, kk = k + b;
+            // edge values at (ii, jj, k), (ii, j, kk), (i, j+a, k+b)
+            e4[a][b] = h * ((U(ii - 1, jj, k) - U(ii - 1, jj - 1, k)) / (yg[jj] - yg[jj - 1]) +
+                            (V(ii, jj - 1, k) - V(ii - 1, jj - 1, k)) / (xg[ii] - xg[ii - 1]));
+            e5[a][b] = h * ((U(ii - 1, j, kk) - U(ii - 1, j, kk - 1)) / (zg[kk] - zg[kk - 1]) +
+                            (W(ii, j, kk - 1) - W(ii - 1, j, kk - 1)) / (xg[ii] - xg[ii - 1]));
+            int j6 = j + a, k6 = k + b;
+            e6[a][b] = h * ((V(i, j6 - 1, k6) - V(i, j6 - 1, k6 - 1)) / (zg[k6] - zg[k6 - 1]) +
+                            (W(i, j6, k6 - 1) - W(i, j6 - 1, k6 - 1)) / (yg[j6] - yg[j6 - 1]));
+        }
+    s[3] = q * (e4[0][0] + e4[1][0] + e4[0][1] + e4[1][1]);
+    s[4] = q * (e5[0][0] + e5[1][0] + e5[0][1] + e5[1][1]);
+    s[5] = q * (e6[0][0] + e6[1][0] + e6[0][1] + e6[1][1]);
+    T a2 = T(0);
+#pragma unroll
+    for (int c = 0; c < 6; c++) a2 += (c < 3 ? T(2) : T(4)) * s[c] * s[c];
+    S = sqrt(a2);
+}
+
+// Stage A: centre velocities, products and |S| S_ij at canonical centres.
+template <typename T>
+__global__ void k_dsm_a(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, T *q, Can c) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    int k = blockIdx.z + 2;
+    if (i > g.nx - 1 || j > g.nyg - 1) return;
+    long o = c(i, j, k), n = c.n;
+    const T h = T(0.5);
+    // subgrid.f90:392-394
+    T uc = h * (U(i - 1, j, k) + U(i, j, k));
+    T vc = h * (V(i, j - 1, k) + V(i, j, k));
+    T wc = h * (W(i, j, k - 1) + W(i, j, k));
+    q[o + Q_UC * n] = uc;
+    q[o + Q_VC * n] = vc;
+    q[o + Q_WC * n] = wc;
+    q[o + Q_UU * n] = uc * uc;
+    q[o + Q_VV * n] = vc * vc;
+    q[o + Q_WW * n] = wc * wc;
+    q[o + Q_UV * n] = uc * vc;
+    q[o + Q_UW * n] = uc * wc;
+    q[o + Q_VW * n] = vc * wc;
+    T s[6], S;
+    sij_point<T>(g, U, V, W, i, j, k, s, S);
+#pragma unroll
+    for (int a = 0; a < 6; a++) q[o + (Q_SS1 + a) * n] = S * s[a];
+    q[o + Q_S * n] = S;
+}
+
+// filter_xzy (subgrid.f90:140-187) of a canonical array at a canonical centre;
+// the y direction is restricted to rows 2..nyg-1 (one-sided at both ends).
+template <typename T>
+__device__ __forceinline__ T filt_can(const T *q, const Can &c, int nyg, int i, int j, int k) {
+    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
+    T wm, w0, wp;
+    if (j == 2) { wm = T(0); w0 = f23; wp = f13; }
+    else if (j == nyg - 1) { wm = f13; w0 = f23; wp = T(0); }
+    else { wm = f6; w0 = f23; wp = f6; }
+    int jm = j > 2 ? j - 1 : j, jp = j < nyg - 1 ? j + 1 : j;
+    const T fw[3] = {f6, f23, f6};
+    T acc = T(0);
+#pragma unroll
+    for (int a = -1; a <= 1; a++) {
+        int ii = wrapc(i + a, c.nxp);
+        T sz = T(0);
+#pragma unroll
+        for (int b = -1; b <= 1; b++) {
+            int kk = wrapc(k + b, c.nzp);
+            T yv = wm * q[c(ii, jm, kk)] + w0 * q[c(ii, j, kk)] + wp * q[c(ii, jp, kk)];
+            sz += fw[b + 1] * yv;
+        }
+        acc += fw[a + 1] * sz;
+    }
+    return acc;
+}
+
+// Stage B: L_ij = hat(ui uj) - hat(ui) hat(uj) and hat(|S| S_ij).
+template <typename T>
+__global__ void k_dsm_b(const T *q, T *lf, Can c, int nx, int nyg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    int k = blockIdx.z + 2;
+    if (i > nx - 1 || j > nyg - 1) return;
+    long o = c(i, j, k), n = c.n;
+    T fu = filt_can<T>(q + Q_UC * n, c, nyg, i, j, k);
+    T fv = filt_can<T>(q + Q_VC * n, c, nyg, i, j, k);
+    T fw = filt_can<T>(q + Q_WC * n, c, nyg, i, j, k);
+    const T fa[6] = {fu, fv, fw, fu, fu, fv}, fb[6] = {fu, fv, fw, fv, fw, fw};
+#pragma unroll
+    for (int a = 0; a < 6; a++) lf[o + (L_1 + a) * n] = filt_can<T>(q + (Q_UU + a) * n, c, nyg, i, j, k) - fa[a] * fb[a];
+#pragma unroll
+    for (int a = 0; a < 6; a++) lf[o + (FSS_1 + a) * n] = filt_can<T>(q + (Q_SS1 + a) * n, c, nyg, i, j, k);
+}
+
+// Stage C: filtered velocities Uf, Vf, Wf (subgrid.f90:431-445) at every
+// element of their arrays; ghost and duplicate elements take the value of the
+// canonical element (the periodic fills of subgrid.f90:448-458).
+// xc/zc: 1 if the field sits at x/z centres; y one-sided at rows 1 and n2.
+template <typename T>
+__global__ void k_dsm_c(Fld<T> A, Fld<T> Af, int n1, int n2, int n3, int nxp, int nzp) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int k = blockIdx.z + 1;
+    if (i > n1 || j > n2) return;
+    int is = wrapc(i, nxp), ks = wrapc(k, nzp);
+    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
+    T wm, w0, wp;
+    if (j == 1) { wm = T(0); w0 = f23; wp = f13; }
+    else if (j == n2) { wm = f13; w0 = f23; wp = T(0); }
+    else { wm = f6; w0 = f23; wp = f6; }
+    int jm = j > 1 ? j - 1 : j, jp = j < n2 ? j + 1 : j;
+    const T fw[3] = {f6, f23, f6};
+    T acc = T(0);
+#pragma unroll
+    for (int a = -1; a <= 1; a++) {
+        T sz = T(0);
+#pragma unroll
+        for (int b = -1; b <= 1; b++) {
+            int ii = is + a, kk = ks + b;
+            T yv = wm * A(ii, jm, kk) + w0 * A(ii, j, kk) + wp * A(ii, jp, kk);
+            sz += fw[b + 1] * yv;
+        }
+        acc += fw[a + 1] * sz;
+    }
+    Af(i, j, k) = acc;
+}
+
+// Stage D: M_ij, L.M and M.M with the plane partial sums.
+// Grid: x = chunks of the (i,k) plane, y = j.
+template <typename T>
+__global__ void k_dsm_d(GeoT<T> g, Fld<T> Uf, Fld<T> Vf, Fld<T> Wf, const T *lf, Can c, double *part, int nchunk) {
+    __shared__ double shl[32], shm[32];
+    int j = blockIdx.y + 2;
+    long nik = (long)c.nxp * c.nzp;
+    double sl = 0.0, sm = 0.0;
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nik; t += (long)gridDim.x * blockDim.x) {
+        int i = (int)(t % c.nxp) + 2, k = (int)(t / c.nxp) + 2;
+        long o = c(i, j, k), n = c.n;
+        T s[6], S;
+        sij_point<T>(g, Uf, Vf, Wf, i, j, k, s, S);
+        const T fs2 = T(4);  // fil_size**2, fil_size = 2 (subgrid.f90:156)
+        T M[6], L[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+            M[a] = fs2 * S * s[a] - lf[o + (FSS_1 + a) * n];
+            L[a] = lf[o + (L_1 + a) * n];
+        }
+        T lm = (L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + T(2) * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]));
+        T mm = (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + T(2) * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]));
+        double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
+        sl += wgt * (double)lm;
+        sm += wgt * (double)mm;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sl += __shfl_down_sync(0xffffffff, sl, o);
+        sm += __shfl_down_sync(0xffffffff, sm, o);
+    }
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { shl[w] = sl; shm[w] = sm; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) { a += shl[q]; b += shm[q]; }
+        part[((long)(j - 2) * nchunk + blockIdx.x) * 2] = a;
+        part[((long)(j - 2) * nchunk + blockIdx.x) * 2 + 1] = b;
+    }
+}
+
+// Stage E: avg_nu_t(j) = <LM>/<MM> (subgrid.f90:516-518) and its ghosts.
+__global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, int dirichlet) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    if (j <= nyg - 1) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < nchunk; q++) {
+            a += part[((long)(j - 2) * nchunk + q) * 2];
+            b += part[((long)(j - 2) * nchunk + q) * 2 + 1];
+        }
+        avg[j] = a / b;
+    }
+}
+__global__ void k_dsm_e2(int nyg, double *avg, int dirichlet) {
+    if (threadIdx.x == 0) {
+        avg[1] = dirichlet ? -avg[2] : avg[2];
+        avg[nyg] = dirichlet ? -avg[nyg - 1] : avg[nyg - 1];
+    }
+}
+
+// Stage F: nu_t = max(-0.5 C(j) |S|, 0) everywhere, periodic copies and the
+// wall ghost rule (subgrid.f90:521-536).
+template <typename T>
+__global__ void k_dsm_f(Fld<T> nt, const T *Sq, const double *avg, Can c, int nxg, int nyg, int nzg, int dirichlet) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    int k = blockIdx.z + 1;
+    if (i > nxg || j > nyg) return;
+    int jj = j == 1 ? 2 : (j == nyg ? nyg - 1 : j);
+    int is = wrapc(i, c.nxp), ks = wrapc(k, c.nzp);
+    T v = T(-0.5) * (T)avg[jj] * Sq[c(is, jj, ks)];
+    v = v > T(0) ? v : T(0);
+    if (jj != j && dirichlet) v = -v;
+    nt(i, j, k) = v;
+}
+
+template <typename T>
+__global__ void k_fill(T *p, long n, T v) {
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) p[t] = v;
+}
+
+template <typename T>
+int launch_nut_zero(cf_ctx *ctx) {
+    k_fill<T><<<cdiv(ctx->nC, 256), 256, 0, ctx->st>>>((T *)ctx->nut, (long)ctx->nC, T(0));
+    count_launch(ctx);
+    k_fill<double><<<1, 256, 0, ctx->st>>>(ctx->avg_nu_t, ctx->nyg + 1, 0.0);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+int launch_dsm(cf_ctx *ctx, int b) {
+    GeoT<T> g = geo_of<T>(ctx);
+    Can c;
+    c.nxp = ctx->nxp; c.nym = ctx->nym; c.nzp = ctx->nzp; c.n = (long)ctx->nCan;
+    Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    T *q = (T *)ctx->dsm_q, *lf = (T *)ctx->dsm_lf;
+    dim3 blk(32, 4, 1);
+    dim3 grdc(cdiv(ctx->nxp, 32), cdiv(ctx->nym, 4), ctx->nzp);
+    k_dsm_a<T><<<grdc, blk, 0, ctx->st>>>(g, U, V, W, q, c);
+    count_launch(ctx);
+    k_dsm_b<T><<<grdc, blk, 0, ctx->st>>>(q, lf, c, ctx->nx, ctx->nyg);
+    count_launch(ctx);
+    Fld<T> Uf = make_fld<T>(ctx->Uf, ctx->nx, ctx->nyg);
+    Fld<T> Vf = make_fld<T>(ctx->Vf, ctx->nxg, ctx->ny);
+    Fld<T> Wf = make_fld<T>(ctx->Wf, ctx->nxg, ctx->nyg);
+    k_dsm_c<T><<<dim3(cdiv(ctx->nx, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(U, Uf, ctx->nx, ctx->nyg, ctx->nzg, ctx->nxp, ctx->nzp);
+    k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->ny, 4), ctx->nzg), blk, 0, ctx->st>>>(V, Vf, ctx->nxg, ctx->ny, ctx->nzg, ctx->nxp, ctx->nzp);
+    k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nz), blk, 0, ctx->st>>>(W, Wf, ctx->nxg, ctx->nyg, ctx->nz, ctx->nxp, ctx->nzp);
+    count_launch(ctx); count_launch(ctx); count_launch(ctx);
+    int nchunk = ctx->dsm_nblk;
+    k_dsm_d<T><<<dim3(nchunk, ctx->nym), 256, 0, ctx->st>>>(g, Uf, Vf, Wf, lf, c, ctx->dsm_part, nchunk);
+    count_launch(ctx);
+    int dir = ctx->prm.Dirichlet_nu_t == 1;
+    k_dsm_e<<<cdiv(ctx->nym, 64), 64, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
+    k_dsm_e2<<<1, 32, 0, ctx->st>>>(ctx->nyg, ctx->avg_nu_t, dir);
+    count_launch(ctx); count_launch(ctx);
+    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+    k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(nt, q + Q_S * c.n, ctx->avg_nu_t, c,
+                                                                                            ctx->nxg, ctx->nyg, ctx->nzg, dir);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template int launch_dsm<double>(cf_ctx *, int);
+template int launch_dsm<float>(cf_ctx *, int);
+template int launch_nut_zero<double>(cf_ctx *);
+template int launch_nut_zero<float>(cf_ctx *);

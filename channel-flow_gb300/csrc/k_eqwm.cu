@@ -1,0 +1,173 @@
+// k_eqwm.cu -- equilibrium wall model (Larsson), wallmodel.f90:591-685 and
+// eqwm.f90:20-223, FP64.
+//
+// W at the matching row is moved to the U location with the 3-point Lagrange
+// interpolations of interpolation.f90:114-252; their stencil choice depends
+// only on indices, so the host precomputes (jj, w0, w1, w2) per output index
+// with the reference's formulas.  One thread solves the ODE of one wall
+// point: Picard iteration on tau_w (<= 101 passes, tol 1e-7), each pass a
+// tridiagonal solve over the ncv cells.  The solve eliminates from the top
+// (the Dirichlet row, x_ncv = |u|) down to the wall row, so x_1 -- the only
+// unknown the stress needs (eqwm.f90:198) -- comes out of one register
+// recurrence without storing the Thomas coefficients of eqwm.f90:52-88.
+#include "cf_internal.cuh"
+
+// temp_1 = interpolate_z_2nd of W(:, jw, :) at both walls: (nxg, 2, nzg)
+template <typename T>
+__global__ void k_eq_zinterp_t(Fld<T> W, int jref, int nxg, int nyg, int nzg, const int *zst, const double *zw,
+                               double *t1) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int k = blockIdx.y + 1;
+    int w = blockIdx.z;
+    if (i > nxg) return;
+    int jw = w == 0 ? jref : nyg - jref + 1;
+    int jj = zst[k];
+    const double *c = zw + 3 * k;
+    t1[(i - 1) + (long)nxg * (w + 2L * (k - 1))] =
+        c[0] * (double)W(i, jw, jj - 1) + c[1] * (double)W(i, jw, jj) + c[2] * (double)W(i, jw, jj + 1);
+}
+
+struct EqParams {
+    int ncv, jref, nx, nxg, nyg, nzg;
+    double nu, h_wm, tau_mean;
+};
+
+// solve_u_eqwm (eqwm.f90:90-223) inline, grid in shared memory:
+// yfa[1..ncv+1], idcv[i] = 1/(y_cv(i+1)-y_cv(i)) (i = 1..ncv-1),
+// rw = 1/(y_cv(1)-y_fa(1)); grid[1..ncv] = y_cv, grid[ncv+1..2ncv+1] = y_fa.
+__global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32, int sy, int sz, const double *t1,
+                           const int *xst, const double *xw, const double *grid, EqParams ep, const double *nut,
+                           int nut_f32, double *tau0, double *alpha_x, double *alpha_zt, int *counters) {
+    extern __shared__ double sg[];
+    const int ncv = ep.ncv;
+    // grid: yfa[1..ncv+1], idcv[1..ncv-1], rw
+    double *yfa = sg, *idcv = sg + ncv + 2;
+    for (int q = threadIdx.x; q < ncv + 2; q += blockDim.x) yfa[q] = q >= 1 && q <= ncv + 1 ? grid[ncv + q] : 0.0;
+    for (int q = threadIdx.x; q < ncv + 1; q += blockDim.x)
+        idcv[q] = (q >= 1 && q <= ncv - 1) ? 1.0 / (grid[q + 1] - grid[q]) : 0.0;
+    __syncthreads();
+    const double rw = 1.0 / (grid[1] - grid[ncv + 1]);
+    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    long npts = (long)ep.nx * ep.nzg * 2;
+    if (t >= npts) return;
+    int i = (int)(t % ep.nx) + 1;
+    long r = t / ep.nx;
+    int w = (int)(r % 2);
+    int k = (int)(r / 2) + 1;
+    const int nxg = ep.nxg, nyg = ep.nyg;
+    int jj = w == 0 ? ep.jref : nyg - ep.jref + 1;
+    // W at the U location (interpolate_x_2nd of temp_1)
+    int xj = xst[i];
+    const double *c = xw + 3 * i;
+    const double *row = t1 + (long)nxg * (w + 2L * (k - 1)) - 1;
+    double wv = c[0] * row[xj - 1] + c[1] * row[xj] + c[2] * row[xj + 1];
+    long uoff = (long)(i - 1) + (long)sy * (jj - 1) + (long)sz * (k - 1);
+    double Uv = use_f32 ? (double)Uf32[uoff] : Ud.p[uoff];
+    double u_les = sqrt(Uv * Uv + wv * wv);
+    // solve_u_eqwm(u_les, nu, 1.0, yg(jref), ncv, stretch, tau, iter, tau_in)
+    const double kappa = 0.41, Aplus = 17.0, tol = 0.0000001, mu_lam = ep.nu, rho = 1.0;
+    const int max_iter = 100;
+    double tau_lam = mu_lam * u_les / ep.h_wm;
+    long toff = (long)(i - 1) + (long)ep.nx * (w + 2L * (k - 1));
+    double tau = tau0[toff];
+    int iter = 0;
+    while (true) {
+        double tau_prev = tau;
+        double nu_eq = mu_lam / rho;
+        double utau = sqrt(tau / rho);
+        double c1 = rho * kappa * utau;
+        double al = u_les, be = 0.0;
+        double yf = yfa[ncv];
+        double D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
+        double mu_up = mu_lam + c1 * yf * (D * D);
+        for (int q = ncv - 1; q >= 2; q--) {
+            yf = yfa[q];
+            D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
+            double mu_q = mu_lam + c1 * yf * (D * D);
+            double sup = mu_up * idcv[q];
+            double sub = mu_q * idcv[q - 1];
+            double m = -1.0 * (sup + sub) + sup * be;
+            double rm = 1.0 / m;
+            al = -sup * al * rm;
+            be = -sub * rm;
+            mu_up = mu_q;
+        }
+        double sup = mu_up * idcv[1];
+        double diag = -1.0 * (sup + mu_lam * rw);
+        double x1 = -sup * al / (diag + sup * be);
+        tau = mu_lam * (x1 - 0.0) * rw;
+        int done = 0;
+        if (fabs((tau - tau_prev) / tau_lam) < tol) done = 1;
+        if (done == 0) iter = iter + 1;
+        if (iter > max_iter) done = 1;
+        if (done) break;
+    }
+    // wallmodel.f90:620-640
+    if (isnan(tau)) {
+        atomicAdd(&counters[0], 1);
+        tau = ep.tau_mean;
+    }
+    if (iter == 100) {
+        tau = ep.tau_mean;
+        atomicAdd(&counters[1], 1);
+    }
+    tau0[toff] = tau;
+    double tx = tau * Uv / u_les, tz = tau * wv / u_les;
+    int ja = w == 0 ? 1 : nyg, jb = w == 0 ? 2 : nyg - 1;
+    long cs = (long)nxg * nyg;
+    auto NT = [&](int ii, int j) -> double {
+        long o = (long)(ii - 1) + (long)nxg * (j - 1) + cs * (k - 1);
+        return nut_f32 ? (double)((const float *)nut)[o] : nut[o];
+    };
+    double nu_t_ik = 0.5 * (0.5 * (NT(i, ja) + NT(i + 1, ja)) + 0.5 * (NT(i, jb) + NT(i + 1, jb)));
+    alpha_x[toff] = tx / (ep.nu + nu_t_ik);
+    alpha_zt[toff] = tz / (ep.nu + nu_t_ik);
+}
+
+// alpha_z: 4-point average of alpha_z_temp and its copies (wallmodel.f90:656-664)
+__global__ void k_eq_alphaz(const double *azt, double *az, int nx, int nxg, int nz, int nzg) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    int k = blockIdx.y + 1;
+    int w = blockIdx.z;
+    if (i > nxg) return;
+    // value of alpha_z(i,w,k) after the three copy statements
+    int ii = i, kk = k;
+    if (kk == nz) kk = 2;
+    if (ii == nxg) ii = 3;
+    else if (ii == nxg - 1) ii = 2;
+    auto T = [&](int a, int c) { return azt[(a - 1) + (long)nx * (w + 2L * (c - 1))]; };
+    double v = 0.25 * (T(ii, kk) + T(ii + 1, kk) + T(ii, kk + 1) + T(ii + 1, kk + 1));
+    az[(i - 1) + (long)nxg * (w + 2L * (k - 1))] = v;
+}
+
+template <typename T>
+int launch_eqwm(cf_ctx *ctx, int b) {
+    int nx = ctx->nx, nxg = ctx->nxg, nyg = ctx->nyg, nz = ctx->nz, nzg = ctx->nzg;
+    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    k_eq_zinterp_t<T><<<dim3(cdiv(nxg, 128), nzg, 2), 128, 0, ctx->st>>>(W, ctx->prm.jref_eqwm, nxg, nyg, nzg,
+                                                                         ctx->eq_zst, ctx->eq_zw, ctx->wtemp1);
+    count_launch(ctx);
+    EqParams ep;
+    ep.ncv = ctx->prm.eqwm_ncv;
+    ep.jref = ctx->prm.jref_eqwm;
+    ep.nx = nx; ep.nxg = nxg; ep.nyg = nyg; ep.nzg = nzg;
+    ep.nu = ctx->prm.nu;
+    ep.h_wm = ctx->hyg[ep.jref];
+    ep.tau_mean = ctx->hs.tau_mean_eqwm;
+    CF_CUDA(cudaMemsetAsync(ctx->d_red, 0, 2 * sizeof(int), ctx->st));
+    long npts = (long)nx * nzg * 2;
+    size_t sh = (size_t)(2 * ep.ncv + 4) * sizeof(double);
+    Fld<double> Ud = make_fld<double>(ctx->U[b], nx, nyg);
+    k_eq_solve<<<cdiv(npts, 128), 128, sh, ctx->st>>>(Ud, (const float *)ctx->U[b], sizeof(T) == 4, nx, nx * nyg,
+                                                     ctx->wtemp1, ctx->eq_xst, ctx->eq_xw, ctx->eq_grid, ep,
+                                                     (const double *)ctx->nut, sizeof(T) == 4, ctx->tau0, ctx->alpha_x,
+                                                     ctx->alpha_zt, (int *)ctx->d_red);
+    count_launch(ctx);
+    k_eq_alphaz<<<dim3(cdiv(nxg, 128), nz, 2), 128, 0, ctx->st>>>(ctx->alpha_zt, ctx->alpha_z, nx, nxg, nz, nzg);
+    count_launch(ctx);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template int launch_eqwm<double>(cf_ctx *, int);
+template int launch_eqwm<float>(cf_ctx *, int);

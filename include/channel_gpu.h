@@ -1,0 +1,163 @@
+/*
+ * channel_gpu.h -- C ABI of the GB300 (sm_103a) RK3-substep library for the
+ * staggered finite-difference channel solver of Adrian-Lozano/channel-flow.
+ *
+ * One context holds one channel, device-resident between calls.  Host arrays
+ * crossing this boundary use the reference's Fortran layout and extents
+ * (column-major, 1-based in the Fortran sense, ghosts and periodic duplicate
+ * planes included):
+ *     U    (nx,  ny+1, nz+1)      V (nx+1, ny, nz+1)      W (nx+1, ny+1, nz)
+ *     P    (nx+1, ny+1, nz+1)     nu_t (nx+1, ny+1, nz+1)
+ * where nx, ny, nz are the face counts of the input_parameters file
+ * (initialization.f90:79-124).  All functions return 0 on success and a
+ * nonzero CF_ERR_* code otherwise; cf_last_error() gives the message.  Calls
+ * on one context must be serialised by the caller; separate contexts are
+ * independent.  The reference has no return codes (it calls Stop); the
+ * checks it makes with Stop are made here and reported as CF_ERR_INVALID.
+ */
+#ifndef CHANNEL_GPU_H
+#define CHANNEL_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cf_ctx cf_ctx;
+
+enum {
+    CF_OK = 0,
+    CF_ERR_INVALID = 1,   /* bad size or parameter (the reference's Stop)      */
+    CF_ERR_CUDA = 2,      /* CUDA runtime error                                */
+    CF_ERR_UNSUPPORTED = 3, /* model the library does not implement           */
+    CF_ERR_IO = 4,        /* file read/write error                             */
+    CF_ERR_NAN = 5        /* NaN found by a check                              */
+};
+
+enum { CF_PREC_FP64 = 0, CF_PREC_SPLIT = 1 };
+
+/* Scalars read by read_input_parameters (input_output.f90:21-133), plus
+ * options of this library that the reference hard-codes. */
+typedef struct {
+    double nu;             /* viscosity                                         */
+    double CFL;            /* CFL number; CFL < 0 means dt = -CFL               */
+    double dPdx, dPdz;     /* imposed pressure gradients                        */
+    double Rossby_plus;    /* Omega_z = Rossby_plus*sqrt(dPdx)/2                */
+    double freq_mult;      /* target centre-line velocity when x_mass_cte == 2  */
+    int Retau_int;         /* mass-flow rescale flag (initialization.f90:433)   */
+    int x_mass_cte;        /* 0 fixed dPdx, 1 constant mass flow, 2 centre-line */
+    int y_mass_cte;        /* 1 constant mass flow in y                         */
+    int LES_model;         /* 0 none, 2 dynamic Smagorinsky                     */
+    int iwall_model;       /* 0 no-slip walls, 3 equilibrium wall model         */
+    int Dirichlet_nu_t;    /* ghost rule for nu_t: 1 Dirichlet, 0 Neumann       */
+    int jref_eqwm;         /* eqwm matching index                               */
+    /* library options (not in input_parameters) */
+    int precision;         /* CF_PREC_FP64 or CF_PREC_SPLIT                     */
+    int eqwm_ncv;          /* eqwm ODE cells (reference: 100, wallmodel.f90:621) */
+    double eqwm_stretch;   /* eqwm ODE stretching (reference: 1.10)             */
+    int sgs_recompute;     /* 1: evaluate the second eddy viscosity of substep 1
+                              (time_integration.f90:103) inside cf_time_step_rk3;
+                              0: reuse the first one (bit-identical inputs)      */
+} cf_params;
+
+/* Fills p with the defaults of the library (reference values where the
+ * reference hard-codes them). */
+void cf_default_params(cf_params *p);
+
+/* ---- lifetime --------------------------------------------------------- */
+/* Replaces initialize (initialization.f90:23-536) for one slab holding the
+ * whole domain.  x, y, z are host face coordinates of lengths nx, ny, nz
+ * (the mesh records of the snapshot file, input_output.f90:244-254). */
+int cf_create(int nx, int ny, int nz, const double *x, const double *y, const double *z,
+              const cf_params *p, int device, cf_ctx **out);
+int cf_destroy(cf_ctx *ctx);
+const char *cf_last_error(const cf_ctx *ctx);
+
+/* ---- state transfer (host <-> device) ---------------------------------- */
+/* Uploads U, V, W (the snapshot body, input_output.f90:276-362) and sets
+ * Uo = U etc. (input_output.f90:380-382). */
+int cf_upload_fields(cf_ctx *ctx, const double *U, const double *V, const double *W);
+/* Any pointer may be NULL.  P is the pressure stored at substep 1 of the last
+ * projection (projection.f90:129-137); nu_t the last eddy viscosity. */
+int cf_download_fields(cf_ctx *ctx, double *U, double *V, double *W, double *P, double *nu_t);
+/* Wall-model arrays: alpha_x (nx,2,nz+1), alpha_z (nx+1,2,nz),
+ * tau_eqwm_initial (nx,2,nz+1).  Any pointer may be NULL. */
+int cf_download_wall(cf_ctx *ctx, double *alpha_x, double *alpha_z, double *tau);
+int cf_upload_wall(cf_ctx *ctx, const double *alpha_x, const double *alpha_z, const double *tau);
+
+/* Module scalars of global.f90 the path reads or writes. */
+int cf_set_scalars(cf_ctx *ctx, double t, double dt, int rk_step, double dPdx, double dPdy);
+int cf_get_scalars(cf_ctx *ctx, double *t, double *dt, int *rk_step, double *dPdx, double *dPdy);
+
+/* initialization.f90:432-463: initial mass flow Qflow_x_0 (with the Retau
+ * rescale of U when Retau_int != 0).  Call after cf_upload_fields. */
+int cf_init_mass_flow(cf_ctx *ctx, double *Qflow_x_0);
+
+/* ---- mirrors of the subroutines time_integration.f90 calls ------------ */
+int cf_compute_dt(cf_ctx *ctx, double *dt);                       /* time_integration.f90:179 */
+int cf_compute_eddy_viscosity(cf_ctx *ctx);                       /* subgrid.f90:23           */
+int cf_compute_wall_model(cf_ctx *ctx);                           /* wallmodel.f90:24         */
+int cf_compute_rhs_u(cf_ctx *ctx, int slot);                      /* equations.f90:24  -> Fu{slot} */
+int cf_compute_rhs_v(cf_ctx *ctx, int slot);                      /* equations.f90:186 -> Fv{slot} */
+int cf_compute_rhs_w(cf_ctx *ctx, int slot);                      /* equations.f90:351 -> Fw{slot} */
+int cf_rk_update(cf_ctx *ctx, int substep);                       /* time_integration.f90:108-146 */
+int cf_apply_boundary_conditions(cf_ctx *ctx);                    /* boundary_conditions.f90:20 */
+int cf_compute_projection_step(cf_ctx *ctx);                      /* projection.f90:20        */
+int cf_compute_dPx_for_constant_mass_flow(cf_ctx *ctx, double *dPdx); /* mass_flow.f90:103  */
+int cf_compute_dPy_for_constant_mass_flow(cf_ctx *ctx, double *dPdy); /* mass_flow.f90:147  */
+int cf_compute_dPx_for_constant_Ucenterline(cf_ctx *ctx, double *dPdx); /* mass_flow.f90:192 */
+int cf_check_divergence(cf_ctx *ctx, double *maxdiv, double *maxabsdiv); /* projection.f90:234 */
+/* U(interior) += value (comp 0) or V(interior) += value (comp 1), then
+ * dPdx (dPdy) = value/dt: the driver lines time_integration.f90:155-156, 168-169. */
+int cf_apply_mass_flow_correction(cf_ctx *ctx, int comp, double value);
+/* Save Uo = U (time_integration.f90:94-97). */
+int cf_save_old_state(cf_ctx *ctx);
+/* Downloads one of the RK right-hand sides Fu/Fv/Fw{slot} with the extents of
+ * the matching velocity field; the interior ranges of initialization.f90:419-429
+ * hold the values, the rest is unspecified. comp: 0 u, 1 v, 2 w. */
+int cf_download_rhs(cf_ctx *ctx, int comp, int slot, double *out);
+/* Downloads avg_nu_t (1, ny+1, 1), the plane coefficient <LM>/<MM>. */
+int cf_download_avg_nu_t(cf_ctx *ctx, double *out);
+/* eqwm counters of the last wall-model call (wallmodel.f90:623-653). */
+int cf_get_eqwm_counters(cf_ctx *ctx, int *n_nan, int *n_iter);
+
+/* ---- fast path ------------------------------------------------------- */
+/* compute_dt followed by compute_time_step_RK3 (time_integration.f90:89-173,
+ * including the mass-flow forcing), nsteps times, fully on the device with
+ * dt and dPdx kept in device memory.  Enqueued on the context's stream; the
+ * call returns without waiting unless sync != 0.  The step sequence is
+ * captured once into a CUDA graph and replayed. */
+int cf_time_step_rk3(cf_ctx *ctx, int nsteps, int sync);
+/* Same sequence with a fixed dt (the reference's CFL < 0 rule). */
+int cf_set_fixed_dt(cf_ctx *ctx, double dt);
+int cf_synchronize(cf_ctx *ctx);
+/* The cudaStream_t the context launches on (for event timing by callers). */
+void *cf_get_stream(cf_ctx *ctx);
+/* Count of kernel launches the last cf_time_step_rk3 step enqueued. */
+int cf_launches_per_step(cf_ctx *ctx);
+
+/* ---- statistics (statistics.f90:22-171) ------------------------------ */
+/* out: 9 profiles of length ny (Umean, Vmean, Wmean, U2mean, V2mean, W2mean,
+ * UVmean, Pmean, P2mean) followed by utau, Retau, Qflow_x, Qflow_y,
+ * dU/dy at the bottom and top walls, and the wall averages of nu_t
+ * (9*ny + 8 values). */
+int cf_compute_statistics(cf_ctx *ctx, double *out);
+
+/* ---- input_parameters file and snapshot format ----------------------- */
+/* Parses the reference's input_parameters text (input_output.f90:29-81).
+ * grid[3] receives nx, ny, nz; files receive filein/fileout (200 chars);
+ * ints[4] nsteps, nsave, nstats, nmonitor; ints2[2] nstep_init, random_init. */
+int cf_read_input_parameters(const char *path, cf_params *p, int grid[3], char filein[200], char fileout[200],
+                             int ints[4], int ints2[2]);
+/* Snapshot in the reference's big-endian stream format
+ * (input_output.f90:231-384 read, 393-544 write): mesh records for x, y, z,
+ * xm, ym, zm, then U, V, W (and, on write, P and nu_t) with int32 shapes.
+ * Read: x,y,z must hold nx,ny,nz doubles; U,V,W reference extents. */
+int cf_read_snapshot(const char *path, int nx, int ny, int nz, double *x, double *y, double *z, double *U,
+                     double *V, double *W);
+int cf_write_snapshot(const char *path, int nx, int ny, int nz, const double *x, const double *y, const double *z,
+                      const double *U, const double *V, const double *W, const double *P, const double *nu_t);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

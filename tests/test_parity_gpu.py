@@ -1,0 +1,197 @@
+"""FP64 parity of the CUDA path (through the C ABI) against the CPU oracle.
+
+Tolerances: per-routine results within 1e-12 (normwise relative), 10 RK3
+steps within 1e-10 with max|div u| <= 1e-10 -- the FP64 gate of the
+reference-port contract.  Bit-exact where the operation is a copy
+(boundary ghosts).
+"""
+import numpy as np
+import pytest
+
+from conftest import assert_close, channel_case, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(case, precision=0, **extra):
+    from oracle import Oracle
+    import channelflow as cf
+    o = Oracle(case["x"], case["y"], case["z"], case["prm"])
+    o.set_fields(case["U"], case["V"], case["W"])
+    kw = dict(case["prm"])
+    kw.update(extra)
+    ch = cf.Channel(case["x"], case["y"], case["z"], precision=precision, **kw)
+    ch.upload(case["U"], case["V"], case["W"])
+    q0 = ch.init_mass_flow()
+    o.init_mass_flow()
+    assert abs(q0 - o.scalar("Qflow_x_0")) <= 1e-14 * abs(q0)
+    return o, ch
+
+
+def compare_fields(o, ch, tol, names=("U", "V", "W"), what=""):
+    g = ch.download()
+    f = o.fields()
+    errs = {}
+    for n in names:
+        errs[n] = assert_close(g[n], f[n], tol, f"{what} {n}")
+    return errs
+
+
+CASES = {
+    "small": (18, 17, 18),
+    "config1": (66, 65, 66),
+}
+
+
+@pytest.mark.parametrize("which", ["small"])
+def test_boundary_conditions_exact(which):
+    case = channel_case(*CASES[which])
+    rng = np.random.default_rng(5)
+    # raw (non-periodic) fields so that every ghost is rewritten
+    for k in ("U", "V", "W"):
+        case[k] = np.asfortranarray(rng.standard_normal(case[k].shape))
+    o, ch = make_pair(case)
+    o.apply_boundary_conditions()
+    ch.apply_boundary_conditions()
+    g, f = ch.download(), o.fields()
+    for n in ("U", "V", "W"):
+        assert np.array_equal(g[n], f[n]), n
+
+
+@pytest.mark.parametrize("which", ["small", "config1"])
+def test_eddy_viscosity_and_rhs(which):
+    case = channel_case(*CASES[which])
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.set_scalar("dt", case["dt"])
+    ch.set_scalars(dt=case["dt"])
+    o.compute_eddy_viscosity()
+    ch.compute_eddy_viscosity()
+    f, g = o.fields(), ch.download()
+    assert_close(g["nu_t"], f["nu_t"], 1e-12, "nu_t")
+    assert_close(ch.avg_nu_t()[1:-1], o.array("avg_nu_t").ravel()[1:-1], 1e-12, "avg_nu_t")
+    for s in (1,):
+        o.compute_rhs_u(s); o.compute_rhs_v(s); o.compute_rhs_w(s)
+        ch.compute_rhs_u(s); ch.compute_rhs_v(s); ch.compute_rhs_w(s)
+        nx, ny, nz = ch.nx, ch.ny, ch.nz
+        gu = ch.download_rhs(0, s)[1:nx - 1, 1:ny, 1:nz]
+        gv = ch.download_rhs(1, s)[1:nx, 1:ny - 1, 1:nz]
+        gw = ch.download_rhs(2, s)[1:nx, 1:ny, 1:nz - 1]
+        assert_close(gu, o.array(f"Fu{s}"), 1e-12, "Fu")
+        assert_close(gv, o.array(f"Fv{s}"), 1e-12, "Fv")
+        assert_close(gw, o.array(f"Fw{s}"), 1e-12, "Fw")
+
+
+@pytest.mark.parametrize("which", ["small", "config1"])
+def test_projection(which):
+    case = channel_case(*CASES[which])
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.set_scalar("dt", case["dt"]); o.set_scalar("rk_step", 1)
+    ch.set_scalars(dt=case["dt"], rk_step=1)
+    o.compute_projection_step(); ch.compute_projection_step()
+    o.apply_boundary_conditions(); ch.apply_boundary_conditions()
+    compare_fields(o, ch, 1e-12, names=("U", "V", "W", "P"), what="projection")
+    d, dabs = ch.check_divergence()
+    assert dabs <= 1e-12, dabs
+    od, odabs = o.check_divergence()
+    assert abs(d - od) <= 1e-12
+
+
+def test_dt_and_mass_flow():
+    case = channel_case(*CASES["small"])
+    case["prm"]["CFL"] = 0.5
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.compute_dt()
+    assert ch.compute_dt() == o.scalar("dt")
+    assert abs(ch.compute_dPx_for_constant_mass_flow() - o.compute_dPx_for_constant_mass_flow()) <= 1e-15
+
+
+@pytest.mark.parametrize("which", ["small"])
+def test_wall_model_eqwm(which):
+    case = channel_case(*CASES[which], stretch=0.0, wall=3, retau=2000.0, profile="plug", jref=3)
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.compute_eddy_viscosity(); ch.compute_eddy_viscosity()
+    o.compute_wall_model(); ch.compute_wall_model()
+    w = ch.download_wall()
+    assert_close(w["alpha_x"], o.array("alpha_x"), 1e-12, "alpha_x")
+    assert_close(w["alpha_z"], o.array("alpha_z"), 1e-12, "alpha_z")
+    assert_close(w["tau_eqwm_initial"], o.array("tau_eqwm_initial"), 1e-12, "tau")
+    assert ch.eqwm_counters() == (int(o.scalar("n_nan_eqwm")), int(o.scalar("n_iter_eqwm")))
+    o.apply_boundary_conditions(); ch.apply_boundary_conditions()
+    compare_fields(o, ch, 1e-12, what="eqwm BC")
+
+
+@pytest.mark.parametrize("which,wall", [("small", 0), ("config1", 0), ("small", 3)])
+def test_ten_steps(which, wall):
+    extra = dict(stretch=0.0, wall=3, retau=2000.0, profile="plug") if wall else {}
+    case = channel_case(*CASES[which], **extra)
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.set_scalar("dt", case["dt"]); o.set_scalar("rk_step", 2)
+    ch.set_scalars(dt=case["dt"], rk_step=2)
+    for a in (o, ch):
+        a.compute_projection_step()
+        a.apply_boundary_conditions()
+    ch.set_fixed_dt(case["dt"])
+    for _ in range(10):
+        o.compute_dt()
+        o.time_step_rk3()
+    ch.time_step_rk3(10)
+    errs = compare_fields(o, ch, 1e-10, names=("U", "V", "W", "P", "nu_t"), what="10 steps")
+    _, dabs = ch.check_divergence()
+    assert dabs <= 1e-10, dabs
+    # dPdx = (Q0 - Q)/dt is a cancellation: compare the correction Q0 - Q
+    # against the mass flow it corrects
+    assert abs(ch.scalars()["dPdx"] - o.scalar("dPdx")) * case["dt"] <= 1e-12 * abs(o.scalar("Qflow_x_0"))
+    print(which, wall, errs)
+
+
+def test_mirror_matches_fast_path():
+    import channelflow as cf
+    case = channel_case(*CASES["small"])
+    chs = []
+    for mode in ("mirror", "fast"):
+        ch = cf.Channel(case["x"], case["y"], case["z"], **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        ch.set_scalars(dt=case["dt"], rk_step=1)
+        ch.set_fixed_dt(case["dt"])
+        if mode == "mirror":
+            for _ in range(2):
+                ch.compute_dt()
+                ch.compute_time_step_rk3_mirror()
+        else:
+            ch.time_step_rk3(2)
+        chs.append(ch.download())
+    for n in ("U", "V", "W", "nu_t"):
+        assert_close(chs[0][n], chs[1][n], 1e-13, n)
+    # P = phi/(dt*8/15) carries the cancellation of div(u*) = O(dt)
+    assert_close(chs[0]["P"], chs[1]["P"], 1e-11, "P")
+
+
+def test_split_precision_short_horizon():
+    """FP32 state/stencils/SGS with the compensated update stays within 1e-4
+    of the FP64 path over 20 steps (pointwise, normwise relative)."""
+    import channelflow as cf
+    case = channel_case(*CASES["config1"])
+    out = []
+    for prec in (0, 1):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=prec, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        ch.set_fixed_dt(case["dt"])
+        ch.time_step_rk3(20)
+        out.append(ch.download())
+    for n in ("U", "V", "W"):
+        e = rel_err(out[1][n], out[0][n])
+        assert e < 1e-4, (n, e)
