@@ -1,0 +1,398 @@
+#!/usr/bin/env python
+"""Throughput of the RK3 step of the staggered finite-difference channel solver.
+
+Workload (default): wall-resolved LES at Re_tau = 550 -- 2*pi x 2 x pi,
+192 x 128 x 192 cells (input_parameters faces 194 129 194), tanh-stretched
+wall-normal grid (stretch 1.5), dynamic Smagorinsky, no-slip walls, constant
+mass flow, seeded perturbed laminar initial field made divergence-free by
+one projection, CFL 0.5 (dt = 5e-3 by the reference's dt rule).  One "step"
+is compute_dt + compute_time_step_RK3 + the mass-flow forcing
+(time_integration.f90:89-227).  Metric: grid-point*steps/s with grid points =
+the 192*128*192 unique cells.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 runs as replicas (one independent channel per rank, launched by
+torch.distributed.run); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "channel-flow_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "grid-pt·steps/s, mixed vs FP64 GPU at ≤1% stats error; HBM % of peak"
+UNIT = "grid-pt·steps/s"
+
+WORKLOADS = {
+    "re550": dict(name="LES Re_tau=550, 192x128x192, DSM, no-slip, constant mass flow", nx=194, ny=129, nz=194,
+                  retau=550.0, stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar"),
+    "re180": dict(name="Re_tau=180, 64x64x64, DSM, no-slip, constant mass flow", nx=66, ny=65, nz=66, retau=180.0,
+                  stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar"),
+    "re2000_eqwm": dict(name="WMLES Re_tau=2000, 256x96x256, DSM + eqwm (ncv 30), uniform y", nx=258, ny=97, nz=258,
+                        retau=2000.0, stretch=0.0, les=2, wall=3, jref=6, ncv=30, profile="plug"),
+}
+
+# Algorithmic bytes per unique cell for one full step: one read or write of a
+# full field per pass over the dependency-forced pass structure (DSM 4, RHS +
+# update 10/13/13, div + forward FFT 4, tridiagonal 2, inverse FFT 2,
+# projection 7, per substep; mass flow 2 and dt 3 per step): 98 accesses.
+# Split path: 73 velocity-class accesses at 4 B, 11 u^n hi+lo at 8 B, 18
+# spectrum/phi accesses at 8 B = 524 B; FP64 path: 98 x 8 = 784 B.
+BYTES_PER_PT_STEP = {"split": 524.0, "fp64": 784.0}
+
+
+def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
+    """Compulsory bytes of one launch of a kernel: every input element read once
+    and every output element written once (es = bytes per state element)."""
+    nC = c.nxp * c.nym * c.nzp  # unique cells
+    cs = 2 * es                  # complex spectrum element
+    nh = (c.nxp // 2 + 1) * c.nym * c.nzp
+    tab = {
+        # 3 velocity components in, |S| Sij (6), products (6), centre velocities (3), |S| out
+        "k_dsm_a": (3 + 16) * nC * es,
+        # 15 filtered inputs, 12 outputs
+        "k_dsm_b": (15 + 12) * nC * es,
+        # one velocity component in and out
+        "k_dsm_c": 2 * nC * es,
+        # Uf, Vf, Wf and 12 L/hat(|S|Sij) arrays in
+        "k_dsm_d": (3 + 12) * nC * es,
+        "k_dsm_f": 2 * nC * es,
+        # U, V, W, nu_t, Uo (+ lo), F1 in; out + F1 (substep 1 of 3 stores it)
+        # one component: U, V, W, nu_t, Uo (+ its low word) and F1 in, the new
+        # component out (F1 written in substep 1 instead of read)
+        "k_rhs": 8 * nC * es,
+        "k_fwd_x": 3 * nC * es + nh * cs,
+        "k_fft_z": 2 * nh * cs,
+        "k_tri": 2 * nh * cs,
+        "k_inv_x": nh * cs + nC * es,
+        # one component: phi in, velocity in and out
+        "k_project": 3 * nC * es,
+        "k_bc": None,
+    }
+    return tab.get(kernel)
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_channel(wl, precision, device, seed, cfl=0.5):
+    import channelflow as cf
+    from channelflow import grids
+    x, y, z = grids.channel_grid(wl["nx"], wl["ny"], wl["nz"], stretch=wl["stretch"])
+    nu = grids.dean_nu(wl["retau"])
+    U, V, W = grids.seeded_fields(x, y, z, seed=seed, profile=wl["profile"])
+    prm = dict(nu=nu, CFL=cfl, dPdx=(wl["retau"] * nu) ** 2, LES_model=wl["les"], iwall_model=wl["wall"],
+               x_mass_cte=1, jref_eqwm=wl["jref"], eqwm_ncv=wl["ncv"], precision=precision)
+    ch = cf.Channel(x, y, z, device=device, **prm)
+    ch.upload(U, V, W)
+    ch.init_mass_flow()
+    ch.apply_boundary_conditions()
+    ch.set_scalars(dt=5e-3, rk_step=2)
+    ch.compute_projection_step()
+    ch.apply_boundary_conditions()
+    return ch, (x, y, z, U, V, W, prm)
+
+
+def cpu_baseline(wl, steps, threads):
+    """The CPU oracle (C restatement of the reference CPU path, OpenMP) on the
+    same workload: `steps` full RK3 steps after one untimed step."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    from channelflow import grids
+    x, y, z = grids.channel_grid(wl["nx"], wl["ny"], wl["nz"], stretch=wl["stretch"])
+    nu = grids.dean_nu(wl["retau"])
+    U, V, W = grids.seeded_fields(x, y, z, seed=1, profile=wl["profile"])
+    prm = dict(nu=nu, CFL=0.5, dPdx=(wl["retau"] * nu) ** 2, LES_model=wl["les"], iwall_model=wl["wall"],
+               x_mass_cte=1, jref_eqwm=wl["jref"], eqwm_ncv=wl["ncv"])
+    o = Oracle(x, y, z, prm, threads=threads)
+    o.set_fields(U, V, W)
+    o.init_mass_flow()
+    o.apply_boundary_conditions()
+    o.compute_dt(); o.time_step_rk3()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        o.compute_dt()
+        o.time_step_rk3()
+    dt = time.perf_counter() - t0
+    o.close()
+    nc = (wl["nx"] - 2) * (wl["ny"] - 1) * (wl["nz"] - 2)
+    return nc * steps / dt, dt
+
+
+def run_reference(args, wl, rank, world):
+    """Reference arm: the reference's CPU path (its C restatement; the Fortran
+    reference needs ifort/MPI/FFTW, absent here) on all host threads."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    nc = (wl["nx"] - 2) * (wl["ny"] - 1) * (wl["nz"] - 2)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from oracle import Oracle
+    from channelflow import grids
+    x, y, z = grids.channel_grid(wl["nx"], wl["ny"], wl["nz"], stretch=wl["stretch"])
+    nu = grids.dean_nu(wl["retau"])
+    U, V, W = grids.seeded_fields(x, y, z, seed=1, profile=wl["profile"])
+    prm = dict(nu=nu, CFL=0.5, dPdx=(wl["retau"] * nu) ** 2, LES_model=wl["les"], iwall_model=wl["wall"],
+               x_mass_cte=1, jref_eqwm=wl["jref"], eqwm_ncv=wl["ncv"])
+    o = Oracle(x, y, z, prm, threads=threads)
+    o.set_fields(U, V, W)
+    o.init_mass_flow()
+    o.apply_boundary_conditions()
+    for _ in range(args.warmup):
+        o.compute_dt(); o.time_step_rk3()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.compute_dt(); o.time_step_rk3()
+    el = time.perf_counter() - t0
+    v = nc * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl["name"], "faces": [wl["nx"], wl["ny"], wl["nz"]], "grid_points": nc},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full RK3 steps of the workload (C restatement of the reference "
+                                   f"CPU path, OpenMP, {threads} threads)"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, rank, world, local):
+    import numpy as np
+    import torch
+    import channelflow as cf
+    dev = local
+    torch.cuda.set_device(dev)
+    dist = world > 1
+    if dist:
+        import torch.distributed as td
+        td.init_process_group("nccl", device_id=torch.device("cuda", dev))
+    nc = (wl["nx"] - 2) * (wl["ny"] - 1) * (wl["nz"] - 2)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            td.barrier()
+        torch.cuda.synchronize()
+
+    # ---- split path (headline) and FP64 path from the same initial field
+    ch, init = make_channel(wl, cf.PREC_SPLIT, dev, seed=1 + rank)
+    ch64, _ = make_channel(wl, cf.PREC_FP64, dev, seed=1 + rank)
+    ncmp = max(args.warmup, 3)
+    ch.time_step_rk3(ncmp)
+    ch64.time_step_rk3(ncmp)
+    s32, s64 = ch.statistics(), ch64.statistics()
+    ny = wl["ny"]
+    prof_err = {}
+    for idx, nm in ((0, "U_mean"), (3, "U2_mean"), (4, "V2_mean"), (5, "W2_mean"), (6, "UV_mean")):
+        a, b = s32[idx * ny:(idx + 1) * ny], s64[idx * ny:(idx + 1) * ny]
+        prof_err[nm] = float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+    stream = torch.cuda.ExternalStream(ch.stream(), device=torch.device("cuda", dev))
+
+    def timed(c, steps, strm):
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(strm)
+        c.time_step_rk3(steps, sync=False)
+        e1.record(strm)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            td.all_reduce(t, op=td.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    sampler = ClockSampler(int(os.environ.get("CUDA_VISIBLE_DEVICES", str(dev)).split(",")[0])
+                           if os.environ.get("CUDA_VISIBLE_DEVICES", "").replace(",", "").isdigit() else dev)
+    sampler.start()
+    ms = timed(ch, args.steps, stream)
+    clocks = sampler.stop()
+    value = world * nc * args.steps / (ms / 1e3)
+
+    # FP64 path (fewer steps: the FP64 units of GB300 run at ~1/40 of FP32)
+    k64 = max(2, min(args.steps, 6))
+    stream64 = torch.cuda.ExternalStream(ch64.stream(), device=torch.device("cuda", dev))
+    ms64 = timed(ch64, k64, stream64)
+    v64 = world * nc * k64 / (ms64 / 1e3)
+
+    # ---- per-kernel device time (eager pass with an event after every launch)
+    prof = ch.profile_steps(2)
+    tot = sum(v[0] for v in prof.values())
+    top = sorted(prof.items(), key=lambda kv: -kv[1][0])
+    dom, (dom_ms, dom_n) = top[0]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    ab = algorithmic_bytes(dom, ch, 4)
+    avg_s = dom_ms / dom_n / 1e3
+    traffic = None
+    try:
+        tj = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        traffic = tj.get(wl["name"], {}).get(dom)
+    except Exception:
+        pass
+    roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak, "peak_source": peak_src,
+            "achieved": (ab / avg_s / 1e9) if ab else None, "frac": (ab / avg_s / 1e9 / hbm_peak) if ab else None,
+            "traffic": traffic, "avg_launch_ms": avg_s * 1e3, "launches_per_step": dom_n / 2,
+            "share_of_step": dom_ms / tot if tot else None}
+
+    # ---- end to end through the public API with host buffers
+    shp = ch.shapes
+    pinned = {}
+    for k in ("U", "V", "W"):
+        n = int(np.prod(shp[k]))
+        t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+        pinned[k] = t.numpy().reshape(shp[k], order="F")
+    d = ch.download()
+    for k in ("U", "V", "W"):
+        pinned[k][...] = d[k]
+    ke = max(2, min(args.steps, 10))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        ch.upload(pinned["U"], pinned["V"], pinned["W"])
+        ch.time_step_rk3(1, sync=False)
+        ch.download_into(U=pinned["U"], V=pinned["V"], W=pinned["W"])
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([te], device="cuda")
+        td.all_reduce(t, op=td.ReduceOp.MAX)
+        te = float(t.item())
+    nbytes = 8 * sum(int(np.prod(shp[k])) for k in ("U", "V", "W"))
+    e2e = {"value": world * nc * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+           "steps": ke, "path": "cf_upload_fields + cf_time_step_rk3 + cf_download_fields, pinned host buffers"}
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        thr = os.cpu_count() or 1
+        cv, csec = cpu_baseline(wl, args.cpu_steps, thr)
+        cpu = {"value": cv, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": f"{args.cpu_steps} full RK3 steps of the same workload after 1 untimed step "
+                         f"({csec:.1f} s; C restatement of the reference CPU path, OpenMP)"}
+
+    launches = ch.launches_per_step() * args.steps
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 (split: FP32 state/stencils/SGS, FP64 tridiagonal, mean mode, "
+                                          "reductions)",
+            "data": "synthetic (seeded perturbed laminar field, projected)",
+            "config": {"workload": wl["name"], "faces": [wl["nx"], wl["ny"], wl["nz"]], "grid_points": nc,
+                       "precision": "split", "dt_rule": "reference compute_dt (CFL 0.5 -> 5e-3 cap)",
+                       "l2": "working set (~1 GB) larger than L2 (129 MB); no flush needed",
+                       "replicas": world, "graph": "one CUDA graph per step",
+                       "sgs_recompute": True},
+            "fp64": {"value": v64, "ms_per_step": ms64 / k64, "steps": k64},
+            "split_over_fp64": value / v64,
+            "stats_err_vs_fp64": {"steps": ncmp, **prof_err},
+            "hbm_frac_step": value / world * BYTES_PER_PT_STEP["split"] / (hbm_peak * 1e9),
+            "roofline": roof,
+            "kernels_ms_per_step": {k: round(v[0] / 2, 4) for k, v in top[:10]},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    ch.close()
+    ch64.close()
+    if dist:
+        td.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="re550", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_info()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl, rank, world)
+    else:
+        run_ours(args, wl, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -97,6 +97,7 @@ def load(build_if_missing: bool = True):
     L.cf_get_stream.argtypes = [vp]
     L.cf_get_stream.restype = vp
     L.cf_compute_statistics.argtypes = [vp, dp]
+    L.cf_profile_steps.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, dp, ip, ip]
     L.cf_read_input_parameters.argtypes = [C.c_char_p, C.POINTER(CfParams), ip, C.c_char_p, C.c_char_p, ip, ip]
     L.cf_read_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp]
     L.cf_write_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
@@ -140,6 +141,8 @@ class Channel:
             raise CfError(msg)
         self.h = h
         self.shapes = grids.field_shapes(self.nx, self.ny, self.nz)
+        # unique (periodic) cells: nxp x nym x nzp (initialization.f90:246-247)
+        self.nxp, self.nym, self.nzp = self.nx - 2, self.ny - 1, self.nz - 2
 
     # ---------------------------------------------------------------- utils
     def _check(self, rc):
@@ -177,6 +180,15 @@ class Channel:
         out = {k: np.zeros(self.shapes[k], order="F") for k in ("U", "V", "W", "P", "nu_t")}
         self._check(self.L.cf_download_fields(self.h, *[_dp(out[k]) for k in ("U", "V", "W", "P", "nu_t")]))
         return out
+
+    def download_into(self, U=None, V=None, W=None, P=None, nu_t=None):
+        """Downloads into caller-owned Fortran-ordered float64 arrays (e.g.
+        pinned host buffers); any may be None."""
+        arrs = [U, V, W, P, nu_t]
+        for a, k in zip(arrs, ("U", "V", "W", "P", "nu_t")):
+            if a is not None and (a.shape != self.shapes[k] or a.dtype != np.float64 or not a.flags.f_contiguous):
+                raise ValueError(f"{k}: need a Fortran-ordered float64 array of shape {self.shapes[k]}")
+        self._check(self.L.cf_download_fields(self.h, *[_dp(a) for a in arrs]))
 
     def download_wall(self):
         nx, nz = self.nx, self.nz
@@ -284,6 +296,21 @@ class Channel:
 
     def launches_per_step(self) -> int:
         return self.L.cf_launches_per_step(self.h)
+
+    def profile_steps(self, nsteps: int = 1) -> dict:
+        """Per-kernel device time (ms, summed) and launch counts over nsteps
+        eager steps, from CUDA events on the context's stream."""
+        mx = 64
+        names = C.create_string_buffer(48 * mx)
+        ms = np.zeros(mx)
+        cnt = (C.c_int * mx)()
+        n = C.c_int()
+        self._check(self.L.cf_profile_steps(self.h, nsteps, mx, names, _dp(ms), cnt, C.byref(n)))
+        out = {}
+        for k in range(n.value):
+            nm = names.raw[48 * k:48 * (k + 1)].split(b"\0", 1)[0].decode()
+            out[nm] = (float(ms[k]), int(cnt[k]))
+        return out
 
     def compute_time_step_rk3_mirror(self):
         """The reference's compute_time_step_RK3 (time_integration.f90:89-173)

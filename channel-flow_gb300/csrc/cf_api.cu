@@ -385,6 +385,7 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
     if (!ctx) return CF_OK;
     cudaSetDevice(ctx->dev);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (auto e : ctx->pev) cudaEventDestroy(e);
     for (auto &g : ctx->graphs)
         if (g) cudaGraphExecDestroy(g);
     void *ptrs[] = {ctx->nut, ctx->P, ctx->dsm_q, ctx->dsm_lf, ctx->Uf, ctx->Vf, ctx->Wf, ctx->dsm_part, ctx->avg_nu_t,
@@ -930,5 +931,61 @@ extern "C" int cf_apply_mass_flow_correction(cf_ctx *ctx, int comp, double value
     int mode = comp == 0 ? 1 : 3;
     TRY(DISPATCH(launch_mass_apply<double>(ctx, ctx->cur, mode), launch_mass_apply<float>(ctx, ctx->cur, mode)));
     CF_CUDA(cudaStreamSynchronize(ctx->st));
+    return CF_OK;
+}
+
+// Per-kernel device time over nsteps eager (non-graph) steps, from one event
+// recorded after every launch on the context's stream.  names: max_names
+// rows of 48 chars.
+extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
+                                int *n_names) {
+    if (!ctx || !names || !total_ms || !counts || !n_names) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    cudaEvent_t start;
+    CF_CUDA(cudaEventCreate(&start));
+    std::vector<std::string> nm;
+    std::vector<double> ms;
+    std::vector<int> cnt;
+    for (int s = 0; s < nsteps; s++) {
+        for (int attempt = 0; attempt < 2; attempt++) {
+            int save_cur = ctx->cur, save_old = ctx->old;
+            ctx->pn = 0;
+            CF_CUDA(cudaEventRecord(start, ctx->st));
+            ctx->profiling = true;
+            int rc = step_eager(ctx);
+            ctx->profiling = false;
+            if (rc) { cudaEventDestroy(start); return rc; }
+            CF_CUDA(cudaStreamSynchronize(ctx->st));
+            if (ctx->pn <= (int)ctx->pev.size()) break;
+            // pool too small: the step ran without complete timing; grow and
+            // time the next step instead
+            size_t old = ctx->pev.size();
+            ctx->pev.resize(ctx->pn + 64);
+            ctx->pname.resize(ctx->pn + 64);
+            for (size_t q = old; q < ctx->pev.size(); q++) CF_CUDA(cudaEventCreate(&ctx->pev[q]));
+            (void)save_cur; (void)save_old;
+        }
+        cudaEvent_t prev = start;
+        for (int q = 0; q < ctx->pn; q++) {
+            float t;
+            CF_CUDA(cudaEventElapsedTime(&t, prev, ctx->pev[q]));
+            prev = ctx->pev[q];
+            std::string n = ctx->pname[q];
+            size_t k = 0;
+            while (k < nm.size() && nm[k] != n) k++;
+            if (k == nm.size()) { nm.push_back(n); ms.push_back(0.0); cnt.push_back(0); }
+            ms[k] += t;
+            cnt[k] += 1;
+        }
+    }
+    cudaEventDestroy(start);
+    int n = std::min((int)nm.size(), max_names);
+    for (int k = 0; k < n; k++) {
+        strncpy(names + 48 * k, nm[k].c_str(), 47);
+        names[48 * k + 47] = 0;
+        total_ms[k] = ms[k];
+        counts[k] = cnt[k];
+    }
+    *n_names = n;
     return CF_OK;
 }

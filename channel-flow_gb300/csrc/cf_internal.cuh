@@ -134,6 +134,11 @@ struct cf_ctx {
     int step_launches = 0;
     int launches = 0;
     bool counting = false;
+    // per-kernel timing pass
+    bool profiling = false;
+    std::vector<cudaEvent_t> pev;
+    std::vector<const char *> pname;
+    int pn = 0;
 };
 
 int cf_fail(cf_ctx *ctx, int code, const std::string &msg);
@@ -155,8 +160,18 @@ template <typename T> int launch_eqwm(cf_ctx *ctx, int buf);
 template <typename T> int launch_copy_state(cf_ctx *ctx, int src, int dst);
 template <typename T> int launch_stats(cf_ctx *ctx, int buf, double *d_out);
 
-static inline void count_launch(cf_ctx *ctx) {
+// Called after every kernel launch.  Counts launches while a step is being
+// captured, and in a profiling pass records an event after each launch: on
+// one stream, launch q runs between event q-1 and event q.
+static inline void count_launch(cf_ctx *ctx, const char *name) {
     if (ctx->counting) ctx->launches++;
+    if (ctx->profiling) {
+        if (ctx->pn < (int)ctx->pev.size()) {
+            cudaEventRecord(ctx->pev[ctx->pn], ctx->st);
+            ctx->pname[ctx->pn] = name;
+        }
+        ctx->pn++;
+    }
 }
 
 template <typename T> static inline GeoT<T> geo_of(cf_ctx *ctx);

@@ -82,7 +82,7 @@ static int bc_field(cf_ctx *ctx, void *p, void *plo, int n1, int n2, int n3, int
     Fld<T> L = make_fld<T>(plo, n1, n2);
     double dyb = ctx->hyg[2] - ctx->hyg[1], dyt = ctx->hyg[ctx->nyg] - ctx->hyg[ctx->nyg - 1];
     k_bc<T><<<cdiv(tot, 256), 256, 0, ctx->st>>>(F, L, n1, n2, n3, xc, zc, ctx->nxp, ctx->nzp, ybc, alpha, dyb, dyt);
-    count_launch(ctx);
+    count_launch(ctx, "k_bc");
     return 0;
 }
 
@@ -333,7 +333,7 @@ static int rhs_launch(cf_ctx *ctx, int comp, int src, int mode, int s, int slot,
     if (comp == 0) k_rhs<T, 0><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
     else if (comp == 1) k_rhs<T, 1><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
     else k_rhs<T, 2><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
-    count_launch(ctx);
+    count_launch(ctx, "k_rhs");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -381,7 +381,7 @@ int launch_rk_update(cf_ctx *ctx, int s) {
                F3 = make_fld<T>(ctx->F[2][comp], n1, n2);
         dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
         k_rk_update<T><<<grd, blk, 0, ctx->st>>>(U, Uo, F1, F2, F3, ctx->ds, s, rk, i1, j1, k1);
-        count_launch(ctx);
+        count_launch(ctx, "k_rk_update");
     }
     CF_CUDA(cudaGetLastError());
     return 0;
@@ -517,9 +517,9 @@ static int mass_partial(cf_ctx *ctx, int b, int mode) {
                                                      ctx->ny, part);
         norm = ctx->mass_norm_vv;
     }
-    count_launch(ctx);
+    count_launch(ctx, "k_mass_partial");
     k_mass_final<<<1, 32, 0, ctx->st>>>(part, nb, ctx->ds, mode, norm);
-    count_launch(ctx);
+    count_launch(ctx, "k_mass_final");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -549,7 +549,7 @@ int launch_mass_apply(cf_ctx *ctx, int b, int mode) {
         k_mass_apply<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg),
                                                   make_fld<T>(ctx->Ulo[b], ctx->nx, ctx->nyg), ctx->ds, i1, j1, k1, mode);
     }
-    count_launch(ctx);
+    count_launch(ctx, "k_mass_apply");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -612,18 +612,18 @@ int launch_dt(cf_ctx *ctx, int b) {
     double *mu = ctx->d_red, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
     int n = ctx->nxg + ctx->nyg + ctx->nzg + 6;
     k_dt_init<<<cdiv(n, 256), 256, 0, ctx->st>>>(mu, n);
-    count_launch(ctx);
+    count_launch(ctx, "k_dt_init");
     k_dt_min<T><<<ctx->nzg - 2, 128, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg),
                                                    make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
                                                    make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->nxg, ctx->nyg,
                                                    ctx->nzg, mu, mv, mw);
-    count_launch(ctx);
+    count_launch(ctx, "k_dt_min");
     double CFL = ctx->prm.CFL;
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
            vw = CFL * pow(ctx->dzmin, 2.0) / ctx->prm.nu;
     double dt_vis = fmin(vu, fmin(vv, vw));
     k_dt_final<<<1, 32, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
-    count_launch(ctx);
+    count_launch(ctx, "k_dt_final");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -664,7 +664,7 @@ int launch_div_check(cf_ctx *ctx, int b, double *d_out) {
     dim3 blk(32, 4, 1), grd(cdiv(ctx->nxg - 2, 32), cdiv(ctx->nyg - 2, 4), ctx->nzg - 2);
     k_div<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
                                        make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->geo, d_out);
-    count_launch(ctx);
+    count_launch(ctx, "k_div");
     CF_CUDA(cudaGetLastError());
     return 0;
 }

@@ -246,9 +246,9 @@ __global__ void k_fill(T *p, long n, T v) {
 template <typename T>
 int launch_nut_zero(cf_ctx *ctx) {
     k_fill<T><<<cdiv(ctx->nC, 256), 256, 0, ctx->st>>>((T *)ctx->nut, (long)ctx->nC, T(0));
-    count_launch(ctx);
+    count_launch(ctx, "k_fill");
     k_fill<double><<<1, 256, 0, ctx->st>>>(ctx->avg_nu_t, ctx->nyg + 1, 0.0);
-    count_launch(ctx);
+    count_launch(ctx, "k_fill");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -265,27 +265,27 @@ int launch_dsm(cf_ctx *ctx, int b) {
     dim3 blk(32, 4, 1);
     dim3 grdc(cdiv(ctx->nxp, 32), cdiv(ctx->nym, 4), ctx->nzp);
     k_dsm_a<T><<<grdc, blk, 0, ctx->st>>>(g, U, V, W, q, c);
-    count_launch(ctx);
+    count_launch(ctx, "k_dsm_a");
     k_dsm_b<T><<<grdc, blk, 0, ctx->st>>>(q, lf, c, ctx->nx, ctx->nyg);
-    count_launch(ctx);
+    count_launch(ctx, "k_dsm_b");
     Fld<T> Uf = make_fld<T>(ctx->Uf, ctx->nx, ctx->nyg);
     Fld<T> Vf = make_fld<T>(ctx->Vf, ctx->nxg, ctx->ny);
     Fld<T> Wf = make_fld<T>(ctx->Wf, ctx->nxg, ctx->nyg);
     k_dsm_c<T><<<dim3(cdiv(ctx->nx, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(U, Uf, ctx->nx, ctx->nyg, ctx->nzg, ctx->nxp, ctx->nzp);
     k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->ny, 4), ctx->nzg), blk, 0, ctx->st>>>(V, Vf, ctx->nxg, ctx->ny, ctx->nzg, ctx->nxp, ctx->nzp);
     k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nz), blk, 0, ctx->st>>>(W, Wf, ctx->nxg, ctx->nyg, ctx->nz, ctx->nxp, ctx->nzp);
-    count_launch(ctx); count_launch(ctx); count_launch(ctx);
+    count_launch(ctx, "k_dsm_c"); count_launch(ctx, "k_dsm_c"); count_launch(ctx, "k_dsm_c");
     int nchunk = ctx->dsm_nblk;
     k_dsm_d<T><<<dim3(nchunk, ctx->nym), 256, 0, ctx->st>>>(g, Uf, Vf, Wf, lf, c, ctx->dsm_part, nchunk);
-    count_launch(ctx);
+    count_launch(ctx, "k_dsm_d");
     int dir = ctx->prm.Dirichlet_nu_t == 1;
     k_dsm_e<<<cdiv(ctx->nym, 64), 64, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
     k_dsm_e2<<<1, 32, 0, ctx->st>>>(ctx->nyg, ctx->avg_nu_t, dir);
-    count_launch(ctx); count_launch(ctx);
+    count_launch(ctx, "k_dsm_e"); count_launch(ctx, "k_dsm_e2");
     Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
     k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(nt, q + Q_S * c.n, ctx->avg_nu_t, c,
                                                                                             ctx->nxg, ctx->nyg, ctx->nzg, dir);
-    count_launch(ctx);
+    count_launch(ctx, "k_dsm_f");
     CF_CUDA(cudaGetLastError());
     return 0;
 }

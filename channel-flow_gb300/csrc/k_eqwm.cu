@@ -146,7 +146,7 @@ int launch_eqwm(cf_ctx *ctx, int b) {
     Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
     k_eq_zinterp_t<T><<<dim3(cdiv(nxg, 128), nzg, 2), 128, 0, ctx->st>>>(W, ctx->prm.jref_eqwm, nxg, nyg, nzg,
                                                                          ctx->eq_zst, ctx->eq_zw, ctx->wtemp1);
-    count_launch(ctx);
+    count_launch(ctx, "k_eq_zinterp_t");
     EqParams ep;
     ep.ncv = ctx->prm.eqwm_ncv;
     ep.jref = ctx->prm.jref_eqwm;
@@ -162,9 +162,9 @@ int launch_eqwm(cf_ctx *ctx, int b) {
                                                      ctx->wtemp1, ctx->eq_xst, ctx->eq_xw, ctx->eq_grid, ep,
                                                      (const double *)ctx->nut, sizeof(T) == 4, ctx->tau0, ctx->alpha_x,
                                                      ctx->alpha_zt, (int *)ctx->d_red);
-    count_launch(ctx);
+    count_launch(ctx, "k_eq_solve");
     k_eq_alphaz<<<dim3(cdiv(nxg, 128), nz, 2), 128, 0, ctx->st>>>(ctx->alpha_zt, ctx->alpha_z, nx, nxg, nz, nzg);
-    count_launch(ctx);
+    count_launch(ctx, "k_eq_alphaz");
     CF_CUDA(cudaGetLastError());
     return 0;
 }

@@ -389,26 +389,26 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p) {
     size_t shx = smem_pairs<T>(nxp, LP);
     // forward x (divergence fused)
     k_fwd_x<T><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP);
-    count_launch(ctx);
+    count_launch(ctx, "k_fwd_x");
     // forward z
     int LB = max(1, 256 / Gz);
     while (LB > 1 && smem_pairs<T>(nzp, LB) > 96 * 1024) LB--;
     int ngrp = (nh + LB - 1) / LB;
     size_t shz = smem_pairs<T>(nzp, LB);
     k_fft_z<T><<<nym * ngrp, LB * Gz, shz, ctx->st>>>(spec, pz, twzf, nym, nh, LB);
-    count_launch(ctx);
+    count_launch(ctx, "k_fft_z");
     // tridiagonal
     dim3 gt(cdiv(nh, 64), nzp);
     if (nym <= 160) k_tri<T, 160><<<gt, 64, 0, ctx->st>>>(spec, ctx->d_tri, nym, nh, nzp, nxp);
     else k_tri<T, 520><<<gt, 64, 0, ctx->st>>>(spec, ctx->d_tri, nym, nh, nzp, nxp);
-    count_launch(ctx);
+    count_launch(ctx, "k_tri");
     // inverse z
     k_fft_z<T><<<nym * ngrp, LB * Gz, shz, ctx->st>>>(spec, pz, twzb, nym, nh, LB);
-    count_launch(ctx);
+    count_launch(ctx, "k_fft_z");
     // inverse x
     double scale = 1.0 / ((double)nxp * (double)nzp);
     k_inv_x<T><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale);
-    count_launch(ctx);
+    count_launch(ctx, "k_inv_x");
     // projection
     PhiView pv;
     pv.nxp = nxp; pv.nym = nym; pv.nzp = nzp;
@@ -428,12 +428,12 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p) {
         k_project<T, 2><<<dim3(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1), blk, 0, ctx->st>>>(
             g, W, make_fld<T>(ctx->Wlo[b], ctx->nxg, ctx->nyg), phi, pv, i1, j1, k1);
     }
-    count_launch(ctx); count_launch(ctx); count_launch(ctx);
+    count_launch(ctx, "k_project"); count_launch(ctx, "k_project"); count_launch(ctx, "k_project");
     if (store_p) {
         Fld<T> P = make_fld<T>(ctx->P, ctx->nxg, ctx->nyg);
         k_store_p<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(
             P, phi, pv, ctx->ds, 8.0 / 15.0, ctx->nxg, ctx->nyg, ctx->nzg);
-        count_launch(ctx);
+        count_launch(ctx, "k_store_p");
     }
     CF_CUDA(cudaGetLastError());
     return 0;

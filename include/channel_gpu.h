@@ -132,8 +132,13 @@ int cf_set_fixed_dt(cf_ctx *ctx, double dt);
 int cf_synchronize(cf_ctx *ctx);
 /* The cudaStream_t the context launches on (for event timing by callers). */
 void *cf_get_stream(cf_ctx *ctx);
-/* Count of kernel launches the last cf_time_step_rk3 step enqueued. */
+/* Count of kernel launches one cf_time_step_rk3 step enqueues. */
 int cf_launches_per_step(cf_ctx *ctx);
+/* Runs nsteps steps of the fast-path sequence without the graph, timing every
+ * kernel with CUDA events on the context's stream; returns per-kernel total
+ * device milliseconds and launch counts (names: max_names rows of 48 chars). */
+int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
+                     int *n_names);
 
 /* ---- statistics (statistics.f90:22-171) ------------------------------ */
 /* out: 9 profiles of length ny (Umean, Vmean, Wmean, U2mean, V2mean, W2mean,
