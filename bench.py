@@ -59,6 +59,8 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
     cs = 2 * es                  # complex spectrum element
     nh = (c.nxp // 2 + 1) * c.nym * c.nzp
     tab = {
+        # the dynamic Smagorinsky pass: read U, V, W, write |S| (4 field accesses per cell)
+        "k_dsm_fused": 4 * nC * es,
         # 3 velocity components in, |S| Sij (6), products (6), centre velocities (3), |S| out
         "k_dsm_a": (3 + 16) * nC * es,
         # 15 filtered inputs, 12 outputs
@@ -385,9 +387,20 @@ def main():
     ap.add_argument("--workload", default="re550", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="only run N steps of the split path after one warm-up step (for ncu)")
+    ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     args = ap.parse_args()
     rank, world, local = dist_info()
     wl = WORKLOADS[args.workload]
+    if args.profile_steps:
+        import channelflow as cf
+        ch, _ = make_channel(wl, cf.PREC_SPLIT if args.precision == "split" else cf.PREC_FP64, local, seed=1)
+        ch.time_step_rk3(1)
+        ch.time_step_rk3(args.profile_steps)
+        print(json.dumps({"profile_steps": args.profile_steps, "launches_per_step": ch.launches_per_step()}))
+        ch.close()
+        return
     if args.impl == "reference":
         run_reference(args, wl, rank, world)
     else:

@@ -33,6 +33,7 @@ class CfParams(C.Structure):
         ("Retau_int", C.c_int), ("x_mass_cte", C.c_int), ("y_mass_cte", C.c_int),
         ("LES_model", C.c_int), ("iwall_model", C.c_int), ("Dirichlet_nu_t", C.c_int), ("jref_eqwm", C.c_int),
         ("precision", C.c_int), ("eqwm_ncv", C.c_int), ("eqwm_stretch", C.c_double), ("sgs_recompute", C.c_int),
+        ("dsm_unfused", C.c_int),
     ]
 
 
@@ -135,7 +136,7 @@ class Channel:
         rc = self.L.cf_create(self.nx, self.ny, self.nz, _dp(self.x), _dp(self.y), _dp(self.z),
                               C.byref(self.params), device, C.byref(h))
         if rc != 0:
-            msg = self.L.cf_last_error(h).decode() if h.value else f"cf_create failed ({rc})"
+            msg = self.L.cf_last_error(h if h.value else None).decode() or f"cf_create failed ({rc})"
             if h.value:
                 self.L.cf_destroy(h)
             raise CfError(msg)

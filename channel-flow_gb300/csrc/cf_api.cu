@@ -8,10 +8,14 @@
 #include "cf_internal.cuh"
 
 int fft_setup_attrs();
+int dsm_fused_setup();
+int dsm_fused_plan(int esz, int nxp, int nym, int nzp, int sms, int *kc, size_t *nchunk);
+
+static thread_local std::string g_last_error;  // failures without a context
 
 int cf_fail(cf_ctx *ctx, int code, const std::string &msg) {
     if (ctx) ctx->err = msg;
-    else fprintf(stderr, "channel_gpu: %s\n", msg.c_str());
+    else g_last_error = msg;
     return code;
 }
 
@@ -29,7 +33,7 @@ extern "C" void cf_default_params(cf_params *p) {
     p->sgs_recompute = 1;
 }
 
-extern "C" const char *cf_last_error(const cf_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+extern "C" const char *cf_last_error(const cf_ctx *ctx) { return ctx ? ctx->err.c_str() : g_last_error.c_str(); }
 
 // ---------------------------------------------------------------------------
 // helpers
@@ -66,6 +70,9 @@ static int alloc(cf_ctx *ctx, void **p, size_t n) {
         int rc_ = (x);          \
         if (rc_) return rc_;    \
     } while (0)
+
+static int push_scal(cf_ctx *ctx);
+static int pull_scal(cf_ctx *ctx);
 
 template <typename T>
 static int alloc_all(cf_ctx *ctx) {
@@ -225,6 +232,20 @@ static void build_dyy(cf_ctx *ctx) {
     ctx->Dl[nym - 2] = c;
 }
 
+// reciprocal spacings r[i] = 1/(a[i] - a[i-1]) (i >= 2) of x, xg, y, yg, z, zg
+template <typename T>
+static int upload_rgeo(cf_ctx *ctx, T **dptr) {
+    const std::vector<double> *v[6] = {&ctx->hx, &ctx->hxg, &ctx->hy, &ctx->hyg, &ctx->hz, &ctx->hzg};
+    size_t tot = 0;
+    for (int q = 0; q < 6; q++) { ctx->rgeo_off[q] = tot; tot += v[q]->size(); }
+    std::vector<T> h(tot, T(0));
+    for (int q = 0; q < 6; q++)
+        for (size_t e = 2; e + 1 < v[q]->size(); e++) h[ctx->rgeo_off[q] + e] = (T)(1.0 / ((*v[q])[e] - (*v[q])[e - 1]));
+    CF_CUDA(cudaMalloc((void **)dptr, tot * sizeof(T)));
+    CF_CUDA(cudaMemcpy(*dptr, h.data(), tot * sizeof(T), cudaMemcpyHostToDevice));
+    return 0;
+}
+
 template <typename T>
 static int upload_geo(cf_ctx *ctx, T **dptr, GeoT<T> *g) {
     const std::vector<double> *v[8] = {&ctx->hx, &ctx->hy, &ctx->hz, &ctx->hxg, &ctx->hyg, &ctx->hzg, &ctx->hw0, &ctx->hw1};
@@ -240,6 +261,62 @@ static int upload_geo(cf_ctx *ctx, T **dptr, GeoT<T> *g) {
     g->nxp = ctx->nxp; g->nym = ctx->nym; g->nzp = ctx->nzp; g->nxh = ctx->nxh;
     const T **dst[8] = {&g->x, &g->y, &g->z, &g->xg, &g->yg, &g->zg, &g->w0, &g->w1};
     for (int q = 0; q < 8; q++) *dst[q] = *dptr + off[q];
+    return 0;
+}
+
+// zgtsv's elimination (LAPACK 3.2.1, restated) applied to every (kx, kz)
+// matrix of projection.f90:97-107 once; the per-row pivot flags and
+// multipliers and the resulting U factor (1/d, du, dl) are what k_tri replays.
+static int tri_factor(cf_ctx *ctx) {
+    const int nym = ctx->nym, nh = ctx->nxh, nzp = ctx->nzp;
+    const size_t nf = (size_t)nym * nzp * nh;
+    std::vector<double> F(4 * nf);
+    std::vector<unsigned char> piv(nf, 0);
+    std::vector<double> d(nym), du(nym), dl(nym);
+    for (int kz = 0; kz < nzp; kz++)
+        for (int kx = 0; kx < nh; kx++) {
+            for (int q = 0; q < nym; q++) {
+                d[q] = ctx->Dd[q] + ctx->hkxx[kx] + ctx->hkzz[kz];
+                du[q] = ctx->Du[q];
+                dl[q] = ctx->Dl[q];
+            }
+            if (kx == 0 && kz == 0) d[0] = 3.0 / 2.0 * d[0];
+            const size_t f0 = (size_t)kz * nh + kx, fs = (size_t)nzp * nh;
+            for (int q = 0; q < nym - 1; q++) {
+                double m = 0.0;
+                unsigned char pv = 0;
+                if (dl[q] == 0.0) {
+                    if (d[q] == 0.0) return cf_fail(ctx, CF_ERR_INVALID, "singular pressure matrix");
+                } else if (fabs(d[q]) >= fabs(dl[q])) {
+                    m = dl[q] / d[q];
+                    d[q + 1] = d[q + 1] - m * du[q];
+                    if (q < nym - 2) dl[q] = 0.0;
+                } else {
+                    pv = 1;
+                    m = d[q] / dl[q];
+                    d[q] = dl[q];
+                    double temp = d[q + 1];
+                    d[q + 1] = du[q] - m * temp;
+                    if (q < nym - 2) {
+                        dl[q] = du[q + 1];
+                        du[q + 1] = -m * dl[q];
+                    }
+                    du[q] = temp;
+                }
+                F[q * fs + f0] = m;
+                piv[q * fs + f0] = pv;
+            }
+            if (d[nym - 1] == 0.0) return cf_fail(ctx, CF_ERR_INVALID, "singular pressure matrix");
+            for (int q = 0; q < nym; q++) {
+                F[nf + q * fs + f0] = 1.0 / d[q];
+                F[2 * nf + q * fs + f0] = q < nym - 1 ? du[q] : 0.0;
+                F[3 * nf + q * fs + f0] = q < nym - 2 ? dl[q] : 0.0;
+            }
+        }
+    CF_CUDA(cudaMalloc(&ctx->tri_fac, F.size() * sizeof(double)));
+    CF_CUDA(cudaMemcpy(ctx->tri_fac, F.data(), F.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CF_CUDA(cudaMalloc(&ctx->tri_piv, piv.size()));
+    CF_CUDA(cudaMemcpy(ctx->tri_piv, piv.data(), piv.size(), cudaMemcpyHostToDevice));
     return 0;
 }
 
@@ -353,6 +430,8 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
 
     TRY(upload_geo<double>(ctx, &ctx->d_geo, &ctx->geo));
     TRY(upload_geo<float>(ctx, &ctx->d_geo_f, &ctx->geof));
+    TRY(upload_rgeo<double>(ctx, &ctx->d_rgeo));
+    TRY(upload_rgeo<float>(ctx, &ctx->d_rgeo_f));
     // tridiagonal data
     {
         int nym = ctx->nym;
@@ -363,19 +442,35 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
         CF_CUDA(cudaMalloc(&ctx->d_tri, t.size() * sizeof(double)));
         CF_CUDA(cudaMemcpy(ctx->d_tri, t.data(), t.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
+    TRY(tri_factor(ctx));
     ctx->esz = p->precision == CF_PREC_SPLIT ? 4 : 8;
     if (ctx->esz == 8) { TRY(alloc_all<double>(ctx)); TRY(upload_twiddles<double>(ctx)); }
     else { TRY(alloc_all<float>(ctx)); TRY(upload_twiddles<float>(ctx)); }
     ctx->dsm_nblk = std::max(1, std::min(64, (int)((long)nxp * nzp / 2048)));
-    CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * ctx->dsm_nblk * sizeof(double)));
-    CF_CUDA(cudaMalloc(&ctx->avg_nu_t, (size_t)(ctx->nyg + 2) * sizeof(double)));
-    CF_CUDA(cudaMemset(ctx->avg_nu_t, 0, (size_t)(ctx->nyg + 2) * sizeof(double)));
+    size_t nch_fused = 0;
+    {
+        // fused pass: column tiles marching in z; chunks sized for one wave
+        int dev_sms = 152;
+        cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device);
+        dsm_fused_setup();
+        dsm_fused_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms, &ctx->dsm_kc, &nch_fused);
+        ctx->use_fused_dsm = !p->dsm_unfused;
+        // fused RHS: 32 x 8 column tiles, z chunks for ~4 resident blocks per SM
+        long rt = (long)cdiv(nx - 1, 32) * cdiv(ctx->nyg - 2, 8);
+        ctx->rhs_nkc = (int)std::max(1L, std::min((long)(ctx->nzg - 2) / 4, (4L * dev_sms) / std::max(1L, rt)));
+    }
+    size_t nch = std::max((size_t)ctx->dsm_nblk, nch_fused);
+    CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));
+    // avg_nu_t (1..nyg) in FP64, followed by an FP32 copy
+    CF_CUDA(cudaMalloc(&ctx->avg_nu_t, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
+    CF_CUDA(cudaMemset(ctx->avg_nu_t, 0, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
     ctx->red_n = std::max(ctx->nzg + 8, ctx->nxg + ctx->nyg + ctx->nzg + 16);
     CF_CUDA(cudaMalloc(&ctx->d_red, (size_t)ctx->red_n * sizeof(double)));
     CF_CUDA(cudaMalloc(&ctx->ds, sizeof(DevScal)));
-    CF_CUDA(cudaMemcpy(ctx->ds, &ctx->hs, sizeof(DevScal), cudaMemcpyHostToDevice));
+    TRY(push_scal(ctx));
     TRY(setup_eqwm(ctx));
     fft_setup_attrs();
+    dsm_fused_setup();
     CF_CUDA(cudaStreamSynchronize(ctx->st));
     CF_CUDA(cudaGetLastError());
     return CF_OK;
@@ -389,9 +484,9 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
     for (auto &g : ctx->graphs)
         if (g) cudaGraphExecDestroy(g);
     void *ptrs[] = {ctx->nut, ctx->P, ctx->dsm_q, ctx->dsm_lf, ctx->Uf, ctx->Vf, ctx->Wf, ctx->dsm_part, ctx->avg_nu_t,
-                    ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
+                    ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
                     ctx->wtemp1, ctx->wtemp2, ctx->eq_grid, ctx->eq_zst, ctx->eq_xst, ctx->eq_zw, ctx->eq_xw, ctx->ds,
-                    ctx->d_red, ctx->d_geo, ctx->d_geo_f, ctx->stage};
+                    ctx->d_red, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (int b = 0; b < 3; b++) {
@@ -456,8 +551,45 @@ static int get(cf_ctx *ctx, double *dst, const void *src, const void *srclo, siz
     return 0;
 }
 
+// True when U, V, W already satisfy the ghost identities that
+// apply_boundary_conditions (iwall_model 0) establishes: periodic copies in x
+// and z and the no-slip wall rows (boundary_conditions.f90:20-75).
+static bool fields_periodic(const cf_ctx *c, const double *U, const double *V, const double *W) {
+    if (c->prm.iwall_model != 0) return false;
+    const int nx = c->nx, ny = c->ny, nz = c->nz, nxg = c->nxg, nyg = c->nyg, nzg = c->nzg;
+    // visits only the ghost and duplicate elements (O(surface))
+    auto chk = [&](const double *F, int n1, int n2, int n3, bool xc, bool zc, int ybc) {
+        auto at = [&](int i, int j, int k) { return F[(size_t)(i - 1) + (size_t)n1 * ((j - 1) + (size_t)n2 * (k - 1))]; };
+        auto one = [&](int i, int j, int k) {
+            int is = wrapc(i, c->nxp), ks = wrapc(k, c->nzp);
+            double want;
+            if (j == 1 || j == n2) want = ybc == 1 ? 0.0 : -at(is, j == 1 ? 2 : n2 - 1, ks);
+            else want = at(is, j, ks);
+            return at(i, j, k) == want;
+        };
+        std::vector<int> gx = {1, n1}, gz = {1, n3};
+        if (xc) gx.push_back(n1 - 1);
+        if (zc) gz.push_back(n3 - 1);
+        for (int k = 1; k <= n3; k++)
+            for (int i = 1; i <= n1; i++)
+                if (!one(i, 1, k) || !one(i, n2, k)) return false;
+        for (int k = 1; k <= n3; k++)
+            for (int j = 2; j <= n2 - 1; j++)
+                for (int i : gx)
+                    if (!one(i, j, k)) return false;
+        for (int k : gz)
+            for (int j = 2; j <= n2 - 1; j++)
+                for (int i = 1; i <= n1; i++)
+                    if (!one(i, j, k)) return false;
+        return true;
+    };
+    (void)nx; (void)ny; (void)nz; (void)nxg; (void)nyg; (void)nzg;
+    return chk(U, nx, nyg, nzg, false, true, 0) && chk(V, nxg, ny, nzg, true, true, 1) && chk(W, nxg, nyg, nz, true, false, 0);
+}
+
 extern "C" int cf_upload_fields(cf_ctx *ctx, const double *U, const double *V, const double *W) {
     if (!ctx || !U || !V || !W) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
+    ctx->state_periodic = fields_periodic(ctx, U, V, W);
     CF_CUDA(cudaSetDevice(ctx->dev));
     int b = ctx->cur;
     TRY(put(ctx, ctx->U[b], ctx->Ulo[b], U, ctx->nU));
@@ -509,6 +641,10 @@ static int pull_scal(cf_ctx *ctx) {
     return 0;
 }
 static int push_scal(cf_ctx *ctx) {
+    ctx->hs.dtf = (float)ctx->hs.dt;
+    ctx->hs.dPdxf = (float)ctx->hs.dPdx;
+    ctx->hs.dPdzf = (float)ctx->hs.dPdz;
+    ctx->hs.corrf = (float)ctx->hs.lmax[2];
     CF_CUDA(cudaMemcpyAsync(ctx->ds, &ctx->hs, sizeof(DevScal), cudaMemcpyHostToDevice, ctx->st));
     CF_CUDA(cudaStreamSynchronize(ctx->st));
     return 0;
@@ -837,6 +973,14 @@ extern "C" int cf_time_step_rk3(cf_ctx *ctx, int nsteps, int sync) {
     CF_CUDA(cudaSetDevice(ctx->dev));
     for (int s = 0; s < nsteps; s++) {
         int X = ctx->cur;
+        if (!ctx->state_periodic && ctx->prm.iwall_model == 0) {
+            // ghosts not yet filled by apply_boundary_conditions: run this
+            // step without a graph (its first eddy viscosity takes the
+            // multi-pass route), later steps are captured
+            int rc = step_eager(ctx);
+            if (rc) return rc;
+            continue;
+        }
         if (!ctx->graphs[X]) {
             // first step from this buffer: count launches eagerly-captured
             cudaGraph_t g;

@@ -63,7 +63,36 @@ struct DevScal {
     double mass_sum;       // mass-flow integral
     double fixed_dt;       // > 0: dt forced (CFL < 0 rule)
     int rk_step, n_nan, n_iter, pad;
+    // FP32 copies for the split path (written next to their FP64 values)
+    float dtf, dPdxf, dPdzf, corrf;
 };
+
+template <typename T> __device__ __forceinline__ T ds_dt(const DevScal *d);
+template <> __device__ __forceinline__ double ds_dt<double>(const DevScal *d) { return d->dt; }
+template <> __device__ __forceinline__ float ds_dt<float>(const DevScal *d) { return d->dtf; }
+template <typename T> __device__ __forceinline__ T ds_dpdx(const DevScal *d);
+template <> __device__ __forceinline__ double ds_dpdx<double>(const DevScal *d) { return d->dPdx; }
+template <> __device__ __forceinline__ float ds_dpdx<float>(const DevScal *d) { return d->dPdxf; }
+template <typename T> __device__ __forceinline__ T ds_dpdz(const DevScal *d);
+template <> __device__ __forceinline__ double ds_dpdz<double>(const DevScal *d) { return d->dPdz; }
+template <> __device__ __forceinline__ float ds_dpdz<float>(const DevScal *d) { return d->dPdzf; }
+
+// Compensated (float-float) state of the split path: hi + lo holds a value
+// to about 2^-48 relative; updates use Knuth's TwoSum so that no FP64
+// arithmetic runs per grid point (GB300's FP64 rate is ~1/40 of FP32).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+// (hi, lo) += d, renormalised
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
+    float s, e;
+    two_sum(hi, d, s, e);
+    e += lo;
+    hi = s + e;
+    lo = e - (hi - s);
+}
 
 __host__ __device__ __forceinline__ int wrapc(int i, int np) {
     // canonical index of a periodic index (faces or centres): 2 + (i-2) mod np
@@ -88,6 +117,9 @@ struct cf_ctx {
     double dxmin, dymin, dzmin, Lx, Ly, Lz, mass_norm, omega_z;
     double *d_geo = nullptr;
     float *d_geo_f = nullptr;
+    double *d_rgeo = nullptr;          // reciprocal spacings (see rgeo_off)
+    float *d_rgeo_f = nullptr;
+    size_t rgeo_off[6] = {};
     Geo geo;
     GeoT<float> geof;
     double mass_norm_vv = 1.0;
@@ -106,10 +138,18 @@ struct cf_ctx {
     double *dsm_part = nullptr;        // plane partial sums
     double *avg_nu_t = nullptr;        // (nyg) device
     int dsm_nblk = 0;
+    int dsm_kc = 0;                    // z-chunk length of the fused pass
+    int dsm_nchunk_fused = 0;
+    bool use_fused_dsm = true;
+    bool use_rhs3 = true;              // one fused RHS + update launch per substep
+    int rhs_nkc = 1;                   // z chunks of the fused RHS
+    bool state_periodic = false;       // U, V, W satisfy the periodic/no-slip ghost identities
     // pressure
     void *phi = nullptr;               // canonical real
     void *spec = nullptr;              // complex spectrum (nxh, nym, nzp)
     double *d_tri = nullptr;           // Dd, Dl, Du (nym each), kxx (nxp), kzz (nzp)
+    double *tri_fac = nullptr;         // zgtsv factors per mode: m, 1/d, du, dl
+    unsigned char *tri_piv = nullptr;  // zgtsv pivot flags per mode
     double *d_tw = nullptr;            // twiddles: x fwd, x bwd, z fwd, z bwd
     int radx[8], nradx, radz[8], nradz;
     // wall model
@@ -149,6 +189,7 @@ template <typename T> int launch_rhs(cf_ctx *ctx, int comp, int slot);     // st
 template <typename T> int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst);  // fused RHS + RK update
 template <typename T> int launch_rk_update(cf_ctx *ctx, int s);            // from stored F slots
 template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // eddy viscosity
+template <typename T> int launch_dsm_fused(cf_ctx *ctx, int buf);          // fused pass (periodic state)
 template <typename T> int launch_nut_zero(cf_ctx *ctx);
 template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p);
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);

@@ -89,6 +89,7 @@ static int bc_field(cf_ctx *ctx, void *p, void *plo, int n1, int n2, int n3, int
 template <typename T>
 int launch_bc(cf_ctx *ctx, int b) {
     int wm = ctx->prm.iwall_model;
+    if (wm == 0) ctx->state_periodic = true;  // holds for every later launch on the stream
     // U: x faces, y centres, z centres
     bc_field<T>(ctx, ctx->U[b], ctx->Ulo[b], ctx->nx, ctx->nyg, ctx->nzg, 0, 1, wm == 3 ? 2 : 0, ctx->alpha_x);
     // V: x centres, y faces, z centres
@@ -106,9 +107,9 @@ struct RkCoef {
     double c[4][4];
 };
 
-template <typename T>
-__device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W,
-                                         const Fld<T> &nt, T nu, T dPdx, T Om, int i, int j, int k) {
+template <typename T, typename A>
+__device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const A &U, const A &V, const A &W,
+                                         const A &nt, T nu, T dPdx, T Om, int i, int j, int k) {
     const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
     // 1) -du^2/dx  (equations.f90:43-57)
@@ -155,9 +156,9 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const Fld<T> &U, cons
     return r;
 }
 
-template <typename T>
-__device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W,
-                                         const Fld<T> &nt, T nu, T Om, int i, int j, int k) {
+template <typename T, typename A>
+__device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const A &U, const A &V, const A &W,
+                                         const A &nt, T nu, T Om, int i, int j, int k) {
     const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5);
     // 1) -dv^2/dy (equations.f90:205-223)
@@ -200,9 +201,9 @@ __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const Fld<T> &U, cons
     return r;
 }
 
-template <typename T>
-__device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W,
-                                         const Fld<T> &nt, T nu, T dPdz, int i, int j, int k) {
+template <typename T, typename A>
+__device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const A &U, const A &V, const A &W,
+                                         const A &nt, T nu, T dPdz, int i, int j, int k) {
     const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
     // 1) -dw^2/dz (equations.f90:370-384)
@@ -244,6 +245,68 @@ __device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const Fld<T> &U, cons
     return r;
 }
 
+// RK3 stage update of one point (time_integration.f90:108-110, 124-126,
+// 140-145) with F2 never reused (rk_coef(3,2) = 0, initialization.f90:416).
+// The split path keeps u^n as hi + lo; substep 3 writes the new low word.
+template <typename T>
+__device__ __forceinline__ void rk_store(T r, int i, int j, int k, const Fld<T> &out, const Fld<T> &F1,
+                                         const Fld<T> &Uo, const Fld<T> &Uolo, const Fld<T> &Unlo, int s,
+                                         const RkCoef &rk, T dt) {
+    T inc;
+    if (s == 1) {
+        F1(i, j, k) = r;
+        inc = dt * T(rk.c[1][1]) * r;
+    } else if (s == 2) {
+        inc = dt * (T(rk.c[2][1]) * F1(i, j, k) + T(rk.c[2][2]) * r);
+    } else {
+        inc = dt * (T(rk.c[3][1]) * F1(i, j, k) + T(rk.c[3][3]) * r);
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (Uolo.p) {
+            float hi = Uo(i, j, k), lo = Uolo(i, j, k);
+            if (Unlo.p) {
+                ff_add(hi, lo, inc);
+                out(i, j, k) = hi;
+                Unlo(i, j, k) = lo;
+            } else {
+                out(i, j, k) = hi + (lo + inc);
+            }
+            return;
+        }
+    }
+    out(i, j, k) = Uo(i, j, k) + inc;
+}
+
+// The same update with its operands already loaded (f1 = F1 for s > 1, uo and
+// uolo = the old state and its low word).
+template <typename T>
+__device__ __forceinline__ void rk_apply(T r, T f1, T uo, T uolo, bool has_lo, int i, int j, int k, const Fld<T> &out,
+                                         const Fld<T> &F1, const Fld<T> &Unlo, int s, const RkCoef &rk, T dt) {
+    T inc;
+    if (s == 1) {
+        F1(i, j, k) = r;
+        inc = dt * T(rk.c[1][1]) * r;
+    } else if (s == 2) {
+        inc = dt * (T(rk.c[2][1]) * f1 + T(rk.c[2][2]) * r);
+    } else {
+        inc = dt * (T(rk.c[3][1]) * f1 + T(rk.c[3][3]) * r);
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (has_lo) {
+            float hi = uo, lo = uolo;
+            if (Unlo.p) {
+                ff_add(hi, lo, inc);
+                out(i, j, k) = hi;
+                Unlo(i, j, k) = lo;
+            } else {
+                out(i, j, k) = hi + (lo + inc);
+            }
+            return;
+        }
+    }
+    out(i, j, k) = uo + inc;
+}
+
 // mode: 0 = store F(slot); 1 = fused update from Uo with F1 (s = 1 stores F1)
 template <typename T, int COMP>
 __global__ void k_rhs(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds, T nu, T Om,
@@ -254,34 +317,14 @@ __global__ void k_rhs(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const 
     int k = blockIdx.z + 2;
     if (i > i1 || j > j1 || k > k1) return;
     T r;
-    if (COMP == 0) r = rhs_u_point<T>(g, U, V, W, nt, nu, (T)ds->dPdx, Om, i, j, k);
-    else if (COMP == 1) r = rhs_v_point<T>(g, U, V, W, nt, nu, Om, i, j, k);
-    else r = rhs_w_point<T>(g, U, V, W, nt, nu, (T)ds->dPdz, i, j, k);
+    if (COMP == 0) r = rhs_u_point<T, Fld<T>>(g, U, V, W, nt, nu, ds_dpdx<T>(ds), Om, i, j, k);
+    else if (COMP == 1) r = rhs_v_point<T, Fld<T>>(g, U, V, W, nt, nu, Om, i, j, k);
+    else r = rhs_w_point<T, Fld<T>>(g, U, V, W, nt, nu, ds_dpdz<T>(ds), i, j, k);
     if (mode == 0) {
         out(i, j, k) = r;
         return;
     }
-    // time_integration.f90:108-110 / 124-126 / 140-145 with F2 never reused
-    // (rk_coef(3,2) = 0, initialization.f90:416)
-    const double dt = ds->dt;
-    double inc;
-    if (s == 1) {
-        F1(i, j, k) = r;
-        inc = dt * rk.c[1][1] * (double)r;
-    } else if (s == 2) {
-        inc = dt * (rk.c[2][1] * (double)F1(i, j, k) + rk.c[2][2] * (double)r);
-    } else {
-        inc = dt * (rk.c[3][1] * (double)F1(i, j, k) + rk.c[3][3] * (double)r);
-    }
-    if (Uolo.p) {
-        // split precision: u^n kept as hi + lo; the new state keeps a low word
-        double v = (double)Uo(i, j, k) + (double)Uolo(i, j, k) + inc;
-        T hi = (T)v;
-        out(i, j, k) = hi;
-        if (Unlo.p) Unlo(i, j, k) = (T)(v - (double)hi);
-    } else {
-        out(i, j, k) = (T)((double)Uo(i, j, k) + inc);
-    }
+    rk_store<T>(r, i, j, k, out, F1, Uo, Uolo, Unlo, s, rk, ds_dt<T>(ds));
 }
 
 
@@ -338,13 +381,183 @@ static int rhs_launch(cf_ctx *ctx, int comp, int src, int mode, int s, int slot,
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Fused right-hand sides of u, v and w with the RK update, one launch per
+// substep.  A block owns a TX x TY tile of (i, j) columns and marches along z
+// over a chunk of planes, keeping planes k-1, k, k+1 of U, V, W and nu_t (tile
+// plus one halo cell) in a shared-memory ring; the per-point formulas above
+// read them through an accessor with the Fld interface.
+// ---------------------------------------------------------------------------
+template <typename T, int TX, int TY>
+struct RingAcc {
+    static constexpr int SX = TX + 2, SY = TY + 2;
+    const T *b[3];  // planes k-1, k, k+1 of one field
+    int i0, j0, kc;
+    __device__ __forceinline__ T operator()(int i, int j, int k) const {
+        return b[k - kc + 1][(j - j0 + 1) * SX + (i - i0 + 1)];
+    }
+};
+
+template <typename T>
+struct Trio {
+    Fld<T> u, v, w;
+};
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds,
+                                                     T nu, T Om, Trio<T> out, Trio<T> F1, Trio<T> Uo, Trio<T> Uolo,
+                                                     Trio<T> Unlo, int s, RkCoef rk, int kc_len) {
+    constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
+    __shared__ T ring[3][4][NP];  // [plane slot][field U V W nu_t][tile]
+    const int nx = g.nx, ny = g.ny, nz = g.nz, nxg = g.nxg, nyg = g.nyg, nzg = g.nzg;
+    const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
+    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, nzg - 1);
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int i = i0 + tx, j = j0 + ty;
+    const T dt = ds_dt<T>(ds), dPdx = ds_dpdx<T>(ds), dPdz = ds_dpdz<T>(ds);
+    // the tile's x and y geometry in shared memory; gl indexes it with the
+    // global 1-based indices (z stays in global memory: uniform per plane)
+    __shared__ T gxs[2][TX + 3], gys[4][TY + 3];
+    for (int t = threadIdx.x; t < TX + 3; t += TX * TY) {
+        int ii = min(i0 - 1 + t, nxg);
+        gxs[0][t] = g.x[min(ii, nx)];
+        gxs[1][t] = g.xg[ii];
+    }
+    for (int t = threadIdx.x; t < TY + 3; t += TX * TY) {
+        int jj = min(j0 - 1 + t, nyg);
+        gys[0][t] = g.y[min(jj, ny)];
+        gys[1][t] = g.yg[jj];
+        gys[2][t] = g.w0[min(jj, ny)];
+        gys[3][t] = g.w1[min(jj, ny)];
+    }
+    GeoT<T> gl = g;
+    gl.x = gxs[0] - (i0 - 1);
+    gl.xg = gxs[1] - (i0 - 1);
+    gl.y = gys[0] - (j0 - 1);
+    gl.yg = gys[1] - (j0 - 1);
+    gl.w0 = gys[2] - (j0 - 1);
+    gl.w1 = gys[3] - (j0 - 1);
+    const bool du = i <= nx - 1 && j <= nyg - 1, dv = i <= nxg - 1 && j <= ny - 1, dw = i <= nxg - 1 && j <= nyg - 1;
+    const bool lo = Uolo.u.p != nullptr;
+    // this thread's tile elements (same for every plane and field)
+    int eia[NL], eja[NL], erem[NL];
+#pragma unroll
+    for (int q = 0; q < NL; q++) {
+        int rem = threadIdx.x + q * NT;
+        erem[q] = rem;
+        int sy = rem / SX, sx = rem - sy * SX;
+        eia[q] = i0 + sx - 1;
+        eja[q] = j0 + sy - 1;
+    }
+    // all loads of one plane are issued before any of them is used
+    T pre[4][NL];
+    auto fetch = [&](int k) {
+#pragma unroll
+        for (int q = 0; q < NL; q++) {
+            const int ia = eia[q], ja = eja[q];
+            const bool in = erem[q] < NP;
+            pre[0][q] = (in && ia <= nx && ja <= nyg && k <= nzg) ? U(ia, ja, k) : T(0);
+            pre[1][q] = (in && ia <= nxg && ja <= ny && k <= nzg) ? V(ia, ja, k) : T(0);
+            pre[2][q] = (in && ia <= nxg && ja <= nyg && k <= nz) ? W(ia, ja, k) : T(0);
+            pre[3][q] = (in && ia <= nxg && ja <= nyg && k <= nzg) ? nt(ia, ja, k) : T(0);
+        }
+    };
+    auto commit = [&](int slot) {
+#pragma unroll
+        for (int q = 0; q < NL; q++)
+            if (erem[q] < NP) {
+#pragma unroll
+                for (int f = 0; f < 4; f++) ring[slot][f][erem[q]] = pre[f][q];
+            }
+    };
+    fetch(kb - 1);
+    commit(0);
+    fetch(kb);
+    commit(1);
+    fetch(kb + 1);
+    commit(2);
+    __syncthreads();
+    int sm1 = 0, s0 = 1, sp1 = 2;
+    for (int k = kb; k <= ke; k++) {
+        if (k + 1 <= ke) fetch(k + 2);  // in flight during this plane's work
+        // RK operands of this plane, loaded before the stencil work
+        const bool cu = du && k <= nzg - 1, cv = dv && k <= nzg - 1, cw = dw && k <= nz - 1;
+        T fu = T(0), fv = T(0), fw = T(0), ou = T(0), ov = T(0), ow = T(0), lu = T(0), lv = T(0), lw = T(0);
+        if (cu) { ou = Uo.u(i, j, k); if (lo) lu = Uolo.u(i, j, k); if (s > 1) fu = F1.u(i, j, k); }
+        if (cv) { ov = Uo.v(i, j, k); if (lo) lv = Uolo.v(i, j, k); if (s > 1) fv = F1.v(i, j, k); }
+        if (cw) { ow = Uo.w(i, j, k); if (lo) lw = Uolo.w(i, j, k); if (s > 1) fw = F1.w(i, j, k); }
+        RingAcc<T, TX, TY> aU, aV, aW, aN;
+        aU.b[0] = ring[sm1][0]; aU.b[1] = ring[s0][0]; aU.b[2] = ring[sp1][0];
+        aV.b[0] = ring[sm1][1]; aV.b[1] = ring[s0][1]; aV.b[2] = ring[sp1][1];
+        aW.b[0] = ring[sm1][2]; aW.b[1] = ring[s0][2]; aW.b[2] = ring[sp1][2];
+        aN.b[0] = ring[sm1][3]; aN.b[1] = ring[s0][3]; aN.b[2] = ring[sp1][3];
+        aU.i0 = aV.i0 = aW.i0 = aN.i0 = i0;
+        aU.j0 = aV.j0 = aW.j0 = aN.j0 = j0;
+        aU.kc = aV.kc = aW.kc = aN.kc = k;
+        if (cu) {
+            T r = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, aU, aV, aW, aN, nu, dPdx, Om, i, j, k);
+            rk_apply<T>(r, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, rk, dt);
+        }
+        if (cv) {
+            T r = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, aU, aV, aW, aN, nu, Om, i, j, k);
+            rk_apply<T>(r, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, rk, dt);
+        }
+        if (cw) {
+            T r = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, aU, aV, aW, aN, nu, dPdz, i, j, k);
+            rk_apply<T>(r, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, rk, dt);
+        }
+        __syncthreads();            // plane k-1 no longer read
+        if (k + 1 <= ke) commit(sm1);  // plane k+2 into the freed slot
+        __syncthreads();
+        int t0 = sm1;
+        sm1 = s0;
+        s0 = sp1;
+        sp1 = t0;
+    }
+}
+
+template <typename T>
+int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
+    constexpr int TX = 32, TY = 8;
+    GeoT<T> g = geo_of<T>(ctx);
+    Fld<T> U = make_fld<T>(ctx->U[src], ctx->nx, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[src], ctx->nxg, ctx->ny);
+    Fld<T> W = make_fld<T>(ctx->W[src], ctx->nxg, ctx->nyg);
+    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+    auto trio = [&](void *a, void *b, void *c) {
+        Trio<T> t;
+        t.u = make_fld<T>(a, ctx->nx, ctx->nyg);
+        t.v = make_fld<T>(b, ctx->nxg, ctx->ny);
+        t.w = make_fld<T>(c, ctx->nxg, ctx->nyg);
+        return t;
+    };
+    const int o = ctx->old;
+    Trio<T> out = trio(ctx->U[dst], ctx->V[dst], ctx->W[dst]);
+    Trio<T> F1 = trio(ctx->F[0][0], ctx->F[0][1], ctx->F[0][2]);
+    Trio<T> Uo = trio(ctx->U[o], ctx->V[o], ctx->W[o]);
+    Trio<T> Uolo = trio(ctx->Ulo[o], ctx->Vlo[o], ctx->Wlo[o]);
+    Trio<T> Unlo = s == 3 ? trio(ctx->Ulo[dst], ctx->Vlo[dst], ctx->Wlo[dst]) : trio(nullptr, nullptr, nullptr);
+    int ntx = cdiv(ctx->nx - 1, TX), nty = cdiv(ctx->nyg - 2, TY);
+    int nkc = ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1;
+    int kc_len = cdiv(ctx->nzg - 2, nkc);
+    k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(ctx->nzg - 2, kc_len)), TX * TY, 0, ctx->st>>>(
+        g, U, V, W, nt, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len);
+    count_launch(ctx, "k_rhs3");
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
 template <typename T>
 int launch_rhs(cf_ctx *ctx, int comp, int slot) {
     return rhs_launch<T>(ctx, comp, ctx->cur, 0, 0, slot, 0);
 }
 
 template <typename T>
+int launch_rhs3(cf_ctx *ctx, int s, int src, int dst);
+
+template <typename T>
 int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst) {
+    if (ctx->use_rhs3) return launch_rhs3<T>(ctx, s, src, dst);
     for (int c = 0; c < 3; c++) {
         int rc = rhs_launch<T>(ctx, c, src, 1, s, 0, dst);
         if (rc) return rc;
@@ -425,14 +638,25 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 // mode 1: trapezoid of U (mass_flow.f90:116-123), one block per k plane
 template <typename T>
 __global__ void k_mass_partial(Fld<T> U, const double *yg, int nx, int nyg, double *part) {
+    // sum_{j=3}^{nyg-1} (U_j + U_{j-1}) (yg_j - yg_{j-1})/2 = sum_j U_j c_j with
+    // c_j the two adjacent half-intervals: one FP64 FMA per element
     __shared__ double sh[32];
+    __shared__ double cw[520];
     int k = blockIdx.x + 2;
+    for (int j = threadIdx.x + 2; j <= nyg - 1; j += blockDim.x)
+        cw[j] = (j >= 3 ? 0.5 * (yg[j] - yg[j - 1]) : 0.0) + (j <= nyg - 2 ? 0.5 * (yg[j + 1] - yg[j]) : 0.0);
+    __syncthreads();
     double s = 0.0;
-    int ni = nx - 2, nj = nyg - 3;
-    for (int t = threadIdx.x; t < ni * nj; t += blockDim.x) {
-        int i = t % ni + 2, j = t / ni + 3;
-        s += ((double)U(i, j, k) + (double)U(i, j - 1, k)) * 0.5 * (yg[j] - yg[j - 1]);
-    }
+    constexpr int JB = 8;
+    for (int i = threadIdx.x + 2; i <= nx - 1; i += blockDim.x)
+        for (int j0 = 2; j0 <= nyg - 1; j0 += JB) {
+            T u[JB];
+#pragma unroll
+            for (int r = 0; r < JB; r++) u[r] = (j0 + r <= nyg - 1) ? U(i, j0 + r, k) : T(0);
+#pragma unroll
+            for (int r = 0; r < JB; r++)
+                if (j0 + r <= nyg - 1) s += cw[j0 + r] * (double)u[r];
+        }
     s = block_sum(s, sh);
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
@@ -474,6 +698,7 @@ __global__ void k_mass_final(const double *part, int n, DevScal *ds, int mode, d
     else if (mode == 2) corr = ds->Ucenterline_x - s / norm;
     else corr = ds->Qflow_y_0 - s / norm;
     ds->lmax[2] = corr;  // scratch slot: correction before division by dt
+    ds->corrf = (float)corr;
 }
 
 // add the correction to the interior and store dPdx = corr/dt
@@ -483,19 +708,26 @@ __global__ void k_mass_apply(Fld<T> F, Fld<T> Flo, DevScal *ds, int i1, int j1, 
     int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
     int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
     int k = blockIdx.z + 2;
-    double corr = ds->lmax[2];
     if (i == 2 && j == 2 && k == 2) {
+        double corr = ds->lmax[2];
         if (mode == 3) ds->dPdy = corr / ds->dt;
-        else ds->dPdx = corr / ds->dt;
+        else {
+            ds->dPdx = corr / ds->dt;
+            ds->dPdxf = (float)ds->dPdx;
+        }
     }
     if (i > i1 || j > j1 || k > k1) return;
-    if (Flo.p) {
-        double v = (double)F(i, j, k) + (double)Flo(i, j, k) + corr;
-        T hi = (T)v;
-        F(i, j, k) = hi;
-        Flo(i, j, k) = (T)(v - (double)hi);
+    if constexpr (sizeof(T) == 4) {
+        if (Flo.p) {
+            float hi = F(i, j, k), lo = Flo(i, j, k);
+            ff_add(hi, lo, ds->corrf);
+            F(i, j, k) = hi;
+            Flo(i, j, k) = lo;
+            return;
+        }
+        F(i, j, k) = F(i, j, k) + ds->corrf;
     } else {
-        F(i, j, k) = (T)((double)F(i, j, k) + corr);
+        F(i, j, k) = F(i, j, k) + ds->lmax[2];
     }
 }
 
@@ -567,21 +799,56 @@ __device__ __forceinline__ void atomic_min_pos(double *a, double v) {
 
 template <typename T>
 __global__ void k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, double *mu, double *mv, double *mw) {
-    int k = blockIdx.x + 2;
-    double wmin = INFINITY;
-    for (int j = 2; j <= nyg - 1; j++) {
-        double vmin = INFINITY;
-        for (int i = threadIdx.x + 2; i <= nxg - 1; i += blockDim.x) {
-            double u = fabs((double)U(i, j, k)), v = fabs((double)V(i, j, k)), w = fabs((double)W(i, j, k));
-            atomic_min_pos(&mu[i], u);
-            vmin = fmin(vmin, v);
-            wmin = fmin(wmin, w);
+    // one block per k plane (blockDim 128): min |U| per i over j, min |V| per j
+    // over i, min |W| over the plane; rows are read JB at a time so that the
+    // loads of a group are in flight together.  One global atomic per index
+    // per block; minima in the state's precision, widened exactly.
+    constexpr int JB = 8;
+    __shared__ T vsm[4][520];
+    int k = blockIdx.x + 2, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    T wmin = T(INFINITY);
+    T umin[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) umin[q] = T(INFINITY);
+    for (int j0 = 2; j0 <= nyg - 1; j0 += JB) {
+        T vmin[JB];
+#pragma unroll
+        for (int r = 0; r < JB; r++) vmin[r] = T(INFINITY);
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+            int i = threadIdx.x + 2 + q * blockDim.x;
+            if (i <= nxg - 1) {
+#pragma unroll
+                for (int r = 0; r < JB; r++) {
+                    int j = j0 + r;
+                    if (j <= nyg - 1) {
+                        umin[q] = fmin(umin[q], fabs(U(i, j, k)));
+                        wmin = fmin(wmin, fabs(W(i, j, k)));
+                        vmin[r] = fmin(vmin[r], fabs(V(i, j, k)));
+                    }
+                }
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) vmin = fmin(vmin, __shfl_down_sync(0xffffffff, vmin, o));
-        if ((threadIdx.x & 31) == 0) atomic_min_pos(&mv[j], vmin);
+#pragma unroll
+        for (int r = 0; r < JB; r++) {
+            T v = vmin[r];
+            for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffff, v, o));
+            if (lane == 0 && j0 + r <= nyg - 1) vsm[wp][j0 + r] = v;
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        int i = threadIdx.x + 2 + q * blockDim.x;
+        if (i <= nxg - 1) atomic_min_pos(&mu[i], (double)umin[q]);
     }
     for (int o = 16; o > 0; o >>= 1) wmin = fmin(wmin, __shfl_down_sync(0xffffffff, wmin, o));
-    if ((threadIdx.x & 31) == 0) atomic_min_pos(&mw[k], wmin);
+    if (lane == 0) atomic_min_pos(&mw[k], (double)wmin);
+    __syncthreads();
+    for (int j = threadIdx.x + 2; j <= nyg - 1; j += blockDim.x) {
+        T m = vsm[0][j];
+        for (int q = 1; q < (int)(blockDim.x >> 5); q++) m = fmin(m, vsm[q][j]);
+        atomic_min_pos(&mv[j], (double)m);
+    }
 }
 
 __global__ void k_dt_init(double *m, int n) {
@@ -591,11 +858,23 @@ __global__ void k_dt_init(double *m, int n) {
 
 __global__ void k_dt_final(const double *mu, const double *mv, const double *mw, Geo g, DevScal *ds, double CFL,
                            double dt_vis) {
-    if (threadIdx.x != 0) return;
+    __shared__ double sh[3][32];
     double lU = 0.0, lV = 0.0, lW = 0.0;
-    for (int i = 2; i <= g.nxg - 1; i++) lU = fmax(lU, (g.xg[i + 1] - g.xg[i]) / mu[i]);
-    for (int j = 2; j <= g.nyg - 1; j++) lV = fmax(lV, (g.yg[j + 1] - g.yg[j]) / mv[j]);
-    for (int k = 2; k <= g.nzg - 1; k++) lW = fmax(lW, (g.zg[k + 1] - g.zg[k]) / mw[k]);
+    for (int i = threadIdx.x + 2; i <= g.nxg - 1; i += blockDim.x) lU = fmax(lU, (g.xg[i + 1] - g.xg[i]) / mu[i]);
+    for (int j = threadIdx.x + 2; j <= g.nyg - 1; j += blockDim.x) lV = fmax(lV, (g.yg[j + 1] - g.yg[j]) / mv[j]);
+    for (int k = threadIdx.x + 2; k <= g.nzg - 1; k += blockDim.x) lW = fmax(lW, (g.zg[k + 1] - g.zg[k]) / mw[k]);
+    for (int o = 16; o > 0; o >>= 1) {
+        lU = fmax(lU, __shfl_down_sync(0xffffffff, lU, o));
+        lV = fmax(lV, __shfl_down_sync(0xffffffff, lV, o));
+        lW = fmax(lW, __shfl_down_sync(0xffffffff, lW, o));
+    }
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[0][w] = lU; sh[1][w] = lV; sh[2][w] = lW; }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+        lU = fmax(lU, sh[0][q]); lV = fmax(lV, sh[1][q]); lW = fmax(lW, sh[2][q]);
+    }
     double du = CFL * lU, dv = CFL * lV, dw = CFL * lW;
     double dt_conv = fmin(du, fmin(dv, dw));
     double dt = fmin(dt_conv, dt_vis);
@@ -603,6 +882,7 @@ __global__ void k_dt_final(const double *mu, const double *mv, const double *mw,
     if (CFL < 0) dt = -CFL;
     if (ds->fixed_dt > 0) dt = ds->fixed_dt;
     ds->dt = dt;
+    ds->dtf = (float)dt;
     ds->lmax[0] = lU;
     ds->lmax[1] = lV;
 }
@@ -622,7 +902,7 @@ int launch_dt(cf_ctx *ctx, int b) {
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
            vw = CFL * pow(ctx->dzmin, 2.0) / ctx->prm.nu;
     double dt_vis = fmin(vu, fmin(vv, vw));
-    k_dt_final<<<1, 32, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
+    k_dt_final<<<1, 256, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
     count_launch(ctx, "k_dt_final");
     CF_CUDA(cudaGetLastError());
     return 0;

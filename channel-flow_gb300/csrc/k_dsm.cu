@@ -212,12 +212,16 @@ __global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, in
             b += part[((long)(j - 2) * nchunk + q) * 2 + 1];
         }
         avg[j] = a / b;
+        ((float *)(avg + nyg + 2))[j] = (float)(a / b);  // FP32 copy for the split path
     }
 }
 __global__ void k_dsm_e2(int nyg, double *avg, int dirichlet) {
     if (threadIdx.x == 0) {
         avg[1] = dirichlet ? -avg[2] : avg[2];
         avg[nyg] = dirichlet ? -avg[nyg - 1] : avg[nyg - 1];
+        float *af = (float *)(avg + nyg + 2);
+        af[1] = (float)avg[1];
+        af[nyg] = (float)avg[nyg];
     }
 }
 
@@ -231,7 +235,10 @@ __global__ void k_dsm_f(Fld<T> nt, const T *Sq, const double *avg, Can c, int nx
     if (i > nxg || j > nyg) return;
     int jj = j == 1 ? 2 : (j == nyg ? nyg - 1 : j);
     int is = wrapc(i, c.nxp), ks = wrapc(k, c.nzp);
-    T v = T(-0.5) * (T)avg[jj] * Sq[c(is, jj, ks)];
+    T a;
+    if constexpr (sizeof(T) == 4) a = ((const float *)(avg + nyg + 2))[jj];
+    else a = avg[jj];
+    T v = T(-0.5) * a * Sq[c(is, jj, ks)];
     v = v > T(0) ? v : T(0);
     if (jj != j && dirichlet) v = -v;
     nt(i, j, k) = v;
@@ -255,14 +262,31 @@ int launch_nut_zero(cf_ctx *ctx) {
 
 template <typename T>
 int launch_dsm(cf_ctx *ctx, int b) {
-    GeoT<T> g = geo_of<T>(ctx);
+    int dir = ctx->prm.Dirichlet_nu_t == 1;
     Can c;
     c.nxp = ctx->nxp; c.nym = ctx->nym; c.nzp = ctx->nzp; c.n = (long)ctx->nCan;
+    dim3 blk(32, 4, 1);
+    if (ctx->use_fused_dsm && ctx->prm.iwall_model == 0 && ctx->state_periodic) {
+        // one pass: |S| and the plane partial sums (k_dsm_fused.cu)
+        int rc = launch_dsm_fused<T>(ctx, b);
+        if (rc) return rc;
+        int nch = ctx->dsm_nchunk_fused;
+        k_dsm_e<<<cdiv(ctx->nym, 64), 64, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir);
+        k_dsm_e2<<<1, 32, 0, ctx->st>>>(ctx->nyg, ctx->avg_nu_t, dir);
+        count_launch(ctx, "k_dsm_e"); count_launch(ctx, "k_dsm_e2");
+        Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+        T *q = (T *)ctx->dsm_q;
+        k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(
+            nt, q + Q_S * c.n, ctx->avg_nu_t, c, ctx->nxg, ctx->nyg, ctx->nzg, dir);
+        count_launch(ctx, "k_dsm_f");
+        CF_CUDA(cudaGetLastError());
+        return 0;
+    }
+    GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
     Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
     T *q = (T *)ctx->dsm_q, *lf = (T *)ctx->dsm_lf;
-    dim3 blk(32, 4, 1);
     dim3 grdc(cdiv(ctx->nxp, 32), cdiv(ctx->nym, 4), ctx->nzp);
     k_dsm_a<T><<<grdc, blk, 0, ctx->st>>>(g, U, V, W, q, c);
     count_launch(ctx, "k_dsm_a");
@@ -278,7 +302,6 @@ int launch_dsm(cf_ctx *ctx, int b) {
     int nchunk = ctx->dsm_nblk;
     k_dsm_d<T><<<dim3(nchunk, ctx->nym), 256, 0, ctx->st>>>(g, Uf, Vf, Wf, lf, c, ctx->dsm_part, nchunk);
     count_launch(ctx, "k_dsm_d");
-    int dir = ctx->prm.Dirichlet_nu_t == 1;
     k_dsm_e<<<cdiv(ctx->nym, 64), 64, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
     k_dsm_e2<<<1, 32, 0, ctx->st>>>(ctx->nyg, ctx->avg_nu_t, dir);
     count_launch(ctx, "k_dsm_e"); count_launch(ctx, "k_dsm_e2");

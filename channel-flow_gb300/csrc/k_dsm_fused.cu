@@ -1,0 +1,376 @@
+// k_dsm_fused.cu -- the dynamic Smagorinsky pass (subgrid.f90:376-538) as one
+// kernel that reads U, V, W once and writes |S| plus the plane partial sums of
+// L.M and M.M.
+//
+// A block owns a TX x TY tile of canonical centres and marches along z over a
+// chunk of planes.  Everything the pass needs at an output plane k is built
+// from shared-memory rings of three planes:
+//   R(p)  raw U, V, W on the tile plus 2 halo cells           (plane p)
+//   G(p)  U, V, W filtered in x and y on the tile + 1 halo    (plane p)
+//   F(p)  Uf, Vf, Wf = z-filter of G(p-1..p+1)                 (plane p)
+//   Q(p)  centre velocities, their products, |S| S_ij and |S| (plane p, one)
+// The x-y filter of the 15 Q quantities at a thread's own point is spread
+// into z-accumulators held in registers (weights 1/6, 2/3, 1/6 to planes
+// p-1, p, p+1), so L_ij and hat(|S| S_ij) of plane k are complete once Q(k+1)
+// has been filtered; M_ij then needs S_ij of Uf, Vf, Wf at k, i.e. F(k-1..k+1).
+// With raw plane r entering the ring, the block therefore emits plane r-2.
+//
+// The halo is read through the periodic wrap, which reproduces the
+// reference's periodic copies whenever U, V, W are themselves periodic in x
+// and z -- true after apply_boundary_conditions with no-slip walls
+// (iwall_model 0).  The plane sums count the duplicate column i = nxg-1 and
+// plane k = nzg-1 of the reference's loops as weight 2 on i = 2, k = 2.
+#include <type_traits>
+
+#include "cf_internal.cuh"
+
+// periodic index for i in [2 - np, 2 np + 1]
+__device__ __forceinline__ int wrapq(int i, int np) { return i < 2 ? i + np : (i > np + 1 ? i - np : i); }
+
+struct RGeo {  // reciprocal spacings, 1-based like the coordinates
+    const void *rdx, *rdxg, *rdy, *rdyg, *rdz, *rdzg;
+};
+
+template <typename T, int TX, int TY>
+struct DsmSmem {
+    static constexpr int RX = TX + 4, RY = TY + 4, QX = TX + 2, QY = TY + 2;
+    static constexpr int NR = 9 * RX * RY, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY;
+    static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ) * sizeof(T);
+};
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld<T> W, RGeo rgv, int nx, int ny, int nyg,
+                                                      int nz, int nxp, int nzp, int kc_len, T *Sout, double *part,
+                                                      int nchunk) {
+    typedef DsmSmem<T, TX, TY> SM;
+    constexpr int RX = SM::RX, RY = SM::RY, QX = SM::QX, QY = SM::QY;
+    extern __shared__ unsigned char sm_raw[];
+    T *R = (T *)sm_raw;         // [slot 3][field 3][RY][RX]
+    T *G = R + SM::NR;          // [slot 3][field 3][QY][QX]
+    T *F = G + SM::NG;          // [slot 3][field 3][QY][QX]
+    T *Qs = F + SM::NF;         // [16][QY][QX]
+    const T *rdx = (const T *)rgv.rdx, *rdxg = (const T *)rgv.rdxg, *rdy = (const T *)rgv.rdy,
+            *rdyg = (const T *)rgv.rdyg, *rdz = (const T *)rgv.rdz, *rdzg = (const T *)rgv.rdzg;
+    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0), h = T(0.5), qq = T(0.25);
+
+    const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
+    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, nz - 1);
+    const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+    const int io = i0 + tx, jo = j0 + ty;
+    const bool own = io <= nx - 1 && jo <= nyg - 1;
+    auto RS = [&](int slot, int f, int sy, int sx) -> T & { return R[((slot * 3 + f) * RY + sy) * RX + sx]; };
+    auto GS = [&](int slot, int f, int sy, int sx) -> T & { return G[((slot * 3 + f) * QY + sy) * QX + sx]; };
+    auto FS = [&](int slot, int f, int sy, int sx) -> T & { return F[((slot * 3 + f) * QY + sy) * QX + sx]; };
+    auto QS = [&](int q, int sy, int sx) -> T & { return Qs[(q * QY + sy) * QX + sx]; };
+
+    // y filter weights of a row in [lo, hi] (one-sided at the ends)
+    auto yw = [&](int j, int lo, int hi, T &wm, T &w0, T &wp) {
+        if (j <= lo) { wm = T(0); w0 = f23; wp = f13; }
+        else if (j >= hi) { wm = f13; w0 = f23; wp = T(0); }
+        else { wm = f6; w0 = f23; wp = f6; }
+    };
+    const T fw[3] = {f6, f23, f6};
+
+    // reciprocal spacings of the region columns and rows (z is per plane)
+    __shared__ T gsx[3][QX], gsy[3][QY];
+    for (int t = tid; t < QX; t += TX * TY) {
+        int ic = wrapq(i0 + t - 1, nxp);
+        gsx[0][t] = rdx[ic];
+        gsx[1][t] = rdxg[ic];
+        gsx[2][t] = rdxg[ic + 1];
+    }
+    for (int t = tid; t < QY; t += TX * TY) {
+        int jj = min(max(j0 + t - 1, 2), nyg - 1);
+        gsy[0][t] = rdy[jj];
+        gsy[1][t] = rdyg[jj];
+        gsy[2][t] = rdyg[jj + 1];
+    }
+    T acc[3][15];
+#pragma unroll
+    for (int s = 0; s < 3; s++)
+#pragma unroll
+        for (int q = 0; q < 15; q++) acc[s][q] = T(0);
+    T Sprev = T(0);
+    T sl = T(0), smm = T(0);  // this thread's plane sums (widened per block)
+
+    const int rs = kb - 2, re = ke + 2;
+    // one march step for raw plane r; PH = (r - rs) % 3 is the ring phase
+    // raw-tile elements of this thread (same for every plane)
+    constexpr int NTH = TX * TY, NRP = RX * RY, NLR = (NRP + NTH - 1) / NTH;
+    int eia[NLR], eja[NLR], ers[NLR];
+#pragma unroll
+    for (int q = 0; q < NLR; q++) {
+        int rem = tid + q * NTH;
+        ers[q] = rem;
+        int sy = rem / RX, sx = rem - sy * RX;
+        eia[q] = wrapq(i0 + sx - 2, nxp);
+        eja[q] = j0 + sy - 2;
+    }
+    T pre[3][NLR];
+    auto fetch = [&](int r) {  // issue every load of raw plane r
+        const int kc = wrapc(r, nzp);
+#pragma unroll
+        for (int q = 0; q < NLR; q++) {
+            const bool in = ers[q] < NRP;
+            const int ia = eia[q], ja = eja[q];
+            pre[0][q] = (in && ja >= 1 && ja <= nyg) ? U(ia, ja, kc) : T(0);
+            pre[1][q] = (in && ja >= 1 && ja <= ny) ? V(ia, ja, kc) : T(0);
+            pre[2][q] = (in && ja >= 1 && ja <= nyg) ? W(ia, ja, kc) : T(0);
+        }
+    };
+    auto commit = [&](int slot) {
+#pragma unroll
+        for (int q = 0; q < NLR; q++)
+            if (ers[q] < NRP) {
+#pragma unroll
+                for (int f = 0; f < 3; f++) R[(slot * 3 + f) * NRP + ers[q]] = pre[f][q];
+            }
+    };
+    // one march step for raw plane r; PH = (r - rs) % 3 is the ring phase.
+    // On entry R(r) is in slot PH; R(r+1) is fetched during the step.
+    auto step = [&](int r, auto PHc) {
+        constexpr int PH = decltype(PHc)::value;
+        constexpr int P1 = (PH + 1) % 3, P2 = (PH + 2) % 3;
+        if (r + 1 <= re) fetch(r + 1);
+        // -- G(r): x-y filtered U, V, W on the tile + 1 halo
+        for (int t = tid; t < 3 * QX * QY; t += TX * TY) {
+            int f = t / (QX * QY), rem = t % (QX * QY), sy = rem / QX, sx = rem % QX;
+            int j = j0 + sy - 1;
+            int jhi = f == 1 ? ny : nyg;
+            T g = T(0);
+            if (j >= 1 && j <= jhi) {
+                T wm, w0, wp;
+                yw(j, 1, jhi, wm, w0, wp);
+                int dm = j > 1 ? -1 : 0, dp = j < jhi ? 1 : 0;
+#pragma unroll
+                for (int a = -1; a <= 1; a++) {
+                    int rx = sx + 1 + a, ry = sy + 1;
+                    T yv = wm * RS(PH, f, ry + dm, rx) + w0 * RS(PH, f, ry, rx) + wp * RS(PH, f, ry + dp, rx);
+                    g += fw[a + 1] * yv;
+                }
+            }
+            GS(PH, f, sy, sx) = g;
+        }
+        __syncthreads();
+        if (r >= kb) {
+            // -- F(r-1) = z filter of G(r-2), G(r-1), G(r)
+            for (int t = tid; t < 3 * QX * QY; t += TX * TY) {
+                int f = t / (QX * QY), rem = t % (QX * QY), sy = rem / QX, sx = rem % QX;
+                FS(P2, f, sy, sx) = f6 * GS(P1, f, sy, sx) + f23 * GS(P2, f, sy, sx) + f6 * GS(PH, f, sy, sx);
+            }
+            // -- Q(r-1) from R(r-2) [P1], R(r-1) [P2], R(r) [PH]
+            const int kq = wrapc(r - 1, nzp);
+            const T rz = rdz[kq], rzg0 = rdzg[kq], rzg1 = rdzg[kq + 1];
+            for (int t = tid; t < QX * QY; t += TX * TY) {
+                int sy = t / QX, sx = t % QX;
+                int j = j0 + sy - 1;
+                if (j < 2 || j > nyg - 1) {
+#pragma unroll
+                    for (int q = 0; q < 16; q++) QS(q, sy, sx) = T(0);
+                    continue;
+                }
+                int rx = sx + 1, ry = sy + 1;  // raw slot of the centre
+                // raw accessors with offsets (di, dj, dk), dk in {-1, 0, 1}
+                auto u = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 0, ry + dj, rx + di); };
+                auto v = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 1, ry + dj, rx + di); };
+                auto w = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 2, ry + dj, rx + di); };
+                T uc = h * (u(-1, 0, 0) + u(0, 0, 0));
+                T vc = h * (v(0, -1, 0) + v(0, 0, 0));
+                T wc = h * (w(0, 0, -1) + w(0, 0, 0));
+                // compute_Sij (subgrid.f90:900-946)
+                const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
+                const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
+                T s0 = (u(0, 0, 0) - u(-1, 0, 0)) * rx0;
+                T s1 = (v(0, 0, 0) - v(0, -1, 0)) * ry0;
+                T s2 = (w(0, 0, 0) - w(0, 0, -1)) * rz;
+                T s3 = T(0), s4 = T(0), s5 = T(0);
+#pragma unroll
+                for (int a = 0; a < 2; a++)
+#pragma unroll
+                    for (int b = 0; b < 2; b++) {
+                        const T rxa = a ? rxg1 : rxg0, ryb = b ? ryg1 : ryg0, rzb = b ? rzg1 : rzg0, rya = a ? ryg1 : ryg0;
+                        s3 += h * ((u(a - 1, b, 0) - u(a - 1, b - 1, 0)) * ryb + (v(a, b - 1, 0) - v(a - 1, b - 1, 0)) * rxa);
+                        s4 += h * ((u(a - 1, 0, b) - u(a - 1, 0, b - 1)) * rzb + (w(a, 0, b - 1) - w(a - 1, 0, b - 1)) * rxa);
+                        s5 += h * ((v(0, a - 1, b) - v(0, a - 1, b - 1)) * rzb + (w(0, a, b - 1) - w(0, a - 1, b - 1)) * rya);
+                    }
+                s3 *= qq; s4 *= qq; s5 *= qq;
+                T S = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
+                           T(4) * s5 * s5);
+                QS(0, sy, sx) = uc; QS(1, sy, sx) = vc; QS(2, sy, sx) = wc;
+                QS(3, sy, sx) = uc * uc; QS(4, sy, sx) = vc * vc; QS(5, sy, sx) = wc * wc;
+                QS(6, sy, sx) = uc * vc; QS(7, sy, sx) = uc * wc; QS(8, sy, sx) = vc * wc;
+                QS(9, sy, sx) = S * s0; QS(10, sy, sx) = S * s1; QS(11, sy, sx) = S * s2;
+                QS(12, sy, sx) = S * s3; QS(13, sy, sx) = S * s4; QS(14, sy, sx) = S * s5;
+                QS(15, sy, sx) = S;
+            }
+        }
+        __syncthreads();
+        if (r >= kb && own) {
+            // -- x-y filter of Q(r-1) at the own point, spread over planes r-2, r-1, r
+            T wm, w0, wp;
+            yw(jo, 2, nyg - 1, wm, w0, wp);
+            const int sx = tx + 1, sy = ty + 1;
+            const int dm = jo > 2 ? -1 : 0, dp = jo < nyg - 1 ? 1 : 0;
+#pragma unroll
+            for (int q = 0; q < 15; q++) {
+                T a = T(0);
+#pragma unroll
+                for (int d = -1; d <= 1; d++)
+                    a += fw[d + 1] * (wm * QS(q, sy + dm, sx + d) + w0 * QS(q, sy, sx + d) + wp * QS(q, sy + dp, sx + d));
+                acc[P1][q] += f6 * a;   // plane r-2 (last contribution)
+                acc[P2][q] += f23 * a;  // plane r-1
+                acc[PH][q] = f6 * a;    // plane r (first contribution; the slot held plane r-3)
+            }
+            if (r >= kb + 2) {
+                // -- output plane k = r-2: S_ij of Uf, Vf, Wf from F(r-3) [PH], F(r-2) [P1], F(r-1) [P2]
+                const int k = r - 2, kcn = wrapc(k, nzp);
+                auto uf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 0, sy + dj, sx + di); };
+                auto vf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 1, sy + dj, sx + di); };
+                auto wf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 2, sy + dj, sx + di); };
+                const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
+                const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
+                const T rz = rdz[kcn], rzg0 = rdzg[kcn], rzg1 = rdzg[kcn + 1];
+                T s0 = (uf(0, 0, 0) - uf(-1, 0, 0)) * rx0;
+                T s1 = (vf(0, 0, 0) - vf(0, -1, 0)) * ry0;
+                T s2 = (wf(0, 0, 0) - wf(0, 0, -1)) * rz;
+                T s3 = T(0), s4 = T(0), s5 = T(0);
+#pragma unroll
+                for (int a = 0; a < 2; a++)
+#pragma unroll
+                    for (int b = 0; b < 2; b++) {
+                        const T rxa = a ? rxg1 : rxg0, ryb = b ? ryg1 : ryg0, rzb = b ? rzg1 : rzg0, rya = a ? ryg1 : ryg0;
+                        s3 += h * ((uf(a - 1, b, 0) - uf(a - 1, b - 1, 0)) * ryb + (vf(a, b - 1, 0) - vf(a - 1, b - 1, 0)) * rxa);
+                        s4 += h * ((uf(a - 1, 0, b) - uf(a - 1, 0, b - 1)) * rzb + (wf(a, 0, b - 1) - wf(a - 1, 0, b - 1)) * rxa);
+                        s5 += h * ((vf(0, a - 1, b) - vf(0, a - 1, b - 1)) * rzb + (wf(0, a, b - 1) - wf(0, a - 1, b - 1)) * rya);
+                    }
+                s3 *= qq; s4 *= qq; s5 *= qq;
+                T Sf = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
+                            T(4) * s5 * s5);
+                const T fs2 = T(4);  // fil_size**2 (subgrid.f90:156, 463)
+                const T sf[6] = {s0, s1, s2, s3, s4, s5};
+                const T fu = acc[P1][0], fv = acc[P1][1], fwv = acc[P1][2];
+                const T pa[6] = {fu, fv, fwv, fu, fu, fv}, pb[6] = {fu, fv, fwv, fv, fwv, fwv};
+                T lm = T(0), mm = T(0);
+#pragma unroll
+                for (int q = 0; q < 6; q++) {
+                    T L = acc[P1][3 + q] - pa[q] * pb[q];
+                    T M = fs2 * Sf * sf[q] - acc[P1][9 + q];
+                    T wq = q < 3 ? T(1) : T(2);
+                    lm += wq * L * M;
+                    mm += wq * M * M;
+                }
+                T wgt = (io == 2 ? T(2) : T(1)) * (kcn == 2 ? T(2) : T(1));
+                sl += wgt * lm;
+                smm += wgt * mm;
+                Sout[(long)(io - 2) + (long)nxp * ((jo - 2) + (long)(nyg - 2) * (kcn - 2))] = Sprev;
+            }
+            Sprev = QS(15, sy, sx);  // |S| at plane r-1 for the next output
+        }
+        // R(r-2) (slot P1) was last read by Q(r-1): R(r+1) takes its place
+        if (r + 1 <= re) commit(P1);
+        __syncthreads();
+    };
+    fetch(rs);
+    commit(0);
+    __syncthreads();
+    std::integral_constant<int, 0> c0;
+    std::integral_constant<int, 1> c1;
+    std::integral_constant<int, 2> c2;
+    for (int r = rs; r <= re; r += 3) {
+        step(r, c0);
+        if (r + 1 <= re) step(r + 1, c1);
+        if (r + 2 <= re) step(r + 2, c2);
+    }
+    // plane partials of this block for row jo: reduce over the TX threads of the row
+    __syncthreads();
+    double *red = (double *)sm_raw;  // 2 * TX * TY doubles fit in the R ring
+    red[2 * tid] = own ? (double)sl : 0.0;
+    red[2 * tid + 1] = own ? (double)smm : 0.0;
+    __syncthreads();
+    if (tx == 0 && jo <= nyg - 1) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < TX; q++) {
+            a += red[2 * (ty * TX + q)];
+            b += red[2 * (ty * TX + q) + 1];
+        }
+        int chunk = blockIdx.x * gridDim.z + blockIdx.z;
+        part[((long)(jo - 2) * nchunk + chunk) * 2] = a;
+        part[((long)(jo - 2) * nchunk + chunk) * 2 + 1] = b;
+    }
+}
+
+template <typename T>
+static void *rgeo_ptr(cf_ctx *ctx) {
+    return sizeof(T) == 8 ? (void *)ctx->d_rgeo : (void *)ctx->d_rgeo_f;
+}
+
+template <typename T, int TX, int TY>
+static int launch_fused_cfg(cf_ctx *ctx, int b, int kc_len) {
+    Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    RGeo rg;
+    T *base = (T *)rgeo_ptr<T>(ctx);
+    rg.rdx = base + ctx->rgeo_off[0];
+    rg.rdxg = base + ctx->rgeo_off[1];
+    rg.rdy = base + ctx->rgeo_off[2];
+    rg.rdyg = base + ctx->rgeo_off[3];
+    rg.rdz = base + ctx->rgeo_off[4];
+    rg.rdzg = base + ctx->rgeo_off[5];
+    int ntx = cdiv(ctx->nxp, TX), nty = cdiv(ctx->nym, TY), nkc = cdiv(ctx->nzp, kc_len);
+    int nchunk = ntx * nkc;
+    T *S = (T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
+    size_t sm = DsmSmem<T, TX, TY>::bytes;
+    k_dsm_fused<T, TX, TY><<<dim3(ntx, nty, nkc), TX * TY, sm, ctx->st>>>(U, V, W, rg, ctx->nx, ctx->ny, ctx->nyg, ctx->nz,
+                                                                        ctx->nxp, ctx->nzp, kc_len, S, ctx->dsm_part,
+                                                                        nchunk);
+    count_launch(ctx, "k_dsm_fused");
+    ctx->dsm_nchunk_fused = nchunk;
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// tile shapes: FP32 32 x 8, FP64 16 x 8 (the FP64 kernel needs more registers
+// and twice the shared memory per tile)
+template <typename T> struct DsmCfg;
+template <> struct DsmCfg<float> { static constexpr int TX = 32, TY = 8; };
+template <> struct DsmCfg<double> { static constexpr int TX = 16, TY = 8; };
+
+int dsm_fused_setup() {
+    cudaFuncSetAttribute(k_dsm_fused<float, DsmCfg<float>::TX, DsmCfg<float>::TY>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)DsmSmem<float, DsmCfg<float>::TX, DsmCfg<float>::TY>::bytes);
+    cudaFuncSetAttribute(k_dsm_fused<double, DsmCfg<double>::TX, DsmCfg<double>::TY>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)DsmSmem<double, DsmCfg<double>::TX, DsmCfg<double>::TY>::bytes);
+    return 0;
+}
+
+// z-chunk length: about one full wave of resident blocks
+template <typename T>
+static int plan_t(int nxp, int nym, int nzp, int sms, int *kc, size_t *nchunk) {
+    constexpr int TX = DsmCfg<T>::TX, TY = DsmCfg<T>::TY;
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dsm_fused<T, TX, TY>, TX * TY,
+                                                  DsmSmem<T, TX, TY>::bytes);
+    per_sm = per_sm < 1 ? 1 : per_sm;
+    long tiles = (long)cdiv(nxp, TX) * cdiv(nym, TY);
+    long nkc = (long)per_sm * sms / (tiles > 0 ? tiles : 1);
+    if (nkc < 1) nkc = 1;
+    if (nkc > nzp / 8) nkc = nzp / 8 > 0 ? nzp / 8 : 1;
+    *kc = cdiv(nzp, nkc);
+    *nchunk = (size_t)cdiv(nxp, TX) * cdiv(nzp, *kc);
+    return 0;
+}
+
+int dsm_fused_plan(int esz, int nxp, int nym, int nzp, int sms, int *kc, size_t *nchunk) {
+    return esz == 8 ? plan_t<double>(nxp, nym, nzp, sms, kc, nchunk) : plan_t<float>(nxp, nym, nzp, sms, kc, nchunk);
+}
+
+template <typename T>
+int launch_dsm_fused(cf_ctx *ctx, int b) {
+    return launch_fused_cfg<T, DsmCfg<T>::TX, DsmCfg<T>::TY>(ctx, b, ctx->dsm_kc);
+}
+
+template int launch_dsm_fused<double>(cf_ctx *, int);
+template int launch_dsm_fused<float>(cf_ctx *, int);

@@ -188,80 +188,109 @@ __global__ void k_fft_z(typename C2<T>::t *spec, FftPlan pl, const typename C2<T
 }
 
 // ---------------------------------------------------------------------------
-// Tridiagonal solve per (kx, kz) along j (projection.f90:90-113) with the
-// zgtsv elimination; one thread per mode, threads adjacent in kx.
+// Tridiagonal solve per (kx, kz) along j (projection.f90:90-113).  The
+// matrices D(j) = Dyy(j,j) + kxx + kzz (with D(2)*1.5 for the (0,0) mode)
+// never change, so zgtsv's elimination -- pivot choices, multipliers and the
+// final U factor -- is done once on the host (tri_factor) and a solve only
+// replays its right-hand-side operations: one thread per mode, adjacent
+// threads adjacent in kx, factors stored (row, kz, kx) for coalescing.
+//   fwd q: no pivot: b[q+1] -= m_q b[q]
+//          pivot:    (b[q], b[q+1]) <- (b[q+1], b[q] - m_q b[q+1])
+//   back:  b[q] = (b[q] - du_q b[q+1] - dl_q b[q+2]) * rd_q
 // ---------------------------------------------------------------------------
-template <typename T, int NMAX>
-__global__ void k_tri(typename C2<T>::t *spec, const double *tri, int nym, int nh, int nzp, int nxp) {
+struct TriFac {
+    const double *m, *rd, *du, *dl;  // [nym][nzp][nh]
+    const unsigned char *piv;        // [nym][nzp][nh]
+};
+
+template <typename T>
+__global__ void __launch_bounds__(64) k_tri(typename C2<T>::t *__restrict__ spec, TriFac f, int nym, int nh, int nzp) {
+    // 64 modes (consecutive kx, one kz) per block; rows move through shared
+    // memory RB at a time with coalesced loads, so each thread's serial
+    // recurrence never waits on a global load.
     typedef typename C2<T>::t C;
-    int kx = blockIdx.x * blockDim.x + threadIdx.x, kz = blockIdx.y;
-    if (kx >= nh) return;
-    const double *Dd = tri, *Dl = tri + nym, *Du = tri + 2 * nym, *kxx = tri + 3 * nym, *kzz = kxx + nxp;
-    double shift = kxx[kx] + kzz[kz];
-    double d[NMAX], du[NMAX], dl[NMAX];
-    const long stride = nh;
-    C *col = spec + (long)kz * nym * nh + kx;
-    for (int q = 0; q < nym; q++) {
-        d[q] = Dd[q] + kxx[kx] + kzz[kz];
-        du[q] = Du[q];
-        dl[q] = Dl[q];
-    }
-    (void)shift;
-    if (kx == 0 && kz == 0) d[0] = 3.0 / 2.0 * d[0];  // projection.f90:107
-    // forward elimination (zgtsv), right-hand side in place in spec
-    C bq = col[0];
-    double br = bq.x, bi = bq.y;
-    for (int q = 0; q < nym - 1; q++) {
-        C bn = col[(q + 1) * stride];
-        double nr = bn.x, ni = bn.y;
-        if (dl[q] == 0.0) {
-            // no elimination needed (a zero pivot is not reachable: Dyy rows
-            // are diagonally dominant with a negative shift)
-        } else if (fabs(d[q]) >= fabs(dl[q])) {
-            double mult = dl[q] / d[q];
-            d[q + 1] = d[q + 1] - mult * du[q];
-            nr = nr - mult * br;
-            ni = ni - mult * bi;
-            if (q < nym - 2) dl[q] = 0.0;
-        } else {
-            double mult = d[q] / dl[q];
-            d[q] = dl[q];
-            double temp = d[q + 1];
-            d[q + 1] = du[q] - mult * temp;
-            if (q < nym - 2) {
-                dl[q] = du[q + 1];
-                du[q + 1] = -mult * dl[q];
+    constexpr int RB = 16, NT = 64;
+    __shared__ C sb[RB][NT];
+    __shared__ double sm_[RB][NT], s2[RB][NT], s3[RB][NT];
+    __shared__ unsigned char sp[RB][NT];
+    const int kx0 = blockIdx.x * NT, kz = blockIdx.y, t = threadIdx.x, kx = kx0 + t;
+    const bool act = kx < nh;
+    const long stride = nh, fs = (long)nzp * nh, f0 = (long)kz * nh;
+    C *col = spec + (long)kz * nym * nh;
+    double br = 0.0, bi = 0.0;
+    if (act) { C b0 = col[kx]; br = b0.x; bi = b0.y; }
+    // forward: rows q = 0 .. nym-2 eliminate into row q+1
+    for (int q0 = 0; q0 < nym - 1; q0 += RB) {
+        int nr = min(RB, nym - 1 - q0);
+        __syncthreads();
+        for (int r = 0; r < nr; r++) {
+            long off = (long)(q0 + r) * fs + f0 + kx;
+            if (act) {
+                sb[r][t] = col[(q0 + r + 1) * stride + kx];
+                sm_[r][t] = f.m[off];
+                sp[r][t] = f.piv[off];
             }
-            du[q] = temp;
-            double tr = br, ti = bi;
-            br = nr;
-            bi = ni;
-            nr = tr - mult * nr;
-            ni = ti - mult * ni;
         }
-        col[q * stride] = cmk<C>(br, bi);
-        br = nr;
-        bi = ni;
+        __syncthreads();
+        if (act) {
+            for (int r = 0; r < nr; r++) {
+                C bn = sb[r][t];
+                double nre = bn.x, nim = bn.y, m = sm_[r][t];
+                C done;
+                if (sp[r][t]) {
+                    done = cmk<C>(nre, nim);
+                    nre = br - m * nre;
+                    nim = bi - m * nim;
+                } else {
+                    done = cmk<C>(br, bi);
+                    nre = nre - m * br;
+                    nim = nim - m * bi;
+                }
+                sb[r][t] = done;  // final row q0 + r
+                br = nre;
+                bi = nim;
+            }
+        }
+        __syncthreads();
+        for (int r = 0; r < nr; r++)
+            if (act) col[(q0 + r) * stride + kx] = sb[r][t];
     }
-    // back substitution
-    double xr = br / d[nym - 1], xi = bi / d[nym - 1];
-    col[(nym - 1) * stride] = cmk<C>(xr, xi);
-    double x1r = xr, x1i = xi, x2r = 0.0, x2i = 0.0;
-    if (nym > 1) {
-        C b2 = col[(nym - 2) * stride];
-        double yr = ((double)b2.x - du[nym - 2] * x1r) / d[nym - 2];
-        double yi = ((double)b2.y - du[nym - 2] * x1i) / d[nym - 2];
-        col[(nym - 2) * stride] = cmk<C>(yr, yi);
-        x2r = x1r; x2i = x1i;
-        x1r = yr; x1i = yi;
+    // back substitution, rows nym-1 .. 0
+    double x1r = 0.0, x1i = 0.0, x2r = 0.0, x2i = 0.0;
+    if (act) {
+        double rd = f.rd[(long)(nym - 1) * fs + f0 + kx];
+        x1r = br * rd;
+        x1i = bi * rd;
+        col[(nym - 1) * stride + kx] = cmk<C>(x1r, x1i);
     }
-    for (int q = nym - 3; q >= 0; q--) {
-        C bb = col[q * stride];
-        double yr = ((double)bb.x - du[q] * x1r - dl[q] * x2r) / d[q];
-        double yi = ((double)bb.y - du[q] * x1i - dl[q] * x2i) / d[q];
-        col[q * stride] = cmk<C>(yr, yi);
-        x2r = x1r; x2i = x1i;
-        x1r = yr; x1i = yi;
+    for (int q1 = nym - 2; q1 >= 0; q1 -= RB) {
+        int nr = min(RB, q1 + 1);
+        __syncthreads();
+        for (int r = 0; r < nr; r++) {
+            int q = q1 - r;
+            long off = (long)q * fs + f0 + kx;
+            if (act) {
+                sb[r][t] = col[q * stride + kx];
+                sm_[r][t] = f.rd[off];
+                s2[r][t] = f.du[off];
+                s3[r][t] = f.dl[off];
+            }
+        }
+        __syncthreads();
+        if (act) {
+            for (int r = 0; r < nr; r++) {
+                C bb = sb[r][t];
+                double du = s2[r][t], dl = s3[r][t], rd = sm_[r][t];
+                double yr = ((double)bb.x - du * x1r - dl * x2r) * rd;
+                double yi = ((double)bb.y - du * x1i - dl * x2i) * rd;
+                sb[r][t] = cmk<C>(yr, yi);
+                x2r = x1r; x2i = x1i;
+                x1r = yr; x1i = yi;
+            }
+        }
+        __syncthreads();
+        for (int r = 0; r < nr; r++)
+            if (act) col[(q1 - r) * stride + kx] = sb[r][t];
     }
 }
 
@@ -310,8 +339,8 @@ __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const
     if (!active) return;
     long base0 = (long)n * (jj + (long)nym * kk), base1 = (long)n * (jj + (long)nym * (kk + 1));
     for (int q = tid; q < n; q += G) {
-        phi[base0 + q] = (T)((double)r[q].x * scale);
-        phi[base1 + q] = (T)((double)r[q].y * scale);
+        phi[base0 + q] = r[q].x * T(scale);
+        phi[base1 + q] = r[q].y * T(scale);
     }
 }
 
@@ -320,10 +349,13 @@ __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const
 // rk_step 1 (projection.f90:129-137).  phi is read through the periodic wrap,
 // which reproduces apply_periodic_xz_pressure (projection.f90:144-162).
 // ---------------------------------------------------------------------------
+// valid for i in [2-np, 2np+1]
+__device__ __forceinline__ int wrapf(int i, int np) { return i < 2 ? i + np : (i > np + 1 ? i - np : i); }
+
 struct PhiView {
     int nxp, nym, nzp;
     __device__ __forceinline__ long operator()(int i, int j, int k) const {
-        return (long)(wrapc(i, nxp) - 2) + (long)nxp * ((j - 2) + (long)nym * (wrapc(k, nzp) - 2));
+        return (long)(wrapf(i, nxp) - 2) + (long)nxp * ((j - 2) + (long)nym * (wrapf(k, nzp) - 2));
     }
 };
 
@@ -337,14 +369,16 @@ __global__ void k_project(GeoT<T> g, Fld<T> F, Fld<T> Flo, const T *phi, PhiView
     if (COMP == 0) grad = (phi[pv(i + 1, j, k)] - phi[pv(i, j, k)]) / (g.xg[i + 1] - g.xg[i]);
     else if (COMP == 1) grad = (phi[pv(i, j + 1, k)] - phi[pv(i, j, k)]) / (g.yg[j + 1] - g.yg[j]);
     else grad = (phi[pv(i, j, k + 1)] - phi[pv(i, j, k)]) / (g.zg[k + 1] - g.zg[k]);
-    if (Flo.p) {
-        double v = (double)F(i, j, k) + (double)Flo(i, j, k) - (double)grad;
-        T hi = (T)v;
-        F(i, j, k) = hi;
-        Flo(i, j, k) = (T)(v - (double)hi);
-    } else {
-        F(i, j, k) = F(i, j, k) - grad;
+    if constexpr (sizeof(T) == 4) {
+        if (Flo.p) {
+            float hi = F(i, j, k), lo = Flo(i, j, k);
+            ff_add(hi, lo, -grad);
+            F(i, j, k) = hi;
+            Flo(i, j, k) = lo;
+            return;
+        }
     }
+    F(i, j, k) = F(i, j, k) - grad;
 }
 
 template <typename T>
@@ -354,7 +388,7 @@ __global__ void k_store_p(Fld<T> P, const T *phi, PhiView pv, const DevScal *ds,
     int k = blockIdx.z + 1;
     if (i > nxg || j > nyg) return;
     int ic = min(max(i, 2), nxg - 1), jc = min(max(j, 2), nyg - 1), kc = min(max(k, 2), nzg - 1);
-    P(i, j, k) = (T)((double)phi[pv(ic, jc, kc)] / (ds->dt * c11));
+    P(i, j, k) = phi[pv(ic, jc, kc)] / (ds_dt<T>(ds) * T(c11));
 }
 
 template <typename T>
@@ -399,8 +433,14 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p) {
     count_launch(ctx, "k_fft_z");
     // tridiagonal
     dim3 gt(cdiv(nh, 64), nzp);
-    if (nym <= 160) k_tri<T, 160><<<gt, 64, 0, ctx->st>>>(spec, ctx->d_tri, nym, nh, nzp, nxp);
-    else k_tri<T, 520><<<gt, 64, 0, ctx->st>>>(spec, ctx->d_tri, nym, nh, nzp, nxp);
+    TriFac tf;
+    size_t nf = (size_t)nym * nzp * nh;
+    tf.m = ctx->tri_fac;
+    tf.rd = ctx->tri_fac + nf;
+    tf.du = ctx->tri_fac + 2 * nf;
+    tf.dl = ctx->tri_fac + 3 * nf;
+    tf.piv = ctx->tri_piv;
+    k_tri<T><<<gt, 64, 0, ctx->st>>>(spec, tf, nym, nh, nzp);
     count_launch(ctx, "k_tri");
     // inverse z
     k_fft_z<T><<<nym * ngrp, LB * Gz, shz, ctx->st>>>(spec, pz, twzb, nym, nh, LB);

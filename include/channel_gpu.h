@@ -57,6 +57,8 @@ typedef struct {
     int sgs_recompute;     /* 1: evaluate the second eddy viscosity of substep 1
                               (time_integration.f90:103) inside cf_time_step_rk3;
                               0: reuse the first one (bit-identical inputs)      */
+    int dsm_unfused;       /* 1: evaluate the dynamic Smagorinsky model with the
+                              multi-pass kernels even where the fused pass applies */
 } cf_params;
 
 /* Fills p with the defaults of the library (reference values where the
@@ -70,6 +72,8 @@ void cf_default_params(cf_params *p);
 int cf_create(int nx, int ny, int nz, const double *x, const double *y, const double *z,
               const cf_params *p, int device, cf_ctx **out);
 int cf_destroy(cf_ctx *ctx);
+/* Message of the last failure on ctx; with ctx == NULL, of the last failure
+ * of this thread that had no context (e.g. cf_create). */
 const char *cf_last_error(const cf_ctx *ctx);
 
 /* ---- state transfer (host <-> device) ---------------------------------- */

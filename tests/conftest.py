@@ -16,8 +16,9 @@ def pytest_configure(config):
 
 def rel_err(a, b):
     """max|a-b| / max|b| (normwise relative error of one array)."""
-    a = np.asarray(a, dtype=np.float64)
-    b = np.asarray(b, dtype=np.float64)
+    dt = np.complex128 if (np.iscomplexobj(a) or np.iscomplexobj(b)) else np.float64
+    a = np.asarray(a, dtype=dt)
+    b = np.asarray(b, dtype=dt)
     den = np.max(np.abs(b))
     if den == 0:
         return float(np.max(np.abs(a - b)))

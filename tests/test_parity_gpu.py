@@ -195,3 +195,20 @@ def test_split_precision_short_horizon():
     for n in ("U", "V", "W"):
         e = rel_err(out[1][n], out[0][n])
         assert e < 1e-4, (n, e)
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 2e-4)])
+def test_dsm_fused_matches_multipass(precision, tol):
+    """The one-pass dynamic Smagorinsky kernel (periodic state) against the
+    multi-pass kernels on the same fields."""
+    import channelflow as cf
+    case = channel_case(*CASES["config1"])
+    out = []
+    for unfused in (0, 1):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=precision, dsm_unfused=unfused, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.apply_boundary_conditions()
+        ch.compute_eddy_viscosity()
+        out.append((ch.download()["nu_t"], ch.avg_nu_t()))
+    assert_close(out[0][0], out[1][0], tol, "nu_t")
+    assert_close(out[0][1][1:-1], out[1][1][1:-1], tol, "avg_nu_t")
