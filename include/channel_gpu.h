@@ -166,6 +166,34 @@ int cf_read_snapshot(const char *path, int nx, int ny, int nz, double *x, double
 int cf_write_snapshot(const char *path, int nx, int ny, int nz, const double *x, const double *y, const double *z,
                       const double *U, const double *V, const double *W, const double *P, const double *nu_t);
 
+/* ---- divergence check without device allocation ---------------------- */
+/* No counterpart in the reference: the arithmetic is check_divergence
+ * (projection.f90:234-256), as in cf_check_divergence, but on caller-owned
+ * device arrays, with no context and no device allocation.  It serves callers
+ * that must not allocate device memory while they run -- all device memory
+ * handed to their own pool at start-up, a fixed memory cap, or no room for the
+ * device synchronisation a cudaMalloc/cudaFree may cause -- and therefore
+ * cannot call cf_create.
+ *   U, V, W  device arrays, reference layout and extents (top of this file)
+ *   x, y, z  face coordinates on the device (nx, ny, nz doubles)
+ *   out      2 device doubles: max(0, max div) and max |div| over the interior
+ *            cells i = 2..nx, j = 2..ny, k = 2..nz
+ *   stream   a cudaStream_t (NULL: the legacy default stream); the work is
+ *            enqueued on it and not waited for.
+ * Scratch: one static device array per device holding CF_NOALLOC_MAX_PLANES
+ * (max div, max |div|) pairs, one per interior z plane; nz - 1 above that is
+ * rejected with CF_ERR_INVALID.  Nothing has to start at zero: every call
+ * writes each scratch slot before it reads it.  Pointers that are not device
+ * or managed memory of the current device are rejected.  The first call on
+ * each device does a one-time setup (it looks up the scratch address with that
+ * device current, which may load the library's device code); a caller that
+ * captures streams should make that first call before any capture begins.
+ * Calls that overlap on one device (several streams or host threads) share the
+ * scratch and race: serialise them.  Errors: cf_last_error(NULL). */
+enum { CF_NOALLOC_MAX_PLANES = 4096 };
+int cf_check_divergence_noalloc(int nx, int ny, int nz, const double *U, const double *V, const double *W,
+                                const double *x, const double *y, const double *z, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
