@@ -76,10 +76,15 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
         "k_rhs": 8 * nC * es,
         "k_fwd_x": 3 * nC * es + nh * cs,
         "k_fft_z": 2 * nh * cs,
-        "k_tri": 2 * nh * cs,
+        # FP32 LU replay: right-hand side in and out, multiplier and 1/d per (mode, row)
+        "k_tri_split": 2 * nh * cs + 2 * nh * 4,
+        # FP64 zgtsv replay (all modes in the FP64 path): data in/out, m, 1/d, du, dl, pivot flag
+        "k_tri_mode": 2 * nh * cs + nh * 33,
         "k_inv_x": nh * cs + nC * es,
-        # one component: phi in, velocity in and out
-        "k_project": 3 * nC * es,
+        # phi in, three velocity components in and out
+        "k_project3": 7 * nC * es,
+        # U, V, W in
+        "k_dt_min": 3 * nC * es,
         "k_bc": None,
     }
     return tab.get(kernel)
@@ -390,6 +395,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only run N steps of the split path after one warm-up step (for ncu)")
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
+    ap.add_argument("--kernel-table", action="store_true",
+                    help="with --profile-steps: also print per-kernel event times of two more steps")
     args = ap.parse_args()
     rank, world, local = dist_info()
     wl = WORKLOADS[args.workload]
@@ -399,6 +406,13 @@ def main():
         ch.time_step_rk3(1)
         ch.time_step_rk3(args.profile_steps)
         print(json.dumps({"profile_steps": args.profile_steps, "launches_per_step": ch.launches_per_step()}))
+        if args.kernel_table:
+            prof = ch.profile_steps(2)
+            tot = sum(v[0] for v in prof.values())
+            for k, (ms, n) in sorted(prof.items(), key=lambda kv: -kv[1][0]):
+                print(f"{k:16s} {n / 2:5.1f}/step {1e3 * ms / 2:9.1f} us/step {100 * ms / tot:5.1f}%"
+                      f"  avg {1e3 * ms / n:8.1f} us")
+            print(f"total {1e3 * tot / 2:.1f} us/step")
         ch.close()
         return
     if args.impl == "reference":

@@ -268,10 +268,18 @@ static int upload_geo(cf_ctx *ctx, T **dptr, GeoT<T> *g) {
 // matrix of projection.f90:97-107 once; the per-row pivot flags and
 // multipliers and the resulting U factor (1/d, du, dl) are what k_tri replays.
 static int tri_factor(cf_ctx *ctx) {
+    // Factors are stored [row q][mode m], m = kz*nh + kx, so that one row of
+    // all modes is contiguous (the spectrum's layout).
     const int nym = ctx->nym, nh = ctx->nxh, nzp = ctx->nzp;
-    const size_t nf = (size_t)nym * nzp * nh;
+    const size_t NM = (size_t)nzp * nh, nf = (size_t)nym * NM;
+    const bool split = ctx->prm.precision == CF_PREC_SPLIT;
     std::vector<double> F(4 * nf);
-    std::vector<unsigned char> piv(nf, 0);
+    std::vector<unsigned char> piv(nf, 0), flag(NM, 0);
+    std::vector<float> l32, ru32;
+    if (split) {
+        l32.assign(nf, 0.0f);
+        ru32.assign(nf, 0.0f);
+    }
     std::vector<double> d(nym), du(nym), dl(nym);
     for (int kz = 0; kz < nzp; kz++)
         for (int kx = 0; kx < nh; kx++) {
@@ -281,7 +289,7 @@ static int tri_factor(cf_ctx *ctx) {
                 dl[q] = ctx->Dl[q];
             }
             if (kx == 0 && kz == 0) d[0] = 3.0 / 2.0 * d[0];
-            const size_t f0 = (size_t)kz * nh + kx, fs = (size_t)nzp * nh;
+            const size_t m0 = (size_t)kz * nh + kx;
             for (int q = 0; q < nym - 1; q++) {
                 double m = 0.0;
                 unsigned char pv = 0;
@@ -303,20 +311,46 @@ static int tri_factor(cf_ctx *ctx) {
                     }
                     du[q] = temp;
                 }
-                F[q * fs + f0] = m;
-                piv[q * fs + f0] = pv;
+                F[q * NM + m0] = m;
+                piv[q * NM + m0] = pv;
+                if (pv) flag[m0] = 1;
             }
             if (d[nym - 1] == 0.0) return cf_fail(ctx, CF_ERR_INVALID, "singular pressure matrix");
             for (int q = 0; q < nym; q++) {
-                F[nf + q * fs + f0] = 1.0 / d[q];
-                F[2 * nf + q * fs + f0] = q < nym - 1 ? du[q] : 0.0;
-                F[3 * nf + q * fs + f0] = q < nym - 2 ? dl[q] : 0.0;
+                F[nf + q * NM + m0] = 1.0 / d[q];
+                F[2 * nf + q * NM + m0] = q < nym - 1 ? du[q] : 0.0;
+                F[3 * nf + q * NM + m0] = q < nym - 2 ? dl[q] : 0.0;
             }
+            if (split && !flag[m0])
+                for (int q = 0; q < nym; q++) {
+                    l32[q * NM + m0] = (float)F[q * NM + m0];
+                    ru32[q * NM + m0] = (float)F[nf + q * NM + m0];
+                }
         }
     CF_CUDA(cudaMalloc(&ctx->tri_fac, F.size() * sizeof(double)));
     CF_CUDA(cudaMemcpy(ctx->tri_fac, F.data(), F.size() * sizeof(double), cudaMemcpyHostToDevice));
     CF_CUDA(cudaMalloc(&ctx->tri_piv, piv.size()));
     CF_CUDA(cudaMemcpy(ctx->tri_piv, piv.data(), piv.size(), cudaMemcpyHostToDevice));
+    if (split) {
+        // without pivoting zgtsv leaves du untouched: the Dyy upper diagonal
+        std::vector<float> du32(nym);
+        for (int q = 0; q < nym; q++) du32[q] = q < nym - 1 ? (float)ctx->Du[q] : 0.0f;
+        std::vector<int> list;
+        for (size_t m = 0; m < NM; m++)
+            if (flag[m]) list.push_back((int)m);
+        ctx->n_tri_list = (int)list.size();
+        CF_CUDA(cudaMalloc(&ctx->tri_l32, nf * sizeof(float)));
+        CF_CUDA(cudaMemcpy(ctx->tri_l32, l32.data(), nf * sizeof(float), cudaMemcpyHostToDevice));
+        CF_CUDA(cudaMalloc(&ctx->tri_ru32, nf * sizeof(float)));
+        CF_CUDA(cudaMemcpy(ctx->tri_ru32, ru32.data(), nf * sizeof(float), cudaMemcpyHostToDevice));
+        CF_CUDA(cudaMalloc(&ctx->tri_du32, nym * sizeof(float)));
+        CF_CUDA(cudaMemcpy(ctx->tri_du32, du32.data(), nym * sizeof(float), cudaMemcpyHostToDevice));
+        CF_CUDA(cudaMalloc(&ctx->tri_flag, NM));
+        CF_CUDA(cudaMemcpy(ctx->tri_flag, flag.data(), NM, cudaMemcpyHostToDevice));
+        CF_CUDA(cudaMalloc(&ctx->tri_list, std::max<size_t>(1, list.size()) * sizeof(int)));
+        if (!list.empty())
+            CF_CUDA(cudaMemcpy(ctx->tri_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+    }
     return 0;
 }
 
@@ -484,7 +518,8 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
     for (auto &g : ctx->graphs)
         if (g) cudaGraphExecDestroy(g);
     void *ptrs[] = {ctx->nut, ctx->P, ctx->dsm_q, ctx->dsm_lf, ctx->Uf, ctx->Vf, ctx->Wf, ctx->dsm_part, ctx->avg_nu_t,
-                    ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
+                    ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->tri_l32, ctx->tri_ru32,
+                    ctx->tri_du32, ctx->tri_flag, ctx->tri_list, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
                     ctx->wtemp1, ctx->wtemp2, ctx->eq_grid, ctx->eq_zst, ctx->eq_xst, ctx->eq_zw, ctx->eq_xw, ctx->ds,
                     ctx->d_red, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage};
     for (void *q : ptrs)
@@ -934,18 +969,20 @@ static int enqueue_step(cf_ctx *ctx) {
     } else if (ctx->prm.sgs_recompute) {
         TRY(eddy(ctx, X));
     }
+    // substeps 1 and 2 hold intermediate stages: the split path keeps a low
+    // word only for u^n and the new state of substep 3
     TRY(launch_rhs_update<T>(ctx, 1, X, a));
     ctx->cur = a;
-    TRY(launch_bc<T>(ctx, a));
-    TRY(launch_projection<T>(ctx, a, true));
-    TRY(launch_bc<T>(ctx, a));
+    TRY(launch_bc<T>(ctx, a, false));
+    TRY(launch_projection<T>(ctx, a, true, false));
+    TRY(launch_bc<T>(ctx, a, false));
     // substep 2 (:118-131)
     TRY(eddy(ctx, a));
     TRY(launch_rhs_update<T>(ctx, 2, a, b));
     ctx->cur = b;
-    TRY(launch_bc<T>(ctx, b));
-    TRY(launch_projection<T>(ctx, b, false));
-    TRY(launch_bc<T>(ctx, b));
+    TRY(launch_bc<T>(ctx, b, false));
+    TRY(launch_projection<T>(ctx, b, false, false));
+    TRY(launch_bc<T>(ctx, b, false));
     // substep 3 (:134-150)
     TRY(eddy(ctx, b));
     TRY(launch_rhs_update<T>(ctx, 3, b, a));

@@ -38,7 +38,7 @@ struct Fld {
 };
 
 template <typename T>
-static inline Fld<T> make_fld(void *p, int n1, int n2) {
+__host__ __device__ static inline Fld<T> make_fld(void *p, int n1, int n2) {
     Fld<T> f;
     f.p = (T *)p;
     f.sy = n1;
@@ -146,10 +146,17 @@ struct cf_ctx {
     bool state_periodic = false;       // U, V, W satisfy the periodic/no-slip ghost identities
     // pressure
     void *phi = nullptr;               // canonical real
-    void *spec = nullptr;              // complex spectrum (nxh, nym, nzp)
+    void *spec = nullptr;              // complex spectrum [j][kz][kx]: mode m = kz*nxh + kx contiguous per row
     double *d_tri = nullptr;           // Dd, Dl, Du (nym each), kxx (nxp), kzz (nzp)
-    double *tri_fac = nullptr;         // zgtsv factors per mode: m, 1/d, du, dl
-    unsigned char *tri_piv = nullptr;  // zgtsv pivot flags per mode
+    double *tri_fac = nullptr;         // zgtsv factors [row][mode]: m, 1/d, du, dl
+    unsigned char *tri_piv = nullptr;  // zgtsv pivot flags [row][mode]
+    // split path: FP32 LU factors of the modes whose elimination never pivots
+    float *tri_l32 = nullptr;          // multipliers [row][mode]
+    float *tri_ru32 = nullptr;         // 1/d [row][mode]
+    float *tri_du32 = nullptr;         // Dyy upper diagonal [row] (shared by all modes)
+    unsigned char *tri_flag = nullptr; // 1: mode pivots somewhere (FP64 replay)
+    int *tri_list = nullptr;           // the flagged modes
+    int n_tri_list = 0;
     double *d_tw = nullptr;            // twiddles: x fwd, x bwd, z fwd, z bwd
     int radx[8], nradx, radz[8], nradz;
     // wall model
@@ -184,14 +191,14 @@ struct cf_ctx {
 int cf_fail(cf_ctx *ctx, int code, const std::string &msg);
 
 // ---- launchers (kernels in the .cu files), all enqueue on ctx->st -------
-template <typename T> int launch_bc(cf_ctx *ctx, int buf);                 // apply_boundary_conditions
+template <typename T> int launch_bc(cf_ctx *ctx, int buf, bool lo = true);  // apply_boundary_conditions (lo: low words too)
 template <typename T> int launch_rhs(cf_ctx *ctx, int comp, int slot);     // store F slot
 template <typename T> int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst);  // fused RHS + RK update
 template <typename T> int launch_rk_update(cf_ctx *ctx, int s);            // from stored F slots
 template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // eddy viscosity
 template <typename T> int launch_dsm_fused(cf_ctx *ctx, int buf);          // fused pass (periodic state)
 template <typename T> int launch_nut_zero(cf_ctx *ctx);
-template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p);
+template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true);
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only

@@ -12,19 +12,30 @@
 // ---------------------------------------------------------------------------
 // ybc: 0 = Dirichlet at centres (ghost = -interior), 1 = zero at faces,
 //      2 = nonzero Neumann at centres (ghost = interior - dy*alpha(i,wall,k))
+struct BcField {
+    void *p, *plo;
+    int n1, n2, n3, xc, zc, ybc;
+    const double *alpha;
+    int n;  // ghost elements of this field
+};
+struct BcSet {
+    BcField f[3];
+    int nxp, nzp;
+    double dyb, dyt;
+};
+
 template <typename T>
-__global__ void k_bc(Fld<T> F, Fld<T> Flo, int n1, int n2, int n3, int xc, int zc, int nxp, int nzp, int ybc,
-                     const double *alpha, double dyb, double dyt) {
+__device__ __forceinline__ void bc_elem(const BcField &d, int nxp, int nzp, double dyb, double dyt, int t) {
+    const Fld<T> F = make_fld<T>(d.p, d.n1, d.n2), Flo = make_fld<T>(d.plo, d.n1, d.n2);
+    const int n1 = d.n1, n2 = d.n2, n3 = d.n3, xc = d.xc, zc = d.zc, ybc = d.ybc;
     const int gx = xc ? 3 : 2, gz = zc ? 3 : 2;
-    const long nY = 2L * n1 * n3;
-    const long nX = (long)gx * (n2 - 2) * n3;
-    const long nZ = (long)gz * (n2 - 2) * (n1 - gx);
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int nY = 2 * n1 * n3;
+    const int nX = gx * (n2 - 2) * n3;
     int i, j, k;
     if (t < nY) {
-        i = (int)(t % n1) + 1;
-        long r = t / n1;
-        k = (int)(r % n3) + 1;
+        i = t % n1 + 1;
+        int r = t / n1;
+        k = r % n3 + 1;
         j = (r / n3) == 0 ? 1 : n2;
         int is = wrapc(i, nxp), ks = wrapc(k, nzp);
         if (ybc == 1) {
@@ -38,7 +49,7 @@ __global__ void k_bc(Fld<T> F, Fld<T> Flo, int n1, int n2, int n3, int xc, int z
                 if (Flo.p) Flo(i, j, k) = -Flo(is, jsrc, ks);
             } else {
                 int w = (j == 1) ? 0 : 1;
-                double a = alpha[(i - 1) + (long)n1 * (w + 2L * (k - 1))];
+                double a = d.alpha[(i - 1) + (long)n1 * (w + 2L * (k - 1))];
                 double dy = (j == 1) ? dyb : dyt;
                 if (Flo.p) {
                     double hv = (double)v + (double)Flo(is, jsrc, ks) - dy * a;
@@ -54,18 +65,17 @@ __global__ void k_bc(Fld<T> F, Fld<T> Flo, int n1, int n2, int n3, int xc, int z
     }
     t -= nY;
     if (t < nX) {
-        int g = (int)(t % gx);
-        long r = t / gx;
-        j = (int)(r % (n2 - 2)) + 2;
-        k = (int)(r / (n2 - 2)) + 1;
+        int g = t % gx;
+        int r = t / gx;
+        j = r % (n2 - 2) + 2;
+        k = r / (n2 - 2) + 1;
         i = (g == 0) ? 1 : (xc ? (g == 1 ? n1 - 1 : n1) : n1);
     } else {
         t -= nX;
-        if (t >= nZ) return;
-        int g = (int)(t % gz);
-        long r = t / gz;
-        j = (int)(r % (n2 - 2)) + 2;
-        i = (int)(r / (n2 - 2)) + 2;  // non-ghost x: 2 .. n1-gx+1
+        int g = t % gz;
+        int r = t / gz;
+        j = r % (n2 - 2) + 2;
+        i = r / (n2 - 2) + 2;  // non-ghost x: 2 .. n1-gx+1
         k = (g == 0) ? 1 : (zc ? (g == 1 ? n3 - 1 : n3) : n3);
     }
     int is = wrapc(i, nxp), ks = wrapc(k, nzp);
@@ -73,29 +83,55 @@ __global__ void k_bc(Fld<T> F, Fld<T> Flo, int n1, int n2, int n3, int xc, int z
     if (Flo.p) Flo(i, j, k) = Flo(is, j, ks);
 }
 
+// The ghost shells of U, V and W in one launch: thread t belongs to the
+// field whose element range contains it.
 template <typename T>
-static int bc_field(cf_ctx *ctx, void *p, void *plo, int n1, int n2, int n3, int xc, int zc, int ybc,
-                    const double *alpha) {
+__global__ void k_bc(BcSet s) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        if (t < s.f[q].n) {
+            bc_elem<T>(s.f[q], s.nxp, s.nzp, s.dyb, s.dyt, t);
+            return;
+        }
+        t -= s.f[q].n;
+    }
+}
+
+static BcField bc_field(void *p, void *plo, int n1, int n2, int n3, int xc, int zc, int ybc, const double *alpha) {
+    BcField f;
     int gx = xc ? 3 : 2, gz = zc ? 3 : 2;
-    long tot = 2L * n1 * n3 + (long)gx * (n2 - 2) * n3 + (long)gz * (n2 - 2) * (n1 - gx);
-    Fld<T> F = make_fld<T>(p, n1, n2);
-    Fld<T> L = make_fld<T>(plo, n1, n2);
-    double dyb = ctx->hyg[2] - ctx->hyg[1], dyt = ctx->hyg[ctx->nyg] - ctx->hyg[ctx->nyg - 1];
-    k_bc<T><<<cdiv(tot, 256), 256, 0, ctx->st>>>(F, L, n1, n2, n3, xc, zc, ctx->nxp, ctx->nzp, ybc, alpha, dyb, dyt);
-    count_launch(ctx, "k_bc");
-    return 0;
+    f.p = p;
+    f.plo = plo;
+    f.n1 = n1;
+    f.n2 = n2;
+    f.n3 = n3;
+    f.xc = xc;
+    f.zc = zc;
+    f.ybc = ybc;
+    f.alpha = alpha;
+    f.n = 2 * n1 * n3 + gx * (n2 - 2) * n3 + gz * (n2 - 2) * (n1 - gx);
+    return f;
 }
 
 template <typename T>
-int launch_bc(cf_ctx *ctx, int b) {
+int launch_bc(cf_ctx *ctx, int b, bool lo) {
     int wm = ctx->prm.iwall_model;
     if (wm == 0) ctx->state_periodic = true;  // holds for every later launch on the stream
+    BcSet s;
     // U: x faces, y centres, z centres
-    bc_field<T>(ctx, ctx->U[b], ctx->Ulo[b], ctx->nx, ctx->nyg, ctx->nzg, 0, 1, wm == 3 ? 2 : 0, ctx->alpha_x);
+    s.f[0] = bc_field(ctx->U[b], lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg, ctx->nzg, 0, 1, wm == 3 ? 2 : 0, ctx->alpha_x);
     // V: x centres, y faces, z centres
-    bc_field<T>(ctx, ctx->V[b], ctx->Vlo[b], ctx->nxg, ctx->ny, ctx->nzg, 1, 1, 1, nullptr);
+    s.f[1] = bc_field(ctx->V[b], lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny, ctx->nzg, 1, 1, 1, nullptr);
     // W: x centres, y centres, z faces
-    bc_field<T>(ctx, ctx->W[b], ctx->Wlo[b], ctx->nxg, ctx->nyg, ctx->nz, 1, 0, wm == 3 ? 2 : 0, ctx->alpha_z);
+    s.f[2] = bc_field(ctx->W[b], lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg, ctx->nz, 1, 0, wm == 3 ? 2 : 0, ctx->alpha_z);
+    s.nxp = ctx->nxp;
+    s.nzp = ctx->nzp;
+    s.dyb = ctx->hyg[2] - ctx->hyg[1];
+    s.dyt = ctx->hyg[ctx->nyg] - ctx->hyg[ctx->nyg - 1];
+    const int tot = s.f[0].n + s.f[1].n + s.f[2].n;
+    k_bc<T><<<cdiv(tot, 256), 256, 0, ctx->st>>>(s);
+    count_launch(ctx, "k_bc");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -798,56 +834,68 @@ __device__ __forceinline__ void atomic_min_pos(double *a, double v) {
 }
 
 template <typename T>
-__global__ void k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, double *mu, double *mv, double *mw) {
-    // one block per k plane (blockDim 128): min |U| per i over j, min |V| per j
-    // over i, min |W| over the plane; rows are read JB at a time so that the
-    // loads of a group are in flight together.  One global atomic per index
-    // per block; minima in the state's precision, widened exactly.
-    constexpr int JB = 8;
-    __shared__ T vsm[4][520];
-    int k = blockIdx.x + 2, lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    T wmin = T(INFINITY);
-    T umin[8];
+__global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, double *mu,
+                                                double *mv, double *mw) {
+    // block (x: 256 x indices, y: JR rows, z: KR planes), thread = x index i:
+    // min |U| per i over the block's rows
+    // and planes, min |V| per row, min |W| per plane; all loads of a plane's
+    // rows are issued together.  One global atomic per index per block;
+    // minima in the state's precision, widened exactly.
+    constexpr int JR = 16, KR = 2;
+    __shared__ T vsm[8][JR];
+    __shared__ T wsm[8][KR];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+    const int i = 2 + blockIdx.x * 256 + threadIdx.x, j0 = 2 + blockIdx.y * JR, k0 = 2 + blockIdx.z * KR;
+    T umin = T(INFINITY);
+    T vmin[JR];
 #pragma unroll
-    for (int q = 0; q < 8; q++) umin[q] = T(INFINITY);
-    for (int j0 = 2; j0 <= nyg - 1; j0 += JB) {
-        T vmin[JB];
+    for (int r = 0; r < JR; r++) vmin[r] = T(INFINITY);
 #pragma unroll
-        for (int r = 0; r < JB; r++) vmin[r] = T(INFINITY);
+    for (int kk = 0; kk < KR; kk++) {
+        const int k = k0 + kk;
+        T wmin = T(INFINITY);
+        if (k <= nzg - 1 && i <= nxg - 1) {
+            T u[JR], v[JR], w[JR];
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            int i = threadIdx.x + 2 + q * blockDim.x;
-            if (i <= nxg - 1) {
+            for (int r = 0; r < JR; r++) {
+                const int j = min(j0 + r, nyg - 1);  // clamped rows repeat row nyg-1
+                u[r] = U(i, j, k);
+                v[r] = V(i, j, k);
+                w[r] = W(i, j, k);
+            }
 #pragma unroll
-                for (int r = 0; r < JB; r++) {
-                    int j = j0 + r;
-                    if (j <= nyg - 1) {
-                        umin[q] = fmin(umin[q], fabs(U(i, j, k)));
-                        wmin = fmin(wmin, fabs(W(i, j, k)));
-                        vmin[r] = fmin(vmin[r], fabs(V(i, j, k)));
-                    }
-                }
+            for (int r = 0; r < JR; r++) {
+                umin = fmin(umin, fabs(u[r]));
+                vmin[r] = fmin(vmin[r], fabs(v[r]));
+                wmin = fmin(wmin, fabs(w[r]));
             }
         }
-#pragma unroll
-        for (int r = 0; r < JB; r++) {
-            T v = vmin[r];
-            for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffff, v, o));
-            if (lane == 0 && j0 + r <= nyg - 1) vsm[wp][j0 + r] = v;
-        }
+        for (int o = 16; o > 0; o >>= 1) wmin = fmin(wmin, __shfl_down_sync(0xffffffff, wmin, o));
+        if (lane == 0) wsm[wp][kk] = wmin;
     }
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        int i = threadIdx.x + 2 + q * blockDim.x;
-        if (i <= nxg - 1) atomic_min_pos(&mu[i], (double)umin[q]);
+    for (int r = 0; r < JR; r++) {
+        T v = vmin[r];
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffff, v, o));
+        if (lane == 0) vsm[wp][r] = v;
     }
-    for (int o = 16; o > 0; o >>= 1) wmin = fmin(wmin, __shfl_down_sync(0xffffffff, wmin, o));
-    if (lane == 0) atomic_min_pos(&mw[k], (double)wmin);
+    if (i <= nxg - 1) atomic_min_pos(&mu[i], (double)umin);
     __syncthreads();
-    for (int j = threadIdx.x + 2; j <= nyg - 1; j += blockDim.x) {
-        T m = vsm[0][j];
-        for (int q = 1; q < (int)(blockDim.x >> 5); q++) m = fmin(m, vsm[q][j]);
-        atomic_min_pos(&mv[j], (double)m);
+    const int nw = blockDim.x >> 5;
+    if (threadIdx.x < JR) {
+        const int j = j0 + threadIdx.x;
+        if (j <= nyg - 1) {
+            T m = vsm[0][threadIdx.x];
+            for (int q = 1; q < nw; q++) m = fmin(m, vsm[q][threadIdx.x]);
+            atomic_min_pos(&mv[j], (double)m);
+        }
+    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + KR) {
+        const int kk = threadIdx.x - 32, k = k0 + kk;
+        if (k <= nzg - 1) {
+            T m = wsm[0][kk];
+            for (int q = 1; q < nw; q++) m = fmin(m, wsm[q][kk]);
+            atomic_min_pos(&mw[k], (double)m);
+        }
     }
 }
 
@@ -893,10 +941,9 @@ int launch_dt(cf_ctx *ctx, int b) {
     int n = ctx->nxg + ctx->nyg + ctx->nzg + 6;
     k_dt_init<<<cdiv(n, 256), 256, 0, ctx->st>>>(mu, n);
     count_launch(ctx, "k_dt_init");
-    k_dt_min<T><<<ctx->nzg - 2, 128, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg),
-                                                   make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
-                                                   make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->nxg, ctx->nyg,
-                                                   ctx->nzg, mu, mv, mw);
+    k_dt_min<T><<<dim3(cdiv(ctx->nxg - 2, 256), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2)), 256, 0, ctx->st>>>(
+        make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
+        make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
     count_launch(ctx, "k_dt_min");
     double CFL = ctx->prm.CFL;
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
@@ -950,7 +997,7 @@ int launch_div_check(cf_ctx *ctx, int b, double *d_out) {
 }
 
 #define INST(T)                                                      \
-    template int launch_bc<T>(cf_ctx *, int);                        \
+    template int launch_bc<T>(cf_ctx *, int, bool);                  \
     template int launch_rhs<T>(cf_ctx *, int, int);                  \
     template int launch_rhs_update<T>(cf_ctx *, int, int, int);      \
     template int launch_rk_update<T>(cf_ctx *, int);                 \

@@ -11,6 +11,8 @@
 // real, so real and imaginary parts share every multiplier and pivot choice.
 // All FFTs are Stockham autosort transforms in shared memory with radices
 // 2, 3, 4 and 5 and twiddles from a table of exp(+-2 pi i e/n).
+#include <algorithm>
+
 #include "cf_internal.cuh"
 
 template <typename T> struct C2;
@@ -100,18 +102,134 @@ __device__ C *fft_smem(C *a, C *b, const FftPlan &pl, const C *tw, int tid, int 
 }
 
 // ---------------------------------------------------------------------------
+// The same Stockham transform for a length N known at compile time (the
+// common grid sizes): radices, strides and loop bounds are constants, the
+// radix sequence is the host plan's (4s, then 2, 3, 5), and the twiddle
+// table sits in shared memory.
+// ---------------------------------------------------------------------------
+constexpr int fft_nrad(int n) {
+    int c = 0;
+    while (n % 4 == 0) { n /= 4; c++; }
+    while (n % 2 == 0) { n /= 2; c++; }
+    while (n % 3 == 0) { n /= 3; c++; }
+    while (n % 5 == 0) { n /= 5; c++; }
+    return n == 1 ? c : -1;
+}
+constexpr int fft_rad(int n, int s) {
+    int c = 0;
+    while (n % 4 == 0) { if (c++ == s) return 4; n /= 4; }
+    while (n % 2 == 0) { if (c++ == s) return 2; n /= 2; }
+    while (n % 3 == 0) { if (c++ == s) return 3; n /= 3; }
+    while (n % 5 == 0) { if (c++ == s) return 5; n /= 5; }
+    return 1;
+}
+
+template <int R, int N, typename C>
+__device__ __forceinline__ void butterfly(C *v, const C *tw) {
+    if constexpr (R == 2) {
+        C t0 = v[0];
+        v[0] = cadd(t0, v[1]);
+        v[1] = csub(t0, v[1]);
+    } else if constexpr (R == 4) {
+        const C w = tw[N / 4];  // sign*i
+        C s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+        C s13 = cadd(v[1], v[3]), d13 = cmul(csub(v[1], v[3]), w);
+        v[0] = cadd(s02, s13);
+        v[2] = csub(s02, s13);
+        v[1] = cadd(d02, d13);
+        v[3] = csub(d02, d13);
+    } else if constexpr (R == 3) {
+        const C w = tw[N / 3];  // (-1/2, sign*sqrt(3)/2)
+        C t = cadd(v[1], v[2]), u = csub(v[1], v[2]);
+        C m;
+        m.x = v[0].x + w.x * t.x;
+        m.y = v[0].y + w.x * t.y;
+        C iu;
+        iu.x = -w.y * u.y;
+        iu.y = w.y * u.x;
+        v[0] = cadd(v[0], t);
+        v[1] = cadd(m, iu);
+        v[2] = csub(m, iu);
+    } else {
+        static_assert(R == 5, "radix");
+        C o[5];
+#pragma unroll
+        for (int q = 0; q < 5; q++) {
+            C acc = v[0];
+#pragma unroll
+            for (int r = 1; r < 5; r++) acc = cadd(acc, cmul(v[r], tw[((q * r) % 5) * (N / 5)]));
+            o[q] = acc;
+        }
+#pragma unroll
+        for (int q = 0; q < 5; q++) v[q] = o[q];
+    }
+}
+
+template <int N, int S, int NS, typename C>
+__device__ __forceinline__ C *fft_fixed(C *a, C *b, const C *tw, int tid, int G) {
+    if constexpr (S == fft_nrad(N)) {
+        return a;
+    } else {
+        constexpr int R = fft_rad(N, S), nb = N / R, step = N / (NS * R);
+        for (int j = tid; j < nb; j += G) {
+            const int k = j % NS;
+            C v[R];
+#pragma unroll
+            for (int r = 0; r < R; r++) v[r] = a[j + r * nb];
+            if constexpr (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; r++) v[r] = cmul(v[r], tw[r * k * step]);
+            }
+            butterfly<R, N>(v, tw);
+            const int d = (j / NS) * NS * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) b[d + r * NS] = v[r];
+        }
+        __syncthreads();
+        return fft_fixed<N, S + 1, NS * R, C>(b, a, tw, tid, G);
+    }
+}
+
+// One line: the compile-time transform when N > 0, else the plan's.
+template <int N, typename C>
+__device__ __forceinline__ C *fft_line(C *a, C *b, const FftPlan &pl, const C *tw, int tid, int G) {
+    if constexpr (N > 0) return fft_fixed<N, 0, 1, C>(a, b, tw, tid, G);
+    else return fft_smem<C>(a, b, pl, tw, tid, G);
+}
+
+// Copies the twiddle table to shared memory (compile-time sizes only).
+template <int N, typename C>
+__device__ __forceinline__ const C *stage_twiddles(const C *tw, C *sm_tw) {
+    if constexpr (N > 0) {
+        for (int e = threadIdx.x; e < N; e += blockDim.x) sm_tw[e] = tw[e];
+        return sm_tw;
+    } else {
+        return tw;
+    }
+}
+
+// threads per line of the x transforms (the host launch uses the same rule)
+__host__ __device__ constexpr int fft_x_threads(int n) { return n >= 128 ? 32 : 16; }
+
+// reciprocal face spacings 1/(x(i)-x(i-1)) etc., 1-based (split path)
+struct RSp {
+    const float *rx, *ry, *rz;
+};
+
+// ---------------------------------------------------------------------------
 // Forward: divergence (projection.f90:45-53) of lines (j, k) and (j, k+1),
 // packed as real and imaginary parts, complex FFT along x, split into the
 // two half spectra.  spec layout: ((kz*nym + j-2)*nxh + kx).
 // Block: LP line pairs x GT threads.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int N>
 __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>::t *spec, FftPlan pl,
-                        const typename C2<T>::t *tw, int LP) {
+                        const typename C2<T>::t *tw_g, int LP, RSp rs) {
     typedef typename C2<T>::t C;
     extern __shared__ unsigned char smraw[];
     C *sm = (C *)smraw;
-    const int n = pl.n, G = blockDim.x / LP;
+    const int n = N > 0 ? N : pl.n, G = N > 0 ? fft_x_threads(N) : blockDim.x / LP;
+    const C *tw = stage_twiddles<N, C>(tw_g, sm + (long)LP * 2 * n);
     const int lp = threadIdx.x / G, tid = threadIdx.x % G;
     long pair = (long)blockIdx.x * LP + lp;
     const int nym = g.nym, nzp = g.nzp;
@@ -124,26 +242,45 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
     }
     C *a = sm + (long)lp * 2 * n, *b = a + n;
     if (active) {
-        for (int i = tid + 2; i <= n + 1; i += G) {
-            T d0 = (U(i, j, k) - U(i - 1, j, k)) / (g.x[i] - g.x[i - 1]) +
-                   (V(i, j, k) - V(i, j - 1, k)) / (g.y[j] - g.y[j - 1]) +
-                   (W(i, j, k) - W(i, j, k - 1)) / (g.z[k] - g.z[k - 1]);
-            int k1 = k + 1;
-            T d1 = (U(i, j, k1) - U(i - 1, j, k1)) / (g.x[i] - g.x[i - 1]) +
-                   (V(i, j, k1) - V(i, j - 1, k1)) / (g.y[j] - g.y[j - 1]) +
-                   (W(i, j, k1) - W(i, j, k1 - 1)) / (g.z[k1] - g.z[k1 - 1]);
-            C z;
-            z.x = d0;
-            z.y = d1;
-            a[i - 2] = z;
+        if constexpr (sizeof(T) == 4) {
+            // split path: reciprocal spacings instead of divisions
+            const float ry = rs.ry[j], rz0 = rs.rz[k], rz1 = rs.rz[k + 1];
+#pragma unroll
+            for (int i = tid + 2; i <= (N > 0 ? N : n) + 1; i += (N > 0 ? fft_x_threads(N) : G)) {
+                const float rx = rs.rx[i];
+                const int k1 = k + 1;
+                const float w0 = W(i, j, k), w1 = W(i, j, k1);
+                T d0 = (U(i, j, k) - U(i - 1, j, k)) * rx + (V(i, j, k) - V(i, j - 1, k)) * ry +
+                       (w0 - W(i, j, k - 1)) * rz0;
+                T d1 = (U(i, j, k1) - U(i - 1, j, k1)) * rx + (V(i, j, k1) - V(i, j - 1, k1)) * ry +
+                       (w1 - w0) * rz1;
+                C z;
+                z.x = d0;
+                z.y = d1;
+                a[i - 2] = z;
+            }
+        } else {
+            for (int i = tid + 2; i <= n + 1; i += G) {
+                T d0 = (U(i, j, k) - U(i - 1, j, k)) / (g.x[i] - g.x[i - 1]) +
+                       (V(i, j, k) - V(i, j - 1, k)) / (g.y[j] - g.y[j - 1]) +
+                       (W(i, j, k) - W(i, j, k - 1)) / (g.z[k] - g.z[k - 1]);
+                int k1 = k + 1;
+                T d1 = (U(i, j, k1) - U(i - 1, j, k1)) / (g.x[i] - g.x[i - 1]) +
+                       (V(i, j, k1) - V(i, j - 1, k1)) / (g.y[j] - g.y[j - 1]) +
+                       (W(i, j, k1) - W(i, j, k1 - 1)) / (g.z[k1] - g.z[k1 - 1]);
+                C z;
+                z.x = d0;
+                z.y = d1;
+                a[i - 2] = z;
+            }
         }
     }
     __syncthreads();
-    C *r = fft_smem<C>(a, b, pl, tw, tid, G);
+    C *r = fft_line<N, C>(a, b, pl, tw, tid, G);
     if (!active) return;
     const int nh = n / 2 + 1;
-    C *o0 = spec + ((long)(k - 2) * nym + (j - 2)) * nh;
-    C *o1 = spec + ((long)(k - 1) * nym + (j - 2)) * nh;
+    C *o0 = spec + ((long)(j - 2) * nzp + (k - 2)) * nh;
+    C *o1 = spec + ((long)(j - 2) * nzp + (k - 1)) * nh;
     for (int q = tid; q < nh; q += G) {
         C Zk = r[q], Zc = cconj(r[(n - q) % n]);
         C A, B;
@@ -158,140 +295,387 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
 }
 
 // ---------------------------------------------------------------------------
-// Complex FFT along z for LB consecutive kx of one j.  Block: LB lines.
+// Complex FFT along z of LB consecutive lines (j, kx), line index j*nh + kx.
+// Element kz of a line sits at ((j*nzp + kz)*nh + kx), so for one kz the
+// lines of a block are (mostly) adjacent in memory.
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_fft_z(typename C2<T>::t *spec, FftPlan pl, const typename C2<T>::t *tw, int nym, int nh, int LB) {
+template <typename T, int N>
+__global__ void k_fft_z(typename C2<T>::t *spec, FftPlan pl, const typename C2<T>::t *tw_g, int nlines, int nh, int LB) {
     typedef typename C2<T>::t C;
     extern __shared__ unsigned char smraw[];
     C *sm = (C *)smraw;
-    const int n = pl.n, G = blockDim.x / LB;
-    int ngrp = (nh + LB - 1) / LB;
-    int j = blockIdx.x / ngrp, kx0 = (blockIdx.x % ngrp) * LB;
-    // load: element (line l, position kz) at sm[l*2n + kz]
-    for (int t = threadIdx.x; t < LB * n; t += blockDim.x) {
-        int l = t % LB, kz = t / LB;
-        C v = cmk<C>(0.0, 0.0);
-        if (kx0 + l < nh) v = spec[((long)kz * nym + j) * nh + kx0 + l];
-        sm[(long)l * 2 * n + kz] = v;
+    const int n = N > 0 ? N : pl.n, G = blockDim.x / LB;
+    const int LS = 2 * n + 1;  // line stride: odd, so that adjacent lines fall in different banks
+    const C *tw = stage_twiddles<N, C>(tw_g, sm + (long)LB * LS);
+    // blockDim.x is a multiple of LB: a thread keeps one line in the copies
+    const int cl = threadIdx.x % LB, kz0 = threadIdx.x / LB, kzs = blockDim.x / LB;
+    const long L = (long)blockIdx.x * LB + cl;
+    const bool lact = L < nlines;
+    long gbase = 0;
+    if (lact) {
+        const long j = L / nh, kx = L - j * nh;
+        gbase = j * n * nh + kx;
     }
+    // load: element (line l, position kz) at sm[l*LS + kz]
+    for (int kz = kz0; kz < n; kz += kzs) sm[(long)cl * LS + kz] = lact ? spec[gbase + (long)kz * nh] : cmk<C>(0.0, 0.0);
     __syncthreads();
     const int l = threadIdx.x / G, tid = threadIdx.x % G;
-    C *a = sm + (long)l * 2 * n, *b = a + n;
-    C *r = fft_smem<C>(a, b, pl, tw, tid, G);
+    C *a = sm + (long)l * LS, *b = a + n;
+    C *r = fft_line<N, C>(a, b, pl, tw, tid, G);
     // r is a or b for every line alike (same number of stages)
     long roff = r - a;
-    for (int t = threadIdx.x; t < LB * n; t += blockDim.x) {
-        int ll = t % LB, kz = t / LB;
-        if (kx0 + ll < nh) spec[((long)kz * nym + j) * nh + kx0 + ll] = sm[(long)ll * 2 * n + roff + kz];
-    }
+    if (lact)
+        for (int kz = kz0; kz < n; kz += kzs) spec[gbase + (long)kz * nh] = sm[(long)cl * LS + roff + kz];
 }
 
 // ---------------------------------------------------------------------------
-// Tridiagonal solve per (kx, kz) along j (projection.f90:90-113).  The
-// matrices D(j) = Dyy(j,j) + kxx + kzz (with D(2)*1.5 for the (0,0) mode)
-// never change, so zgtsv's elimination -- pivot choices, multipliers and the
-// final U factor -- is done once on the host (tri_factor) and a solve only
-// replays its right-hand-side operations: one thread per mode, adjacent
-// threads adjacent in kx, factors stored (row, kz, kx) for coalescing.
+// Tridiagonal solve per mode m = kz*nh + kx along j (projection.f90:90-113).
+// The matrices D(j) = Dyy(j,j) + kxx + kzz (with D(2)*1.5 for the (0,0)
+// mode) never change, so zgtsv's elimination -- pivot choices, multipliers
+// and the final U factor -- is done once on the host (tri_factor) and a
+// solve only replays its right-hand-side operations:
 //   fwd q: no pivot: b[q+1] -= m_q b[q]
 //          pivot:    (b[q], b[q+1]) <- (b[q+1], b[q] - m_q b[q+1])
 //   back:  b[q] = (b[q] - du_q b[q+1] - dl_q b[q+2]) * rd_q
+// Spectrum and factors are stored [row][mode].
 // ---------------------------------------------------------------------------
 struct TriFac {
-    const double *m, *rd, *du, *dl;  // [nym][nzp][nh]
-    const unsigned char *piv;        // [nym][nzp][nh]
+    const double *m, *rd, *du, *dl;  // [nym][NM]
+    const unsigned char *piv;        // [nym][NM]
 };
 
+// FP64 replay, one 32-thread block per mode (all modes, or the modes of
+// `list`): the warp stages the mode's right-hand side and factors in shared
+// memory with independent loads, then lane 0 runs the serial recurrence out
+// of shared memory.
 template <typename T>
-__global__ void __launch_bounds__(64) k_tri(typename C2<T>::t *__restrict__ spec, TriFac f, int nym, int nh, int nzp) {
-    // 64 modes (consecutive kx, one kz) per block; rows move through shared
-    // memory RB at a time with coalesced loads, so each thread's serial
-    // recurrence never waits on a global load.
+__global__ void __launch_bounds__(32) k_tri_mode(typename C2<T>::t *__restrict__ spec, TriFac f, int nym, long NM,
+                                                 const int *__restrict__ list) {
     typedef typename C2<T>::t C;
-    constexpr int RB = 16, NT = 64;
-    __shared__ C sb[RB][NT];
-    __shared__ double sm_[RB][NT], s2[RB][NT], s3[RB][NT];
-    __shared__ unsigned char sp[RB][NT];
-    const int kx0 = blockIdx.x * NT, kz = blockIdx.y, t = threadIdx.x, kx = kx0 + t;
-    const bool act = kx < nh;
-    const long stride = nh, fs = (long)nzp * nh, f0 = (long)kz * nh;
-    C *col = spec + (long)kz * nym * nh;
-    double br = 0.0, bi = 0.0;
-    if (act) { C b0 = col[kx]; br = b0.x; bi = b0.y; }
-    // forward: rows q = 0 .. nym-2 eliminate into row q+1
-    for (int q0 = 0; q0 < nym - 1; q0 += RB) {
-        int nr = min(RB, nym - 1 - q0);
-        __syncthreads();
-        for (int r = 0; r < nr; r++) {
-            long off = (long)(q0 + r) * fs + f0 + kx;
-            if (act) {
-                sb[r][t] = col[(q0 + r + 1) * stride + kx];
-                sm_[r][t] = f.m[off];
-                sp[r][t] = f.piv[off];
-            }
-        }
-        __syncthreads();
-        if (act) {
-            for (int r = 0; r < nr; r++) {
-                C bn = sb[r][t];
-                double nre = bn.x, nim = bn.y, m = sm_[r][t];
-                C done;
-                if (sp[r][t]) {
-                    done = cmk<C>(nre, nim);
-                    nre = br - m * nre;
-                    nim = bi - m * nim;
-                } else {
-                    done = cmk<C>(br, bi);
-                    nre = nre - m * br;
-                    nim = nim - m * bi;
-                }
-                sb[r][t] = done;  // final row q0 + r
-                br = nre;
-                bi = nim;
-            }
-        }
-        __syncthreads();
-        for (int r = 0; r < nr; r++)
-            if (act) col[(q0 + r) * stride + kx] = sb[r][t];
+    extern __shared__ double tsm[];
+    double *br = tsm, *bi = br + nym, *fm = bi + nym, *frd = fm + nym, *fdu = frd + nym, *fdl = fdu + nym;
+    unsigned char *fp = (unsigned char *)(fdl + nym);
+    const long mo = list ? list[blockIdx.x] : blockIdx.x;
+    for (int q = threadIdx.x; q < nym; q += 32) {
+        const long o = (long)q * NM + mo;
+        C v = spec[o];
+        br[q] = v.x;
+        bi[q] = v.y;
+        fm[q] = f.m[o];
+        frd[q] = f.rd[o];
+        fdu[q] = f.du[o];
+        fdl[q] = f.dl[o];
+        fp[q] = f.piv[o];
     }
-    // back substitution, rows nym-1 .. 0
-    double x1r = 0.0, x1i = 0.0, x2r = 0.0, x2i = 0.0;
-    if (act) {
-        double rd = f.rd[(long)(nym - 1) * fs + f0 + kx];
-        x1r = br * rd;
-        x1i = bi * rd;
-        col[(nym - 1) * stride + kx] = cmk<C>(x1r, x1i);
+    __syncwarp();
+    if (threadIdx.x == 0) {
+        double r0 = br[0], i0 = bi[0];
+        for (int q = 0; q < nym - 1; q++) {
+            double nre = br[q + 1], nim = bi[q + 1], m = fm[q];
+            if (fp[q]) {
+                br[q] = nre;
+                bi[q] = nim;
+                nre = r0 - m * nre;
+                nim = i0 - m * nim;
+            } else {
+                br[q] = r0;
+                bi[q] = i0;
+                nre = nre - m * r0;
+                nim = nim - m * i0;
+            }
+            r0 = nre;
+            i0 = nim;
+        }
+        double x1r = r0 * frd[nym - 1], x1i = i0 * frd[nym - 1], x2r = 0.0, x2i = 0.0;
+        br[nym - 1] = x1r;
+        bi[nym - 1] = x1i;
+        for (int q = nym - 2; q >= 0; q--) {
+            double yr = (br[q] - fdu[q] * x1r - fdl[q] * x2r) * frd[q];
+            double yi = (bi[q] - fdu[q] * x1i - fdl[q] * x2i) * frd[q];
+            br[q] = yr;
+            bi[q] = yi;
+            x2r = x1r;
+            x2i = x1i;
+            x1r = yr;
+            x1i = yi;
+        }
     }
-    for (int q1 = nym - 2; q1 >= 0; q1 -= RB) {
-        int nr = min(RB, q1 + 1);
-        __syncthreads();
-        for (int r = 0; r < nr; r++) {
-            int q = q1 - r;
-            long off = (long)q * fs + f0 + kx;
-            if (act) {
-                sb[r][t] = col[q * stride + kx];
-                sm_[r][t] = f.rd[off];
-                s2[r][t] = f.du[off];
-                s3[r][t] = f.dl[off];
+    __syncwarp();
+    for (int q = threadIdx.x; q < nym; q += 32) spec[(long)q * NM + mo] = cmk<C>(br[q], bi[q]);
+}
+
+static size_t tri_mode_smem(int nym) { return (size_t)nym * (6 * sizeof(double) + 1); }
+
+
+// Split path, one launch for every mode.
+//  * Blocks nlist.. : MB modes whose elimination never pivots, one thread each
+//    (adjacent in memory): zgtsv's no-pivot replay
+//      b[q+1] -= m_q b[q];  b[q] = (b[q] - du_q b[q+1]) rd_q
+//    in FP32 with the FP64 factors rounded once.  The block copies every row
+//    of its modes' right-hand sides and factors into shared memory with
+//    asynchronous copies (all in flight at once), then each thread runs its
+//    recurrence out of shared memory.
+//  * Blocks 0..nlist-1: one mode whose elimination pivots (the lowest
+//    wavenumbers, condition numbers up to ~1e5).  An FP32 replay of the full
+//    pivoting elimination is refined once against the FP64 residual b - A x
+//    (rows in parallel, x accumulated in FP64): the refined error (~1e-6
+//    relative for the (0,0) mode, less elsewhere) is near the FP32 rounding
+//    of the stored result, without a serial FP64 chain (dependent FP64
+//    operations are slow on this GPU).  The block's first warp does the
+//    work; its lane 0 runs the recurrences.
+struct TriSplit {
+    const float *l, *ru, *du;        // FP32 no-pivot factors [nym][NM], du [nym]
+    const unsigned char *flag;       // [NM] 1: the mode pivots
+    const int *list;                 // flagged modes
+    int nlist;
+    const double *Dd, *Dl, *Du;      // Dyy rows (nym each): diagonal, A(q+1,q), A(q,q+1)
+    const double *kxx, *kzz;
+    int nh;
+};
+
+__device__ void tri_refined_mode(float2 *__restrict__ spec, const TriFac &f, const TriSplit &ts, int nym, long NM,
+                                 long mo, unsigned char *smraw) {
+    double *b_re = (double *)smraw, *b_im = b_re + nym, *x_re = b_im + nym, *x_im = x_re + nym;
+    float *w_re = (float *)(x_im + nym), *w_im = w_re + nym, *fm = w_im + nym, *frd = fm + nym, *fdu = frd + nym,
+          *fdl = fdu + nym;
+    unsigned char *fp = (unsigned char *)(fdl + nym);
+    const int lane = threadIdx.x, nt = 32;
+    const int kx = (int)(mo % ts.nh), kz = (int)(mo / ts.nh);
+    const double k2 = ts.kxx[kx] + ts.kzz[kz];
+    for (int q = lane; q < nym; q += nt) {
+        const long o = (long)q * NM + mo;
+        const float2 v = spec[o];
+        b_re[q] = v.x;
+        b_im[q] = v.y;
+        x_re[q] = 0.0;
+        x_im[q] = 0.0;
+        w_re[q] = v.x;
+        w_im[q] = v.y;
+        fm[q] = (float)f.m[o];
+        frd[q] = (float)f.rd[o];
+        fdu[q] = (float)f.du[o];
+        fdl[q] = (float)f.dl[o];
+        fp[q] = f.piv[o];
+    }
+    __syncwarp();
+    for (int it = 0; it < 2; it++) {
+        if (lane == 0) {
+            // loads of a group of 8 rows are issued together ahead of the
+            // dependent arithmetic
+            float r0 = w_re[0], i0 = w_im[0];
+            for (int q0 = 0; q0 < nym - 1; q0 += 8) {
+                float gr[8], gi[8], gm[8];
+                unsigned char gp[8];
+#pragma unroll
+                for (int r = 0; r < 8; r++)
+                    if (q0 + r < nym - 1) {
+                        gr[r] = w_re[q0 + r + 1];
+                        gi[r] = w_im[q0 + r + 1];
+                        gm[r] = fm[q0 + r];
+                        gp[r] = fp[q0 + r];
+                    }
+#pragma unroll
+                for (int r = 0; r < 8; r++)
+                    if (q0 + r < nym - 1) {
+                        const float m = gm[r];
+                        float nre = gr[r], nim = gi[r];
+                        if (gp[r]) {
+                            w_re[q0 + r] = nre;
+                            w_im[q0 + r] = nim;
+                            nre = r0 - m * nre;
+                            nim = i0 - m * nim;
+                        } else {
+                            w_re[q0 + r] = r0;
+                            w_im[q0 + r] = i0;
+                            nre = nre - m * r0;
+                            nim = nim - m * i0;
+                        }
+                        r0 = nre;
+                        i0 = nim;
+                    }
+            }
+            float x1r = r0 * frd[nym - 1], x1i = i0 * frd[nym - 1], x2r = 0.0f, x2i = 0.0f;
+            w_re[nym - 1] = x1r;
+            w_im[nym - 1] = x1i;
+            for (int q1 = nym - 2; q1 >= 0; q1 -= 8) {
+                float gr[8], gi[8], gu[8], gl[8], gd[8];
+#pragma unroll
+                for (int r = 0; r < 8; r++)
+                    if (q1 - r >= 0) {
+                        gr[r] = w_re[q1 - r];
+                        gi[r] = w_im[q1 - r];
+                        gu[r] = fdu[q1 - r];
+                        gl[r] = fdl[q1 - r];
+                        gd[r] = frd[q1 - r];
+                    }
+#pragma unroll
+                for (int r = 0; r < 8; r++)
+                    if (q1 - r >= 0) {
+                        const float yr = (gr[r] - gu[r] * x1r - gl[r] * x2r) * gd[r];
+                        const float yi = (gi[r] - gu[r] * x1i - gl[r] * x2i) * gd[r];
+                        w_re[q1 - r] = yr;
+                        w_im[q1 - r] = yi;
+                        x2r = x1r;
+                        x2i = x1i;
+                        x1r = yr;
+                        x1i = yi;
+                    }
             }
         }
-        __syncthreads();
-        if (act) {
-            for (int r = 0; r < nr; r++) {
-                C bb = sb[r][t];
-                double du = s2[r][t], dl = s3[r][t], rd = sm_[r][t];
-                double yr = ((double)bb.x - du * x1r - dl * x2r) * rd;
-                double yi = ((double)bb.y - du * x1i - dl * x2i) * rd;
-                sb[r][t] = cmk<C>(yr, yi);
-                x2r = x1r; x2i = x1i;
-                x1r = yr; x1i = yi;
+        __syncwarp();
+        for (int q = lane; q < nym; q += nt) {
+            x_re[q] += (double)w_re[q];
+            x_im[q] += (double)w_im[q];
+        }
+        __syncwarp();
+        if (it == 1) break;
+        // residual of the original matrix (projection.f90:97-107) in FP64
+        for (int q = lane; q < nym; q += nt) {
+            double d = ts.Dd[q] + k2;
+            if (q == 0 && kx == 0 && kz == 0) d = 1.5 * d;
+            double ar = d * x_re[q], ai = d * x_im[q];
+            if (q > 0) {
+                ar += ts.Dl[q - 1] * x_re[q - 1];
+                ai += ts.Dl[q - 1] * x_im[q - 1];
+            }
+            if (q < nym - 1) {
+                ar += ts.Du[q] * x_re[q + 1];
+                ai += ts.Du[q] * x_im[q + 1];
+            }
+            w_re[q] = (float)(b_re[q] - ar);
+            w_im[q] = (float)(b_im[q] - ai);
+        }
+        __syncwarp();
+    }
+    for (int q = lane; q < nym; q += nt) spec[(long)q * NM + mo] = make_float2((float)x_re[q], (float)x_im[q]);
+}
+
+static size_t tri_refined_smem(int nym) { return (size_t)nym * (4 * sizeof(double) + 6 * sizeof(float) + 1); }
+
+// Bulk modes: the no-pivot replay y_j = b_j - m_{j-1} y_{j-1},
+// x_j = (y_j - du_j x_{j+1}) rd_j split over P = blockDim.y segments of
+// TRI_RS rows, one thread per (mode, segment), 32 adjacent modes per warp.
+// Each segment runs both first-order recurrences locally from a zero carry
+// while tracking the carry's coefficient (a product of |m| < 1 or
+// |du rd| < 1: the matrices are diagonally dominant); the segment-end values
+// are combined across segments through shared memory and each row is then
+// corrected by coefficient x true carry.
+template <int TRI_RS>
+__device__ void tri_bulk_segmented(float2 *__restrict__ spec, const TriSplit &ts, int nym, long NM, int blk,
+                                   unsigned char *smraw) {
+    const int lane = threadIdx.x, p = threadIdx.y, P = blockDim.y;
+    const long mo = (long)blk * 32 + lane;
+    const bool act = mo < NM && !ts.flag[mo];
+    float2 *sY = (float2 *)smraw;      // [P][32] segment-end values
+    float *sC = (float *)(sY + P * 32);  // [P][32] their carry coefficients
+    const int j0 = p * TRI_RS;
+    float2 y[TRI_RS];
+    float c[TRI_RS], rd[TRI_RS], g[TRI_RS];
+    // loads: right-hand side, multiplier of the row above, 1/d, du
+#pragma unroll
+    for (int r = 0; r < TRI_RS; r++) {
+        const int j = j0 + r;
+        y[r] = make_float2(0.f, 0.f);
+        c[r] = 0.f;
+        rd[r] = 0.f;
+        g[r] = 0.f;
+        if (act && j < nym) {
+            const long o = (long)j * NM + mo;
+            y[r] = spec[o];
+            c[r] = j > 0 ? ts.l[o - NM] : 0.f;  // m_{j-1}
+            rd[r] = ts.ru[o];
+            g[r] = ts.du[j];
+        }
+    }
+    // forward, local: y_j -= m_{j-1} y_{j-1}; coefficient of the incoming carry
+    {
+        float2 yp = make_float2(0.f, 0.f);
+        float cp = 1.f;
+#pragma unroll
+        for (int r = 0; r < TRI_RS; r++) {
+            const float m = c[r];
+            y[r].x = y[r].x - m * yp.x;
+            y[r].y = y[r].y - m * yp.y;
+            cp = -m * cp;
+            c[r] = cp;
+            yp = y[r];
+        }
+        sY[p * 32 + lane] = yp;
+        sC[p * 32 + lane] = cp;
+    }
+    __syncthreads();
+    {
+        float2 carry = make_float2(0.f, 0.f);  // true y at the row before this segment
+        for (int q = 0; q < p; q++) {
+            const float2 Yq = sY[q * 32 + lane];
+            const float Cq = sC[q * 32 + lane];
+            carry.x = Yq.x + Cq * carry.x;
+            carry.y = Yq.y + Cq * carry.y;
+        }
+#pragma unroll
+        for (int r = 0; r < TRI_RS; r++) {
+            y[r].x += c[r] * carry.x;
+            y[r].y += c[r] * carry.y;
+        }
+    }
+    __syncthreads();
+    // backward, local: x_j = y_j rd_j - du_j rd_j x_{j+1}
+    {
+        float2 xn = make_float2(0.f, 0.f);
+        float en = 1.f;
+#pragma unroll
+        for (int r = TRI_RS - 1; r >= 0; r--) {
+            const float gg = -g[r] * rd[r];
+            float2 x;
+            x.x = (y[r].x - g[r] * xn.x) * rd[r];
+            x.y = (y[r].y - g[r] * xn.y) * rd[r];
+            en = gg * en;
+            y[r] = x;
+            c[r] = en;
+            xn = x;
+        }
+        sY[p * 32 + lane] = xn;  // x at the segment's first row
+        sC[p * 32 + lane] = en;
+    }
+    __syncthreads();
+    {
+        float2 carry = make_float2(0.f, 0.f);  // true x at the row after this segment
+        for (int q = P - 1; q > p; q--) {
+            const float2 Xq = sY[q * 32 + lane];
+            const float Eq = sC[q * 32 + lane];
+            carry.x = Xq.x + Eq * carry.x;
+            carry.y = Xq.y + Eq * carry.y;
+        }
+#pragma unroll
+        for (int r = 0; r < TRI_RS; r++) {
+            const int j = j0 + r;
+            if (act && j < nym) {
+                float2 x = y[r];
+                x.x += c[r] * carry.x;
+                x.y += c[r] * carry.y;
+                spec[(long)j * NM + mo] = x;
             }
         }
-        __syncthreads();
-        for (int r = 0; r < nr; r++)
-            if (act) col[(q1 - r) * stride + kx] = sb[r][t];
     }
+}
+
+// Blocks 0..nlist-1: one pivoting mode each (the threadIdx.y == 0 warp);
+// blocks nlist..: 32 bulk modes x P segments of RS rows.
+template <int RS>
+__global__ void __launch_bounds__(512) k_tri_split(float2 *__restrict__ spec, TriFac f, TriSplit ts, int nym, long NM) {
+    extern __shared__ float2 t32[];
+    if ((int)blockIdx.x < ts.nlist) {
+        if (threadIdx.y == 0) tri_refined_mode(spec, f, ts, nym, NM, ts.list[blockIdx.x], (unsigned char *)t32);
+        return;
+    }
+    tri_bulk_segmented<RS>(spec, ts, nym, NM, blockIdx.x - ts.nlist, (unsigned char *)t32);
+}
+
+// rows per segment: 16 up to 256 rows (at most 16 segments), else 32
+static int tri_split_rs(int nym) { return nym <= 256 ? 16 : 32; }
+static size_t tri_split_smem(int nym) {
+    const int P = (nym + tri_split_rs(nym) - 1) / tri_split_rs(nym);
+    return std::max((size_t)P * 32 * 12, tri_refined_smem(nym));
 }
 
 // ---------------------------------------------------------------------------
@@ -299,13 +683,14 @@ __global__ void __launch_bounds__(64) k_tri(typename C2<T>::t *__restrict__ spec
 // lines (j,k), (j,k+1) into phi (canonical), scaled by 1/(nxp*nzp)
 // (projection.f90:116-120).
 // ---------------------------------------------------------------------------
-template <typename T>
-__global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const typename C2<T>::t *tw, int nym, int nzp,
+template <typename T, int N>
+__global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const typename C2<T>::t *tw_g, int nym, int nzp,
                         int LP, double scale) {
     typedef typename C2<T>::t C;
     extern __shared__ unsigned char smraw[];
     C *sm = (C *)smraw;
-    const int n = pl.n, G = blockDim.x / LP, nh = n / 2 + 1;
+    const int n = N > 0 ? N : pl.n, G = N > 0 ? fft_x_threads(N) : blockDim.x / LP, nh = n / 2 + 1;
+    const C *tw = stage_twiddles<N, C>(tw_g, sm + (long)LP * 2 * n);
     const int lp = threadIdx.x / G, tid = threadIdx.x % G;
     long pair = (long)blockIdx.x * LP + lp;
     long npairs = (long)nym * (nzp / 2);
@@ -317,8 +702,9 @@ __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const
     }
     C *a = sm + (long)lp * 2 * n, *b = a + n;
     if (active) {
-        const C *s0 = spec + ((long)kk * nym + jj) * nh, *s1 = spec + ((long)(kk + 1) * nym + jj) * nh;
-        for (int q = tid; q < n; q += G) {
+        const C *s0 = spec + ((long)jj * nzp + kk) * nh, *s1 = spec + ((long)jj * nzp + kk + 1) * nh;
+#pragma unroll
+        for (int q = tid; q < (N > 0 ? N : n); q += (N > 0 ? fft_x_threads(N) : G)) {
             C A, B;
             if (q < nh) {
                 A = s0[q];
@@ -335,10 +721,11 @@ __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const
         }
     }
     __syncthreads();
-    C *r = fft_smem<C>(a, b, pl, tw, tid, G);
+    C *r = fft_line<N, C>(a, b, pl, tw, tid, G);
     if (!active) return;
     long base0 = (long)n * (jj + (long)nym * kk), base1 = (long)n * (jj + (long)nym * (kk + 1));
-    for (int q = tid; q < n; q += G) {
+#pragma unroll
+    for (int q = tid; q < (N > 0 ? N : n); q += (N > 0 ? fft_x_threads(N) : G)) {
         phi[base0 + q] = r[q].x * T(scale);
         phi[base1 + q] = r[q].y * T(scale);
     }
@@ -359,16 +746,14 @@ struct PhiView {
     }
 };
 
-template <typename T, int COMP>
-__global__ void k_project(GeoT<T> g, Fld<T> F, Fld<T> Flo, const T *phi, PhiView pv, int i1, int j1, int k1) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
-    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-    int k = blockIdx.z + 2;
-    if (i > i1 || j > j1 || k > k1) return;
-    T grad;
-    if (COMP == 0) grad = (phi[pv(i + 1, j, k)] - phi[pv(i, j, k)]) / (g.xg[i + 1] - g.xg[i]);
-    else if (COMP == 1) grad = (phi[pv(i, j + 1, k)] - phi[pv(i, j, k)]) / (g.yg[j + 1] - g.yg[j]);
-    else grad = (phi[pv(i, j, k + 1)] - phi[pv(i, j, k)]) / (g.zg[k + 1] - g.zg[k]);
+// The three components in one pass: phi(i,j,k) is read once for the three
+// gradients (one thread per cell of the union of the three interior ranges).
+struct RSpG {
+    const float *rxg, *ryg, *rzg;  // 1/(xg(i)-xg(i-1)) etc., 1-based
+};
+
+template <typename T>
+__device__ __forceinline__ void proj_update(const Fld<T> &F, const Fld<T> &Flo, int i, int j, int k, T grad) {
     if constexpr (sizeof(T) == 4) {
         if (Flo.p) {
             float hi = F(i, j, k), lo = Flo(i, j, k);
@@ -379,6 +764,30 @@ __global__ void k_project(GeoT<T> g, Fld<T> F, Fld<T> Flo, const T *phi, PhiView
         }
     }
     F(i, j, k) = F(i, j, k) - grad;
+}
+
+template <typename T>
+__global__ void k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ulo, Fld<T> V, Fld<T> Vlo, Fld<T> W, Fld<T> Wlo, const T *phi,
+                           PhiView pv, RSpG rs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    const int k = blockIdx.z + 2;
+    if (i > g.nxg - 1 || j > g.nyg - 1) return;
+    const T p0 = phi[pv(i, j, k)];
+    T gx = T(0), gy = T(0), gz = T(0);
+    const bool du = i <= g.nx - 1, dv = j <= g.ny - 1, dw = k <= g.nz - 1;
+    if constexpr (sizeof(T) == 4) {
+        if (du) gx = (phi[pv(i + 1, j, k)] - p0) * rs.rxg[i + 1];
+        if (dv) gy = (phi[pv(i, j + 1, k)] - p0) * rs.ryg[j + 1];
+        if (dw) gz = (phi[pv(i, j, k + 1)] - p0) * rs.rzg[k + 1];
+    } else {
+        if (du) gx = (phi[pv(i + 1, j, k)] - p0) / (g.xg[i + 1] - g.xg[i]);
+        if (dv) gy = (phi[pv(i, j + 1, k)] - p0) / (g.yg[j + 1] - g.yg[j]);
+        if (dw) gz = (phi[pv(i, j, k + 1)] - p0) / (g.zg[k + 1] - g.zg[k]);
+    }
+    if (du) proj_update(U, Ulo, i, j, k, gx);
+    if (dv) proj_update(V, Vlo, i, j, k, gy);
+    if (dw) proj_update(W, Wlo, i, j, k, gz);
 }
 
 template <typename T>
@@ -397,7 +806,7 @@ static size_t smem_pairs(int n, int LP) {
 }
 
 template <typename T>
-int launch_projection(cf_ctx *ctx, int b, bool store_p) {
+int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo) {
     typedef typename C2<T>::t C;
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
@@ -413,62 +822,106 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p) {
     // twiddle tables (complex of T): x fwd, x bwd, z fwd, z bwd
     const C *tw = (const C *)ctx->d_tw;
     const C *twxf = tw, *twxb = tw + nxp, *twzf = tw + 2 * nxp, *twzb = tw + 2 * nxp + nzp;
-    int minrx = 5, minrz = 5;
-    for (int q = 0; q < px.nrad; q++) minrx = min(minrx, px.rad[q]);
-    for (int q = 0; q < pz.nrad; q++) minrz = min(minrz, pz.rad[q]);
-    int Gx = max(32, ((nxp / minrx + 31) / 32) * 32), Gz = max(32, ((nzp / minrz + 31) / 32) * 32);
-    int LP = max(1, 256 / Gx);
-    while (LP > 1 && smem_pairs<T>(nxp, LP) > 96 * 1024) LP--;
-    long npairs = (long)nym * (nzp / 2);
-    size_t shx = smem_pairs<T>(nxp, LP);
+    const long npairs = (long)nym * (nzp / 2);
+    const long nlines = (long)nym * nh;
+    // x transforms: LP line pairs per block, Gx threads per line
+    const int Gx = fft_x_threads(nxp);
+    int LP = 8;
+    while (LP > 1 && smem_pairs<T>(nxp, LP) + nxp * sizeof(C) > 96 * 1024) LP /= 2;
+    const size_t shx = smem_pairs<T>(nxp, LP) + nxp * sizeof(C);
+    // z transforms: LB lines per block, Gz threads per line
+    const int Gz = nzp >= 128 ? 16 : 8;
+    int LB = 16;
+    while (LB > 1 && smem_pairs<T>(nzp, LB) + (LB + nzp) * sizeof(C) > 96 * 1024) LB /= 2;
+    const size_t shz = smem_pairs<T>(nzp, LB) + (LB + nzp) * sizeof(C);
+    RSp rs;
+    rs.rx = ctx->d_rgeo_f + ctx->rgeo_off[0];
+    rs.ry = ctx->d_rgeo_f + ctx->rgeo_off[2];
+    rs.rz = ctx->d_rgeo_f + ctx->rgeo_off[4];
+#define CF_FFT_SIZES(X) X(16) X(32) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
+#define CF_FWDX(N) case N: k_fwd_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP, rs); break;
+#define CF_FFTZ(N, TW) case N: k_fft_z<T, N><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, TW, (int)nlines, nh, LB); break;
+#define CF_FFTZF(N) CF_FFTZ(N, twzf)
+#define CF_FFTZB(N) CF_FFTZ(N, twzb)
+#define CF_INVX(N) case N: k_inv_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale); break;
     // forward x (divergence fused)
-    k_fwd_x<T><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP);
+    switch (nxp) {
+        CF_FFT_SIZES(CF_FWDX)
+        default: k_fwd_x<T, 0><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP, rs);
+    }
     count_launch(ctx, "k_fwd_x");
     // forward z
-    int LB = max(1, 256 / Gz);
-    while (LB > 1 && smem_pairs<T>(nzp, LB) > 96 * 1024) LB--;
-    int ngrp = (nh + LB - 1) / LB;
-    size_t shz = smem_pairs<T>(nzp, LB);
-    k_fft_z<T><<<nym * ngrp, LB * Gz, shz, ctx->st>>>(spec, pz, twzf, nym, nh, LB);
+    switch (nzp) {
+        CF_FFT_SIZES(CF_FFTZF)
+        default: k_fft_z<T, 0><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, twzf, (int)nlines, nh, LB);
+    }
     count_launch(ctx, "k_fft_z");
     // tridiagonal
-    dim3 gt(cdiv(nh, 64), nzp);
+    const long NM = (long)nzp * nh;
     TriFac tf;
-    size_t nf = (size_t)nym * nzp * nh;
+    size_t nf = (size_t)nym * NM;
     tf.m = ctx->tri_fac;
     tf.rd = ctx->tri_fac + nf;
     tf.du = ctx->tri_fac + 2 * nf;
     tf.dl = ctx->tri_fac + 3 * nf;
     tf.piv = ctx->tri_piv;
-    k_tri<T><<<gt, 64, 0, ctx->st>>>(spec, tf, nym, nh, nzp);
-    count_launch(ctx, "k_tri");
+    if (sizeof(T) == 4) {
+        TriSplit ts;
+        ts.l = ctx->tri_l32;
+        ts.ru = ctx->tri_ru32;
+        ts.du = ctx->tri_du32;
+        ts.flag = ctx->tri_flag;
+        ts.list = ctx->tri_list;
+        ts.nlist = ctx->n_tri_list;
+        ts.Dd = ctx->d_tri;
+        ts.Dl = ctx->d_tri + nym;
+        ts.Du = ctx->d_tri + 2 * nym;
+        ts.kxx = ctx->d_tri + 3 * nym;
+        ts.kzz = ctx->d_tri + 3 * nym + nxp;
+        ts.nh = nh;
+        const int rs = tri_split_rs(nym);
+        const dim3 tb(32, (nym + rs - 1) / rs);
+        const unsigned nb = (unsigned)(ts.nlist + cdiv(NM, 32));
+        if (rs == 16) k_tri_split<16><<<nb, tb, tri_split_smem(nym), ctx->st>>>((float2 *)spec, tf, ts, nym, NM);
+        else k_tri_split<32><<<nb, tb, tri_split_smem(nym), ctx->st>>>((float2 *)spec, tf, ts, nym, NM);
+        count_launch(ctx, "k_tri_split");
+    } else {
+        k_tri_mode<T><<<(unsigned)NM, 32, tri_mode_smem(nym), ctx->st>>>(spec, tf, nym, NM, nullptr);
+        count_launch(ctx, "k_tri_mode");
+    }
     // inverse z
-    k_fft_z<T><<<nym * ngrp, LB * Gz, shz, ctx->st>>>(spec, pz, twzb, nym, nh, LB);
+    switch (nzp) {
+        CF_FFT_SIZES(CF_FFTZB)
+        default: k_fft_z<T, 0><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, twzb, (int)nlines, nh, LB);
+    }
     count_launch(ctx, "k_fft_z");
     // inverse x
-    double scale = 1.0 / ((double)nxp * (double)nzp);
-    k_inv_x<T><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale);
+    const double scale = 1.0 / ((double)nxp * (double)nzp);
+    switch (nxp) {
+        CF_FFT_SIZES(CF_INVX)
+        default: k_inv_x<T, 0><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale);
+    }
     count_launch(ctx, "k_inv_x");
+#undef CF_FWDX
+#undef CF_FFTZ
+#undef CF_FFTZF
+#undef CF_FFTZB
+#undef CF_INVX
     // projection
     PhiView pv;
     pv.nxp = nxp; pv.nym = nym; pv.nzp = nzp;
     dim3 blk(32, 4, 1);
     {
-        int i1 = ctx->nx - 1, j1 = ctx->nyg - 1, k1 = ctx->nzg - 1;
-        k_project<T, 0><<<dim3(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1), blk, 0, ctx->st>>>(
-            g, U, make_fld<T>(ctx->Ulo[b], ctx->nx, ctx->nyg), phi, pv, i1, j1, k1);
+        RSpG rg;
+        rg.rxg = ctx->d_rgeo_f + ctx->rgeo_off[1];
+        rg.ryg = ctx->d_rgeo_f + ctx->rgeo_off[3];
+        rg.rzg = ctx->d_rgeo_f + ctx->rgeo_off[5];
+        k_project3<T><<<dim3(cdiv(ctx->nxg - 2, 32), cdiv(ctx->nyg - 2, 4), ctx->nzg - 2), blk, 0, ctx->st>>>(
+            g, U, make_fld<T>(lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg), V,
+            make_fld<T>(lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny), W,
+            make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg), phi, pv, rg);
+        count_launch(ctx, "k_project3");
     }
-    {
-        int i1 = ctx->nxg - 1, j1 = ctx->ny - 1, k1 = ctx->nzg - 1;
-        k_project<T, 1><<<dim3(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1), blk, 0, ctx->st>>>(
-            g, V, make_fld<T>(ctx->Vlo[b], ctx->nxg, ctx->ny), phi, pv, i1, j1, k1);
-    }
-    {
-        int i1 = ctx->nxg - 1, j1 = ctx->nyg - 1, k1 = ctx->nz - 1;
-        k_project<T, 2><<<dim3(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1), blk, 0, ctx->st>>>(
-            g, W, make_fld<T>(ctx->Wlo[b], ctx->nxg, ctx->nyg), phi, pv, i1, j1, k1);
-    }
-    count_launch(ctx, "k_project"); count_launch(ctx, "k_project"); count_launch(ctx, "k_project");
     if (store_p) {
         Fld<T> P = make_fld<T>(ctx->P, ctx->nxg, ctx->nyg);
         k_store_p<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(
@@ -480,15 +933,21 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p) {
 }
 
 // smem opt-in for the FFT kernels (called once at context creation)
+template <typename T, int N>
+static void fft_attrs_one() {
+    cudaFuncSetAttribute(k_fwd_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_inv_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    cudaFuncSetAttribute(k_fft_z<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+}
+
+// smem opt-in for the FFT and tridiagonal kernels (called once at context creation)
 int fft_setup_attrs() {
-    cudaFuncSetAttribute(k_fwd_x<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_fwd_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_inv_x<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_inv_x<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_fft_z<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    cudaFuncSetAttribute(k_fft_z<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+#define CF_ATTRS(N) fft_attrs_one<double, N>(); fft_attrs_one<float, N>();
+    CF_FFT_SIZES(CF_ATTRS)
+    CF_ATTRS(0)
+#undef CF_ATTRS
     return 0;
 }
 
-template int launch_projection<double>(cf_ctx *, int, bool);
-template int launch_projection<float>(cf_ctx *, int, bool);
+template int launch_projection<double>(cf_ctx *, int, bool, bool);
+template int launch_projection<float>(cf_ctx *, int, bool, bool);
