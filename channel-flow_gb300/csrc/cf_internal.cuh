@@ -55,6 +55,13 @@ struct GeoT {
 };
 typedef GeoT<double> Geo;
 
+// Reciprocal spacings r[e] = 1/(a[e] - a[e-1]) (e >= 2) of the face (x, y, z)
+// and centre (xg, yg, zg) coordinates, 1-based like the coordinates.
+template <typename T>
+struct RcpT {
+    const T *dx, *dxg, *dy, *dyg, *dz, *dzg;
+};
+
 // Device-resident scalars (module globals of global.f90 touched per step).
 struct DevScal {
     double dt, t, dPdx, dPdy, dPdz;
@@ -220,6 +227,19 @@ static inline void count_launch(cf_ctx *ctx, const char *name) {
         }
         ctx->pn++;
     }
+}
+
+template <typename T>
+static inline RcpT<T> rcp_of(cf_ctx *ctx) {
+    const T *b = sizeof(T) == 8 ? (const T *)ctx->d_rgeo : (const T *)ctx->d_rgeo_f;
+    RcpT<T> r;
+    r.dx = b + ctx->rgeo_off[0];
+    r.dxg = b + ctx->rgeo_off[1];
+    r.dy = b + ctx->rgeo_off[2];
+    r.dyg = b + ctx->rgeo_off[3];
+    r.dz = b + ctx->rgeo_off[4];
+    r.dzg = b + ctx->rgeo_off[5];
+    return r;
 }
 
 template <typename T> static inline GeoT<T> geo_of(cf_ctx *ctx);

@@ -1,5 +1,7 @@
 // k_core.cu -- boundary conditions, momentum right-hand sides, RK3 update,
 // mass-flow forcing, time-step and divergence reductions.
+#include <algorithm>
+
 #include "cf_internal.cuh"
 
 // ---------------------------------------------------------------------------
@@ -143,33 +145,35 @@ struct RkCoef {
     double c[4][4];
 };
 
-template <typename T, typename A>
-__device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const A &U, const A &V, const A &W,
+// The spacings enter as reciprocals (rc): 1/(xg(i+1)-xg(i)) = rc.dxg[i+1],
+// 1/(x(i)-x(i-1)) = rc.dx[i], and so on.
+template <typename T, typename A, typename RC>
+__device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
                                          const A &nt, T nu, T dPdx, T Om, int i, int j, int k) {
-    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
+    const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
+    const T rdx1 = rc.dx[i], rdx2 = rc.dx[i + 1], rdx3 = rc.dxg[i + 1];
+    const T rdy3 = rc.dy[j];
+    const T rdz1 = rc.dzg[k], rdz2 = rc.dzg[k + 1], rdz3 = rc.dz[k];
     // 1) -du^2/dx  (equations.f90:43-57)
     T a = h * (U(i, j, k) + U(i + 1, j, k));
     T b = h * (U(i - 1, j, k) + U(i, j, k));
-    T r = -(a * a - b * b) / (xg[i + 1] - xg[i]);
+    T r = -(a * a - b * b) * rdx3;
     // 2) -duv/dy   (:62-79)
     T uy1 = w0[j] * U(i, j, k) + w1[j] * U(i, j + 1, k);
     T uy0 = w0[j - 1] * U(i, j - 1, k) + w1[j - 1] * U(i, j, k);
     T vx1 = h * (V(i, j, k) + V(i + 1, j, k));
     T vx0 = h * (V(i, j - 1, k) + V(i + 1, j - 1, k));
-    r += -(uy1 * vx1 - uy0 * vx0) / (y[j] - y[j - 1]);
+    r += -(uy1 * vx1 - uy0 * vx0) * rdy3;
     // 3) -duw/dz   (:84-101)
     T uz1 = h * (U(i, j, k) + U(i, j, k + 1));
     T uz0 = h * (U(i, j, k - 1) + U(i, j, k));
     T wx1 = h * (W(i, j, k) + W(i + 1, j, k));
     T wx0 = h * (W(i, j, k - 1) + W(i + 1, j, k - 1));
-    r += -(uz1 * wx1 - uz0 * wx0) / (z[k] - z[k - 1]);
+    r += -(uz1 * wx1 - uz0 * wx0) * rdz3;
     // 4) viscous   (:108-163)
-    T dx_1 = x[i] - x[i - 1], dx_2 = x[i + 1] - x[i], dx_3 = xg[i + 1] - xg[i];
-    T dy_3 = y[j] - y[j - 1];
-    T dz_1 = zg[k] - zg[k - 1], dz_2 = zg[k + 1] - zg[k], dz_3 = z[k] - z[k - 1];
-    T t2j = (U(i, j + 1, k) - U(i, j, k)) / (yg[j + 1] - yg[j]);
-    T t2jm = (U(i, j, k) - U(i, j - 1, k)) / (yg[j] - yg[j - 1]);
+    T t2j = (U(i, j + 1, k) - U(i, j, k)) * rc.dyg[j + 1];
+    T t2jm = (U(i, j, k) - U(i, j - 1, k)) * rc.dyg[j];
     T nu_x1 = nu + nt(i, j, k);
     T nu_x2 = nu + nt(i + 1, j, k);
     T nu_y1 = nu + h * (w0[j - 1] * nt(i, j - 1, k) + w1[j - 1] * nt(i, j, k) + w0[j - 1] * nt(i + 1, j - 1, k) +
@@ -177,11 +181,11 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const A &U, const A &
     T nu_y2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i + 1, j, k) + w1[j] * nt(i + 1, j + 1, k));
     T nu_z1 = nu + q * (nt(i, j, k) + nt(i, j, k - 1) + nt(i + 1, j, k) + nt(i + 1, j, k - 1));
     T nu_z2 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i + 1, j, k) + nt(i + 1, j, k + 1));
-    T visc = T(2) / dx_3 * (nu_x2 * (U(i + 1, j, k) - U(i, j, k)) / dx_2 - nu_x1 * (U(i, j, k) - U(i - 1, j, k)) / dx_1) +
-             T(1) / dy_3 * (nu_y2 * (t2j + (V(i + 1, j, k) - V(i, j, k)) / dx_2) -
-                            nu_y1 * (t2jm + (V(i + 1, j - 1, k) - V(i, j - 1, k)) / dx_1)) +
-             T(1) / dz_3 * (nu_z2 * ((U(i, j, k + 1) - U(i, j, k)) / dz_2 + (W(i + 1, j, k) - W(i, j, k)) / dx_2) -
-                            nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) / dz_1 + (W(i + 1, j, k - 1) - W(i, j, k - 1)) / dx_1));
+    T visc = T(2) * rdx3 * (nu_x2 * (U(i + 1, j, k) - U(i, j, k)) * rdx2 - nu_x1 * (U(i, j, k) - U(i - 1, j, k)) * rdx1) +
+             rdy3 * (nu_y2 * (t2j + (V(i + 1, j, k) - V(i, j, k)) * rdx2) -
+                     nu_y1 * (t2jm + (V(i + 1, j - 1, k) - V(i, j - 1, k)) * rdx1)) +
+             rdz3 * (nu_z2 * ((U(i, j, k + 1) - U(i, j, k)) * rdz2 + (W(i + 1, j, k) - W(i, j, k)) * rdx2) -
+                     nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) * rdz1 + (W(i + 1, j, k - 1) - W(i, j, k - 1)) * rdx1));
     r += visc;
     r += dPdx;  // :166
     if (fabs((double)Om) > 1e-6) {  // :169-177
@@ -192,42 +196,42 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const A &U, const A &
     return r;
 }
 
-template <typename T, typename A>
-__device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const A &U, const A &V, const A &W,
+template <typename T, typename A, typename RC>
+__device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
                                          const A &nt, T nu, T Om, int i, int j, int k) {
-    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
+    const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5);
+    const T rdx1 = rc.dxg[i], rdx2 = rc.dxg[i + 1], rdx3 = rc.dx[i];
+    const T rdy1 = rc.dy[j], rdy2 = rc.dy[j + 1], rdy3 = rc.dyg[j + 1];
+    const T rdz1 = rc.dzg[k], rdz2 = rc.dzg[k + 1], rdz3 = rc.dz[k];
     // 1) -dv^2/dy (equations.f90:205-223)
     T a = h * (V(i, j, k) + V(i, j + 1, k));
     T b = h * (V(i, j - 1, k) + V(i, j, k));
-    T r = -(a * a - b * b) / (yg[j + 1] - yg[j]);
+    T r = -(a * a - b * b) * rdy3;
     // 2) -duv/dx (:228-245)
     T uy1 = w0[j] * U(i, j, k) + w1[j] * U(i, j + 1, k);
     T uy0 = w0[j] * U(i - 1, j, k) + w1[j] * U(i - 1, j + 1, k);
     T vx1 = h * (V(i, j, k) + V(i + 1, j, k));
     T vx0 = h * (V(i - 1, j, k) + V(i, j, k));
-    r += -(uy1 * vx1 - uy0 * vx0) / (x[i] - x[i - 1]);
+    r += -(uy1 * vx1 - uy0 * vx0) * rdx3;
     // 3) -dvw/dz (:250-267)
     T vz1 = h * (V(i, j, k) + V(i, j, k + 1));
     T vz0 = h * (V(i, j, k - 1) + V(i, j, k));
     T wy1 = w0[j] * W(i, j, k) + w1[j] * W(i, j + 1, k);
     T wy0 = w0[j] * W(i, j, k - 1) + w1[j] * W(i, j + 1, k - 1);
-    r += -(vz1 * wy1 - vz0 * wy0) / (z[k] - z[k - 1]);
+    r += -(vz1 * wy1 - vz0 * wy0) * rdz3;
     // 4) viscous (:276-331)
-    T dx_1 = xg[i] - xg[i - 1], dx_2 = xg[i + 1] - xg[i], dx_3 = x[i] - x[i - 1];
-    T dy_1 = y[j] - y[j - 1], dy_2 = y[j + 1] - y[j], dy_3 = yg[j + 1] - yg[j];
-    T dz_1 = zg[k] - zg[k - 1], dz_2 = zg[k + 1] - zg[k], dz_3 = z[k] - z[k - 1];
     T nu_x1 = nu + h * (w0[j] * nt(i - 1, j, k) + w1[j] * nt(i - 1, j + 1, k) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
     T nu_x2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i + 1, j, k) + w1[j] * nt(i + 1, j + 1, k));
     T nu_y1 = nu + nt(i, j, k);
     T nu_y2 = nu + nt(i, j + 1, k);
     T nu_z1 = nu + h * (w0[j] * nt(i, j, k - 1) + w1[j] * nt(i, j + 1, k - 1) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
     T nu_z2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i, j, k + 1) + w1[j] * nt(i, j + 1, k + 1));
-    T visc = T(1) / dx_3 * (nu_x2 * ((V(i + 1, j, k) - V(i, j, k)) / dx_2 + (U(i, j + 1, k) - U(i, j, k)) / dy_3) -
-                            nu_x1 * ((V(i, j, k) - V(i - 1, j, k)) / dx_1 + (U(i - 1, j + 1, k) - U(i - 1, j, k)) / dy_3)) +
-             T(2) / dy_3 * (nu_y2 * (V(i, j + 1, k) - V(i, j, k)) / dy_2 - nu_y1 * (V(i, j, k) - V(i, j - 1, k)) / dy_1) +
-             T(1) / dz_3 * (nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) / dz_2 + (W(i, j + 1, k) - W(i, j, k)) / dy_3) -
-                            nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) / dz_1 + (W(i, j + 1, k - 1) - W(i, j, k - 1)) / dy_3));
+    T visc = rdx3 * (nu_x2 * ((V(i + 1, j, k) - V(i, j, k)) * rdx2 + (U(i, j + 1, k) - U(i, j, k)) * rdy3) -
+                     nu_x1 * ((V(i, j, k) - V(i - 1, j, k)) * rdx1 + (U(i - 1, j + 1, k) - U(i - 1, j, k)) * rdy3)) +
+             T(2) * rdy3 * (nu_y2 * (V(i, j + 1, k) - V(i, j, k)) * rdy2 - nu_y1 * (V(i, j, k) - V(i, j - 1, k)) * rdy1) +
+             rdz3 * (nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) * rdz2 + (W(i, j + 1, k) - W(i, j, k)) * rdy3) -
+                     nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) * rdz1 + (W(i, j + 1, k - 1) - W(i, j, k - 1)) * rdy3));
     r += visc;
     if (fabs((double)Om) > 1e-6) {  // :334-342
         T tu0 = h * (U(i - 1, j, k) + U(i, j, k));
@@ -237,33 +241,33 @@ __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const A &U, const A &
     return r;
 }
 
-template <typename T, typename A>
-__device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const A &U, const A &V, const A &W,
+template <typename T, typename A, typename RC>
+__device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
                                          const A &nt, T nu, T dPdz, int i, int j, int k) {
-    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg, *w0 = g.w0, *w1 = g.w1;
+    const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
+    const T rdx1 = rc.dxg[i], rdx2 = rc.dxg[i + 1], rdx3 = rc.dx[i];
+    const T rdy3 = rc.dy[j];
+    const T rdz1 = rc.dz[k], rdz2 = rc.dz[k + 1], rdz3 = rc.dzg[k + 1];
     // 1) -dw^2/dz (equations.f90:370-384)
     T a = h * (W(i, j, k) + W(i, j, k + 1));
     T b = h * (W(i, j, k - 1) + W(i, j, k));
-    T r = -(a * a - b * b) / (zg[k + 1] - zg[k]);
+    T r = -(a * a - b * b) * rdz3;
     // 2) -duw/dx (:389-406)
     T uz1 = h * (U(i, j, k) + U(i, j, k + 1));
     T uz0 = h * (U(i - 1, j, k) + U(i - 1, j, k + 1));
     T wx1 = h * (W(i, j, k) + W(i + 1, j, k));
     T wx0 = h * (W(i - 1, j, k) + W(i, j, k));
-    r += -(uz1 * wx1 - uz0 * wx0) / (x[i] - x[i - 1]);
+    r += -(uz1 * wx1 - uz0 * wx0) * rdx3;
     // 3) -dvw/dy (:411-428)
     T vz1 = h * (V(i, j, k) + V(i, j, k + 1));
     T vz0 = h * (V(i, j - 1, k) + V(i, j - 1, k + 1));
     T wy1 = w0[j] * W(i, j, k) + w1[j] * W(i, j + 1, k);
     T wy0 = w0[j - 1] * W(i, j - 1, k) + w1[j - 1] * W(i, j, k);
-    r += -(vz1 * wy1 - vz0 * wy0) / (y[j] - y[j - 1]);
+    r += -(vz1 * wy1 - vz0 * wy0) * rdy3;
     // 4) viscous (:435-493)
-    T dx_1 = xg[i] - xg[i - 1], dx_2 = xg[i + 1] - xg[i], dx_3 = x[i] - x[i - 1];
-    T dy_3 = y[j] - y[j - 1];
-    T dz_1 = z[k] - z[k - 1], dz_2 = z[k + 1] - z[k], dz_3 = zg[k + 1] - zg[k];
-    T t2j = (W(i, j + 1, k) - W(i, j, k)) / (yg[j + 1] - yg[j]);
-    T t2jm = (W(i, j, k) - W(i, j - 1, k)) / (yg[j] - yg[j - 1]);
+    T t2j = (W(i, j + 1, k) - W(i, j, k)) * rc.dyg[j + 1];
+    T t2jm = (W(i, j, k) - W(i, j - 1, k)) * rc.dyg[j];
     T nu_x1 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i - 1, j, k) + nt(i - 1, j, k + 1));
     T nu_x2 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i + 1, j, k) + nt(i + 1, j, k + 1));
     T nu_y1 = nu + h * (w0[j - 1] * nt(i, j - 1, k) + w1[j - 1] * nt(i, j, k) + w0[j - 1] * nt(i, j - 1, k + 1) +
@@ -271,11 +275,11 @@ __device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const A &U, const A &
     T nu_y2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i, j, k + 1) + w1[j] * nt(i, j + 1, k + 1));
     T nu_z1 = nu + nt(i, j, k);
     T nu_z2 = nu + nt(i, j, k + 1);
-    T visc = T(1) / dx_3 * (nu_x2 * ((W(i + 1, j, k) - W(i, j, k)) / dx_2 + (U(i, j, k + 1) - U(i, j, k)) / dz_2) -
-                            nu_x1 * ((W(i, j, k) - W(i - 1, j, k)) / dx_1 + (U(i - 1, j, k + 1) - U(i - 1, j, k)) / dz_1)) +
-             T(1) / dy_3 * (nu_y2 * (t2j + (V(i, j, k + 1) - V(i, j, k)) / dz_2) -
-                            nu_y1 * (t2jm + (V(i, j - 1, k + 1) - V(i, j - 1, k)) / dz_1)) +
-             T(2) / dz_3 * (nu_z2 * (W(i, j, k + 1) - W(i, j, k)) / dz_2 - nu_z1 * (W(i, j, k) - W(i, j, k - 1)) / dz_1);
+    T visc = rdx3 * (nu_x2 * ((W(i + 1, j, k) - W(i, j, k)) * rdx2 + (U(i, j, k + 1) - U(i, j, k)) * rdz2) -
+                     nu_x1 * ((W(i, j, k) - W(i - 1, j, k)) * rdx1 + (U(i - 1, j, k + 1) - U(i - 1, j, k)) * rdz1)) +
+             rdy3 * (nu_y2 * (t2j + (V(i, j, k + 1) - V(i, j, k)) * rdz2) -
+                     nu_y1 * (t2jm + (V(i, j - 1, k + 1) - V(i, j - 1, k)) * rdz1)) +
+             T(2) * rdz3 * (nu_z2 * (W(i, j, k + 1) - W(i, j, k)) * rdz2 - nu_z1 * (W(i, j, k) - W(i, j, k - 1)) * rdz1);
     r += visc;
     r += dPdz;  // :496
     return r;
@@ -345,7 +349,7 @@ __device__ __forceinline__ void rk_apply(T r, T f1, T uo, T uolo, bool has_lo, i
 
 // mode: 0 = store F(slot); 1 = fused update from Uo with F1 (s = 1 stores F1)
 template <typename T, int COMP>
-__global__ void k_rhs(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds, T nu, T Om,
+__global__ void k_rhs(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds, T nu, T Om,
                       Fld<T> out, Fld<T> F1, Fld<T> Uo, Fld<T> Uolo, Fld<T> Unlo, int mode, int s, RkCoef rk,
                       int i1, int j1, int k1) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
@@ -353,9 +357,9 @@ __global__ void k_rhs(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const 
     int k = blockIdx.z + 2;
     if (i > i1 || j > j1 || k > k1) return;
     T r;
-    if (COMP == 0) r = rhs_u_point<T, Fld<T>>(g, U, V, W, nt, nu, ds_dpdx<T>(ds), Om, i, j, k);
-    else if (COMP == 1) r = rhs_v_point<T, Fld<T>>(g, U, V, W, nt, nu, Om, i, j, k);
-    else r = rhs_w_point<T, Fld<T>>(g, U, V, W, nt, nu, ds_dpdz<T>(ds), i, j, k);
+    if (COMP == 0) r = rhs_u_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdx<T>(ds), Om, i, j, k);
+    else if (COMP == 1) r = rhs_v_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, Om, i, j, k);
+    else r = rhs_w_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdz<T>(ds), i, j, k);
     if (mode == 0) {
         out(i, j, k) = r;
         return;
@@ -409,9 +413,9 @@ static int rhs_launch(cf_ctx *ctx, int comp, int src, int mode, int s, int slot,
     dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
     T nu = (T)ctx->prm.nu, Om = (T)ctx->omega_z;
     RkCoef rk = rk_coefs();
-    if (comp == 0) k_rhs<T, 0><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
-    else if (comp == 1) k_rhs<T, 1><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
-    else k_rhs<T, 2><<<grd, blk, 0, ctx->st>>>(g, U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    if (comp == 0) k_rhs<T, 0><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    else if (comp == 1) k_rhs<T, 1><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    else k_rhs<T, 2><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
     count_launch(ctx, "k_rhs");
     CF_CUDA(cudaGetLastError());
     return 0;
@@ -439,8 +443,11 @@ struct Trio {
     Fld<T> u, v, w;
 };
 
+// planes per z chunk of the fused RHS (its z spacings sit in shared memory)
+constexpr int RHS_ZMAX = 256;
+
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds,
+__global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds,
                                                      T nu, T Om, Trio<T> out, Trio<T> F1, Trio<T> Uo, Trio<T> Uolo,
                                                      Trio<T> Unlo, int s, RkCoef rk, int kc_len) {
     constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
@@ -451,28 +458,37 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, Fld<T> U, Fld<T> 
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int i = i0 + tx, j = j0 + ty;
     const T dt = ds_dt<T>(ds), dPdx = ds_dpdx<T>(ds), dPdz = ds_dpdz<T>(ds);
-    // the tile's x and y geometry in shared memory; gl indexes it with the
-    // global 1-based indices (z stays in global memory: uniform per plane)
-    __shared__ T gxs[2][TX + 3], gys[4][TY + 3];
+    // the tile's x and y reciprocal spacings and interpolation weights, and
+    // the chunk's z reciprocal spacings, in shared memory; gl and rcs index
+    // them with the global 1-based indices
+    __shared__ T gxs[2][TX + 3], gys[4][TY + 3], gzs[2][RHS_ZMAX + 2];
     for (int t = threadIdx.x; t < TX + 3; t += TX * TY) {
-        int ii = min(i0 - 1 + t, nxg);
-        gxs[0][t] = g.x[min(ii, nx)];
-        gxs[1][t] = g.xg[ii];
+        const int ii = i0 - 1 + t;
+        gxs[0][t] = rc.dx[min(ii, nx + 1)];
+        gxs[1][t] = rc.dxg[min(ii, nxg + 1)];
     }
     for (int t = threadIdx.x; t < TY + 3; t += TX * TY) {
-        int jj = min(j0 - 1 + t, nyg);
-        gys[0][t] = g.y[min(jj, ny)];
-        gys[1][t] = g.yg[jj];
+        const int jj = j0 - 1 + t;
+        gys[0][t] = rc.dy[min(jj, ny + 1)];
+        gys[1][t] = rc.dyg[min(jj, nyg + 1)];
         gys[2][t] = g.w0[min(jj, ny)];
         gys[3][t] = g.w1[min(jj, ny)];
     }
+    for (int t = threadIdx.x; t < ke - kb + 2; t += TX * TY) {
+        const int kk = kb + t;
+        gzs[0][t] = rc.dz[min(kk, nz + 1)];
+        gzs[1][t] = rc.dzg[min(kk, nzg + 1)];
+    }
     GeoT<T> gl = g;
-    gl.x = gxs[0] - (i0 - 1);
-    gl.xg = gxs[1] - (i0 - 1);
-    gl.y = gys[0] - (j0 - 1);
-    gl.yg = gys[1] - (j0 - 1);
     gl.w0 = gys[2] - (j0 - 1);
     gl.w1 = gys[3] - (j0 - 1);
+    RcpT<T> rcs;
+    rcs.dx = gxs[0] - (i0 - 1);
+    rcs.dxg = gxs[1] - (i0 - 1);
+    rcs.dy = gys[0] - (j0 - 1);
+    rcs.dyg = gys[1] - (j0 - 1);
+    rcs.dz = gzs[0] - kb;
+    rcs.dzg = gzs[1] - kb;
     const bool du = i <= nx - 1 && j <= nyg - 1, dv = i <= nxg - 1 && j <= ny - 1, dw = i <= nxg - 1 && j <= nyg - 1;
     const bool lo = Uolo.u.p != nullptr;
     // this thread's tile elements (same for every plane and field)
@@ -531,15 +547,15 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, Fld<T> U, Fld<T> 
         aU.j0 = aV.j0 = aW.j0 = aN.j0 = j0;
         aU.kc = aV.kc = aW.kc = aN.kc = k;
         if (cu) {
-            T r = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, aU, aV, aW, aN, nu, dPdx, Om, i, j, k);
+            T r = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, i, j, k);
             rk_apply<T>(r, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, rk, dt);
         }
         if (cv) {
-            T r = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, aU, aV, aW, aN, nu, Om, i, j, k);
+            T r = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, i, j, k);
             rk_apply<T>(r, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, rk, dt);
         }
         if (cw) {
-            T r = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, aU, aV, aW, aN, nu, dPdz, i, j, k);
+            T r = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k);
             rk_apply<T>(r, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, rk, dt);
         }
         __syncthreads();            // plane k-1 no longer read
@@ -574,10 +590,10 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
     Trio<T> Uolo = trio(ctx->Ulo[o], ctx->Vlo[o], ctx->Wlo[o]);
     Trio<T> Unlo = s == 3 ? trio(ctx->Ulo[dst], ctx->Vlo[dst], ctx->Wlo[dst]) : trio(nullptr, nullptr, nullptr);
     int ntx = cdiv(ctx->nx - 1, TX), nty = cdiv(ctx->nyg - 2, TY);
-    int nkc = ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1;
+    int nkc = std::max(ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1, cdiv(ctx->nzg - 2, RHS_ZMAX));
     int kc_len = cdiv(ctx->nzg - 2, nkc);
     k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(ctx->nzg - 2, kc_len)), TX * TY, 0, ctx->st>>>(
-        g, U, V, W, nt, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len);
+        g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len);
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
     return 0;
