@@ -65,6 +65,7 @@ static int alloc(cf_ctx *ctx, void **p, size_t n) {
     return 0;
 }
 
+#define DISPATCH(call_d, call_f) (ctx->esz == 8 ? (call_d) : (call_f))
 #define TRY(x)                  \
     do {                        \
         int rc_ = (x);          \
@@ -643,7 +644,10 @@ extern "C" int cf_download_fields(cf_ctx *ctx, double *U, double *V, double *W, 
     if (V) TRY(get(ctx, V, ctx->V[b], ctx->Vlo[b], ctx->nV));
     if (W) TRY(get(ctx, W, ctx->W[b], ctx->Wlo[b], ctx->nW));
     if (P) TRY(get(ctx, P, ctx->P, nullptr, ctx->nC));
-    if (nu_t) TRY(get(ctx, nu_t, ctx->nut, nullptr, ctx->nC));
+    if (nu_t) {
+        TRY(DISPATCH(launch_nut_materialize<double>(ctx), launch_nut_materialize<float>(ctx)));
+        TRY(get(ctx, nu_t, ctx->nut, nullptr, ctx->nC));
+    }
     CF_CUDA(cudaStreamSynchronize(ctx->st));
     return CF_OK;
 }
@@ -717,7 +721,6 @@ extern "C" int cf_set_fixed_dt(cf_ctx *ctx, double dt) {
 // ---------------------------------------------------------------------------
 // dispatch on precision
 // ---------------------------------------------------------------------------
-#define DISPATCH(call_d, call_f) (ctx->esz == 8 ? (call_d) : (call_f))
 
 __global__ void k_scale(double *p, long n, const double *f) {
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;

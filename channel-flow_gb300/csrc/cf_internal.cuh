@@ -101,6 +101,9 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
     lo = e - (hi - s);
 }
 
+// periodic index for i in [2 - np, 2 np + 1] (compares only)
+__host__ __device__ __forceinline__ int wrapn(int i, int np) { return i < 2 ? i + np : (i > np + 1 ? i - np : i); }
+
 __host__ __device__ __forceinline__ int wrapc(int i, int np) {
     // canonical index of a periodic index (faces or centres): 2 + (i-2) mod np
     int r = (i - 2) % np;
@@ -151,6 +154,10 @@ struct cf_ctx {
     bool use_rhs3 = true;              // one fused RHS + update launch per substep
     int rhs_nkc = 1;                   // z chunks of the fused RHS
     bool state_periodic = false;       // U, V, W satisfy the periodic/no-slip ghost identities
+    // After the one-pass eddy viscosity, nu_t is held as |S| (canonical) and
+    // the plane coefficient <LM>/<MM>: the fused RHS forms nu_t on the fly and
+    // the nut buffer is filled only when another reader needs it.
+    bool nut_lazy = false;
     // pressure
     void *phi = nullptr;               // canonical real
     void *spec = nullptr;              // complex spectrum [j][kz][kx]: mode m = kz*nxh + kx contiguous per row
@@ -205,6 +212,7 @@ template <typename T> int launch_rk_update(cf_ctx *ctx, int s);            // fr
 template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // eddy viscosity
 template <typename T> int launch_dsm_fused(cf_ctx *ctx, int buf);          // fused pass (periodic state)
 template <typename T> int launch_nut_zero(cf_ctx *ctx);
+template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut if held lazily
 template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true);
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode);  // 1: x mass flow, 2: centre-line, 3: y

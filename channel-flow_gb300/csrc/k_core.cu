@@ -149,7 +149,7 @@ struct RkCoef {
 // 1/(x(i)-x(i-1)) = rc.dx[i], and so on.
 template <typename T, typename A, typename RC>
 __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
-                                         const A &nt, T nu, T dPdx, T Om, int i, int j, int k) {
+                                         const A &nt, T nu, T dPdx, T Om, bool rot, int i, int j, int k) {
     const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
     const T rdx1 = rc.dx[i], rdx2 = rc.dx[i + 1], rdx3 = rc.dxg[i + 1];
@@ -188,7 +188,7 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A
                      nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) * rdz1 + (W(i + 1, j, k - 1) - W(i, j, k - 1)) * rdx1));
     r += visc;
     r += dPdx;  // :166
-    if (fabs((double)Om) > 1e-6) {  // :169-177
+    if (rot) {  // |Om| > 1e-6, :169-177
         T tv0 = h * (V(i, j - 1, k) + V(i, j, k));
         T tv1 = h * (V(i + 1, j - 1, k) + V(i + 1, j, k));
         r += T(2) * Om * (h * (tv0 + tv1));
@@ -198,7 +198,7 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A
 
 template <typename T, typename A, typename RC>
 __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
-                                         const A &nt, T nu, T Om, int i, int j, int k) {
+                                         const A &nt, T nu, T Om, bool rot, int i, int j, int k) {
     const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5);
     const T rdx1 = rc.dxg[i], rdx2 = rc.dxg[i + 1], rdx3 = rc.dx[i];
@@ -233,7 +233,7 @@ __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const RC &rc, const A
              rdz3 * (nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) * rdz2 + (W(i, j + 1, k) - W(i, j, k)) * rdy3) -
                      nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) * rdz1 + (W(i, j + 1, k - 1) - W(i, j, k - 1)) * rdy3));
     r += visc;
-    if (fabs((double)Om) > 1e-6) {  // :334-342
+    if (rot) {  // :334-342
         T tu0 = h * (U(i - 1, j, k) + U(i, j, k));
         T tu1 = h * (U(i - 1, j + 1, k) + U(i, j + 1, k));
         r -= T(2) * Om * (w0[j] * tu0 + w1[j] * tu1);
@@ -318,18 +318,17 @@ __device__ __forceinline__ void rk_store(T r, int i, int j, int k, const Fld<T> 
 }
 
 // The same update with its operands already loaded (f1 = F1 for s > 1, uo and
-// uolo = the old state and its low word).
+// uolo = the old state and its low word) and the substep's coefficients in T
+// (ca: of F1 -- or of r when s = 1 --, cb: of r).
 template <typename T>
 __device__ __forceinline__ void rk_apply(T r, T f1, T uo, T uolo, bool has_lo, int i, int j, int k, const Fld<T> &out,
-                                         const Fld<T> &F1, const Fld<T> &Unlo, int s, const RkCoef &rk, T dt) {
+                                         const Fld<T> &F1, const Fld<T> &Unlo, int s, T ca, T cb, T dt) {
     T inc;
     if (s == 1) {
         F1(i, j, k) = r;
-        inc = dt * T(rk.c[1][1]) * r;
-    } else if (s == 2) {
-        inc = dt * (T(rk.c[2][1]) * f1 + T(rk.c[2][2]) * r);
+        inc = dt * ca * r;
     } else {
-        inc = dt * (T(rk.c[3][1]) * f1 + T(rk.c[3][3]) * r);
+        inc = dt * (ca * f1 + cb * r);
     }
     if constexpr (sizeof(T) == 4) {
         if (has_lo) {
@@ -357,8 +356,9 @@ __global__ void k_rhs(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T
     int k = blockIdx.z + 2;
     if (i > i1 || j > j1 || k > k1) return;
     T r;
-    if (COMP == 0) r = rhs_u_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdx<T>(ds), Om, i, j, k);
-    else if (COMP == 1) r = rhs_v_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, Om, i, j, k);
+    const bool rot = fabs((double)Om) > 1e-6;
+    if (COMP == 0) r = rhs_u_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdx<T>(ds), Om, rot, i, j, k);
+    else if (COMP == 1) r = rhs_v_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, Om, rot, i, j, k);
     else r = rhs_w_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdz<T>(ds), i, j, k);
     if (mode == 0) {
         out(i, j, k) = r;
@@ -381,6 +381,7 @@ static RkCoef rk_coefs() {
 
 template <typename T>
 static int rhs_launch(cf_ctx *ctx, int comp, int src, int mode, int s, int slot, int dst) {
+    if (int rc = launch_nut_materialize<T>(ctx)) return rc;
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[src], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[src], ctx->nxg, ctx->ny);
@@ -443,13 +444,25 @@ struct Trio {
     Fld<T> u, v, w;
 };
 
+// nu_t held as |S| on canonical cells and the plane coefficient C(j):
+// nu_t(i,j,k) = max(-C(jj)|S|(wrap i, jj, wrap k)/2, 0), jj = j clamped to
+// the interior, negated on the wall ghost rows for Dirichlet_nu_t
+// (subgrid.f90:521-536).  S == nullptr: read the nut field instead.
+template <typename T>
+struct NutSrc {
+    const T *S;
+    const T *C;  // 1-based rows
+    int nxp, nym, nzp, dirichlet;
+};
+
 // planes per z chunk of the fused RHS (its z spacings sit in shared memory)
 constexpr int RHS_ZMAX = 256;
 
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds,
-                                                     T nu, T Om, Trio<T> out, Trio<T> F1, Trio<T> Uo, Trio<T> Uolo,
-                                                     Trio<T> Unlo, int s, RkCoef rk, int kc_len) {
+__global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
+                                                     NutSrc<T> ns, const DevScal *ds, T nu, T Om, Trio<T> out,
+                                                     Trio<T> F1, Trio<T> Uo, Trio<T> Uolo, Trio<T> Unlo, int s,
+                                                     RkCoef rk, int kc_len) {
     constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
     __shared__ T ring[3][4][NP];  // [plane slot][field U V W nu_t][tile]
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxg = g.nxg, nyg = g.nyg, nzg = g.nzg;
@@ -458,6 +471,9 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int i = i0 + tx, j = j0 + ty;
     const T dt = ds_dt<T>(ds), dPdx = ds_dpdx<T>(ds), dPdz = ds_dpdz<T>(ds);
+    const T ca = T(s == 1 ? rk.c[1][1] : (s == 2 ? rk.c[2][1] : rk.c[3][1]));
+    const T cb = T(s == 1 ? 0.0 : (s == 2 ? rk.c[2][2] : rk.c[3][3]));
+    const bool rot = fabs((double)Om) > 1e-6;
     // the tile's x and y reciprocal spacings and interpolation weights, and
     // the chunk's z reciprocal spacings, in shared memory; gl and rcs index
     // them with the global 1-based indices
@@ -501,9 +517,27 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T
         eia[q] = i0 + sx - 1;
         eja[q] = j0 + sy - 1;
     }
+    // nu_t from |S|: per element the plane coefficient (with the ghost-row
+    // sign folded in; 0 outside the field) and the (i, j) part of the
+    // canonical index are fixed for the whole march
+    T ncf[NL], nsg[NL];
+    int nbase[NL];
+    const long nplane = (long)ns.nxp * ns.nym;
+    if (ns.S) {
+#pragma unroll
+        for (int q = 0; q < NL; q++) {
+            const int ia = eia[q], ja = eja[q];
+            const bool ok = erem[q] < NP && ia <= nxg && ja <= nyg;
+            const int jj = ja == 1 ? 2 : (ja == nyg ? nyg - 1 : ja);
+            nsg[q] = ok ? ((jj != ja && ns.dirichlet) ? T(-1) : T(1)) : T(0);
+            ncf[q] = ok ? T(-0.5) * ns.C[jj] : T(0);
+            nbase[q] = ok ? (wrapn(ia, ns.nxp) - 2) + ns.nxp * (jj - 2) : 0;
+        }
+    }
     // all loads of one plane are issued before any of them is used
     T pre[4][NL];
     auto fetch = [&](int k) {
+        const long koff = nplane * (wrapn(k, ns.nzp) - 2);
 #pragma unroll
         for (int q = 0; q < NL; q++) {
             const int ia = eia[q], ja = eja[q];
@@ -511,7 +545,8 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T
             pre[0][q] = (in && ia <= nx && ja <= nyg && k <= nzg) ? U(ia, ja, k) : T(0);
             pre[1][q] = (in && ia <= nxg && ja <= ny && k <= nzg) ? V(ia, ja, k) : T(0);
             pre[2][q] = (in && ia <= nxg && ja <= nyg && k <= nz) ? W(ia, ja, k) : T(0);
-            pre[3][q] = (in && ia <= nxg && ja <= nyg && k <= nzg) ? nt(ia, ja, k) : T(0);
+            if (ns.S) pre[3][q] = (nsg[q] != T(0) && k <= nzg) ? ns.S[nbase[q] + koff] : T(0);  // |S|, formed at commit
+            else pre[3][q] = (in && ia <= nxg && ja <= nyg && k <= nzg) ? nt(ia, ja, k) : T(0);
         }
     };
     auto commit = [&](int slot) {
@@ -519,7 +554,14 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T
         for (int q = 0; q < NL; q++)
             if (erem[q] < NP) {
 #pragma unroll
-                for (int f = 0; f < 4; f++) ring[slot][f][erem[q]] = pre[f][q];
+                for (int f = 0; f < 3; f++) ring[slot][f][erem[q]] = pre[f][q];
+                T n = pre[3][q];
+                if (ns.S) {
+                    // max(-C|S|/2, 0), negated on Dirichlet ghost rows (nsg = -1), 0 outside (nsg = 0)
+                    const T v = ncf[q] * n;
+                    n = nsg[q] * (v > T(0) ? v : T(0));
+                }
+                ring[slot][3][erem[q]] = n;
             }
     };
     fetch(kb - 1);
@@ -547,16 +589,16 @@ __global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T
         aU.j0 = aV.j0 = aW.j0 = aN.j0 = j0;
         aU.kc = aV.kc = aW.kc = aN.kc = k;
         if (cu) {
-            T r = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, i, j, k);
-            rk_apply<T>(r, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, rk, dt);
+            T r = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, rot, i, j, k);
+            rk_apply<T>(r, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, ca, cb, dt);
         }
         if (cv) {
-            T r = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, i, j, k);
-            rk_apply<T>(r, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, rk, dt);
+            T r = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, rot, i, j, k);
+            rk_apply<T>(r, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, ca, cb, dt);
         }
         if (cw) {
             T r = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k);
-            rk_apply<T>(r, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, rk, dt);
+            rk_apply<T>(r, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, ca, cb, dt);
         }
         __syncthreads();            // plane k-1 no longer read
         if (k + 1 <= ke) commit(sm1);  // plane k+2 into the freed slot
@@ -592,8 +634,17 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
     int ntx = cdiv(ctx->nx - 1, TX), nty = cdiv(ctx->nyg - 2, TY);
     int nkc = std::max(ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1, cdiv(ctx->nzg - 2, RHS_ZMAX));
     int kc_len = cdiv(ctx->nzg - 2, nkc);
+    NutSrc<T> ns = {};
+    if (ctx->nut_lazy) {
+        ns.S = (const T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
+        ns.C = sizeof(T) == 8 ? (const T *)ctx->avg_nu_t : (const T *)(ctx->avg_nu_t + ctx->nyg + 2);
+        ns.nxp = ctx->nxp;
+        ns.nym = ctx->nym;
+        ns.nzp = ctx->nzp;
+        ns.dirichlet = ctx->prm.Dirichlet_nu_t == 1;
+    }
     k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(ctx->nzg - 2, kc_len)), TX * TY, 0, ctx->st>>>(
-        g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len);
+        g, rcp_of<T>(ctx), U, V, W, nt, ns, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len);
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
     return 0;

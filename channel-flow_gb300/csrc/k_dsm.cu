@@ -203,28 +203,36 @@ __global__ void k_dsm_d(GeoT<T> g, Fld<T> Uf, Fld<T> Vf, Fld<T> Wf, const T *lf,
 }
 
 // Stage E: avg_nu_t(j) = <LM>/<MM> (subgrid.f90:516-518) and its ghosts.
+// <LM>/<MM> per row from the block partial sums: one warp per row, lanes
+// over chunks in a fixed order, then the ghost rows (subgrid.f90:515-519).
 __global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, int dirichlet) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x + 2;
-    if (j <= nyg - 1) {
-        double a = 0.0, b = 0.0;
-        for (int q = 0; q < nchunk; q++) {
-            a += part[((long)(j - 2) * nchunk + q) * 2];
-            b += part[((long)(j - 2) * nchunk + q) * 2 + 1];
+    const int lane = threadIdx.x & 31;
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) + 2;
+    if (j > nyg - 1) return;
+    double a = 0.0, b = 0.0;
+    for (int q = lane; q < nchunk; q += 32) {
+        a += part[((long)(j - 2) * nchunk + q) * 2];
+        b += part[((long)(j - 2) * nchunk + q) * 2 + 1];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        float *af = (float *)(avg + nyg + 2);  // FP32 copy for the split path
+        const double c = a / b;
+        avg[j] = c;
+        af[j] = (float)c;
+        if (j == 2) {
+            avg[1] = dirichlet ? -c : c;
+            af[1] = (float)avg[1];
         }
-        avg[j] = a / b;
-        ((float *)(avg + nyg + 2))[j] = (float)(a / b);  // FP32 copy for the split path
+        if (j == nyg - 1) {
+            avg[nyg] = dirichlet ? -c : c;
+            af[nyg] = (float)avg[nyg];
+        }
     }
 }
-__global__ void k_dsm_e2(int nyg, double *avg, int dirichlet) {
-    if (threadIdx.x == 0) {
-        avg[1] = dirichlet ? -avg[2] : avg[2];
-        avg[nyg] = dirichlet ? -avg[nyg - 1] : avg[nyg - 1];
-        float *af = (float *)(avg + nyg + 2);
-        af[1] = (float)avg[1];
-        af[nyg] = (float)avg[nyg];
-    }
-}
-
 // Stage F: nu_t = max(-0.5 C(j) |S|, 0) everywhere, periodic copies and the
 // wall ghost rule (subgrid.f90:521-536).
 template <typename T>
@@ -250,8 +258,25 @@ __global__ void k_fill(T *p, long n, T v) {
     if (t < n) p[t] = v;
 }
 
+// Fills nut from |S| and the plane coefficient when it is held lazily.
+template <typename T>
+int launch_nut_materialize(cf_ctx *ctx) {
+    if (!ctx->nut_lazy) return 0;
+    Can c;
+    c.nxp = ctx->nxp; c.nym = ctx->nym; c.nzp = ctx->nzp; c.n = (long)ctx->nCan;
+    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+    T *q = (T *)ctx->dsm_q;
+    k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), dim3(32, 4, 1), 0, ctx->st>>>(
+        nt, q + Q_S * c.n, ctx->avg_nu_t, c, ctx->nxg, ctx->nyg, ctx->nzg, ctx->prm.Dirichlet_nu_t == 1);
+    count_launch(ctx, "k_dsm_f");
+    ctx->nut_lazy = false;
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
 template <typename T>
 int launch_nut_zero(cf_ctx *ctx) {
+    ctx->nut_lazy = false;
     k_fill<T><<<cdiv(ctx->nC, 256), 256, 0, ctx->st>>>((T *)ctx->nut, (long)ctx->nC, T(0));
     count_launch(ctx, "k_fill");
     k_fill<double><<<1, 256, 0, ctx->st>>>(ctx->avg_nu_t, ctx->nyg + 1, 0.0);
@@ -271,17 +296,13 @@ int launch_dsm(cf_ctx *ctx, int b) {
         int rc = launch_dsm_fused<T>(ctx, b);
         if (rc) return rc;
         int nch = ctx->dsm_nchunk_fused;
-        k_dsm_e<<<cdiv(ctx->nym, 64), 64, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir);
-        k_dsm_e2<<<1, 32, 0, ctx->st>>>(ctx->nyg, ctx->avg_nu_t, dir);
-        count_launch(ctx, "k_dsm_e"); count_launch(ctx, "k_dsm_e2");
-        Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
-        T *q = (T *)ctx->dsm_q;
-        k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(
-            nt, q + Q_S * c.n, ctx->avg_nu_t, c, ctx->nxg, ctx->nyg, ctx->nzg, dir);
-        count_launch(ctx, "k_dsm_f");
+        k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir);
+        count_launch(ctx, "k_dsm_e");
+        ctx->nut_lazy = true;  // nu_t = max(-C(j)|S|/2, 0) is formed by its readers
         CF_CUDA(cudaGetLastError());
         return 0;
     }
+    ctx->nut_lazy = false;
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
@@ -302,9 +323,8 @@ int launch_dsm(cf_ctx *ctx, int b) {
     int nchunk = ctx->dsm_nblk;
     k_dsm_d<T><<<dim3(nchunk, ctx->nym), 256, 0, ctx->st>>>(g, Uf, Vf, Wf, lf, c, ctx->dsm_part, nchunk);
     count_launch(ctx, "k_dsm_d");
-    k_dsm_e<<<cdiv(ctx->nym, 64), 64, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
-    k_dsm_e2<<<1, 32, 0, ctx->st>>>(ctx->nyg, ctx->avg_nu_t, dir);
-    count_launch(ctx, "k_dsm_e"); count_launch(ctx, "k_dsm_e2");
+    k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
+    count_launch(ctx, "k_dsm_e");
     Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
     k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(nt, q + Q_S * c.n, ctx->avg_nu_t, c,
                                                                                             ctx->nxg, ctx->nyg, ctx->nzg, dir);
@@ -316,4 +336,6 @@ int launch_dsm(cf_ctx *ctx, int b) {
 template int launch_dsm<double>(cf_ctx *, int);
 template int launch_dsm<float>(cf_ctx *, int);
 template int launch_nut_zero<double>(cf_ctx *);
+template int launch_nut_materialize<double>(cf_ctx *);
+template int launch_nut_materialize<float>(cf_ctx *);
 template int launch_nut_zero<float>(cf_ctx *);

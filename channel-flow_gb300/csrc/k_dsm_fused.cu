@@ -27,6 +27,22 @@
 // periodic index for i in [2 - np, 2 np + 1]
 __device__ __forceinline__ int wrapq(int i, int np) { return i < 2 ? i + np : (i > np + 1 ? i - np : i); }
 
+// Pairs of quantities filtered together: packed FP32x2 arithmetic (one
+// instruction for two lanes of work) in the split path, plain FP64 pairs
+// otherwise.
+template <typename T> struct PairT;
+template <> struct PairT<float> { typedef float2 t; };
+template <> struct PairT<double> { typedef double2 t; };
+
+__device__ __forceinline__ float2 pfma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 pmul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 psplat(float a) { return make_float2(a, a); }
+__device__ __forceinline__ double2 pfma(double2 a, double2 b, double2 c) {
+    return make_double2(fma(a.x, b.x, c.x), fma(a.y, b.y, c.y));
+}
+__device__ __forceinline__ double2 pmul(double2 a, double2 b) { return make_double2(a.x * b.x, a.y * b.y); }
+__device__ __forceinline__ double2 psplat(double a) { return make_double2(a, a); }
+
 struct RGeo {  // reciprocal spacings, 1-based like the coordinates
     const void *rdx, *rdxg, *rdy, *rdyg, *rdz, *rdzg;
 };
@@ -48,7 +64,8 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
     T *R = (T *)sm_raw;         // [slot 3][field 3][RY][RX]
     T *G = R + SM::NR;          // [slot 3][field 3][QY][QX]
     T *F = G + SM::NG;          // [slot 3][field 3][QY][QX]
-    T *Qs = F + SM::NF;         // [16][QY][QX]
+    typedef typename PairT<T>::t PT;
+    PT *Qs = (PT *)(F + SM::NF);  // [8 pairs][QY][QX]
     const T *rdx = (const T *)rgv.rdx, *rdxg = (const T *)rgv.rdxg, *rdy = (const T *)rgv.rdy,
             *rdyg = (const T *)rgv.rdyg, *rdz = (const T *)rgv.rdz, *rdzg = (const T *)rgv.rdzg;
     const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0), h = T(0.5), qq = T(0.25);
@@ -61,7 +78,7 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
     auto RS = [&](int slot, int f, int sy, int sx) -> T & { return R[((slot * 3 + f) * RY + sy) * RX + sx]; };
     auto GS = [&](int slot, int f, int sy, int sx) -> T & { return G[((slot * 3 + f) * QY + sy) * QX + sx]; };
     auto FS = [&](int slot, int f, int sy, int sx) -> T & { return F[((slot * 3 + f) * QY + sy) * QX + sx]; };
-    auto QS = [&](int q, int sy, int sx) -> T & { return Qs[(q * QY + sy) * QX + sx]; };
+    auto QS = [&](int p, int sy, int sx) -> PT & { return Qs[(p * QY + sy) * QX + sx]; };
 
     // y filter weights of a row in [lo, hi] (one-sided at the ends)
     auto yw = [&](int j, int lo, int hi, T &wm, T &w0, T &wp) {
@@ -85,14 +102,25 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
         gsy[1][t] = rdyg[jj];
         gsy[2][t] = rdyg[jj + 1];
     }
-    T acc[3][15];
+    // z-accumulators of the x-y filtered pairs (uc,vc) (wc,uu) (vv,ww) (uv,uw)
+    // (vw,|S|S11) (|S|S22,|S|S33) (|S|S12,|S|S13) (|S|S23,|S|) for the three
+    // planes in flight
+    PT acc[3][8];
 #pragma unroll
     for (int s = 0; s < 3; s++)
 #pragma unroll
-        for (int q = 0; q < 15; q++) acc[s][q] = T(0);
+        for (int q = 0; q < 8; q++) acc[s][q] = psplat(T(0));
     T Sprev = T(0);
     T sl = T(0), smm = T(0);  // this thread's plane sums (widened per block)
 
+    // this thread's point of the halo ring of the QX x QY region (top row,
+    // bottom row, left column, right column), if any
+    const bool hal = tid < 2 * QX + 2 * TY;
+    int hsx = 0, hsy = 0;
+    if (tid < QX) { hsx = tid; hsy = 0; }
+    else if (tid < 2 * QX) { hsx = tid - QX; hsy = QY - 1; }
+    else if (tid < 2 * QX + TY) { hsx = 0; hsy = tid - 2 * QX + 1; }
+    else if (hal) { hsx = QX - 1; hsy = tid - 2 * QX - TY + 1; }
     const int rs = kb - 2, re = ke + 2;
     // one march step for raw plane r; PH = (r - rs) % 3 is the ring phase
     // raw-tile elements of this thread (same for every plane)
@@ -132,44 +160,48 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
         constexpr int PH = decltype(PHc)::value;
         constexpr int P1 = (PH + 1) % 3, P2 = (PH + 2) % 3;
         if (r + 1 <= re) fetch(r + 1);
-        // -- G(r): x-y filtered U, V, W on the tile + 1 halo
-        for (int t = tid; t < 3 * QX * QY; t += TX * TY) {
-            int f = t / (QX * QY), rem = t % (QX * QY), sy = rem / QX, sx = rem % QX;
-            int j = j0 + sy - 1;
-            int jhi = f == 1 ? ny : nyg;
-            T g = T(0);
-            if (j >= 1 && j <= jhi) {
-                T wm, w0, wp;
-                yw(j, 1, jhi, wm, w0, wp);
-                int dm = j > 1 ? -1 : 0, dp = j < jhi ? 1 : 0;
+        // G(r), F(r-1) and Q(r-1) at this thread's points of the tile + 1 halo
+        // (its own point, and one point of the halo ring for the first
+        // 2 QX + 2 TY threads): G and F at a point only need that point's G
+        // history, and Q only the raw planes already in the ring.
+        const int kq = wrapc(r - 1, nzp);
+        const T rz = rdz[kq], rzg0 = rdzg[kq], rzg1 = rdzg[kq + 1];
+        for (int pt = 0; pt < 2; pt++) {
+            if (pt == 1 && !hal) break;
+            const int sx = pt ? hsx : tx + 1, sy = pt ? hsy : ty + 1;
+            const int j = j0 + sy - 1;
+            // -- G(r): x-y filtered U, V, W
+            T gc[3];
 #pragma unroll
-                for (int a = -1; a <= 1; a++) {
-                    int rx = sx + 1 + a, ry = sy + 1;
-                    T yv = wm * RS(PH, f, ry + dm, rx) + w0 * RS(PH, f, ry, rx) + wp * RS(PH, f, ry + dp, rx);
-                    g += fw[a + 1] * yv;
+            for (int f = 0; f < 3; f++) {
+                const int jhi = f == 1 ? ny : nyg;
+                T g = T(0);
+                if (j >= 1 && j <= jhi) {
+                    T wm, w0, wp;
+                    yw(j, 1, jhi, wm, w0, wp);
+                    const int dm = j > 1 ? -1 : 0, dp = j < jhi ? 1 : 0;
+#pragma unroll
+                    for (int a = -1; a <= 1; a++) {
+                        const int rx = sx + 1 + a, ry = sy + 1;
+                        const T yv = wm * RS(PH, f, ry + dm, rx) + w0 * RS(PH, f, ry, rx) + wp * RS(PH, f, ry + dp, rx);
+                        g += fw[a + 1] * yv;
+                    }
                 }
+                GS(PH, f, sy, sx) = g;
+                gc[f] = g;
             }
-            GS(PH, f, sy, sx) = g;
-        }
-        __syncthreads();
-        if (r >= kb) {
+            if (r < kb) continue;
             // -- F(r-1) = z filter of G(r-2), G(r-1), G(r)
-            for (int t = tid; t < 3 * QX * QY; t += TX * TY) {
-                int f = t / (QX * QY), rem = t % (QX * QY), sy = rem / QX, sx = rem % QX;
-                FS(P2, f, sy, sx) = f6 * GS(P1, f, sy, sx) + f23 * GS(P2, f, sy, sx) + f6 * GS(PH, f, sy, sx);
-            }
-            // -- Q(r-1) from R(r-2) [P1], R(r-1) [P2], R(r) [PH]
-            const int kq = wrapc(r - 1, nzp);
-            const T rz = rdz[kq], rzg0 = rdzg[kq], rzg1 = rdzg[kq + 1];
-            for (int t = tid; t < QX * QY; t += TX * TY) {
-                int sy = t / QX, sx = t % QX;
-                int j = j0 + sy - 1;
-                if (j < 2 || j > nyg - 1) {
 #pragma unroll
-                    for (int q = 0; q < 16; q++) QS(q, sy, sx) = T(0);
-                    continue;
-                }
-                int rx = sx + 1, ry = sy + 1;  // raw slot of the centre
+            for (int f = 0; f < 3; f++) FS(P2, f, sy, sx) = f6 * GS(P1, f, sy, sx) + f23 * GS(P2, f, sy, sx) + f6 * gc[f];
+            // -- Q(r-1) from R(r-2) [P1], R(r-1) [P2], R(r) [PH]
+            if (j < 2 || j > nyg - 1) {
+#pragma unroll
+                for (int q = 0; q < 8; q++) QS(q, sy, sx) = psplat(T(0));
+                continue;
+            }
+            {
+                const int rx = sx + 1, ry = sy + 1;  // raw slot of the centre
                 // raw accessors with offsets (di, dj, dk), dk in {-1, 0, 1}
                 auto u = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 0, ry + dj, rx + di); };
                 auto v = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 1, ry + dj, rx + di); };
@@ -196,12 +228,17 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
                 s3 *= qq; s4 *= qq; s5 *= qq;
                 T S = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
                            T(4) * s5 * s5);
-                QS(0, sy, sx) = uc; QS(1, sy, sx) = vc; QS(2, sy, sx) = wc;
-                QS(3, sy, sx) = uc * uc; QS(4, sy, sx) = vc * vc; QS(5, sy, sx) = wc * wc;
-                QS(6, sy, sx) = uc * vc; QS(7, sy, sx) = uc * wc; QS(8, sy, sx) = vc * wc;
-                QS(9, sy, sx) = S * s0; QS(10, sy, sx) = S * s1; QS(11, sy, sx) = S * s2;
-                QS(12, sy, sx) = S * s3; QS(13, sy, sx) = S * s4; QS(14, sy, sx) = S * s5;
-                QS(15, sy, sx) = S;
+                PT q0, q1, q2, q3, q4, q5, q6, q7;
+                q0.x = uc; q0.y = vc;
+                q1.x = wc; q1.y = uc * uc;
+                q2.x = vc * vc; q2.y = wc * wc;
+                q3.x = uc * vc; q3.y = uc * wc;
+                q4.x = vc * wc; q4.y = S * s0;
+                q5.x = S * s1; q5.y = S * s2;
+                q6.x = S * s3; q6.y = S * s4;
+                q7.x = S * s5; q7.y = S;
+                QS(0, sy, sx) = q0; QS(1, sy, sx) = q1; QS(2, sy, sx) = q2; QS(3, sy, sx) = q3;
+                QS(4, sy, sx) = q4; QS(5, sy, sx) = q5; QS(6, sy, sx) = q6; QS(7, sy, sx) = q7;
             }
         }
         __syncthreads();
@@ -211,15 +248,20 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
             yw(jo, 2, nyg - 1, wm, w0, wp);
             const int sx = tx + 1, sy = ty + 1;
             const int dm = jo > 2 ? -1 : 0, dp = jo < nyg - 1 ? 1 : 0;
+            const PT pwm = psplat(wm), pw0 = psplat(w0), pwp = psplat(wp), pf6 = psplat(f6), pf23 = psplat(f23);
 #pragma unroll
-            for (int q = 0; q < 15; q++) {
-                T a = T(0);
+            for (int q = 0; q < 8; q++) {
+                PT a = psplat(T(0));
 #pragma unroll
-                for (int d = -1; d <= 1; d++)
-                    a += fw[d + 1] * (wm * QS(q, sy + dm, sx + d) + w0 * QS(q, sy, sx + d) + wp * QS(q, sy + dp, sx + d));
-                acc[P1][q] += f6 * a;   // plane r-2 (last contribution)
-                acc[P2][q] += f23 * a;  // plane r-1
-                acc[PH][q] = f6 * a;    // plane r (first contribution; the slot held plane r-3)
+                for (int d = -1; d <= 1; d++) {
+                    PT c = pmul(pw0, QS(q, sy, sx + d));
+                    c = pfma(pwm, QS(q, sy + dm, sx + d), c);
+                    c = pfma(pwp, QS(q, sy + dp, sx + d), c);
+                    a = pfma(psplat(fw[d + 1]), c, a);
+                }
+                acc[P1][q] = pfma(pf6, a, acc[P1][q]);   // plane r-2 (last contribution)
+                acc[P2][q] = pfma(pf23, a, acc[P2][q]);  // plane r-1
+                acc[PH][q] = pmul(pf6, a);               // plane r (first contribution; the slot held plane r-3)
             }
             if (r >= kb + 2) {
                 // -- output plane k = r-2: S_ij of Uf, Vf, Wf from F(r-3) [PH], F(r-2) [P1], F(r-1) [P2]
@@ -248,13 +290,21 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
                             T(4) * s5 * s5);
                 const T fs2 = T(4);  // fil_size**2 (subgrid.f90:156, 463)
                 const T sf[6] = {s0, s1, s2, s3, s4, s5};
-                const T fu = acc[P1][0], fv = acc[P1][1], fwv = acc[P1][2];
+                // filtered quantities of plane r-2 in the order uc vc wc uu vv ww uv uw vw |S|S11..|S|S23
+                T fq[15];
+#pragma unroll
+                for (int q = 0; q < 7; q++) {
+                    fq[2 * q] = acc[P1][q].x;
+                    fq[2 * q + 1] = acc[P1][q].y;
+                }
+                fq[14] = acc[P1][7].x;
+                const T fu = fq[0], fv = fq[1], fwv = fq[2];
                 const T pa[6] = {fu, fv, fwv, fu, fu, fv}, pb[6] = {fu, fv, fwv, fv, fwv, fwv};
                 T lm = T(0), mm = T(0);
 #pragma unroll
                 for (int q = 0; q < 6; q++) {
-                    T L = acc[P1][3 + q] - pa[q] * pb[q];
-                    T M = fs2 * Sf * sf[q] - acc[P1][9 + q];
+                    T L = fq[3 + q] - pa[q] * pb[q];
+                    T M = fs2 * Sf * sf[q] - fq[9 + q];
                     T wq = q < 3 ? T(1) : T(2);
                     lm += wq * L * M;
                     mm += wq * M * M;
@@ -264,7 +314,7 @@ __global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld
                 smm += wgt * mm;
                 Sout[(long)(io - 2) + (long)nxp * ((jo - 2) + (long)(nyg - 2) * (kcn - 2))] = Sprev;
             }
-            Sprev = QS(15, sy, sx);  // |S| at plane r-1 for the next output
+            Sprev = QS(7, sy, sx).y;  // |S| at plane r-1 for the next output
         }
         // R(r-2) (slot P1) was last read by Q(r-1): R(r+1) takes its place
         if (r + 1 <= re) commit(P1);

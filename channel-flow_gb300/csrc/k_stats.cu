@@ -98,6 +98,7 @@ __global__ void k_stats_wall(Geo g, Fld<T> U, Fld<T> V, Fld<T> nt, double *out) 
 
 template <typename T>
 int launch_stats(cf_ctx *ctx, int b, double *d_out) {
+    if (int rc = launch_nut_materialize<T>(ctx)) return rc;
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
     Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
