@@ -499,7 +499,9 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     // avg_nu_t (1..nyg) in FP64, followed by an FP32 copy
     CF_CUDA(cudaMalloc(&ctx->avg_nu_t, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
     CF_CUDA(cudaMemset(ctx->avg_nu_t, 0, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
-    ctx->red_n = std::max(ctx->nzg + 8, ctx->nxg + ctx->nyg + ctx->nzg + 16);
+    // reduction scratch: dt minima, mass-flow partials (one per plane and
+    // chunk of 16 rows), the divergence check in the last 4 slots
+    ctx->red_n = std::max({ctx->nzg + 8, ctx->nxg + ctx->nyg + ctx->nzg + 16, (ctx->nzg - 2) * cdiv(ctx->nyg - 2, 16) + 16});
     CF_CUDA(cudaMalloc(&ctx->d_red, (size_t)ctx->red_n * sizeof(double)));
     CF_CUDA(cudaMalloc(&ctx->ds, sizeof(DevScal)));
     TRY(push_scal(ctx));
@@ -973,34 +975,39 @@ static int enqueue_step(cf_ctx *ctx) {
         TRY(eddy(ctx, X));
     }
     // substeps 1 and 2 hold intermediate stages: the split path keeps a low
-    // word only for u^n and the new state of substep 3
+    // word only for u^n and the new state of substep 3.  The boundary
+    // conditions between the RK update and the projection
+    // (time_integration.f90:113) are not launched: the projection reads
+    // only interior values plus the periodic neighbours below the first
+    // interior index, which it takes through the wrap, and the update itself
+    // reproduces the periodic duplicate columns bit for bit; the call after
+    // the projection fills every ghost.
     TRY(launch_rhs_update<T>(ctx, 1, X, a));
     ctx->cur = a;
-    TRY(launch_bc<T>(ctx, a, false));
     TRY(launch_projection<T>(ctx, a, true, false));
     TRY(launch_bc<T>(ctx, a, false));
     // substep 2 (:118-131)
     TRY(eddy(ctx, a));
     TRY(launch_rhs_update<T>(ctx, 2, a, b));
     ctx->cur = b;
-    TRY(launch_bc<T>(ctx, b, false));
     TRY(launch_projection<T>(ctx, b, false, false));
     TRY(launch_bc<T>(ctx, b, false));
     // substep 3 (:134-150)
     TRY(eddy(ctx, b));
     TRY(launch_rhs_update<T>(ctx, 3, b, a));
     ctx->cur = a;
-    TRY(launch_bc<T>(ctx, a));
     TRY(launch_projection<T>(ctx, a, false));
     TRY(launch_bc<T>(ctx, a));
-    // mass-flow forcing (:153-171)
+    // mass-flow forcing (:153-171); with no-slip walls the correction is
+    // added to the ghosts as apply_boundary_conditions would propagate it
+    const bool g = ctx->prm.iwall_model == 0;
     if (ctx->prm.x_mass_cte == 1 || ctx->prm.x_mass_cte == 2) {
-        TRY(launch_mass_flow<T>(ctx, a, ctx->prm.x_mass_cte));
-        TRY(launch_bc<T>(ctx, a));
+        TRY(launch_mass_flow<T>(ctx, a, ctx->prm.x_mass_cte, g));
+        if (!g) TRY(launch_bc<T>(ctx, a));
     }
     if (ctx->prm.y_mass_cte == 1) {
-        TRY(launch_mass_flow<T>(ctx, a, 3));
-        TRY(launch_bc<T>(ctx, a));
+        TRY(launch_mass_flow<T>(ctx, a, 3, g));
+        if (!g) TRY(launch_bc<T>(ctx, a));
     }
     ctx->old = a;
     return 0;

@@ -215,9 +215,9 @@ template <typename T> int launch_nut_zero(cf_ctx *ctx);
 template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut if held lazily
 template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true);
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
-template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode);  // 1: x mass flow, 2: centre-line, 3: y
+template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only
-template <typename T> int launch_mass_apply(cf_ctx *ctx, int buf, int mode); // add ds->lmax[2], dPdx = it/dt
+template <typename T> int launch_mass_apply(cf_ctx *ctx, int buf, int mode, bool ghosts = false); // add ds->lmax[2], dPdx = it/dt (ghosts: whole array, as the BCs would)
 template <typename T> int launch_dt(cf_ctx *ctx, int buf);
 template <typename T> int launch_eqwm(cf_ctx *ctx, int buf);
 template <typename T> int launch_copy_state(cf_ctx *ctx, int src, int dst);

@@ -738,30 +738,46 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
     return r;
 }
 
-// mode 1: trapezoid of U (mass_flow.f90:116-123), one block per k plane
+// mode 1: trapezoid of U (mass_flow.f90:116-123):
+//   sum_{j=3}^{nyg-1} (U_j + U_{j-1}) (yg_j - yg_{j-1})/2 = sum_j c_j sum_i U_ij
+// with c_j the two adjacent half-intervals.  Block (k plane, MASS_JR rows),
+// one warp per row at a time: the row sum over i is accumulated
+// compensated (hi + lo TwoSum) in the state's precision, so that the FP64
+// work is one multiply-add per row.
+constexpr int MASS_JR = 16;
 template <typename T>
-__global__ void k_mass_partial(Fld<T> U, const double *yg, int nx, int nyg, double *part) {
-    // sum_{j=3}^{nyg-1} (U_j + U_{j-1}) (yg_j - yg_{j-1})/2 = sum_j U_j c_j with
-    // c_j the two adjacent half-intervals: one FP64 FMA per element
-    __shared__ double sh[32];
-    __shared__ double cw[520];
-    int k = blockIdx.x + 2;
-    for (int j = threadIdx.x + 2; j <= nyg - 1; j += blockDim.x)
-        cw[j] = (j >= 3 ? 0.5 * (yg[j] - yg[j - 1]) : 0.0) + (j <= nyg - 2 ? 0.5 * (yg[j + 1] - yg[j]) : 0.0);
-    __syncthreads();
-    double s = 0.0;
-    constexpr int JB = 8;
-    for (int i = threadIdx.x + 2; i <= nx - 1; i += blockDim.x)
-        for (int j0 = 2; j0 <= nyg - 1; j0 += JB) {
-            T u[JB];
-#pragma unroll
-            for (int r = 0; r < JB; r++) u[r] = (j0 + r <= nyg - 1) ? U(i, j0 + r, k) : T(0);
-#pragma unroll
-            for (int r = 0; r < JB; r++)
-                if (j0 + r <= nyg - 1) s += cw[j0 + r] * (double)u[r];
+__global__ void __launch_bounds__(256) k_mass_partial(Fld<T> U, const double *yg, int nx, int nyg, double *part) {
+    __shared__ double sh[8];
+    const int k = blockIdx.x + 2, j0 = 2 + blockIdx.y * MASS_JR;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    double acc = 0.0;
+    for (int r = wp; r < MASS_JR; r += nw) {
+        const int j = j0 + r;
+        if (j > nyg - 1) break;
+        double rsum;
+        if constexpr (sizeof(T) == 4) {
+            float hi = 0.f, lo = 0.f;
+#pragma unroll 8
+            for (int i = lane + 2; i <= nx - 1; i += 32) ff_add(hi, lo, U(i, j, k));
+            rsum = (double)hi + (double)lo;
+        } else {
+            rsum = 0.0;
+#pragma unroll 8
+            for (int i = lane + 2; i <= nx - 1; i += 32) rsum += U(i, j, k);
         }
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) part[blockIdx.x] = s;
+        for (int o = 16; o > 0; o >>= 1) rsum += __shfl_down_sync(0xffffffffu, rsum, o);
+        if (lane == 0) {
+            const double c = (j >= 3 ? 0.5 * (yg[j] - yg[j - 1]) : 0.0) + (j <= nyg - 2 ? 0.5 * (yg[j + 1] - yg[j]) : 0.0);
+            acc += c * rsum;
+        }
+    }
+    if (lane == 0) sh[wp] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int q = 0; q < nw; q++) s += sh[q];
+        part[blockIdx.x * gridDim.y + blockIdx.y] = s;
+    }
 }
 
 // mode 2: centre-line sum (mass_flow.f90:203-204), planes k = 1..nzg-2
@@ -790,11 +806,14 @@ __global__ void k_massv_partial(Fld<T> V, const double *y, int nxg, int ny, doub
     if (threadIdx.x == 0) part[blockIdx.x] = s;
 }
 
-// final: the correction into ds (mass_flow.f90:130, 174, 209)
-__global__ void k_mass_final(const double *part, int n, DevScal *ds, int mode, double norm) {
-    if (threadIdx.x != 0) return;
+// final: the correction into ds (mass_flow.f90:130, 174, 209); the
+// partials are summed in a fixed order (lane-strided, then the block tree)
+__global__ void __launch_bounds__(256) k_mass_final(const double *part, int n, DevScal *ds, int mode, double norm) {
+    __shared__ double sh[32];
     double s = 0.0;
-    for (int q = 0; q < n; q++) s += part[q];
+    for (int q = threadIdx.x; q < n; q += blockDim.x) s += part[q];
+    s = block_sum(s, sh);
+    if (threadIdx.x != 0) return;
     ds->mass_sum = s;
     double corr;
     if (mode == 1) corr = ds->Qflow_x_0 - s / norm;
@@ -806,12 +825,19 @@ __global__ void k_mass_final(const double *part, int n, DevScal *ds, int mode, d
 
 // add the correction to the interior and store dPdx = corr/dt
 // (time_integration.f90:154-156, 159-161, 167-169)
+// KP planes per thread, every load issued before the first store
+constexpr int MASS_KP = 4;
+// i0 = 2: interior only (i0..i1, i0..j1, i0..k1).  i0 = 1: the whole array,
+// ghosts included, as apply_boundary_conditions would leave it afterwards:
+// +c on the rows 2..j1 (periodic copies included) and wsign*c on the wall
+// ghost rows 1 and j1+1 (-1: no-slip ghosts of U, 0: the wall faces of V).
 template <typename T>
-__global__ void k_mass_apply(Fld<T> F, Fld<T> Flo, DevScal *ds, int i1, int j1, int k1, int mode) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
-    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-    int k = blockIdx.z + 2;
-    if (i == 2 && j == 2 && k == 2) {
+__global__ void __launch_bounds__(128) k_mass_apply(Fld<T> F, Fld<T> Flo, DevScal *ds, int i1, int j1, int k1, int mode,
+                                                    int i0, int wsign) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + i0;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + i0;
+    const int k0 = blockIdx.z * MASS_KP + i0;
+    if (i == i0 && j == i0 && k0 == i0) {
         double corr = ds->lmax[2];
         if (mode == 3) ds->dPdy = corr / ds->dt;
         else {
@@ -819,18 +845,37 @@ __global__ void k_mass_apply(Fld<T> F, Fld<T> Flo, DevScal *ds, int i1, int j1, 
             ds->dPdxf = (float)ds->dPdx;
         }
     }
-    if (i > i1 || j > j1 || k > k1) return;
+    if (i > i1 || j > j1) return;
+    const bool wall = i0 == 1 && (j == 1 || j == j1);
+    if (wall && wsign == 0) return;
+    T h[MASS_KP], l[MASS_KP];
+    const bool lo = Flo.p != nullptr;
+#pragma unroll
+    for (int q = 0; q < MASS_KP; q++) {
+        const int k = k0 + q;
+        h[q] = k <= k1 ? F(i, j, k) : T(0);
+        l[q] = (lo && k <= k1) ? Flo(i, j, k) : T(0);
+    }
     if constexpr (sizeof(T) == 4) {
-        if (Flo.p) {
-            float hi = F(i, j, k), lo = Flo(i, j, k);
-            ff_add(hi, lo, ds->corrf);
-            F(i, j, k) = hi;
-            Flo(i, j, k) = lo;
-            return;
+        const float c = wall ? -ds->corrf : ds->corrf;
+#pragma unroll
+        for (int q = 0; q < MASS_KP; q++) {
+            const int k = k0 + q;
+            if (k > k1) break;
+            if (lo) {
+                float hi = h[q], lw = l[q];
+                ff_add(hi, lw, c);
+                F(i, j, k) = hi;
+                Flo(i, j, k) = lw;
+            } else {
+                F(i, j, k) = h[q] + c;
+            }
         }
-        F(i, j, k) = F(i, j, k) + ds->corrf;
     } else {
-        F(i, j, k) = F(i, j, k) + ds->lmax[2];
+        const double c = wall ? -ds->lmax[2] : ds->lmax[2];
+#pragma unroll
+        for (int q = 0; q < MASS_KP; q++)
+            if (k0 + q <= k1) F(i, j, k0 + q) = h[q] + c;
     }
 }
 
@@ -840,8 +885,10 @@ static int mass_partial(cf_ctx *ctx, int b, int mode) {
     int nb = ctx->nzg - 2;
     double norm;
     if (mode == 1) {
-        k_mass_partial<T><<<nb, 256, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), ctx->geo.yg, ctx->nx,
-                                                    ctx->nyg, part);
+        const int njc = cdiv(ctx->nyg - 2, MASS_JR);
+        k_mass_partial<T><<<dim3(nb, njc), 256, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), ctx->geo.yg,
+                                                               ctx->nx, ctx->nyg, part);
+        nb *= njc;
         norm = ctx->mass_norm;
     } else if (mode == 2) {
         int jc = ctx->ny / 2 + 1;
@@ -853,7 +900,7 @@ static int mass_partial(cf_ctx *ctx, int b, int mode) {
         norm = ctx->mass_norm_vv;
     }
     count_launch(ctx, "k_mass_partial");
-    k_mass_final<<<1, 32, 0, ctx->st>>>(part, nb, ctx->ds, mode, norm);
+    k_mass_final<<<1, 256, 0, ctx->st>>>(part, nb, ctx->ds, mode, norm);
     count_launch(ctx, "k_mass_final");
     CF_CUDA(cudaGetLastError());
     return 0;
@@ -865,24 +912,39 @@ int launch_mass_value(cf_ctx *ctx, int b, int mode) {
 }
 
 template <typename T>
-int launch_mass_flow(cf_ctx *ctx, int b, int mode) {
+int launch_mass_flow(cf_ctx *ctx, int b, int mode, bool ghosts) {
     int rc = mass_partial<T>(ctx, b, mode);
     if (rc) return rc;
-    return launch_mass_apply<T>(ctx, b, mode);
+    return launch_mass_apply<T>(ctx, b, mode, ghosts);
 }
 
 template <typename T>
-int launch_mass_apply(cf_ctx *ctx, int b, int mode) {
+int launch_mass_apply(cf_ctx *ctx, int b, int mode, bool ghosts) {
+    dim3 blk(32, 4, 1);
     if (mode == 3) {
-        int i1 = ctx->nxg - 1, j1 = ctx->ny - 1, k1 = ctx->nzg - 1;
-        dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
-        k_mass_apply<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
-                                                  make_fld<T>(ctx->Vlo[b], ctx->nxg, ctx->ny), ctx->ds, i1, j1, k1, mode);
+        if (ghosts) {
+            int i1 = ctx->nxg, j1 = ctx->ny, k1 = ctx->nzg;
+            k_mass_apply<T><<<dim3(cdiv(i1, 32), cdiv(j1, 4), cdiv(k1, MASS_KP)), blk, 0, ctx->st>>>(
+                make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny), make_fld<T>(ctx->Vlo[b], ctx->nxg, ctx->ny), ctx->ds, i1, j1,
+                k1, mode, 1, 0);
+        } else {
+            int i1 = ctx->nxg - 1, j1 = ctx->ny - 1, k1 = ctx->nzg - 1;
+            k_mass_apply<T><<<dim3(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), cdiv(k1 - 1, MASS_KP)), blk, 0, ctx->st>>>(
+                make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny), make_fld<T>(ctx->Vlo[b], ctx->nxg, ctx->ny), ctx->ds, i1, j1,
+                k1, mode, 2, 0);
+        }
     } else {
-        int i1 = ctx->nx - 1, j1 = ctx->nyg - 1, k1 = ctx->nzg - 1;
-        dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
-        k_mass_apply<T><<<grd, blk, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg),
-                                                  make_fld<T>(ctx->Ulo[b], ctx->nx, ctx->nyg), ctx->ds, i1, j1, k1, mode);
+        if (ghosts) {
+            int i1 = ctx->nx, j1 = ctx->nyg, k1 = ctx->nzg;
+            k_mass_apply<T><<<dim3(cdiv(i1, 32), cdiv(j1, 4), cdiv(k1, MASS_KP)), blk, 0, ctx->st>>>(
+                make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->Ulo[b], ctx->nx, ctx->nyg), ctx->ds, i1, j1,
+                k1, mode, 1, -1);
+        } else {
+            int i1 = ctx->nx - 1, j1 = ctx->nyg - 1, k1 = ctx->nzg - 1;
+            k_mass_apply<T><<<dim3(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), cdiv(k1 - 1, MASS_KP)), blk, 0, ctx->st>>>(
+                make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->Ulo[b], ctx->nx, ctx->nyg), ctx->ds, i1, j1,
+                k1, mode, 2, 0);
+        }
     }
     count_launch(ctx, "k_mass_apply");
     CF_CUDA(cudaGetLastError());
@@ -1069,9 +1131,9 @@ int launch_div_check(cf_ctx *ctx, int b, double *d_out) {
     template int launch_rhs_update<T>(cf_ctx *, int, int, int);      \
     template int launch_rk_update<T>(cf_ctx *, int);                 \
     template int launch_copy_state<T>(cf_ctx *, int, int);           \
-    template int launch_mass_flow<T>(cf_ctx *, int, int);            \
+    template int launch_mass_flow<T>(cf_ctx *, int, int, bool);      \
     template int launch_mass_value<T>(cf_ctx *, int, int);           \
-    template int launch_mass_apply<T>(cf_ctx *, int, int);           \
+    template int launch_mass_apply<T>(cf_ctx *, int, int, bool);     \
     template int launch_dt<T>(cf_ctx *, int);                        \
     template int launch_div_check<T>(cf_ctx *, int, double *);
 INST(double)

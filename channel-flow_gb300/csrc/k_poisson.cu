@@ -241,6 +241,10 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
         k = (int)(pair / nym) * 2 + 2;
     }
     C *a = sm + (long)lp * 2 * n, *b = a + n;
+    // the x and z neighbours below the first interior index are read through
+    // the periodic wrap (U(1) = U(nxp+1), W(k=1) = W(nzp+1)), so the ghosts
+    // need not be filled before this kernel
+    const int km = k == 2 ? nzp + 1 : k - 1;
     if (active) {
         if constexpr (sizeof(T) == 4) {
             // split path: reciprocal spacings instead of divisions
@@ -248,11 +252,11 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
 #pragma unroll
             for (int i = tid + 2; i <= (N > 0 ? N : n) + 1; i += (N > 0 ? fft_x_threads(N) : G)) {
                 const float rx = rs.rx[i];
-                const int k1 = k + 1;
+                const int k1 = k + 1, im = i == 2 ? n + 1 : i - 1;
                 const float w0 = W(i, j, k), w1 = W(i, j, k1);
-                T d0 = (U(i, j, k) - U(i - 1, j, k)) * rx + (V(i, j, k) - V(i, j - 1, k)) * ry +
-                       (w0 - W(i, j, k - 1)) * rz0;
-                T d1 = (U(i, j, k1) - U(i - 1, j, k1)) * rx + (V(i, j, k1) - V(i, j - 1, k1)) * ry +
+                T d0 = (U(i, j, k) - U(im, j, k)) * rx + (V(i, j, k) - V(i, j - 1, k)) * ry +
+                       (w0 - W(i, j, km)) * rz0;
+                T d1 = (U(i, j, k1) - U(im, j, k1)) * rx + (V(i, j, k1) - V(i, j - 1, k1)) * ry +
                        (w1 - w0) * rz1;
                 C z;
                 z.x = d0;
@@ -261,11 +265,12 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
             }
         } else {
             for (int i = tid + 2; i <= n + 1; i += G) {
-                T d0 = (U(i, j, k) - U(i - 1, j, k)) / (g.x[i] - g.x[i - 1]) +
+                const int im = i == 2 ? n + 1 : i - 1;
+                T d0 = (U(i, j, k) - U(im, j, k)) / (g.x[i] - g.x[i - 1]) +
                        (V(i, j, k) - V(i, j - 1, k)) / (g.y[j] - g.y[j - 1]) +
-                       (W(i, j, k) - W(i, j, k - 1)) / (g.z[k] - g.z[k - 1]);
+                       (W(i, j, k) - W(i, j, km)) / (g.z[k] - g.z[k - 1]);
                 int k1 = k + 1;
-                T d1 = (U(i, j, k1) - U(i - 1, j, k1)) / (g.x[i] - g.x[i - 1]) +
+                T d1 = (U(i, j, k1) - U(im, j, k1)) / (g.x[i] - g.x[i - 1]) +
                        (V(i, j, k1) - V(i, j - 1, k1)) / (g.y[j] - g.y[j - 1]) +
                        (W(i, j, k1) - W(i, j, k1 - 1)) / (g.z[k1] - g.z[k1 - 1]);
                 C z;
@@ -299,6 +304,10 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
 // Element kz of a line sits at ((j*nzp + kz)*nh + kx), so for one kz the
 // lines of a block are (mostly) adjacent in memory.
 // ---------------------------------------------------------------------------
+// compile-time z transforms run with 16 lines x 16 threads per block, so a
+// thread copies every 16th element of its line
+constexpr int FFTZ_KZS = 16;
+
 template <typename T, int N>
 __global__ void k_fft_z(typename C2<T>::t *spec, FftPlan pl, const typename C2<T>::t *tw_g, int nlines, int nh, int LB) {
     typedef typename C2<T>::t C;
@@ -316,8 +325,18 @@ __global__ void k_fft_z(typename C2<T>::t *spec, FftPlan pl, const typename C2<T
         const long j = L / nh, kx = L - j * nh;
         gbase = j * n * nh + kx;
     }
-    // load: element (line l, position kz) at sm[l*LS + kz]
-    for (int kz = kz0; kz < n; kz += kzs) sm[(long)cl * LS + kz] = lact ? spec[gbase + (long)kz * nh] : cmk<C>(0.0, 0.0);
+    // load: element (line l, position kz) at sm[l*LS + kz]; with a
+    // compile-time length every load of the thread is issued first
+    if constexpr (N > 0) {
+        constexpr int NPT = N / FFTZ_KZS;
+        C v[NPT];
+#pragma unroll
+        for (int e = 0; e < NPT; e++) v[e] = lact ? spec[gbase + (long)(kz0 + e * FFTZ_KZS) * nh] : cmk<C>(0.0, 0.0);
+#pragma unroll
+        for (int e = 0; e < NPT; e++) sm[(long)cl * LS + kz0 + e * FFTZ_KZS] = v[e];
+    } else {
+        for (int kz = kz0; kz < n; kz += kzs) sm[(long)cl * LS + kz] = lact ? spec[gbase + (long)kz * nh] : cmk<C>(0.0, 0.0);
+    }
     __syncthreads();
     const int l = threadIdx.x / G, tid = threadIdx.x % G;
     C *a = sm + (long)l * LS, *b = a + n;
@@ -766,38 +785,106 @@ __device__ __forceinline__ void proj_update(const Fld<T> &F, const Fld<T> &Flo, 
     F(i, j, k) = F(i, j, k) - grad;
 }
 
-template <typename T>
-__global__ void k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ulo, Fld<T> V, Fld<T> Vlo, Fld<T> W, Fld<T> Wlo, const T *phi,
-                           PhiView pv, RSpG rs) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-    const int k = blockIdx.z + 2;
-    if (i > g.nxg - 1 || j > g.nyg - 1) return;
-    const T p0 = phi[pv(i, j, k)];
-    T gx = T(0), gy = T(0), gz = T(0);
-    const bool du = i <= g.nx - 1, dv = j <= g.ny - 1, dw = k <= g.nz - 1;
-    if constexpr (sizeof(T) == 4) {
-        if (du) gx = (phi[pv(i + 1, j, k)] - p0) * rs.rxg[i + 1];
-        if (dv) gy = (phi[pv(i, j + 1, k)] - p0) * rs.ryg[j + 1];
-        if (dw) gz = (phi[pv(i, j, k + 1)] - p0) * rs.rzg[k + 1];
-    } else {
-        if (du) gx = (phi[pv(i + 1, j, k)] - p0) / (g.xg[i + 1] - g.xg[i]);
-        if (dv) gy = (phi[pv(i, j + 1, k)] - p0) / (g.yg[j + 1] - g.yg[j]);
-        if (dw) gz = (phi[pv(i, j, k + 1)] - p0) / (g.zg[k + 1] - g.zg[k]);
-    }
-    if (du) proj_update(U, Ulo, i, j, k, gx);
-    if (dv) proj_update(V, Vlo, i, j, k, gy);
-    if (dw) proj_update(W, Wlo, i, j, k, gz);
-}
+// KP consecutive planes per thread: every load of the thread is issued
+// before the first store (the fields may alias as far as the compiler knows).
+constexpr int PROJ_KP = 4;
 
 template <typename T>
-__global__ void k_store_p(Fld<T> P, const T *phi, PhiView pv, const DevScal *ds, double c11, int nxg, int nyg, int nzg) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    int k = blockIdx.z + 1;
+__global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ulo, Fld<T> V, Fld<T> Vlo, Fld<T> W,
+                                                  Fld<T> Wlo, const T *__restrict__ phi, PhiView pv, RSpG rs) {
+    constexpr int KP = PROJ_KP;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
+    const int k0 = blockIdx.z * KP + 2;
+    if (i > g.nxg - 1 || j > g.nyg - 1) return;
+    const bool du = i <= g.nx - 1, dv = j <= g.ny - 1;
+    const bool lo = Ulo.p != nullptr;
+    T p0[KP + 1], px[KP], py[KP];
+    T u[KP], v[KP], w[KP], ul[KP], vl[KP], wl[KP];
+#pragma unroll
+    for (int q = 0; q <= KP; q++) {
+        const int k = k0 + q;
+        p0[q] = k <= g.nzg - 1 ? phi[pv(i, j, k)] : T(0);  // plane k0+KP: the z neighbour of the last plane
+    }
+#pragma unroll
+    for (int q = 0; q < KP; q++) {
+        const int k = k0 + q;
+        const bool kin = k <= g.nzg - 1, dw = k <= g.nz - 1;
+        px[q] = du && kin ? phi[pv(i + 1, j, k)] : T(0);
+        py[q] = dv && kin ? phi[pv(i, j + 1, k)] : T(0);
+        u[q] = du && kin ? U(i, j, k) : T(0);
+        v[q] = dv && kin ? V(i, j, k) : T(0);
+        w[q] = dw ? W(i, j, k) : T(0);
+        if (lo) {
+            ul[q] = du && kin ? Ulo(i, j, k) : T(0);
+            vl[q] = dv && kin ? Vlo(i, j, k) : T(0);
+            wl[q] = dw ? Wlo(i, j, k) : T(0);
+        }
+    }
+    T rx, ry;
+    if constexpr (sizeof(T) == 4) {
+        rx = du ? rs.rxg[i + 1] : T(0);
+        ry = dv ? rs.ryg[j + 1] : T(0);
+    } else {
+        rx = du ? T(1) / (g.xg[i + 1] - g.xg[i]) : T(0);
+        ry = dv ? T(1) / (g.yg[j + 1] - g.yg[j]) : T(0);
+    }
+#pragma unroll
+    for (int q = 0; q < KP; q++) {
+        const int k = k0 + q;
+        if (k > g.nzg - 1) break;
+        T gx, gy, gz;
+        if constexpr (sizeof(T) == 4) {
+            gx = (px[q] - p0[q]) * rx;
+            gy = (py[q] - p0[q]) * ry;
+            gz = k <= g.nz - 1 ? (p0[q + 1] - p0[q]) * rs.rzg[k + 1] : T(0);
+        } else {
+            // projection.f90:209-223 divides by the spacings
+            gx = du ? (px[q] - p0[q]) / (g.xg[i + 1] - g.xg[i]) : T(0);
+            gy = dv ? (py[q] - p0[q]) / (g.yg[j + 1] - g.yg[j]) : T(0);
+            gz = k <= g.nz - 1 ? (p0[q + 1] - p0[q]) / (g.zg[k + 1] - g.zg[k]) : T(0);
+        }
+        (void)rx;
+        (void)ry;
+        auto upd = [&](const Fld<T> &F, const Fld<T> &Flo, T f, T fl, T gr) {
+            if constexpr (sizeof(T) == 4) {
+                if (lo) {
+                    float hi = f, l = fl;
+                    ff_add(hi, l, -gr);
+                    F(i, j, k) = hi;
+                    Flo(i, j, k) = l;
+                    return;
+                }
+            }
+            F(i, j, k) = f - gr;
+        };
+        if (du) upd(U, Ulo, u[q], ul[q], gx);
+        if (dv) upd(V, Vlo, v[q], vl[q], gy);
+        if (k <= g.nz - 1) upd(W, Wlo, w[q], wl[q], gz);
+    }
+}
+
+// P = phi/(dt rk_coef(1,1)) on the full extents, ghosts from the nearest
+// interior cell (projection.f90:129-137, 144-162); KP planes per thread.
+template <typename T>
+__global__ void __launch_bounds__(128) k_store_p(Fld<T> P, const T *__restrict__ phi, PhiView pv, const DevScal *ds,
+                                                 double c11, int nxg, int nyg, int nzg) {
+    constexpr int KP = PROJ_KP;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k0 = blockIdx.z * KP + 1;
     if (i > nxg || j > nyg) return;
-    int ic = min(max(i, 2), nxg - 1), jc = min(max(j, 2), nyg - 1), kc = min(max(k, 2), nzg - 1);
-    P(i, j, k) = phi[pv(ic, jc, kc)] / (ds_dt<T>(ds) * T(c11));
+    const int ic = min(max(i, 2), nxg - 1), jc = min(max(j, 2), nyg - 1);
+    T v[KP];
+#pragma unroll
+    for (int q = 0; q < KP; q++) {
+        const int kc = min(max(k0 + q, 2), nzg - 1);
+        v[q] = k0 + q <= nzg ? phi[pv(ic, jc, kc)] : T(0);
+    }
+    const T den = ds_dt<T>(ds) * T(c11);
+#pragma unroll
+    for (int q = 0; q < KP; q++)
+        if (k0 + q <= nzg) P(i, j, k0 + q) = v[q] / den;
 }
 
 template <typename T>
@@ -830,8 +917,8 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo) {
     while (LP > 1 && smem_pairs<T>(nxp, LP) + nxp * sizeof(C) > 96 * 1024) LP /= 2;
     const size_t shx = smem_pairs<T>(nxp, LP) + nxp * sizeof(C);
     // z transforms: LB lines per block, Gz threads per line
-    const int Gz = nzp >= 128 ? 16 : 8;
-    int LB = 16;
+    const int Gz = 16;
+    int LB = 16;  // with Gz = 16: FFTZ_KZS elements apart per thread in the copies
     while (LB > 1 && smem_pairs<T>(nzp, LB) + (LB + nzp) * sizeof(C) > 96 * 1024) LB /= 2;
     const size_t shz = smem_pairs<T>(nzp, LB) + (LB + nzp) * sizeof(C);
     RSp rs;
@@ -916,7 +1003,7 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo) {
         rg.rxg = ctx->d_rgeo_f + ctx->rgeo_off[1];
         rg.ryg = ctx->d_rgeo_f + ctx->rgeo_off[3];
         rg.rzg = ctx->d_rgeo_f + ctx->rgeo_off[5];
-        k_project3<T><<<dim3(cdiv(ctx->nxg - 2, 32), cdiv(ctx->nyg - 2, 4), ctx->nzg - 2), blk, 0, ctx->st>>>(
+        k_project3<T><<<dim3(cdiv(ctx->nxg - 2, 32), cdiv(ctx->nyg - 2, 4), cdiv(ctx->nzg - 2, PROJ_KP)), blk, 0, ctx->st>>>(
             g, U, make_fld<T>(lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg), V,
             make_fld<T>(lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny), W,
             make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg), phi, pv, rg);
@@ -924,7 +1011,7 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo) {
     }
     if (store_p) {
         Fld<T> P = make_fld<T>(ctx->P, ctx->nxg, ctx->nyg);
-        k_store_p<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(
+        k_store_p<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), cdiv(ctx->nzg, PROJ_KP)), blk, 0, ctx->st>>>(
             P, phi, pv, ctx->ds, 8.0 / 15.0, ctx->nxg, ctx->nyg, ctx->nzg);
         count_launch(ctx, "k_store_p");
     }
