@@ -492,7 +492,9 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
         ctx->use_fused_dsm = !p->dsm_unfused;
         // fused RHS: 32 x 8 column tiles, z chunks for ~4 resident blocks per SM
         long rt = (long)cdiv(nx - 1, 32) * cdiv(ctx->nyg - 2, 8);
-        ctx->rhs_nkc = (int)std::max(1L, std::min((long)(ctx->nzg - 2) / 4, (4L * dev_sms) / std::max(1L, rt)));
+        // z chunks: one wave of resident blocks
+        const long res = (long)rhs3_blocks_per_sm(p->precision == CF_PREC_SPLIT ? 4 : 8) * dev_sms;
+        ctx->rhs_nkc = (int)std::max(1L, std::min((long)(ctx->nzg - 2) / 4, res / std::max(1L, rt)));
     }
     size_t nch = std::max((size_t)ctx->dsm_nblk, nch_fused);
     CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));

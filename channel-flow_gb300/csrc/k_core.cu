@@ -457,9 +457,13 @@ struct NutSrc {
 
 // planes per z chunk of the fused RHS (its z spacings sit in shared memory)
 constexpr int RHS_ZMAX = 256;
+// resident blocks per SM the fused RHS is compiled for: three in FP32 (80
+// registers; the kernel waits on shared-memory and arithmetic latency, so
+// more warps pay), two in FP64
+template <typename T> struct RhsMinB { static constexpr int v = sizeof(T) == 4 ? 3 : 2; };
 
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, 2) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
+__global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
                                                      NutSrc<T> ns, const DevScal *ds, T nu, T Om, Trio<T> out,
                                                      Trio<T> F1, Trio<T> Uo, Trio<T> Uolo, Trio<T> Unlo, int s,
                                                      RkCoef rk, int kc_len) {
@@ -648,6 +652,14 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
     return 0;
+}
+
+// resident fused-RHS blocks per SM (for the z-chunk plan)
+int rhs3_blocks_per_sm(int esz) {
+    int n = 1;
+    if (esz == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rhs3<float, 32, 8>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rhs3<double, 32, 8>, 256, 0);
+    return n < 1 ? 1 : n;
 }
 
 template <typename T>

@@ -54,8 +54,12 @@ struct DsmSmem {
     static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ) * sizeof(T);
 };
 
+// resident blocks per SM the pass is compiled for (three blocks at 80
+// registers spill and run slower than two)
+template <typename T> struct DsmMinB { static constexpr int v = 2; };
+
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, 2) k_dsm_fused(Fld<T> U, Fld<T> V, Fld<T> W, RGeo rgv, int nx, int ny, int nyg,
+__global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, Fld<T> V, Fld<T> W, RGeo rgv, int nx, int ny, int nyg,
                                                       int nz, int nxp, int nzp, int kc_len, T *Sout, double *part,
                                                       int nchunk) {
     typedef DsmSmem<T, TX, TY> SM;
