@@ -505,6 +505,11 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     // chunk of 16 rows), the divergence check in the last 4 slots
     ctx->red_n = std::max({ctx->nzg + 8, ctx->nxg + ctx->nyg + ctx->nzg + 16, (ctx->nzg - 2) * cdiv(ctx->nyg - 2, 16) + 16});
     CF_CUDA(cudaMalloc(&ctx->d_red, (size_t)ctx->red_n * sizeof(double)));
+    {
+        std::vector<double> inf((size_t)ctx->nxg + ctx->nyg + ctx->nzg + 6, INFINITY);
+        CF_CUDA(cudaMalloc(&ctx->d_dtmin, inf.size() * sizeof(double)));
+        CF_CUDA(cudaMemcpy(ctx->d_dtmin, inf.data(), inf.size() * sizeof(double), cudaMemcpyHostToDevice));
+    }
     CF_CUDA(cudaMalloc(&ctx->ds, sizeof(DevScal)));
     TRY(push_scal(ctx));
     TRY(setup_eqwm(ctx));
@@ -526,7 +531,7 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
                     ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->tri_l32, ctx->tri_ru32,
                     ctx->tri_du32, ctx->tri_flag, ctx->tri_list, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
                     ctx->wtemp1, ctx->wtemp2, ctx->eq_grid, ctx->eq_zst, ctx->eq_xst, ctx->eq_zw, ctx->eq_xw, ctx->ds,
-                    ctx->d_red, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage};
+                    ctx->d_red, ctx->d_dtmin, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (int b = 0; b < 3; b++) {

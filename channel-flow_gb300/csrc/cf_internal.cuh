@@ -184,6 +184,7 @@ struct cf_ctx {
     DevScal hs;
     DevScal *ds = nullptr;
     double *d_red = nullptr;           // reduction scratch
+    double *d_dtmin = nullptr;         // compute_dt minima per x, y, z index (+inf between calls)
     int red_n = 0;
     // staging for transfers
     double *stage = nullptr;

@@ -768,16 +768,22 @@ __global__ void __launch_bounds__(256) k_mass_partial(Fld<T> U, const double *yg
         if (j > nyg - 1) break;
         double rsum;
         if constexpr (sizeof(T) == 4) {
+            // lanes and the warp tree in float-float: no FP64 per element or per lane
             float hi = 0.f, lo = 0.f;
 #pragma unroll 8
             for (int i = lane + 2; i <= nx - 1; i += 32) ff_add(hi, lo, U(i, j, k));
+            for (int o = 16; o > 0; o >>= 1) {
+                const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+                ff_add(hi, lo, oh);
+                lo += ol;
+            }
             rsum = (double)hi + (double)lo;
         } else {
             rsum = 0.0;
 #pragma unroll 8
             for (int i = lane + 2; i <= nx - 1; i += 32) rsum += U(i, j, k);
+            for (int o = 16; o > 0; o >>= 1) rsum += __shfl_down_sync(0xffffffffu, rsum, o);
         }
-        for (int o = 16; o > 0; o >>= 1) rsum += __shfl_down_sync(0xffffffffu, rsum, o);
         if (lane == 0) {
             const double c = (j >= 3 ? 0.5 * (yg[j] - yg[j - 1]) : 0.0) + (j <= nyg - 2 ? 0.5 * (yg[j + 1] - yg[j]) : 0.0);
             acc += c * rsum;
@@ -1040,28 +1046,39 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
     }
 }
 
-__global__ void k_dt_init(double *m, int n) {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) m[t] = INFINITY;
-}
 
-__global__ void k_dt_final(const double *mu, const double *mv, const double *mw, Geo g, DevScal *ds, double CFL,
-                           double dt_vis) {
+// The maxima dx/min|u| per direction (one quotient per thread: FP64
+// divisions are slow here, so they run side by side), dt, and the minima
+// reset to +inf for the next call.
+__global__ void __launch_bounds__(1024) k_dt_final(double *mu, double *mv, double *mw, Geo g, DevScal *ds, double CFL,
+                                                   double dt_vis) {
     __shared__ double sh[3][32];
-    double lU = 0.0, lV = 0.0, lW = 0.0;
-    for (int i = threadIdx.x + 2; i <= g.nxg - 1; i += blockDim.x) lU = fmax(lU, (g.xg[i + 1] - g.xg[i]) / mu[i]);
-    for (int j = threadIdx.x + 2; j <= g.nyg - 1; j += blockDim.x) lV = fmax(lV, (g.yg[j + 1] - g.yg[j]) / mv[j]);
-    for (int k = threadIdx.x + 2; k <= g.nzg - 1; k += blockDim.x) lW = fmax(lW, (g.zg[k + 1] - g.zg[k]) / mw[k]);
-    for (int o = 16; o > 0; o >>= 1) {
-        lU = fmax(lU, __shfl_down_sync(0xffffffff, lU, o));
-        lV = fmax(lV, __shfl_down_sync(0xffffffff, lV, o));
-        lW = fmax(lW, __shfl_down_sync(0xffffffff, lW, o));
+    const int nxi = g.nxg - 2, nyi = g.nyg - 2, nzi = g.nzg - 2;
+    double l[3] = {0.0, 0.0, 0.0};
+    for (int t = threadIdx.x; t < nxi + nyi + nzi; t += blockDim.x) {
+        if (t < nxi) {
+            const int i = t + 2;
+            l[0] = fmax(l[0], (g.xg[i + 1] - g.xg[i]) / mu[i]);
+        } else if (t < nxi + nyi) {
+            const int j = t - nxi + 2;
+            l[1] = fmax(l[1], (g.yg[j + 1] - g.yg[j]) / mv[j]);
+        } else {
+            const int k = t - nxi - nyi + 2;
+            l[2] = fmax(l[2], (g.zg[k + 1] - g.zg[k]) / mw[k]);
+        }
     }
-    int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sh[0][w] = lU; sh[1][w] = lV; sh[2][w] = lW; }
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+        for (int o = 16; o > 0; o >>= 1) l[d] = fmax(l[d], __shfl_down_sync(0xffffffff, l[d], o));
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) { sh[0][w] = l[0]; sh[1][w] = l[1]; sh[2][w] = l[2]; }
     __syncthreads();
+    for (int t = threadIdx.x; t < g.nxg + 2; t += blockDim.x) mu[t] = INFINITY;
+    for (int t = threadIdx.x; t < g.nyg + 2; t += blockDim.x) mv[t] = INFINITY;
+    for (int t = threadIdx.x; t < g.nzg + 2; t += blockDim.x) mw[t] = INFINITY;
     if (threadIdx.x != 0) return;
-    for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+    double lU = sh[0][0], lV = sh[1][0], lW = sh[2][0];
+    for (int q = 1; q < nw; q++) {
         lU = fmax(lU, sh[0][q]); lV = fmax(lV, sh[1][q]); lW = fmax(lW, sh[2][q]);
     }
     double du = CFL * lU, dv = CFL * lV, dw = CFL * lW;
@@ -1078,10 +1095,8 @@ __global__ void k_dt_final(const double *mu, const double *mv, const double *mw,
 
 template <typename T>
 int launch_dt(cf_ctx *ctx, int b) {
-    double *mu = ctx->d_red, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
-    int n = ctx->nxg + ctx->nyg + ctx->nzg + 6;
-    k_dt_init<<<cdiv(n, 256), 256, 0, ctx->st>>>(mu, n);
-    count_launch(ctx, "k_dt_init");
+    // minima start at +inf: set at context creation and reset by k_dt_final
+    double *mu = ctx->d_dtmin, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
     k_dt_min<T><<<dim3(cdiv(ctx->nxg - 2, 256), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2)), 256, 0, ctx->st>>>(
         make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
         make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
@@ -1090,7 +1105,7 @@ int launch_dt(cf_ctx *ctx, int b) {
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
            vw = CFL * pow(ctx->dzmin, 2.0) / ctx->prm.nu;
     double dt_vis = fmin(vu, fmin(vv, vw));
-    k_dt_final<<<1, 256, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
+    k_dt_final<<<1, 1024, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
     count_launch(ctx, "k_dt_final");
     CF_CUDA(cudaGetLastError());
     return 0;
