@@ -558,28 +558,46 @@ static int ensure_stage(cf_ctx *ctx, size_t n) {
     return 0;
 }
 
-__global__ void k_split(const double *a, float *hi, float *lo, long n) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) {
-        double v = a[t];
-        float h = (float)v;
+// The split path keeps doubles as hi + lo floats.  Host arrays in pinned
+// (page-locked) memory are read or written by the conversion kernels
+// directly over the host link; pageable ones go through a device staging
+// buffer and a copy.
+__global__ void k_split(const double *__restrict__ a, float *__restrict__ hi, float *__restrict__ lo, long n) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+        const double v = a[t];
+        const float h = (float)v;
         hi[t] = h;
         if (lo) lo[t] = (float)(v - (double)h);
     }
 }
-__global__ void k_join(const float *hi, const float *lo, double *a, long n) {
-    long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) a[t] = (double)hi[t] + (lo ? (double)lo[t] : 0.0);
+__global__ void k_join(const float *__restrict__ hi, const float *__restrict__ lo, double *__restrict__ a, long n) {
+    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x)
+        a[t] = (double)hi[t] + (lo ? (double)lo[t] : 0.0);
 }
+
+// device address of a host array the GPU can access directly, or nullptr
+static const void *mapped_host(const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
+static int conv_blocks(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
 
 // host -> device state element array (double on the host)
 static int put(cf_ctx *ctx, void *dst, void *dstlo, const double *src, size_t n) {
     if (ctx->esz == 8) {
         CF_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    } else if (const double *m = (const double *)mapped_host(src)) {
+        k_split<<<conv_blocks(n), 256, 0, ctx->st>>>(m, (float *)dst, (float *)dstlo, (long)n);
+        CF_CUDA(cudaGetLastError());
     } else {
         TRY(ensure_stage(ctx, n));
         CF_CUDA(cudaMemcpyAsync(ctx->stage, src, n * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
-        k_split<<<cdiv(n, 256), 256, 0, ctx->st>>>(ctx->stage, (float *)dst, (float *)dstlo, (long)n);
+        k_split<<<conv_blocks(n), 256, 0, ctx->st>>>(ctx->stage, (float *)dst, (float *)dstlo, (long)n);
         CF_CUDA(cudaGetLastError());
     }
     return 0;
@@ -587,61 +605,31 @@ static int put(cf_ctx *ctx, void *dst, void *dstlo, const double *src, size_t n)
 static int get(cf_ctx *ctx, double *dst, const void *src, const void *srclo, size_t n) {
     if (ctx->esz == 8) {
         CF_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    } else if (double *m = (double *)mapped_host(dst)) {
+        k_join<<<conv_blocks(n), 256, 0, ctx->st>>>((const float *)src, (const float *)srclo, m, (long)n);
+        CF_CUDA(cudaGetLastError());
     } else {
         TRY(ensure_stage(ctx, n));
-        k_join<<<cdiv(n, 256), 256, 0, ctx->st>>>((const float *)src, (const float *)srclo, ctx->stage, (long)n);
+        k_join<<<conv_blocks(n), 256, 0, ctx->st>>>((const float *)src, (const float *)srclo, ctx->stage, (long)n);
         CF_CUDA(cudaGetLastError());
         CF_CUDA(cudaMemcpyAsync(dst, ctx->stage, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
     }
     return 0;
 }
 
-// True when U, V, W already satisfy the ghost identities that
-// apply_boundary_conditions (iwall_model 0) establishes: periodic copies in x
-// and z and the no-slip wall rows (boundary_conditions.f90:20-75).
-static bool fields_periodic(const cf_ctx *c, const double *U, const double *V, const double *W) {
-    if (c->prm.iwall_model != 0) return false;
-    const int nx = c->nx, ny = c->ny, nz = c->nz, nxg = c->nxg, nyg = c->nyg, nzg = c->nzg;
-    // visits only the ghost and duplicate elements (O(surface))
-    auto chk = [&](const double *F, int n1, int n2, int n3, bool xc, bool zc, int ybc) {
-        auto at = [&](int i, int j, int k) { return F[(size_t)(i - 1) + (size_t)n1 * ((j - 1) + (size_t)n2 * (k - 1))]; };
-        auto one = [&](int i, int j, int k) {
-            int is = wrapc(i, c->nxp), ks = wrapc(k, c->nzp);
-            double want;
-            if (j == 1 || j == n2) want = ybc == 1 ? 0.0 : -at(is, j == 1 ? 2 : n2 - 1, ks);
-            else want = at(is, j, ks);
-            return at(i, j, k) == want;
-        };
-        std::vector<int> gx = {1, n1}, gz = {1, n3};
-        if (xc) gx.push_back(n1 - 1);
-        if (zc) gz.push_back(n3 - 1);
-        for (int k = 1; k <= n3; k++)
-            for (int i = 1; i <= n1; i++)
-                if (!one(i, 1, k) || !one(i, n2, k)) return false;
-        for (int k = 1; k <= n3; k++)
-            for (int j = 2; j <= n2 - 1; j++)
-                for (int i : gx)
-                    if (!one(i, j, k)) return false;
-        for (int k : gz)
-            for (int j = 2; j <= n2 - 1; j++)
-                for (int i = 1; i <= n1; i++)
-                    if (!one(i, j, k)) return false;
-        return true;
-    };
-    (void)nx; (void)ny; (void)nz; (void)nxg; (void)nyg; (void)nzg;
-    return chk(U, nx, nyg, nzg, false, true, 0) && chk(V, nxg, ny, nzg, true, true, 1) && chk(W, nxg, nyg, nz, true, false, 0);
-}
-
 extern "C" int cf_upload_fields(cf_ctx *ctx, const double *U, const double *V, const double *W) {
     if (!ctx || !U || !V || !W) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
-    ctx->state_periodic = fields_periodic(ctx, U, V, W);
     CF_CUDA(cudaSetDevice(ctx->dev));
     int b = ctx->cur;
     TRY(put(ctx, ctx->U[b], ctx->Ulo[b], U, ctx->nU));
     TRY(put(ctx, ctx->V[b], ctx->Vlo[b], V, ctx->nV));
     TRY(put(ctx, ctx->W[b], ctx->Wlo[b], W, ctx->nW));
     ctx->old = ctx->cur;
-    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    // do the ghosts already hold what apply_boundary_conditions would put
+    // there? (checked on the device copy; synchronises the stream)
+    bool ok = false;
+    TRY(DISPATCH(check_bc<double>(ctx, b, &ok), check_bc<float>(ctx, b, &ok)));
+    ctx->state_periodic = ok;
     return CF_OK;
 }
 

@@ -207,6 +207,7 @@ int cf_fail(cf_ctx *ctx, int code, const std::string &msg);
 
 // ---- launchers (kernels in the .cu files), all enqueue on ctx->st -------
 template <typename T> int launch_bc(cf_ctx *ctx, int buf, bool lo = true);  // apply_boundary_conditions (lo: low words too)
+template <typename T> int check_bc(cf_ctx *ctx, int buf, bool *ok);      // ghosts already as the BCs leave them?
 template <typename T> int launch_rhs(cf_ctx *ctx, int comp, int slot);     // store F slot
 int rhs3_blocks_per_sm(int esz);
 template <typename T> int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst);  // fused RHS + RK update

@@ -100,6 +100,55 @@ __global__ void k_bc(BcSet s) {
     }
 }
 
+// Whether the ghosts already hold what apply_boundary_conditions would put
+// there (no-slip walls): element t of the same enumeration as k_bc compared
+// with its source; any mismatch sets *bad.
+template <typename T>
+__device__ __forceinline__ bool bc_elem_ok(const BcField &d, int nxp, int nzp, int t) {
+    const Fld<T> F = make_fld<T>(d.p, d.n1, d.n2), Flo = make_fld<T>(d.plo, d.n1, d.n2);
+    const int n1 = d.n1, n2 = d.n2, n3 = d.n3, xc = d.xc, zc = d.zc, ybc = d.ybc;
+    const int gx = xc ? 3 : 2, gz = zc ? 3 : 2;
+    const int nY = 2 * n1 * n3, nX = gx * (n2 - 2) * n3;
+    int i, j, k;
+    if (t < nY) {
+        i = t % n1 + 1;
+        const int r = t / n1;
+        k = r % n3 + 1;
+        j = (r / n3) == 0 ? 1 : n2;
+        const int is = wrapc(i, nxp), ks = wrapc(k, nzp), jsrc = (j == 1) ? 2 : n2 - 1;
+        if (ybc == 1) return F(i, j, k) == T(0) && (!Flo.p || Flo(i, j, k) == T(0));
+        return F(i, j, k) == -F(is, jsrc, ks) && (!Flo.p || Flo(i, j, k) == -Flo(is, jsrc, ks));
+    }
+    t -= nY;
+    if (t < nX) {
+        const int g = t % gx, r = t / gx;
+        j = r % (n2 - 2) + 2;
+        k = r / (n2 - 2) + 1;
+        i = (g == 0) ? 1 : (xc ? (g == 1 ? n1 - 1 : n1) : n1);
+    } else {
+        t -= nX;
+        const int g = t % gz, r = t / gz;
+        j = r % (n2 - 2) + 2;
+        i = r / (n2 - 2) + 2;
+        k = (g == 0) ? 1 : (zc ? (g == 1 ? n3 - 1 : n3) : n3);
+    }
+    const int is = wrapc(i, nxp), ks = wrapc(k, nzp);
+    return F(i, j, k) == F(is, j, ks) && (!Flo.p || Flo(i, j, k) == Flo(is, j, ks));
+}
+
+template <typename T>
+__global__ void k_bc_check(BcSet s, int *bad) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        if (t < s.f[q].n) {
+            if (!bc_elem_ok<T>(s.f[q], s.nxp, s.nzp, t)) atomicOr(bad, 1);
+            return;
+        }
+        t -= s.f[q].n;
+    }
+}
+
 static BcField bc_field(void *p, void *plo, int n1, int n2, int n3, int xc, int zc, int ybc, const double *alpha) {
     BcField f;
     int gx = xc ? 3 : 2, gz = zc ? 3 : 2;
@@ -1152,7 +1201,33 @@ int launch_div_check(cf_ctx *ctx, int b, double *d_out) {
     return 0;
 }
 
+// True when buffer b satisfies the no-slip ghost identities (one kernel and a
+// 4-byte read back); false for the wall model, whose ghosts depend on alpha.
+template <typename T>
+int check_bc(cf_ctx *ctx, int b, bool *ok) {
+    *ok = false;
+    if (ctx->prm.iwall_model != 0) return 0;
+    BcSet s;
+    s.f[0] = bc_field(ctx->U[b], ctx->Ulo[b], ctx->nx, ctx->nyg, ctx->nzg, 0, 1, 0, nullptr);
+    s.f[1] = bc_field(ctx->V[b], ctx->Vlo[b], ctx->nxg, ctx->ny, ctx->nzg, 1, 1, 1, nullptr);
+    s.f[2] = bc_field(ctx->W[b], ctx->Wlo[b], ctx->nxg, ctx->nyg, ctx->nz, 1, 0, 0, nullptr);
+    s.nxp = ctx->nxp;
+    s.nzp = ctx->nzp;
+    s.dyb = s.dyt = 0.0;
+    int *flag = (int *)(ctx->d_red + ctx->red_n - 6);
+    CF_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), ctx->st));
+    const int tot = s.f[0].n + s.f[1].n + s.f[2].n;
+    k_bc_check<T><<<cdiv(tot, 256), 256, 0, ctx->st>>>(s, flag);
+    CF_CUDA(cudaGetLastError());
+    int h = 1;
+    CF_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    *ok = h == 0;
+    return 0;
+}
+
 #define INST(T)                                                      \
+    template int check_bc<T>(cf_ctx *, int, bool *);                 \
     template int launch_bc<T>(cf_ctx *, int, bool);                  \
     template int launch_rhs<T>(cf_ctx *, int, int);                  \
     template int launch_rhs_update<T>(cf_ctx *, int, int, int);      \

@@ -212,3 +212,29 @@ def test_dsm_fused_matches_multipass(precision, tol):
         out.append((ch.download()["nu_t"], ch.avg_nu_t()))
     assert_close(out[0][0], out[1][0], tol, "nu_t")
     assert_close(out[0][1][1:-1], out[1][1][1:-1], tol, "avg_nu_t")
+
+
+def test_pinned_host_buffers_match_pageable():
+    """Uploads and downloads through page-locked host arrays (converted by the
+    kernels over the host link) give the same bits as pageable arrays
+    (staged copies), in both precisions."""
+    torch = pytest.importorskip("torch")
+    import channelflow as cf
+    case = channel_case(34, 33, 34, seed=4)
+    for prec in (cf.PREC_SPLIT, cf.PREC_FP64):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=prec, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ref = ch.download()
+        pinned = {}
+        for k in ("U", "V", "W"):
+            shp = ch.shapes[k]
+            t = torch.empty(int(np.prod(shp)), dtype=torch.float64, pin_memory=True)
+            pinned[k] = t.numpy().reshape(shp, order="F")
+            pinned[k][...] = case[k]
+        ch.upload(pinned["U"], pinned["V"], pinned["W"])
+        for k in ("U", "V", "W"):
+            pinned[k][...] = np.nan
+        ch.download_into(U=pinned["U"], V=pinned["V"], W=pinned["W"])
+        for k in ("U", "V", "W"):
+            assert np.array_equal(pinned[k], ref[k]), (prec, k)
+        ch.close()
