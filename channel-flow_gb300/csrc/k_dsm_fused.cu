@@ -47,6 +47,9 @@ struct RGeo {  // reciprocal spacings, 1-based like the coordinates
     const void *rdx, *rdxg, *rdy, *rdyg, *rdz, *rdzg;
 };
 
+// planes per z chunk at most (their z spacings sit in static shared memory)
+constexpr int DSM_ZMAX = 256;
+
 template <typename T, int TX, int TY>
 struct DsmSmem {
     static constexpr int RX = TX + 4, RY = TY + 4, QX = TX + 2, QY = TY + 2;
@@ -94,6 +97,18 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
 
     // reciprocal spacings of the region columns and rows (z is per plane)
     __shared__ T gsx[3][QX], gsy[3][QY];
+    // z spacings of every plane the chunk touches (rs .. re), so that no
+    // plane starts with a global load
+    __shared__ T gsz[3][DSM_ZMAX + 4];
+    {
+        const int zs = 2 + blockIdx.z * kc_len - 2, ze = min(2 + blockIdx.z * kc_len + kc_len - 1, nz - 1) + 2;
+        for (int t = tid; t <= ze - zs; t += TX * TY) {
+            const int kc = wrapc(zs + t, nzp);
+            gsz[0][t] = rdz[kc];
+            gsz[1][t] = rdzg[kc];
+            gsz[2][t] = rdzg[kc + 1];
+        }
+    }
     for (int t = tid; t < QX; t += TX * TY) {
         int ic = wrapq(i0 + t - 1, nxp);
         gsx[0][t] = rdx[ic];
@@ -140,7 +155,7 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
     }
     T pre[3][NLR];
     auto fetch = [&](int r) {  // issue every load of raw plane r
-        const int kc = wrapc(r, nzp);
+        const int kc = wrapn(r, nzp);
 #pragma unroll
         for (int q = 0; q < NLR; q++) {
             const bool in = ers[q] < NRP;
@@ -168,8 +183,8 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
         // (its own point, and one point of the halo ring for the first
         // 2 QX + 2 TY threads): G and F at a point only need that point's G
         // history, and Q only the raw planes already in the ring.
-        const int kq = wrapc(r - 1, nzp);
-        const T rz = rdz[kq], rzg0 = rdzg[kq], rzg1 = rdzg[kq + 1];
+        const int zq = max(r - 1 - rs, 0);  // plane r-1 (used from r = kb on)
+        const T rz = gsz[0][zq], rzg0 = gsz[1][zq], rzg1 = gsz[2][zq];
         for (int pt = 0; pt < 2; pt++) {
             if (pt == 1 && !hal) break;
             const int sx = pt ? hsx : tx + 1, sy = pt ? hsy : ty + 1;
@@ -269,13 +284,13 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
             }
             if (r >= kb + 2) {
                 // -- output plane k = r-2: S_ij of Uf, Vf, Wf from F(r-3) [PH], F(r-2) [P1], F(r-1) [P2]
-                const int k = r - 2, kcn = wrapc(k, nzp);
+                const int k = r - 2, kcn = wrapn(k, nzp);
                 auto uf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 0, sy + dj, sx + di); };
                 auto vf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 1, sy + dj, sx + di); };
                 auto wf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 2, sy + dj, sx + di); };
                 const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
                 const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
-                const T rz = rdz[kcn], rzg0 = rdzg[kcn], rzg1 = rdzg[kcn + 1];
+                const T rz = gsz[0][k - rs], rzg0 = gsz[1][k - rs], rzg1 = gsz[2][k - rs];
                 T s0 = (uf(0, 0, 0) - uf(-1, 0, 0)) * rx0;
                 T s1 = (vf(0, 0, 0) - vf(0, -1, 0)) * ry0;
                 T s2 = (wf(0, 0, 0) - wf(0, 0, -1)) * rz;
@@ -413,6 +428,7 @@ static int plan_t(int nxp, int nym, int nzp, int sms, int *kc, size_t *nchunk) {
     long nkc = (long)per_sm * sms / (tiles > 0 ? tiles : 1);
     if (nkc < 1) nkc = 1;
     if (nkc > nzp / 8) nkc = nzp / 8 > 0 ? nzp / 8 : 1;
+    if (nkc < cdiv(nzp, DSM_ZMAX)) nkc = cdiv(nzp, DSM_ZMAX);
     *kc = cdiv(nzp, nkc);
     *nchunk = (size_t)cdiv(nxp, TX) * cdiv(nzp, *kc);
     return 0;
