@@ -491,10 +491,18 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
         dsm_fused_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms, &ctx->dsm_kc, &nch_fused);
         ctx->use_fused_dsm = !p->dsm_unfused;
         // fused RHS: 32 x 8 column tiles, z chunks for ~4 resident blocks per SM
-        long rt = (long)cdiv(nx - 1, 32) * cdiv(ctx->nyg - 2, 8);
-        // z chunks: one wave of resident blocks
+        long rt = (long)cdiv(ctx->nxp, 32) * cdiv(ctx->nyg - 2, 8);
+        // z chunks: the count that minimises (waves of resident blocks) x
+        // (planes per chunk + the 2 halo planes a chunk loads again)
         const long res = (long)rhs3_blocks_per_sm(p->precision == CF_PREC_SPLIT ? 4 : 8) * dev_sms;
-        ctx->rhs_nkc = (int)std::max(1L, std::min((long)(ctx->nzg - 2) / 4, res / std::max(1L, rt)));
+        long best = 1;
+        double best_cost = 1e300;
+        for (long n = 1; n <= std::max(1L, (long)ctx->nzp / 4); n++) {
+            const double waves = (double)((rt * n + res - 1) / res);
+            const double cost = waves * ((double)cdiv(ctx->nzp, n) + 2.0);
+            if (cost < best_cost - 1e-9) { best_cost = cost; best = n; }
+        }
+        ctx->rhs_nkc = (int)best;
     }
     size_t nch = std::max((size_t)ctx->dsm_nblk, nch_fused);
     CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));
@@ -979,19 +987,19 @@ static int enqueue_step(cf_ctx *ctx) {
     // the projection fills every ghost.
     TRY(launch_rhs_update<T>(ctx, 1, X, a));
     ctx->cur = a;
-    TRY(launch_projection<T>(ctx, a, true, false));
+    TRY(launch_projection<T>(ctx, a, true, false, true));
     TRY(launch_bc<T>(ctx, a, false));
     // substep 2 (:118-131)
     TRY(eddy(ctx, a));
     TRY(launch_rhs_update<T>(ctx, 2, a, b));
     ctx->cur = b;
-    TRY(launch_projection<T>(ctx, b, false, false));
+    TRY(launch_projection<T>(ctx, b, false, false, true));
     TRY(launch_bc<T>(ctx, b, false));
     // substep 3 (:134-150)
     TRY(eddy(ctx, b));
     TRY(launch_rhs_update<T>(ctx, 3, b, a));
     ctx->cur = a;
-    TRY(launch_projection<T>(ctx, a, false));
+    TRY(launch_projection<T>(ctx, a, false, true, true));
     TRY(launch_bc<T>(ctx, a));
     // mass-flow forcing (:153-171); with no-slip walls the correction is
     // added to the ghosts as apply_boundary_conditions would propagate it

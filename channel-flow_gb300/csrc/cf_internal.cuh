@@ -216,7 +216,9 @@ template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // ed
 template <typename T> int launch_dsm_fused(cf_ctx *ctx, int buf);          // fused pass (periodic state)
 template <typename T> int launch_nut_zero(cf_ctx *ctx);
 template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut if held lazily
-template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true);
+// canon: project the canonical cells only (the boundary conditions that
+// follow rewrite the periodic duplicates)
+template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true, bool canon = false);
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only

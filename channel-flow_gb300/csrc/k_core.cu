@@ -515,12 +515,12 @@ template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
                                                      NutSrc<T> ns, const DevScal *ds, T nu, T Om, Trio<T> out,
                                                      Trio<T> F1, Trio<T> Uo, Trio<T> Uolo, Trio<T> Unlo, int s,
-                                                     RkCoef rk, int kc_len) {
+                                                     RkCoef rk, int kc_len, int ilim, int klim) {
     constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
     __shared__ T ring[3][4][NP];  // [plane slot][field U V W nu_t][tile]
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxg = g.nxg, nyg = g.nyg, nzg = g.nzg;
     const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
-    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, nzg - 1);
+    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, klim);
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int i = i0 + tx, j = j0 + ty;
     const T dt = ds_dt<T>(ds), dPdx = ds_dpdx<T>(ds), dPdz = ds_dpdz<T>(ds);
@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<
     rcs.dyg = gys[1] - (j0 - 1);
     rcs.dz = gzs[0] - kb;
     rcs.dzg = gzs[1] - kb;
-    const bool du = i <= nx - 1 && j <= nyg - 1, dv = i <= nxg - 1 && j <= ny - 1, dw = i <= nxg - 1 && j <= nyg - 1;
+    const bool du = i <= nx - 1 && j <= nyg - 1, dv = i <= ilim && j <= ny - 1, dw = i <= ilim && j <= nyg - 1;
     const bool lo = Uolo.u.p != nullptr;
     // this thread's tile elements (same for every plane and field)
     int eia[NL], eja[NL], erem[NL];
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<
     for (int k = kb; k <= ke; k++) {
         if (k + 1 <= ke) fetch(k + 2);  // in flight during this plane's work
         // RK operands of this plane, loaded before the stencil work
-        const bool cu = du && k <= nzg - 1, cv = dv && k <= nzg - 1, cw = dw && k <= nz - 1;
+        const bool cu = du && k <= klim, cv = dv && k <= klim, cw = dw && k <= nz - 1;
         T fu = T(0), fv = T(0), fw = T(0), ou = T(0), ov = T(0), ow = T(0), lu = T(0), lv = T(0), lw = T(0);
         if (cu) { ou = Uo.u(i, j, k); if (lo) lu = Uolo.u(i, j, k); if (s > 1) fu = F1.u(i, j, k); }
         if (cv) { ov = Uo.v(i, j, k); if (lo) lv = Uolo.v(i, j, k); if (s > 1) fv = F1.v(i, j, k); }
@@ -684,9 +684,14 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
     Trio<T> Uo = trio(ctx->U[o], ctx->V[o], ctx->W[o]);
     Trio<T> Uolo = trio(ctx->Ulo[o], ctx->Vlo[o], ctx->Wlo[o]);
     Trio<T> Unlo = s == 3 ? trio(ctx->Ulo[dst], ctx->Vlo[dst], ctx->Wlo[dst]) : trio(nullptr, nullptr, nullptr);
-    int ntx = cdiv(ctx->nx - 1, TX), nty = cdiv(ctx->nyg - 2, TY);
-    int nkc = std::max(ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1, cdiv(ctx->nzg - 2, RHS_ZMAX));
-    int kc_len = cdiv(ctx->nzg - 2, nkc);
+    // canonical cells only (i <= nxp+1, k <= nzp+1): the periodic duplicate
+    // column of V, W and plane of U, V are rewritten by the boundary
+    // conditions after the projection and read by nothing before them (the
+    // divergence takes canonical cells only)
+    const int ilim = ctx->nxp + 1, klim = ctx->nzp + 1;
+    int ntx = cdiv(ilim - 1, TX), nty = cdiv(ctx->nyg - 2, TY);
+    int nkc = std::max(ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1, cdiv(ctx->nzp, RHS_ZMAX));
+    int kc_len = cdiv(klim - 1, nkc);
     NutSrc<T> ns = {};
     if (ctx->nut_lazy) {
         ns.S = (const T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
@@ -696,8 +701,9 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
         ns.nzp = ctx->nzp;
         ns.dirichlet = ctx->prm.Dirichlet_nu_t == 1;
     }
-    k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(ctx->nzg - 2, kc_len)), TX * TY, 0, ctx->st>>>(
-        g, rcp_of<T>(ctx), U, V, W, nt, ns, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len);
+    k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(klim - 1, kc_len)), TX * TY, 0, ctx->st>>>(
+        g, rcp_of<T>(ctx), U, V, W, nt, ns, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len,
+        ilim, klim);
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
     return 0;

@@ -789,14 +789,17 @@ __device__ __forceinline__ void proj_update(const Fld<T> &F, const Fld<T> &Flo, 
 // before the first store (the fields may alias as far as the compiler knows).
 constexpr int PROJ_KP = 4;
 
+// ilim, klim: last x and z index projected (nxg-1 and nzg-1 for the full
+// interior; nxp+1 and nzp+1 for the canonical cells only)
 template <typename T>
 __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ulo, Fld<T> V, Fld<T> Vlo, Fld<T> W,
-                                                  Fld<T> Wlo, const T *__restrict__ phi, PhiView pv, RSpG rs) {
+                                                  Fld<T> Wlo, const T *__restrict__ phi, PhiView pv, RSpG rs, int ilim,
+                                                  int klim) {
     constexpr int KP = PROJ_KP;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
     const int k0 = blockIdx.z * KP + 2;
-    if (i > g.nxg - 1 || j > g.nyg - 1) return;
+    if (i > ilim || j > g.nyg - 1) return;
     const bool du = i <= g.nx - 1, dv = j <= g.ny - 1;
     const bool lo = Ulo.p != nullptr;
     T p0[KP + 1], px[KP], py[KP];
@@ -809,7 +812,7 @@ __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ul
 #pragma unroll
     for (int q = 0; q < KP; q++) {
         const int k = k0 + q;
-        const bool kin = k <= g.nzg - 1, dw = k <= g.nz - 1;
+        const bool kin = k <= klim, dw = k <= g.nz - 1;
         px[q] = du && kin ? phi[pv(i + 1, j, k)] : T(0);
         py[q] = dv && kin ? phi[pv(i, j + 1, k)] : T(0);
         u[q] = du && kin ? U(i, j, k) : T(0);
@@ -832,7 +835,7 @@ __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ul
 #pragma unroll
     for (int q = 0; q < KP; q++) {
         const int k = k0 + q;
-        if (k > g.nzg - 1) break;
+        if (k > klim) break;
         T gx, gy, gz;
         if constexpr (sizeof(T) == 4) {
             gx = (px[q] - p0[q]) * rx;
@@ -893,7 +896,7 @@ static size_t smem_pairs(int n, int LP) {
 }
 
 template <typename T>
-int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo) {
+int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon) {
     typedef typename C2<T>::t C;
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
@@ -1003,10 +1006,11 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo) {
         rg.rxg = ctx->d_rgeo_f + ctx->rgeo_off[1];
         rg.ryg = ctx->d_rgeo_f + ctx->rgeo_off[3];
         rg.rzg = ctx->d_rgeo_f + ctx->rgeo_off[5];
-        k_project3<T><<<dim3(cdiv(ctx->nxg - 2, 32), cdiv(ctx->nyg - 2, 4), cdiv(ctx->nzg - 2, PROJ_KP)), blk, 0, ctx->st>>>(
+        const int ilim = canon ? ctx->nxp + 1 : ctx->nxg - 1, klim = canon ? ctx->nzp + 1 : ctx->nzg - 1;
+        k_project3<T><<<dim3(cdiv(ilim - 1, 32), cdiv(ctx->nyg - 2, 4), cdiv(klim - 1, PROJ_KP)), blk, 0, ctx->st>>>(
             g, U, make_fld<T>(lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg), V,
             make_fld<T>(lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny), W,
-            make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg), phi, pv, rg);
+            make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg), phi, pv, rg, ilim, klim);
         count_launch(ctx, "k_project3");
     }
     if (store_p) {
@@ -1036,5 +1040,5 @@ int fft_setup_attrs() {
     return 0;
 }
 
-template int launch_projection<double>(cf_ctx *, int, bool, bool);
-template int launch_projection<float>(cf_ctx *, int, bool, bool);
+template int launch_projection<double>(cf_ctx *, int, bool, bool, bool);
+template int launch_projection<float>(cf_ctx *, int, bool, bool, bool);
