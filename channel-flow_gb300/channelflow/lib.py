@@ -81,7 +81,8 @@ def load(build_if_missing: bool = True):
     L.cf_init_mass_flow.argtypes = [vp, dp]
     L.cf_compute_dt.argtypes = [vp, dp]
     for n in ["cf_compute_eddy_viscosity", "cf_compute_wall_model", "cf_apply_boundary_conditions",
-              "cf_compute_projection_step", "cf_save_old_state", "cf_synchronize", "cf_launches_per_step"]:
+              "cf_compute_projection_step", "cf_save_old_state", "cf_synchronize", "cf_launches_per_step",
+              "cf_compute_pressure"]:
         getattr(L, n).argtypes = [vp]
     for n in ["cf_compute_rhs_u", "cf_compute_rhs_v", "cf_compute_rhs_w", "cf_rk_update", "cf_set_fixed_dt"]:
         getattr(L, n).argtypes = [vp, C.c_int]
@@ -102,6 +103,8 @@ def load(build_if_missing: bool = True):
     L.cf_read_input_parameters.argtypes = [C.c_char_p, C.POINTER(CfParams), ip, C.c_char_p, C.c_char_p, ip, ip]
     L.cf_read_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp]
     L.cf_write_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
+    L.cf_write_statistics.argtypes = [C.c_char_p, C.c_double, C.c_double, C.c_int, C.c_int, C.c_int, C.c_int, dp, dp]
+    L.cf_statistics_file_name.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_char_p, C.c_int]
     _lib = L
     return L
 
@@ -259,6 +262,10 @@ class Channel:
     def compute_projection_step(self):
         self._check(self.L.cf_compute_projection_step(self.h))
 
+    def compute_pressure(self):
+        """Actual pressure of the current fields into P (pressure.f90:21)."""
+        self._check(self.L.cf_compute_pressure(self.h))
+
     def compute_dPx_for_constant_mass_flow(self):
         v = C.c_double()
         self._check(self.L.cf_compute_dPx_for_constant_mass_flow(self.h, C.byref(v)))
@@ -281,6 +288,16 @@ class Channel:
         out = np.zeros(9 * self.ny + 8)
         self._check(self.L.cf_compute_statistics(self.h, _dp(out)))
         return out
+
+    def output_statistics(self, fileout: str, istep: int, nstep_init: int = 0, stats=None) -> str:
+        """output_statistics (input_output.f90:549-570): writes
+        fileout.<istep+nstep_init>.stats.txt from compute_statistics (or the
+        given statistics vector) and returns the file name."""
+        if stats is None:
+            stats = self.statistics()
+        path = statistics_file_name(fileout, istep, nstep_init)
+        write_statistics(path, self.scalars()["t"], self.params.nu, self.nx, self.ny, self.nz, istep, self.y, stats)
+        return path
 
     # ------------------------------------------------------------ fast path
     def time_step_rk3(self, nsteps: int = 1, sync: bool = True):
@@ -376,3 +393,25 @@ def write_snapshot(path: str, x, y, z, U, V, W, P=None, nu_t=None):
                              _dp(P), _dp(nu_t))
     if rc != 0:
         raise CfError(f"cannot write snapshot {path} ({rc})")
+
+
+def statistics_file_name(fileout: str, istep: int, nstep_init: int = 0) -> str:
+    """fileout.<istep+nstep_init>.stats.txt (input_output.f90:557-558)."""
+    L = load()
+    buf = C.create_string_buffer(512)
+    rc = L.cf_statistics_file_name(fileout.encode(), istep, nstep_init, buf, len(buf))
+    if rc != 0:
+        raise CfError(f"statistics file name too long ({rc})")
+    return buf.value.decode()
+
+
+def write_statistics(path: str, t: float, nu: float, nx: int, ny: int, nz: int, istep: int, y, stats):
+    """output_statistics (input_output.f90:549-570) from the cf_compute_statistics vector."""
+    L = load()
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    stats = np.ascontiguousarray(stats, dtype=np.float64)
+    if y.size != ny or stats.size != 9 * ny + 8:
+        raise CfError("y needs ny values and stats 9*ny+8")
+    rc = L.cf_write_statistics(path.encode(), t, nu, nx, ny, nz, istep, _dp(y), _dp(stats))
+    if rc != 0:
+        raise CfError(f"cannot write statistics {path} ({rc})")

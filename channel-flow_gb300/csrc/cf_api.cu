@@ -933,6 +933,14 @@ extern "C" int cf_compute_projection_step(cf_ctx *ctx) {
     return CF_OK;
 }
 
+extern "C" int cf_compute_pressure(cf_ctx *ctx) {
+    if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    TRY(DISPATCH(launch_pressure<double>(ctx, ctx->cur), launch_pressure<float>(ctx, ctx->cur)));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    return CF_OK;
+}
+
 static int mass_mirror(cf_ctx *ctx, int mode, double *out) {
     if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
     CF_CUDA(cudaSetDevice(ctx->dev));

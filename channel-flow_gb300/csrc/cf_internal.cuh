@@ -219,6 +219,7 @@ template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut
 // canon: project the canonical cells only (the boundary conditions that
 // follow rewrite the periodic duplicates)
 template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true, bool canon = false);
+template <typename T> int launch_pressure(cf_ctx *ctx, int buf);  // actual pressure into P (pressure.f90:21)
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only

@@ -5,6 +5,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <cmath>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -222,6 +223,84 @@ extern "C" int cf_write_snapshot(const char *path, int nx, int ny, int nz, const
         if (!fld[q]) continue;
         ok = ok && write_i32(f, shp[q][0]) && write_i32(f, shp[q][1]) && write_i32(f, shp[q][2]);
         ok = ok && write_f64(f, fld[q], (size_t)shp[q][0] * shp[q][1] * shp[q][2]);
+    }
+    ok = (fclose(f) == 0) && ok;
+    return ok ? CF_OK : CF_ERR_IO;
+}
+
+// ---------------------------------------------------------------------------
+// Statistics text file, output_statistics (input_output.f90:549-570).
+// ---------------------------------------------------------------------------
+namespace {
+
+// Fortran Fw.d output of one REAL(8): correctly rounded fixed point, right
+// justified; w asterisks when it does not fit (after dropping the optional
+// leading zero).  IEEE -0.0 is written without sign (the default
+// "nominus0" behaviour of the Intel compiler the reference targets); other
+// negative values keep it, also when they round to zero.
+std::string fortran_f(double v, int w, int d) {
+    std::string s;
+    if (std::isnan(v)) {
+        s = "NaN";
+    } else if (std::isinf(v)) {
+        s = v > 0 ? (w >= 8 ? "Infinity" : "Inf") : (w >= 9 ? "-Infinity" : "-Inf");
+    } else {
+        char buf[400];
+        snprintf(buf, sizeof buf, "%.*f", d, v == 0.0 ? 0.0 : v);
+        s = buf;
+        if ((int)s.size() > w) {
+            if (s.compare(0, 2, "0.") == 0) s.erase(0, 1);
+            else if (s.compare(0, 3, "-0.") == 0) s.erase(1, 1);
+        }
+    }
+    if ((int)s.size() > w) return std::string((size_t)w, '*');
+    return std::string((size_t)(w - (int)s.size()), ' ') + s;
+}
+
+// Fortran Iw output
+std::string fortran_i(long v, int w) {
+    char buf[32];
+    snprintf(buf, sizeof buf, "%ld", v);
+    std::string s = buf;
+    if ((int)s.size() > w) return std::string((size_t)w, '*');
+    return std::string((size_t)(w - (int)s.size()), ' ') + s;
+}
+
+}  // namespace
+
+extern "C" int cf_statistics_file_name(const char *fileout, int istep, int nstep_init, char *name, int cap) {
+    if (!fileout || !name || cap <= 0) return CF_ERR_INVALID;
+    // Trim(Adjustl(fileout)) // '.' // Trim(Adjustl(ext)) // '.stats.txt', ext written with I8
+    std::string f = fileout;
+    size_t a = f.find_first_not_of(' ');
+    f = a == std::string::npos ? std::string() : f.substr(a);
+    while (!f.empty() && f.back() == ' ') f.pop_back();
+    std::string ext = fortran_i((long)istep + nstep_init, 8);
+    ext.erase(0, ext.find_first_not_of(' '));
+    std::string n = f + "." + ext + ".stats.txt";
+    if ((int)n.size() + 1 > cap) return CF_ERR_INVALID;
+    memcpy(name, n.c_str(), n.size() + 1);
+    return CF_OK;
+}
+
+extern "C" int cf_write_statistics(const char *path, double t, double nu, int nx, int ny, int nz, int istep,
+                                   const double *y, const double *stats) {
+    if (!path || !y || !stats || ny < 1) return CF_ERR_INVALID;
+    FILE *f = fopen(path, "w");
+    if (!f) return CF_ERR_IO;
+    const double *Um = stats, *U2 = stats + 3 * ny, *V2 = stats + 4 * ny, *W2 = stats + 5 * ny, *UV = stats + 6 * ny,
+                 *P2 = stats + 8 * ny;
+    const double utau = stats[9 * ny], Retau = stats[9 * ny + 1];
+    // '(A,4F15.8,4I)': the Intel compiler's default width for an INTEGER(4)
+    // I descriptor without width is 12
+    std::string line = "%" + fortran_f(t, 15, 8) + fortran_f(Retau, 15, 8) + fortran_f(utau, 15, 8) +
+                       fortran_f(nu, 15, 8) + fortran_i(nx, 12) + fortran_i(ny, 12) + fortran_i(nz, 12) +
+                       fortran_i(istep, 12) + "\n";
+    bool ok = fputs(line.c_str(), f) >= 0;
+    for (int j = 0; j < ny && ok; j++) {  // '(8F15.8)' with seven items per record
+        line = fortran_f(y[j], 15, 8) + fortran_f(Um[j], 15, 8) + fortran_f(U2[j], 15, 8) + fortran_f(V2[j], 15, 8) +
+               fortran_f(W2[j], 15, 8) + fortran_f(UV[j], 15, 8) + fortran_f(P2[j], 15, 8) + "\n";
+        ok = fputs(line.c_str(), f) >= 0;
     }
     ok = (fclose(f) == 0) && ok;
     return ok ? CF_OK : CF_ERR_IO;

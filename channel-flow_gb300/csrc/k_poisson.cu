@@ -895,13 +895,15 @@ static size_t smem_pairs(int n, int LP) {
     return (size_t)LP * 2 * n * sizeof(typename C2<T>::t);
 }
 
+// phi = Laplacian^-1 div(U, V, W) on the canonical cells: the forward
+// transforms with the divergence fused, the per-mode tridiagonal solves and
+// the inverse transforms (projection.f90:40-120).  U, V, W have the extents
+// of the velocity fields; only their canonical cells, the x and z neighbours
+// below them (read through the periodic wrap) and the wall rows of V are read.
 template <typename T>
-int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon) {
+static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
     typedef typename C2<T>::t C;
     GeoT<T> g = geo_of<T>(ctx);
-    Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
-    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
-    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
     C *spec = (C *)ctx->spec;
     T *phi = (T *)ctx->phi;
     const int nxp = ctx->nxp, nzp = ctx->nzp, nym = ctx->nym, nh = ctx->nxh;
@@ -997,6 +999,19 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon) {
 #undef CF_FFTZF
 #undef CF_FFTZB
 #undef CF_INVX
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template <typename T>
+int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon) {
+    GeoT<T> g = geo_of<T>(ctx);
+    Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    if (int rc = poisson_solve<T>(ctx, U, V, W)) return rc;
+    T *phi = (T *)ctx->phi;
+    const int nxp = ctx->nxp, nzp = ctx->nzp, nym = ctx->nym;
     // projection
     PhiView pv;
     pv.nxp = nxp; pv.nym = nym; pv.nzp = nzp;
@@ -1023,6 +1038,113 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon) {
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// Actual pressure, pressure.f90:21-172.
+//
+// The reference sets the wall rows of rhs_v to bc_1, bc_2 = d/dy(nu dV/dy)
+// (pressure.f90:237-247), which puts -bc_1/(y(2)-y(1)) into the divergence
+// of row 2 and +bc_2/(y(ny)-y(ny-1)) into row nyg-1, and then adds
+// coef_bc_1 (yg(2)-yg(1)) bc_1_hat = bc_1_hat/(y(2)-y(1)) to row 2 and
+// subtracts bc_2_hat/(y(ny)-y(ny-1)) from row nyg-1 of every mode
+// (pressure.f90:137-139; coef_bc_1 and coef_bc_2 from initialization.f90:
+// 357-373).  The transform is linear, so the two contributions cancel
+// exactly: the solve below takes zero wall rows in rhs_v and no boundary
+// term.  bc_1 and bc_2 then only enter the ghost rows (pressure.f90:158-159).
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_zero_vwall(Fld<T> F, int nxg, int ny, int nzg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int k = blockIdx.y + 1;
+    if (i > nxg) return;
+    F(i, 1, k) = T(0);
+    F(i, ny, k) = T(0);
+}
+
+// metric factors of the one-sided derivatives at the two walls
+// (pressure.f90:283-286, 314-317) and the ghost-row spacings
+struct PWall {
+    double g[2], g2[2], dyg[2];
+};
+
+// d/dy(nu dV/dy) at a wall from V and avg_nu_t (pressure.f90:288-307,
+// 319-338); w = 0 bottom, 1 top.  v0..v3: V at the wall and the three faces
+// inside, a0 = avg_nu_t at the ghost row, a1 at the first interior row.
+__device__ __forceinline__ double wall_dnu_dv(const PWall &pw, int w, double nu, double v0, double v1, double v2,
+                                              double v3, double a0, double a1) {
+    const double nui = nu + 0.5 * (a0 + a1);
+    const double dnu = w == 0 ? (a1 - a0) / pw.dyg[0] : (a0 - a1) / pw.dyg[1];
+    const double s = w == 0 ? -1.0 : 1.0;  // the top wall's first derivative runs downwards
+    const double dV = (s * 3.0 * v0 - s * 4.0 * v1 + s * v2) / 2.0 / pw.g[w];
+    double ddV = 2.0 * v0 - 5.0 * v1 + 4.0 * v2 - 1.0 * v3;
+    ddV = (ddV - dV * pw.g2[w]) / (pw.g[w] * pw.g[w]);
+    return dnu * dV + nui * ddV;
+}
+
+// P on i = 2..nxg-1, j = 1..nyg, k = 2..nzg-1: phi read through the wrap
+// (apply_periodic_xz_pressure, pressure.f90:177-195), the wall rows
+// P(1) = P(2) - (yg(2)-yg(1)) bc_1 and P(nyg) = P(nyg-1) + (yg(nyg)-yg(nyg-1))
+// bc_2 with bc taken at the wrapped column, as the periodic copies that
+// follow them in the reference leave it.  The x and z ghost columns are not
+// written.
+template <typename T>
+__global__ void __launch_bounds__(128) k_pressure_store(Fld<T> P, const T *__restrict__ phi, PhiView pv, Fld<T> V,
+                                                        const double *__restrict__ avg, PWall pw, double nu, int nxg,
+                                                        int ny, int nyg, int nzg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 2;
+    if (i > nxg - 1 || j > nyg) return;
+    if (j >= 2 && j <= nyg - 1) {
+        P(i, j, k) = phi[pv(i, j, k)];
+        return;
+    }
+    const int iw = wrapf(i, pv.nxp), kw = wrapf(k, pv.nzp);
+    double bc, pin;
+    if (j == 1) {
+        bc = wall_dnu_dv(pw, 0, nu, (double)V(iw, 1, kw), (double)V(iw, 2, kw), (double)V(iw, 3, kw),
+                         (double)V(iw, 4, kw), avg[1], avg[2]);
+        pin = (double)phi[pv(i, 2, k)];
+        P(i, j, k) = (T)(pin - pw.dyg[0] * bc);
+    } else {
+        bc = wall_dnu_dv(pw, 1, nu, (double)V(iw, ny, kw), (double)V(iw, ny - 1, kw), (double)V(iw, ny - 2, kw),
+                         (double)V(iw, ny - 3, kw), avg[nyg], avg[nyg - 1]);
+        pin = (double)phi[pv(i, nyg - 1, k)];
+        P(i, j, k) = (T)(pin + pw.dyg[1] * bc);
+    }
+}
+
+template <typename T>
+int launch_pressure(cf_ctx *ctx, int b) {
+    if (ctx->ny < 4) return cf_fail(ctx, CF_ERR_INVALID, "the wall derivatives of the pressure need ny >= 4");
+    // right-hand sides of the current fields into slot 1 (pressure.f90:49-51)
+    for (int c = 0; c < 3; c++)
+        if (int rc = launch_rhs<T>(ctx, c, 0)) return rc;
+    Fld<T> Fu = make_fld<T>(ctx->F[0][0], ctx->nx, ctx->nyg);
+    Fld<T> Fv = make_fld<T>(ctx->F[0][1], ctx->nxg, ctx->ny);
+    Fld<T> Fw = make_fld<T>(ctx->F[0][2], ctx->nxg, ctx->nyg);
+    k_zero_vwall<T><<<dim3(cdiv(ctx->nxg, 128), ctx->nzg), 128, 0, ctx->st>>>(Fv, ctx->nxg, ctx->ny, ctx->nzg);
+    count_launch(ctx, "k_zero_vwall");
+    if (int rc = poisson_solve<T>(ctx, Fu, Fv, Fw)) return rc;
+    const double *y = ctx->hy.data(), *yg = ctx->hyg.data();  // 1-based
+    const int ny = ctx->ny, nyg = ctx->nyg;
+    PWall pw;
+    pw.g[0] = (-3.0 * y[1] + 4.0 * y[2] - y[3]) / 2.0;
+    pw.g2[0] = 2.0 * y[1] - 5.0 * y[2] + 4.0 * y[3] - 1.0 * y[4];
+    pw.g[1] = (3.0 * y[ny] - 4.0 * y[ny - 1] + y[ny - 2]) / 2.0;
+    pw.g2[1] = 2.0 * y[ny] - 5.0 * y[ny - 1] + 4.0 * y[ny - 2] - 1.0 * y[ny - 3];
+    pw.dyg[0] = yg[2] - yg[1];
+    pw.dyg[1] = yg[nyg] - yg[nyg - 1];
+    PhiView pv;
+    pv.nxp = ctx->nxp; pv.nym = ctx->nym; pv.nzp = ctx->nzp;
+    Fld<T> P = make_fld<T>(ctx->P, ctx->nxg, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    k_pressure_store<T><<<dim3(cdiv(ctx->nxg - 2, 32), cdiv(nyg, 4), ctx->nzg - 2), dim3(32, 4), 0, ctx->st>>>(
+        P, (const T *)ctx->phi, pv, V, ctx->avg_nu_t, pw, ctx->prm.nu, ctx->nxg, ny, nyg, ctx->nzg);
+    count_launch(ctx, "k_pressure_store");
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
 // smem opt-in for the FFT kernels (called once at context creation)
 template <typename T, int N>
 static void fft_attrs_one() {
@@ -1042,3 +1164,5 @@ int fft_setup_attrs() {
 
 template int launch_projection<double>(cf_ctx *, int, bool, bool, bool);
 template int launch_projection<float>(cf_ctx *, int, bool, bool, bool);
+template int launch_pressure<double>(cf_ctx *, int);
+template int launch_pressure<float>(cf_ctx *, int);

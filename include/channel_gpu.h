@@ -110,6 +110,16 @@ int cf_compute_dPx_for_constant_mass_flow(cf_ctx *ctx, double *dPdx); /* mass_fl
 int cf_compute_dPy_for_constant_mass_flow(cf_ctx *ctx, double *dPdy); /* mass_flow.f90:147  */
 int cf_compute_dPx_for_constant_Ucenterline(cf_ctx *ctx, double *dPdx); /* mass_flow.f90:192 */
 int cf_check_divergence(cf_ctx *ctx, double *maxdiv, double *maxabsdiv); /* projection.f90:234 */
+/* Actual pressure of the current fields into P: compute_pressure
+ * (pressure.f90:21), which output_data calls before writing a snapshot
+ * (input_output.f90:401-404).  Uses the current nu_t and avg_nu_t and the
+ * Poisson matrix of the projection.  Writes P on i = 2..nxg-1, j = 1..nyg,
+ * k = 2..nzg-1 (the z duplicate plane and the x duplicate column included);
+ * the x ghost columns i = 1, nxg and z ghost planes k = 1, nzg keep their
+ * values.  Overwrites the right-hand sides of slot 1 (with zero wall rows in
+ * Fv1).  The next rk_step-1 projection replaces P with the pseudo-pressure,
+ * as in the reference. */
+int cf_compute_pressure(cf_ctx *ctx);
 /* U(interior) += value (comp 0) or V(interior) += value (comp 1), then
  * dPdx (dPdy) = value/dt: the driver lines time_integration.f90:155-156, 168-169. */
 int cf_apply_mass_flow_correction(cf_ctx *ctx, int comp, double value);
@@ -165,6 +175,16 @@ int cf_read_snapshot(const char *path, int nx, int ny, int nz, double *x, double
                      double *V, double *W);
 int cf_write_snapshot(const char *path, int nx, int ny, int nz, const double *x, const double *y, const double *z,
                       const double *U, const double *V, const double *W, const double *P, const double *nu_t);
+/* Statistics text file of output_statistics (input_output.f90:549-570):
+ * a header '%', t, Retau, utau, nu (F15.8), nx, ny, nz, istep (I12), then
+ * one record per face row j = 1..ny of y, Umean, U2mean, V2mean, W2mean,
+ * UVmean, P2mean (F15.8).  stats is the output of cf_compute_statistics
+ * (Retau and utau are taken from it); y holds ny faces. */
+int cf_write_statistics(const char *path, double t, double nu, int nx, int ny, int nz, int istep, const double *y,
+                        const double *stats);
+/* The reference's file name for it: fileout.<istep+nstep_init>.stats.txt
+ * (input_output.f90:557-558); fails when it needs more than cap bytes. */
+int cf_statistics_file_name(const char *fileout, int istep, int nstep_init, char *name, int cap);
 
 /* ---- divergence check without device allocation ---------------------- */
 /* No counterpart in the reference: the arithmetic is check_divergence

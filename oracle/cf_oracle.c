@@ -1463,6 +1463,159 @@ void cfo_compute_projection_step(cfo *o) {
     cfo_project_velocity(o);
 }
 
+/* ------------------------------------------------------------------------ */
+/* Actual pressure, pressure.f90                                             */
+/* ------------------------------------------------------------------------ */
+/* bc_1, bc_2 = d/dy(nu dV/dy) at the walls on (2:nxg-1, 2:nzg-1), one-sided
+ * 2nd-order derivatives in the index coordinate with metric factors;
+ * pressure.f90:270-341. */
+static void pressure_bc(cfo *o, fa *bc1, fa *bc2) {
+    const double *y = o->y, *yg = o->yg;
+    int nxg = o->nxg, nzg = o->nzg, ny = o->ny, nyg = o->nyg;
+    double dzeta = 1.0;
+    double g = (-3.0 * y[1] + 4.0 * y[2] - y[3]) / (2.0 * dzeta);
+    double g2 = (2.0 * y[1] - 5.0 * y[2] + 4.0 * y[3] - 1.0 * y[4]) / pow(dzeta, 2.0);
+    double a1 = F3(o->avg_nu_t, 1, 1, 1), a2 = F3(o->avg_nu_t, 1, 2, 1);
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int i = 2; i <= nxg - 1; i++) {
+            double nui = o->nu + 0.5 * (a1 + a2);
+            double dnu = (a2 - a1) / (yg[2] - yg[1]);
+            double dV = (-3.0 * F3(o->V, i, 1, k) + 4.0 * F3(o->V, i, 2, k) - F3(o->V, i, 3, k)) / (2.0 * dzeta) * 1.0 / g;
+            double ddV = (2.0 * F3(o->V, i, 1, k) - 5.0 * F3(o->V, i, 2, k) + 4.0 * F3(o->V, i, 3, k) - 1.0 * F3(o->V, i, 4, k)) /
+                         pow(dzeta, 2.0);
+            ddV = (ddV - dV * g2) / pow(g, 2.0);
+            F3(*bc1, i, k, 1) = dnu * dV + nui * ddV;
+        }
+    g = (3.0 * y[ny] - 4.0 * y[ny - 1] + y[ny - 2]) / (2.0 * dzeta);
+    g2 = (2.0 * y[ny] - 5.0 * y[ny - 1] + 4.0 * y[ny - 2] - 1.0 * y[ny - 3]) / pow(dzeta, 2.0);
+    double b1 = F3(o->avg_nu_t, 1, nyg, 1), b2 = F3(o->avg_nu_t, 1, nyg - 1, 1);
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int i = 2; i <= nxg - 1; i++) {
+            double nui = o->nu + 0.5 * (b1 + b2);
+            double dnu = (b1 - b2) / (yg[nyg] - yg[nyg - 1]);
+            double dV = (3.0 * F3(o->V, i, ny, k) - 4.0 * F3(o->V, i, ny - 1, k) + F3(o->V, i, ny - 2, k)) / (2.0 * dzeta) * 1.0 / g;
+            double ddV = (2.0 * F3(o->V, i, ny, k) - 5.0 * F3(o->V, i, ny - 1, k) + 4.0 * F3(o->V, i, ny - 2, k) -
+                          1.0 * F3(o->V, i, ny - 3, k)) / pow(dzeta, 2.0);
+            ddV = (ddV - dV * g2) / pow(g, 2.0);
+            F3(*bc2, i, k, 1) = dnu * dV + nui * ddV;
+        }
+}
+
+/* 2-D transform of bc(2:nxp+1, 2:nzp+1) into hat (x fastest); pressure.f90:109-115 */
+static void bc_hat(cfo *o, fa *bc, double complex *hat) {
+    int nxp = o->nxp, nzp = o->nzp;
+    for (int k = 0; k < nzp; k++)
+        for (int i = 0; i < nxp; i++) hat[(size_t)k * nxp + i] = F3(*bc, i + 2, k + 2, 1);
+    fft2d(hat, nxp, nzp, o->twx_f, o->twz_f);
+}
+
+void cfo_compute_pressure(cfo *o) {
+    /* pressure.f90:21-29 */
+    int nx = o->nx, ny = o->ny, nz = o->nz, nxg = o->nxg, nyg = o->nyg, nzg = o->nzg;
+    int nxp = o->nxp, nzp = o->nzp, nym = o->nym;
+    fa bc1 = fa_new3(2, nxg - 1, 2, nzg - 1, 1, 1), bc2 = fa_new3(2, nxg - 1, 2, nzg - 1, 1, 1);
+    pressure_bc(o, &bc1, &bc2);
+
+    /* compute_pressure_rhs, pressure.f90:42-70.  The right-hand sides go to
+     * rhs_uf/vf/wf (full extents); the RK slot 1 arrays are borrowed for the
+     * calls and left as they were. */
+    fa ru = fa_new3(1, nx, 1, nyg, 1, nzg), rv = fa_new3(1, nxg, 1, ny, 1, nzg), rw = fa_new3(1, nxg, 1, nyg, 1, nz);
+    fa su = o->Fu[1], sv = o->Fv[1], sw = o->Fw[1];
+    o->Fu[1] = fa_new3(2, nx - 1, 2, nyg - 1, 2, nzg - 1);
+    o->Fv[1] = fa_new3(2, nxg - 1, 2, ny - 1, 2, nzg - 1);
+    o->Fw[1] = fa_new3(2, nxg - 1, 2, nyg - 1, 2, nz - 1);
+    cfo_compute_rhs_u(o, 1);
+    cfo_compute_rhs_v(o, 1);
+    cfo_compute_rhs_w(o, 1);
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int j = 2; j <= nyg - 1; j++)
+            for (int i = 2; i <= nx - 1; i++) F3(ru, i, j, k) = F3(o->Fu[1], i, j, k);
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int j = 2; j <= ny - 1; j++)
+            for (int i = 2; i <= nxg - 1; i++) F3(rv, i, j, k) = F3(o->Fv[1], i, j, k);
+    for (int k = 2; k <= nz - 1; k++)
+        for (int j = 2; j <= nyg - 1; j++)
+            for (int i = 2; i <= nxg - 1; i++) F3(rw, i, j, k) = F3(o->Fw[1], i, j, k);
+    fa_free(&o->Fu[1]); fa_free(&o->Fv[1]); fa_free(&o->Fw[1]);
+    o->Fu[1] = su; o->Fv[1] = sv; o->Fw[1] = sw;
+    periodic_x(&ru, 1, nx, nxg, 1);
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int i = 2; i <= nxg - 1; i++) {
+            F3(rv, i, 1, k) = F3(bc1, i, k, 1);   /* compute_rhs_v_boundary, pressure.f90:237-247 */
+            F3(rv, i, ny, k) = F3(bc2, i, k, 1);
+        }
+    periodic_z(&rw, 3, nz, nzg, 1);
+    for (size_t q = 0; q < fa_size(&o->rhs_p); q++) o->rhs_p.p[q] = 0.0;
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int j = 2; j <= nyg - 1; j++)
+            for (int i = 2; i <= nxg - 1; i++)
+                F3(o->rhs_p, i, j, k) = (F3(ru, i, j, k) - F3(ru, i - 1, j, k)) / (o->x[i] - o->x[i - 1]) +
+                                        (F3(rv, i, j, k) - F3(rv, i, j - 1, k)) / (o->y[j] - o->y[j - 1]) +
+                                        (F3(rw, i, j, k) - F3(rw, i, j, k - 1)) / (o->z[k] - o->z[k - 1]);
+    fa_free(&ru); fa_free(&rv); fa_free(&rw);
+
+    /* solve_poisson_equation_for_pressure, pressure.f90:94-172 */
+    double complex *hat = o->rhs_p_hat;
+    for (int j = 2; j <= nyg - 1; j++) {
+        for (int k = 0; k < nzp; k++)
+            for (int i = 0; i < nxp; i++) o->plane[(size_t)k * nxp + i] = F3(o->rhs_p, i + 2, j, k + 2);
+        fft2d(o->plane, nxp, nzp, o->twx_f, o->twz_f);
+        for (int k = 0; k < nzp; k++)
+            for (int i = 0; i < nxp; i++) hat[(size_t)i + (size_t)nxp * ((j - 2) + (size_t)nym * k)] = o->plane[(size_t)k * nxp + i];
+    }
+    double complex *b1h = (double complex *)malloc(sizeof(double complex) * (size_t)nxp * nzp);
+    double complex *b2h = (double complex *)malloc(sizeof(double complex) * (size_t)nxp * nzp);
+    bc_hat(o, &bc1, b1h);
+    bc_hat(o, &bc2, b2h);
+    const double e1 = o->coef_bc_1 * (o->yg[2] - o->yg[1]), e2 = o->coef_bc_2 * (o->yg[nyg] - o->yg[nyg - 1]);
+#pragma omp parallel
+    {
+        double complex *D = (double complex *)malloc(sizeof(double complex) * (size_t)nym);
+        double complex *DL = (double complex *)malloc(sizeof(double complex) * (size_t)nym);
+        double complex *DU = (double complex *)malloc(sizeof(double complex) * (size_t)nym);
+        double complex *b = (double complex *)malloc(sizeof(double complex) * (size_t)nym);
+#pragma omp for schedule(static)
+        for (int k = 0; k < nzp; k++)
+            for (int i = 0; i < nxp; i++) {
+                for (int j = 2; j <= nyg - 1; j++) D[j - 2] = F3(o->Dyy, j, j, 1) + o->kxx[i] + o->kzz[k];
+                for (int j = 2; j <= nyg - 2; j++) DL[j - 2] = F3(o->Dyy, j + 1, j, 1);
+                for (int j = 2; j <= nyg - 2; j++) DU[j - 2] = F3(o->Dyy, j, j + 1, 1);
+                if (i == 0 && k == 0) D[0] = 3.0 / 2.0 * D[0];
+                for (int j = 0; j < nym; j++) b[j] = hat[(size_t)i + (size_t)nxp * (j + (size_t)nym * k)];
+                b[0] = b[0] + e1 * b1h[(size_t)k * nxp + i];
+                b[nym - 1] = b[nym - 1] - e2 * b2h[(size_t)k * nxp + i];
+                zgtsv_c(nym, DL, D, DU, b);
+                for (int j = 0; j < nym; j++) hat[(size_t)i + (size_t)nxp * (j + (size_t)nym * k)] = b[j];
+            }
+        free(D); free(DL); free(DU); free(b);
+    }
+    free(b1h); free(b2h);
+    double norm = (double)((long)nxp * nzp);
+    for (int j = 2; j <= nyg - 1; j++) {
+        for (int k = 0; k < nzp; k++)
+            for (int i = 0; i < nxp; i++) o->plane[(size_t)k * nxp + i] = hat[(size_t)i + (size_t)nxp * ((j - 2) + (size_t)nym * k)];
+        fft2d(o->plane, nxp, nzp, o->twx_b, o->twz_b);
+        for (int k = 0; k < nzp; k++)
+            for (int i = 0; i < nxp; i++) F3(o->P, i + 2, j, k + 2) = creal(o->plane[(size_t)k * nxp + i] / norm);
+    }
+    /* pressure.f90:158-159.  The reference assigns the (nxg-2, nzg-2) array
+     * bc_1 to the (nxg, nzg) section P(:,1,:); the restatement applies it on
+     * the conforming part i = 2..nxg-1, k = 2..nzg-1 and leaves the x and z
+     * ghost columns of rows 1 and nyg as they were. */
+    for (int k = 2; k <= nzg - 1; k++)
+        for (int i = 2; i <= nxg - 1; i++) {
+            F3(o->P, i, 1, k) = F3(o->P, i, 2, k) - (o->yg[2] - o->yg[1]) * F3(bc1, i, k, 1);
+            F3(o->P, i, nyg, k) = F3(o->P, i, nyg - 1, k) + (o->yg[nyg] - o->yg[nyg - 1]) * F3(bc2, i, k, 1);
+        }
+    /* apply_periodic_xz_pressure, pressure.f90:177-195 (one slab); the
+     * interior-plane exchange of pressure.f90:200-225 has nothing to do */
+    for (int k = 1; k <= nzg; k++)
+        for (int j = 1; j <= nyg; j++) F3(o->P, nxg - 1, j, k) = F3(o->P, 2, j, k);
+    for (int j = 1; j <= nyg; j++)
+        for (int i = 2; i <= nxg - 1; i++) F3(o->P, i, j, nzp + 2) = F3(o->P, i, j, 2);
+    fa_free(&bc1); fa_free(&bc2);
+}
+
 double cfo_check_divergence(cfo *o, double *maxabs) {
     /* projection.f90:234-256 (signed maximum, plus max |div| for the gate) */
     double div = 0.0, adiv = 0.0;

@@ -74,6 +74,7 @@ void cfo_compute_rhs_w(cfo *o, int slot);          /* equations.f90:351 -> Fw{sl
 void cfo_rk_update(cfo *o, int substep);           /* time_integration.f90:108-146 */
 void cfo_apply_boundary_conditions(cfo *o);        /* boundary_conditions.f90:20 */
 void cfo_compute_projection_step(cfo *o);          /* projection.f90:20        */
+void cfo_compute_pressure(cfo *o);                 /* pressure.f90:21          */
 void cfo_compute_pseudo_pressure_rhs(cfo *o);      /* projection.f90:40        */
 void cfo_solve_poisson_equation(cfo *o);           /* projection.f90:74        */
 void cfo_project_velocity(cfo *o);                 /* projection.f90:203       */

@@ -58,7 +58,8 @@ def lib(check: bool = False):
         L.cfo_set_scalar.argtypes = [vp, C.c_char_p, C.c_double]
         for name in ["cfo_init_mass_flow", "cfo_compute_dt", "cfo_time_step_rk3", "cfo_compute_eddy_viscosity",
                      "cfo_compute_wall_model", "cfo_apply_boundary_conditions", "cfo_compute_projection_step",
-                     "cfo_compute_pseudo_pressure_rhs", "cfo_solve_poisson_equation", "cfo_project_velocity"]:
+                     "cfo_compute_pseudo_pressure_rhs", "cfo_solve_poisson_equation", "cfo_project_velocity",
+                     "cfo_compute_pressure"]:
             getattr(L, name).argtypes = [vp]
         for name in ["cfo_compute_rhs_u", "cfo_compute_rhs_v", "cfo_compute_rhs_w", "cfo_rk_update"]:
             getattr(L, name).argtypes = [vp, C.c_int]

@@ -78,3 +78,37 @@ def test_create_rejects_odd_nx_without_gpu_work():
     x, y, z = grids.channel_grid(11, 9, 8)
     with pytest.raises(cf.CfError, match="nx must be even"):
         cf.Channel(x, y, z)
+
+
+def test_statistics_text_file_known_answer(tmp_path):
+    """output_statistics (input_output.f90:549-570): '(A,4F15.8,4I)' header
+    and '(8F15.8)' records of seven values, written by hand from the Fortran
+    edit rules: right-justified fields, eight decimals, a minus sign on
+    negative values that round to zero but not on IEEE -0.0, asterisks when
+    the value does not fit, I12 for the widthless integer descriptor."""
+    import channelflow as cf
+    ny = 3
+    y = np.array([0.0, 1.0, 2.0])
+    st = np.zeros(9 * ny + 8)
+    prof = {0: [1.5, -1e-12, 2.25], 3: [0.125, -0.0, 999999.5], 4: [1234567.0, -99999.5, np.nan],
+            5: [1e-9, 6e-9, -0.333333333333], 6: [0.0, 0.5, -0.5], 8: [7.0, 8.0, 9.0]}
+    for q, v in prof.items():
+        st[q * ny:(q + 1) * ny] = v
+    st[9 * ny], st[9 * ny + 1] = 0.0638, 180.123456789  # utau, Retau
+    p = tmp_path / "s.txt"
+    cf.write_statistics(str(p), 0.125, 3.547e-4, 66, ny, 66, 200, y, st)
+    got = p.read_text().split("\n")
+    want = [
+        "%" + "     0.12500000" + "   180.12345679" + "     0.06380000" + "     0.00035470"
+        + "          66" + "           3" + "          66" + "         200",
+        "     0.00000000" + "     1.50000000" + "     0.12500000" + "***************" + "     0.00000000"
+        + "     0.00000000" + "     7.00000000",
+        "     1.00000000" + "    -0.00000000" + "     0.00000000" + "-99999.50000000" + "     0.00000001"
+        + "     0.50000000" + "     8.00000000",
+        "     2.00000000" + "     2.25000000" + "999999.50000000" + "            NaN" + "    -0.33333333"
+        + "    -0.50000000" + "     9.00000000",
+        "",
+    ]
+    assert got == want
+    assert cf.statistics_file_name("  run/out  ", 200, 1000) == "run/out.1200.stats.txt"
+    assert cf.statistics_file_name("o", 123456789, 0) == "o.********.stats.txt"

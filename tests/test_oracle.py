@@ -249,3 +249,38 @@ def test_bounds_checked_oracle_runs_a_step():
     o.compute_dt()
     o.time_step_rk3()
     assert np.isfinite(o.array("U")).all()
+
+
+@pytest.mark.parametrize("check", [False, True])
+def test_pressure_solves_discrete_poisson(check):
+    """compute_pressure (pressure.f90:21): with its wall rows, the 3-point
+    Laplacian of P (x and z through the periodic wrap) equals div(rhs) on
+    every interior row; on row 2 up to one constant, the gauge of the (0,0)
+    mode (D(2)*3/2).  The periodic copies are exact."""
+    from oracle import Oracle
+    nx, ny, nz = 18, 17, 14
+    case = channel_case(nx, ny, nz, stretch=1.5)
+    o = Oracle(case["x"], case["y"], case["z"], case["prm"], check=check)
+    o.set_fields(case["U"], case["V"], case["W"])
+    o.apply_boundary_conditions()
+    o.compute_eddy_viscosity()
+    o.compute_pressure()
+    P, rp = o.array("P"), o.array("rhs_p")
+    nxg, nyg, nzg, nxp, nzp = nx + 1, ny + 1, nz + 1, nx - 2, nz - 2
+    x, y, z, yg = o.array("x"), o.array("y"), o.array("z"), o.array("yg")
+    dx, dz = x[1] - x[0], z[1] - z[0]
+    Pc = P[1:nxp + 1, :, 1:nzp + 1]
+    lap = (np.roll(Pc, -1, 0) - 2 * Pc + np.roll(Pc, 1, 0)) / dx ** 2 + \
+          (np.roll(Pc, -1, 2) - 2 * Pc + np.roll(Pc, 1, 2)) / dz ** 2
+    res = np.zeros((nxp, nyg - 2, nzp))
+    for j in range(2, nyg):  # Fortran row j; arrays are 0-based
+        a = 1 / (y[j - 1] - y[j - 2]) / (yg[j] - yg[j - 1])
+        c = 1 / (y[j - 1] - y[j - 2]) / (yg[j - 1] - yg[j - 2])
+        res[:, j - 2, :] = lap[:, j - 1, :] + c * Pc[:, j - 2, :] - (a + c) * Pc[:, j - 1, :] + a * Pc[:, j, :]
+    res -= rp[:nxp, :, :nzp]
+    scale = abs(rp).max()
+    assert abs(res[:, 1:, :]).max() < 1e-12 * scale
+    assert abs(res[:, 0, :] - res[:, 0, :].mean()).max() < 1e-12 * scale
+    assert np.array_equal(P[nxg - 2], P[1])
+    assert np.array_equal(P[1:nxg - 1, :, nzg - 2], P[1:nxg - 1, :, 1])
+    assert abs(P[1:-1, 0, 1:-1] - P[1:-1, 1, 1:-1]).max() > 1e-6 * abs(P).max()

@@ -24,7 +24,8 @@ def make_pair(case, precision=0, **extra):
     ch.upload(case["U"], case["V"], case["W"])
     q0 = ch.init_mass_flow()
     o.init_mass_flow()
-    assert abs(q0 - o.scalar("Qflow_x_0")) <= 1e-14 * abs(q0)
+    # FP64: the same sums; split: the FP32 state (hi word) against FP64
+    assert abs(q0 - o.scalar("Qflow_x_0")) <= (1e-14 if precision == 0 else 1e-7) * abs(q0)
     return o, ch
 
 
@@ -238,3 +239,66 @@ def test_pinned_host_buffers_match_pageable():
         for k in ("U", "V", "W"):
             assert np.array_equal(pinned[k], ref[k]), (prec, k)
         ch.close()
+
+
+@pytest.mark.parametrize("which,wall,precision,tol", [("small", 0, 0, 1e-11), ("config1", 0, 0, 1e-11),
+                                                       ("small", 3, 0, 1e-11), ("config1", 0, 1, 1e-4)])
+def test_actual_pressure(which, wall, precision, tol):
+    """compute_pressure (pressure.f90:21) on the fields left by a projection
+    of rk_step 1: P everywhere, ghost columns included (those keep the
+    projection's values on both sides).  The oracle follows the reference's
+    boundary terms; the CUDA path drops the two that cancel."""
+    extra = dict(stretch=0.0, wall=3, retau=2000.0, profile="plug") if wall else {}
+    case = channel_case(*CASES[which], **extra)
+    o, ch = make_pair(case, precision=precision)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.set_scalar("dt", case["dt"]); o.set_scalar("rk_step", 1)
+    ch.set_scalars(dt=case["dt"], rk_step=1)
+    o.compute_eddy_viscosity(); ch.compute_eddy_viscosity()
+    if wall:
+        o.compute_wall_model(); ch.compute_wall_model()
+    o.compute_projection_step(); ch.compute_projection_step()
+    o.apply_boundary_conditions(); ch.apply_boundary_conditions()
+    o.compute_pressure(); ch.compute_pressure()
+    g, f = ch.download(), o.fields()
+    P0 = f["P"]
+    # the wall rows carry the boundary condition: they must differ from the
+    # first interior row, or the check of the ghost formula is empty
+    assert abs(P0[1:-1, 0, 1:-1] - P0[1:-1, 1, 1:-1]).max() > 1e-6 * abs(P0).max()
+    assert_close(g["P"], P0, tol, "P")
+    # rows 1 and nyg alone, relative to the size of the wall jump
+    for j0, j1 in ((0, 1), (-1, -2)):
+        jg, jo = g["P"][1:-1, j0, 1:-1] - g["P"][1:-1, j1, 1:-1], P0[1:-1, j0, 1:-1] - P0[1:-1, j1, 1:-1]
+        assert_close(jg, jo, max(tol, 1e-10) * 10, f"wall jump {j0}")
+
+
+def test_statistics_and_text_file(tmp_path):
+    """compute_statistics (statistics.f90:22-171) after five steps against the
+    oracle, and the text file of output_statistics written from it."""
+    import channelflow as cf
+    case = channel_case(*CASES["config1"])
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    ch.set_fixed_dt(case["dt"])
+    for _ in range(5):
+        o.compute_dt()
+        o.time_step_rk3()
+    ch.time_step_rk3(5)
+    sg, so = ch.statistics(), o.statistics()
+    ny = ch.ny
+    for q in range(9):  # profiles, normwise
+        assert_close(sg[q * ny:(q + 1) * ny], so[q * ny:(q + 1) * ny], 1e-11, f"profile {q}")
+    assert_close(sg[9 * ny:], so[9 * ny:], 1e-9, "scalars")
+    path = ch.output_statistics(str(tmp_path / "run"), istep=5, nstep_init=100)
+    assert path.endswith("run.105.stats.txt")
+    lines = open(path).read().split("\n")
+    assert len(lines) == ny + 2 and lines[-1] == ""
+    hdr = lines[0]
+    assert hdr[0] == "%" and len(hdr) == 1 + 4 * 15 + 4 * 12
+    assert [int(hdr[61 + 12 * q:73 + 12 * q]) for q in range(4)] == [ch.nx, ny, ch.nz, 5]
+    assert abs(float(hdr[16:31]) - so[9 * ny + 1]) <= 1e-8  # Retau
+    rows = np.array([[float(l[15 * c:15 * (c + 1)]) for c in range(7)] for l in lines[1:-1]])
+    want = np.stack([o.array("y")] + [so[q * ny:(q + 1) * ny] for q in (0, 3, 4, 5, 6, 8)], axis=1)
+    assert abs(rows - want).max() <= 5.1e-9
