@@ -37,6 +37,8 @@ UNIT = "grid-pt·steps/s"
 WORKLOADS = {
     "re550": dict(name="LES Re_tau=550, 192x128x192, DSM, no-slip, constant mass flow", nx=194, ny=129, nz=194,
                   retau=550.0, stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar"),
+    "re550_amd": dict(name="LES Re_tau=550, 192x128x192, AMD, no-slip, constant mass flow", nx=194, ny=129, nz=194,
+                      retau=550.0, stretch=1.5, les=3, wall=0, jref=3, ncv=100, profile="laminar"),
     "re180": dict(name="Re_tau=180, 64x64x64, DSM, no-slip, constant mass flow", nx=66, ny=65, nz=66, retau=180.0,
                   stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar"),
     "re2000_eqwm": dict(name="WMLES Re_tau=2000, 256x96x256, DSM + eqwm (ncv 30), uniform y", nx=258, ny=97, nz=258,
@@ -61,6 +63,8 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
     tab = {
         # the dynamic Smagorinsky pass: read U, V, W, write |S| (4 field accesses per cell)
         "k_dsm_fused": 4 * nC * es,
+        # the AMD pass: read U, V, W, write nu_t
+        "k_amd": 4 * nC * es,
         # 3 velocity components in, |S| Sij (6), products (6), centre velocities (3), |S| out
         "k_dsm_a": (3 + 16) * nC * es,
         # 15 filtered inputs, 12 outputs

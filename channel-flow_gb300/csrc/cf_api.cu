@@ -362,8 +362,13 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     if (nx % 2 != 0) return cf_fail(nullptr, CF_ERR_INVALID, "Error: nx must be even");  // initialization.f90:54
     if (nz % 2 != 0) return cf_fail(nullptr, CF_ERR_INVALID, "Error: nz must be even");  // initialization.f90:55
     if (nx < 6 || nz < 6 || ny < 5) return cf_fail(nullptr, CF_ERR_INVALID, "grid too small (nx, nz >= 6, ny >= 5)");
-    if (p->LES_model != 0 && p->LES_model != 2)
-        return cf_fail(nullptr, CF_ERR_UNSUPPORTED, "LES_model must be 0 (none) or 2 (dynamic Smagorinsky)");
+    if (p->LES_model != 0 && p->LES_model != 2 && p->LES_model != 3)
+        return cf_fail(nullptr, CF_ERR_UNSUPPORTED,
+                       "LES_model must be 0 (none), 2 (dynamic Smagorinsky) or 3 (anisotropic minimum dissipation)");
+    // the wall rules of the eddy viscosity ghosts: subgrid.f90:530-536 (dynamic
+    // Smagorinsky: 1 Dirichlet, otherwise Neumann), :866-876 (AMD: 0, 1, 2)
+    if (p->LES_model == 3 && (p->Dirichlet_nu_t < 0 || p->Dirichlet_nu_t > 2))
+        return cf_fail(nullptr, CF_ERR_UNSUPPORTED, "Dirichlet_nu_t must be 0, 1 or 2 with LES_model 3");
     if (p->iwall_model != 0 && p->iwall_model != 3)
         return cf_fail(nullptr, CF_ERR_UNSUPPORTED, "iwall_model must be 0 (no-slip) or 3 (equilibrium wall model)");
     if (p->iwall_model == 3 && (p->jref_eqwm < 2 || p->jref_eqwm > ny / 2))
@@ -483,6 +488,7 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     else { TRY(alloc_all<float>(ctx)); TRY(upload_twiddles<float>(ctx)); }
     ctx->dsm_nblk = std::max(1, std::min(64, (int)((long)nxp * nzp / 2048)));
     size_t nch_fused = 0;
+    int amd_parts = 0;
     {
         // fused pass: column tiles marching in z; chunks sized for one wave
         int dev_sms = 152;
@@ -503,8 +509,9 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
             if (cost < best_cost - 1e-9) { best_cost = cost; best = n; }
         }
         ctx->rhs_nkc = (int)best;
+        if (p->LES_model == 3) amd_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms, &ctx->amd_nkc, &amd_parts);
     }
-    size_t nch = std::max((size_t)ctx->dsm_nblk, nch_fused);
+    size_t nch = std::max({(size_t)ctx->dsm_nblk, nch_fused, (size_t)cdiv(amd_parts, 2)});
     CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));
     // avg_nu_t (1..nyg) in FP64, followed by an FP32 copy
     CF_CUDA(cudaMalloc(&ctx->avg_nu_t, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
@@ -817,6 +824,7 @@ extern "C" int cf_compute_dt(cf_ctx *ctx, double *dt) {
 
 static int eddy(cf_ctx *ctx, int b) {
     if (ctx->prm.LES_model == 2) return DISPATCH(launch_dsm<double>(ctx, b), launch_dsm<float>(ctx, b));
+    if (ctx->prm.LES_model == 3) return DISPATCH(launch_amd<double>(ctx, b), launch_amd<float>(ctx, b));
     return DISPATCH(launch_nut_zero<double>(ctx), launch_nut_zero<float>(ctx));
 }
 
@@ -911,6 +919,9 @@ extern "C" int cf_download_rhs(cf_ctx *ctx, int comp, int slot, double *out) {
 
 extern "C" int cf_download_avg_nu_t(cf_ctx *ctx, double *out) {
     if (!ctx || !out) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    TRY(launch_avg_nu_t_flush(ctx));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
     CF_CUDA(cudaMemcpy(out, ctx->avg_nu_t + 1, ctx->nyg * sizeof(double), cudaMemcpyDeviceToHost));
     return CF_OK;
 }

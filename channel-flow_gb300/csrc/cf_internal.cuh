@@ -113,6 +113,40 @@ __host__ __device__ __forceinline__ int wrapc(int i, int np) {
 
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
+// compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual indices.
+template <typename T>
+__device__ __forceinline__ void sij_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W, int i,
+                                          int j, int k, T s[6], T &S) {
+    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg;
+    const T h = T(0.5), q = T(0.25);
+    s[0] = (U(i, j, k) - U(i - 1, j, k)) / (x[i] - x[i - 1]);
+    s[1] = (V(i, j, k) - V(i, j - 1, k)) / (y[j] - y[j - 1]);
+    s[2] = (W(i, j, k) - W(i, j, k - 1)) / (z[k] - z[k - 1]);
+    T e4[2][2], e5[2][2], e6[2][2];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 2; b++) {
+            int ii = i + a, jj = j + b, kk = k + b;
+            // edge values at (ii, jj, k), (ii, j, kk), (i, j+a, k+b)
+            e4[a][b] = h * ((U(ii - 1, jj, k) - U(ii - 1, jj - 1, k)) / (yg[jj] - yg[jj - 1]) +
+                            (V(ii, jj - 1, k) - V(ii - 1, jj - 1, k)) / (xg[ii] - xg[ii - 1]));
+            e5[a][b] = h * ((U(ii - 1, j, kk) - U(ii - 1, j, kk - 1)) / (zg[kk] - zg[kk - 1]) +
+                            (W(ii, j, kk - 1) - W(ii - 1, j, kk - 1)) / (xg[ii] - xg[ii - 1]));
+            int j6 = j + a, k6 = k + b;
+            e6[a][b] = h * ((V(i, j6 - 1, k6) - V(i, j6 - 1, k6 - 1)) / (zg[k6] - zg[k6 - 1]) +
+                            (W(i, j6, k6 - 1) - W(i, j6 - 1, k6 - 1)) / (yg[j6] - yg[j6 - 1]));
+        }
+    s[3] = q * (e4[0][0] + e4[1][0] + e4[0][1] + e4[1][1]);
+    s[4] = q * (e5[0][0] + e5[1][0] + e5[0][1] + e5[1][1]);
+    s[5] = q * (e6[0][0] + e6[1][0] + e6[0][1] + e6[1][1]);
+    T a2 = T(0);
+#pragma unroll
+    for (int c = 0; c < 6; c++) a2 += (c < 3 ? T(2) : T(4)) * s[c] * s[c];
+    S = sqrt(a2);
+}
+
+
 struct cf_ctx {
     int dev = 0;
     cf_params prm;
@@ -153,6 +187,9 @@ struct cf_ctx {
     bool use_fused_dsm = true;
     bool use_rhs3 = true;              // one fused RHS + update launch per substep
     int rhs_nkc = 1;                   // z chunks of the fused RHS
+    int amd_nkc = 1;                   // z chunks of the AMD pass
+    int amd_nparts = 0;                // partial sums per row of the last AMD pass
+    bool amd_avg_pending = false;      // avg_nu_t not yet formed from them
     bool state_periodic = false;       // U, V, W satisfy the periodic/no-slip ghost identities
     // After the one-pass eddy viscosity, nu_t is held as |S| (canonical) and
     // the plane coefficient <LM>/<MM>: the fused RHS forms nu_t on the fly and
@@ -220,6 +257,9 @@ template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut
 // follow rewrite the periodic duplicates)
 template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true, bool canon = false);
 template <typename T> int launch_pressure(cf_ctx *ctx, int buf);  // actual pressure into P (pressure.f90:21)
+template <typename T> int launch_amd(cf_ctx *ctx, int buf);  // AMD eddy viscosity (subgrid.f90:639)
+void amd_plan(int esz, int nxp, int nym, int nzp, int sms, int *nkc, int *nparts);  // z chunks of the AMD pass
+int launch_avg_nu_t_flush(cf_ctx *ctx);  // AMD plane means of the last pass, if not formed yet
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only

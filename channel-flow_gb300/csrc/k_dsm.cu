@@ -21,39 +21,6 @@ struct Can {
     }
 };
 
-// compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual indices.
-template <typename T>
-__device__ __forceinline__ void sij_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W, int i,
-                                          int j, int k, T s[6], T &S) {
-    const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg;
-    const T h = T(0.5), q = T(0.25);
-    s[0] = (U(i, j, k) - U(i - 1, j, k)) / (x[i] - x[i - 1]);
-    s[1] = (V(i, j, k) - V(i, j - 1, k)) / (y[j] - y[j - 1]);
-    s[2] = (W(i, j, k) - W(i, j, k - 1)) / (z[k] - z[k - 1]);
-    T e4[2][2], e5[2][2], e6[2][2];
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 2; b++) {
-            int ii = i + a, jj = j + b, kk = k + b;
-            // edge values at (ii, jj, k), (ii, j, kk), (i, j+a, k+b)
-            e4[a][b] = h * ((U(ii - 1, jj, k) - U(ii - 1, jj - 1, k)) / (yg[jj] - yg[jj - 1]) +
-                            (V(ii, jj - 1, k) - V(ii - 1, jj - 1, k)) / (xg[ii] - xg[ii - 1]));
-            e5[a][b] = h * ((U(ii - 1, j, kk) - U(ii - 1, j, kk - 1)) / (zg[kk] - zg[kk - 1]) +
-                            (W(ii, j, kk - 1) - W(ii - 1, j, kk - 1)) / (xg[ii] - xg[ii - 1]));
-            int j6 = j + a, k6 = k + b;
-            e6[a][b] = h * ((V(i, j6 - 1, k6) - V(i, j6 - 1, k6 - 1)) / (zg[k6] - zg[k6 - 1]) +
-                            (W(i, j6, k6 - 1) - W(i, j6 - 1, k6 - 1)) / (yg[j6] - yg[j6 - 1]));
-        }
-    s[3] = q * (e4[0][0] + e4[1][0] + e4[0][1] + e4[1][1]);
-    s[4] = q * (e5[0][0] + e5[1][0] + e5[0][1] + e5[1][1]);
-    s[5] = q * (e6[0][0] + e6[1][0] + e6[0][1] + e6[1][1]);
-    T a2 = T(0);
-#pragma unroll
-    for (int c = 0; c < 6; c++) a2 += (c < 3 ? T(2) : T(4)) * s[c] * s[c];
-    S = sqrt(a2);
-}
-
 // Stage A: centre velocities, products and |S| S_ij at canonical centres.
 template <typename T>
 __global__ void k_dsm_a(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, T *q, Can c) {

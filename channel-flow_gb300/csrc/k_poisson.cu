@@ -1125,6 +1125,7 @@ int launch_pressure(cf_ctx *ctx, int b) {
     k_zero_vwall<T><<<dim3(cdiv(ctx->nxg, 128), ctx->nzg), 128, 0, ctx->st>>>(Fv, ctx->nxg, ctx->ny, ctx->nzg);
     count_launch(ctx, "k_zero_vwall");
     if (int rc = poisson_solve<T>(ctx, Fu, Fv, Fw)) return rc;
+    if (int rc = launch_avg_nu_t_flush(ctx)) return rc;
     const double *y = ctx->hy.data(), *yg = ctx->hyg.data();  // 1-based
     const int ny = ctx->ny, nyg = ctx->nyg;
     PWall pw;

@@ -100,6 +100,7 @@ struct cfo {
     fa alpha_x, alpha_y, alpha_z, alpha_z_temp, tau_eqwm_initial;
     fa temp_1, temp_2, temp_3, temp_4;
     int n_nan_eqwm, n_iter_eqwm;
+    int amd_nan_canonical; /* canonical cells of the last sgs_AMD whose quotient was NaN */
     double complex *plane; /* nxp*nzp spectrum plane */
     double complex *rhs_p_hat; /* (0:mx, 2:nyg-1, 0:mz) */
     double complex *twx_f, *twx_b, *twz_f, *twz_b; /* DFT twiddles */
@@ -473,6 +474,7 @@ double cfo_scalar(cfo *o, const char *name) {
     if (!strcmp(name, "Omega_z")) return o->Omega_z;
     if (!strcmp(name, "rk_step")) return o->rk_step;
     if (!strcmp(name, "n_nan_eqwm")) return o->n_nan_eqwm;
+    if (!strcmp(name, "amd_nan_canonical")) return o->amd_nan_canonical;
     if (!strcmp(name, "n_iter_eqwm")) return o->n_iter_eqwm;
     if (!strcmp(name, "tau_mean_eqwm")) return o->tau_mean_eqwm;
     if (!strcmp(name, "dxmin")) return o->dxmin;
@@ -1140,10 +1142,310 @@ static void sgs_dynamic_smagorinsky(cfo *o) {
     }
 }
 
+/* ------------------------------------------------------------------------ */
+/* Anisotropic minimum dissipation model, subgrid.f90:639-881.               */
+/* The reference works on whole arrays and array sections of the module     */
+/* temporaries term, term_1..term_4, some of which it only partly sets; the */
+/* restatement performs the same section operations on temporaries filled  */
+/* with NaN, so a value the reference would take from an unset (stale)      */
+/* part of a temporary shows as NaN.  amd_nan_canonical counts the          */
+/* canonical cells whose quotient came out NaN.                             */
+/* ------------------------------------------------------------------------ */
+typedef struct { int l[3], u[3]; } sec3;
+static sec3 SEC(int l0, int u0, int l1, int u1, int l2, int u2) {
+    sec3 r = {{l0, l1, l2}, {u0, u1, u2}};
+    return r;
+}
+/* interpolate_x/_y/_z(u = A(a), ui = B(b), 1), interpolation.f90:24-105:
+ * ui = 0, then ui(1:n-1 along dir) = 0.5 (u(m) + u(m+1)) with n = shape(u). */
+static void interp_sec(int dir, fa *A, sec3 a, fa *B, sec3 b) {
+    int m[3];
+    for (int d = 0; d < 3; d++) m[d] = a.u[d] - a.l[d] + 1;
+    m[dir] -= 1;
+    for (int d = 0; d < 3; d++)
+        if (b.l[d] + m[d] - 1 > b.u[d]) {
+            fprintf(stderr, "cf_oracle: interpolation section overflow\n");
+            abort();
+        }
+    for (int k = b.l[2]; k <= b.u[2]; k++)
+        for (int j = b.l[1]; j <= b.u[1]; j++)
+            for (int i = b.l[0]; i <= b.u[0]; i++) F3(*B, i, j, k) = 0.0;
+    for (int r = 0; r < m[2]; r++)
+        for (int q = 0; q < m[1]; q++)
+            for (int p = 0; p < m[0]; p++) {
+                int e[3] = {p, q, r};
+                e[dir] += 1;
+                F3(*B, b.l[0] + p, b.l[1] + q, b.l[2] + r) =
+                    0.5 * (F3(*A, a.l[0] + p, a.l[1] + q, a.l[2] + r) + F3(*A, a.l[0] + e[0], a.l[1] + e[1], a.l[2] + e[2]));
+            }
+}
+#define AMD_LOOP(i0, i1, j0, j1, k0, k1) \
+    for (int k = (k0); k <= (k1); k++)    \
+        for (int j = (j0); j <= (j1); j++) \
+            for (int i = (i0); i <= (i1); i++)
+static double sq(double a) { return pow(a, 2.0); }
+
+static void sgs_amd(cfo *o) {
+    int nx = o->nx, ny = o->ny, nz = o->nz, nxg = o->nxg, nyg = o->nyg, nzg = o->nzg;
+    const double *x = o->x, *y = o->y, *z = o->z, *xg = o->xg, *yg = o->yg, *zg = o->zg;
+    fa *U = &o->U, *V = &o->V, *W = &o->W, *Sij = &o->Sij, *nt = &o->nu_t;
+    const double C = 0.3;
+    fa t0 = fa_new3(1, nxg, 1, nyg, 1, nzg), t1 = fa_new3(1, nxg, 1, nyg, 1, nzg), t2 = fa_new3(1, nxg, 1, nyg, 1, nzg);
+    fa t3 = fa_new3(1, nxg, 1, nyg, 1, nzg), t4 = fa_new3(1, nxg, 1, nyg, 1, nzg);
+    fa *tt[5] = {&t0, &t1, &t2, &t3, &t4};
+    for (int q = 0; q < 5; q++)
+        for (size_t e = 0; e < fa_size(tt[q]); e++) tt[q]->p[e] = NAN;
+    const sec3 ALL = SEC(1, nxg, 1, nyg, 1, nzg);
+    /* Part 1: subgrid.f90:658 */
+    compute_Sij(o, U, V, W, Sij, &o->S);
+    /* nu += f * T(2:nxg,2:nyg,2:nzg) * Sij(:,:,:,c) */
+#define NU_ADD(f, T, c) AMD_LOOP(2, nxg, 2, nyg, 2, nzg) F3(*nt, i, j, k) = F3(*nt, i, j, k) + (f) * F3(T, i, j, k) * F4(*Sij, i, j, k, c)
+#define NU_ADD1(T, c) AMD_LOOP(2, nxg, 2, nyg, 2, nzg) F3(*nt, i, j, k) = F3(*nt, i, j, k) + F3(T, i, j, k) * F4(*Sij, i, j, k, c)
+#define WHOLE(stmt) AMD_LOOP(ALL.l[0], ALL.u[0], ALL.l[1], ALL.u[1], ALL.l[2], ALL.u[2]) stmt
+
+    /* (d_hat_i U)^2 S11, (d_i U)^2: subgrid.f90:660-695 */
+    for (int i = 2; i <= nx; i++)
+        for (int k = 1; k <= nzg; k++)
+            for (int j = 1; j <= nyg; j++) {
+                F3(t2, i, j, k) = sq(F3(*U, i, j, k) - F3(*U, i - 1, j, k));
+                F3(t4, i, j, k) = sq(F3(*U, i, j, k) - F3(*U, i - 1, j, k)) / sq(x[i] - x[i - 1]);
+            }
+    AMD_LOOP(2, nxg, 2, nyg, 2, nzg) F3(*nt, i, j, k) = F3(t2, i, j, k) * F4(*Sij, i, j, k, 1);
+    for (int j = 2; j <= nyg; j++)
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 1; i <= nx; i++) {
+                F3(t0, i, j, k) = sq(F3(*U, i, j, k) - F3(*U, i, j - 1, k));
+                F3(t1, i, j, k) = F3(t0, i, j, k) / sq(yg[j] - yg[j - 1]);
+            }
+    interp_sec(0, &t1, SEC(1, nx, 2, nyg, 1, nzg), &t2, SEC(2, nx, 2, nyg, 1, nzg));
+    interp_sec(1, &t2, SEC(2, nx, 2, nyg, 1, nzg), &t3, SEC(2, nx, 2, nyg - 1, 1, nzg));
+    WHOLE(F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t3, i, j, k));
+    interp_sec(0, &t0, SEC(1, nx, 2, nyg, 1, nzg), &t1, SEC(2, nx, 2, nyg, 1, nzg));
+    interp_sec(1, &t1, SEC(2, nx, 2, nyg, 1, nzg), &t2, SEC(2, nx, 2, nyg - 1, 1, nzg));
+    NU_ADD1(t2, 1);
+    for (int k = 2; k <= nzg; k++)
+        for (int j = 1; j <= nyg; j++)
+            for (int i = 1; i <= nx; i++) {
+                F3(t0, i, j, k) = sq(F3(*U, i, j, k) - F3(*U, i, j, k - 1));
+                F3(t1, i, j, k) = F3(t0, i, j, k) / sq(zg[k] - zg[k - 1]);
+            }
+    interp_sec(0, &t1, SEC(1, nx, 1, nyg, 2, nzg), &t2, SEC(2, nx, 1, nyg, 2, nzg));
+    interp_sec(2, &t2, SEC(2, nx, 1, nyg, 2, nzg), &t3, SEC(2, nx, 1, nyg, 2, nzg - 1));
+    WHOLE(F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t3, i, j, k));
+    interp_sec(0, &t0, SEC(1, nx, 1, nyg, 2, nzg), &t1, SEC(2, nx, 1, nyg, 2, nzg));
+    interp_sec(2, &t1, SEC(2, nx, 1, nyg, 2, nzg), &t2, SEC(2, nx, 1, nyg, 2, nzg - 1));
+    NU_ADD1(t2, 1);
+
+    /* (d_hat_i V)^2 S22, (d_i V)^2: subgrid.f90:697-731 */
+    for (int j = 2; j <= ny; j++)
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 1; i <= nxg; i++) {
+                F3(t2, i, j, k) = sq(F3(*V, i, j, k) - F3(*V, i, j - 1, k));
+                F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t2, i, j, k) / sq(y[j] - y[j - 1]);
+            }
+    NU_ADD1(t2, 2);
+    for (int i = 2; i <= nxg; i++)
+        for (int k = 1; k <= nzg; k++)
+            for (int j = 1; j <= ny; j++) {
+                F3(t0, i, j, k) = sq(F3(*V, i, j, k) - F3(*V, i - 1, j, k));
+                F3(t1, i, j, k) = F3(t0, i, j, k) / sq(xg[i] - xg[i - 1]);
+            }
+    interp_sec(1, &t1, SEC(2, nxg, 1, ny, 1, nzg), &t2, SEC(2, nxg, 2, ny, 1, nzg));
+    interp_sec(0, &t2, SEC(2, nxg, 2, ny, 1, nzg), &t3, SEC(2, nxg - 1, 2, ny, 1, nzg));
+    WHOLE(F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t3, i, j, k));
+    interp_sec(1, &t0, SEC(2, nxg, 1, ny, 1, nzg), &t1, SEC(2, nxg, 2, ny, 1, nzg));
+    interp_sec(0, &t1, SEC(2, nxg, 2, ny, 1, nzg), &t2, SEC(2, nxg - 1, 2, ny, 1, nzg));
+    NU_ADD1(t2, 2);
+    for (int k = 2; k <= nzg; k++)
+        for (int j = 1; j <= ny; j++)
+            for (int i = 1; i <= nxg; i++) {
+                F3(t0, i, j, k) = sq(F3(*V, i, j, k) - F3(*V, i, j, k - 1));
+                F3(t1, i, j, k) = F3(t0, i, j, k) / sq(zg[k] - zg[k - 1]);
+            }
+    interp_sec(1, &t1, SEC(1, nxg, 1, ny, 2, nzg), &t2, SEC(1, nxg, 2, ny, 2, nzg));
+    interp_sec(2, &t2, SEC(1, nxg, 2, ny, 2, nzg), &t3, SEC(1, nxg, 2, ny, 2, nzg - 1));
+    WHOLE(F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t3, i, j, k));
+    interp_sec(1, &t0, SEC(1, nxg, 1, ny, 2, nzg), &t1, SEC(1, nxg, 2, ny, 2, nzg));
+    interp_sec(2, &t1, SEC(1, nxg, 2, ny, 2, nzg), &t2, SEC(1, nxg, 2, ny, 2, nzg - 1));
+    NU_ADD1(t2, 2);
+
+    /* (d_hat_i W)^2 S33, (d_i W)^2: subgrid.f90:733-767 */
+    for (int k = 2; k <= nz; k++)
+        for (int j = 1; j <= nyg; j++)
+            for (int i = 1; i <= nxg; i++) {
+                F3(t2, i, j, k) = sq(F3(*W, i, j, k) - F3(*W, i, j, k - 1));
+                F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t2, i, j, k) / sq(z[k] - z[k - 1]);
+            }
+    NU_ADD1(t2, 3);
+    for (int i = 2; i <= nxg; i++)
+        for (int k = 1; k <= nz; k++)
+            for (int j = 1; j <= nyg; j++) {
+                F3(t0, i, j, k) = sq(F3(*W, i, j, k) - F3(*W, i - 1, j, k));
+                F3(t1, i, j, k) = F3(t0, i, j, k) / sq(xg[i] - xg[i - 1]);
+            }
+    interp_sec(2, &t1, SEC(2, nxg, 1, nyg, 1, nz), &t2, SEC(2, nxg, 1, nyg, 2, nz));
+    interp_sec(0, &t2, SEC(2, nxg, 1, nyg, 2, nz), &t3, SEC(2, nxg - 1, 1, nyg, 2, nz));
+    WHOLE(F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t3, i, j, k));
+    interp_sec(2, &t0, SEC(2, nxg, 1, nyg, 1, nz), &t1, SEC(2, nxg, 1, nyg, 2, nz));
+    interp_sec(0, &t1, SEC(2, nxg, 1, nyg, 2, nz), &t2, SEC(2, nxg - 1, 1, nyg, 2, nz));
+    NU_ADD1(t2, 3);
+    for (int j = 2; j <= nyg; j++)
+        for (int k = 1; k <= nz; k++)
+            for (int i = 1; i <= nxg; i++) {
+                F3(t0, i, j, k) = sq(F3(*W, i, j, k) - F3(*W, i, j - 1, k));
+                F3(t1, i, j, k) = F3(t0, i, j, k) / sq(yg[j] - yg[j - 1]);
+            }
+    interp_sec(2, &t1, SEC(1, nxg, 2, nyg, 1, nz), &t2, SEC(1, nxg, 2, nyg, 2, nz));
+    interp_sec(1, &t2, SEC(1, nxg, 2, nyg, 2, nz), &t3, SEC(1, nxg, 2, nyg - 1, 2, nz));
+    WHOLE(F3(t4, i, j, k) = F3(t4, i, j, k) + F3(t3, i, j, k));
+    interp_sec(2, &t0, SEC(1, nxg, 2, nyg, 1, nz), &t1, SEC(1, nxg, 2, nyg, 2, nz));
+    interp_sec(1, &t1, SEC(1, nxg, 2, nyg, 2, nz), &t2, SEC(1, nxg, 2, nyg - 1, 2, nz));
+    NU_ADD1(t2, 3);
+
+    /* 2 (d_hat_i U)(d_hat_i V) S12: subgrid.f90:769-800 */
+    for (int i = 2; i <= nxg; i++)
+        for (int k = 1; k <= nzg; k++)
+            for (int j = 1; j <= ny; j++) F3(t0, i, j, k) = F3(*V, i, j, k) - F3(*V, i - 1, j, k);
+    interp_sec(1, &t0, SEC(2, nxg, 1, ny, 1, nzg), &t1, SEC(2, nxg, 2, ny, 1, nzg));
+    interp_sec(0, &t1, SEC(2, nxg, 2, ny, 1, nzg), &t2, SEC(2, nxg - 1, 2, ny, 1, nzg));
+    for (int i = 2; i <= nx; i++)
+        for (int k = 1; k <= nzg; k++)
+            for (int j = 2; j <= nyg - 1; j++)
+                F3(t1, i, j, k) = F3(t2, i, j, k) * (F3(*U, i, j, k) - F3(*U, i - 1, j, k));
+    NU_ADD(2.0, t1, 4);
+    for (int j = 2; j <= nyg; j++)
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 1; i <= nx; i++) F3(t0, i, j, k) = F3(*U, i, j, k) - F3(*U, i, j - 1, k);
+    interp_sec(0, &t0, SEC(1, nx, 2, nyg, 1, nzg), &t1, SEC(2, nx, 2, nyg, 1, nzg));
+    interp_sec(1, &t1, SEC(2, nx, 2, nyg, 1, nzg), &t2, SEC(2, nx, 2, nyg - 1, 1, nzg));
+    for (int j = 2; j <= ny; j++)
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 2; i <= nxg - 1; i++)
+                F3(t1, i, j, k) = F3(t2, i, j, k) * (F3(*V, i, j, k) - F3(*V, i, j - 1, k));
+    NU_ADD(2.0, t1, 4);
+    for (int k = 2; k <= nzg; k++)
+        for (int j = 1; j <= nyg; j++)
+            for (int i = 1; i <= nx; i++) F3(t0, i, j, k) = F3(*U, i, j, k) - F3(*U, i, j, k - 1);
+    interp_sec(0, &t0, SEC(1, nx, 1, nyg, 2, nzg), &t1, SEC(2, nx, 1, nyg, 2, nzg));
+    for (int k = 2; k <= nzg; k++)
+        for (int j = 1; j <= ny; j++)
+            for (int i = 1; i <= nxg; i++) F3(t0, i, j, k) = F3(*V, i, j, k) - F3(*V, i, j, k - 1);
+    interp_sec(1, &t0, SEC(1, nxg, 1, ny, 2, nzg), &t2, SEC(1, nxg, 2, ny, 2, nzg));
+    WHOLE(F3(t3, i, j, k) = F3(t1, i, j, k) * F3(t2, i, j, k));
+    interp_sec(2, &t3, SEC(2, nxg - 1, 2, nyg - 1, 2, nzg), &t1, SEC(2, nxg - 1, 2, nyg - 1, 2, nzg - 1));
+    NU_ADD(2.0, t1, 4);
+
+    /* 2 (d_hat_i U)(d_hat_i W) S13: subgrid.f90:802-833 */
+    for (int i = 2; i <= nxg; i++)
+        for (int k = 1; k <= nz; k++)
+            for (int j = 1; j <= nyg; j++) F3(t0, i, j, k) = F3(*W, i, j, k) - F3(*W, i - 1, j, k);
+    interp_sec(2, &t0, SEC(2, nxg, 1, nyg, 1, nz), &t1, SEC(2, nxg, 1, nyg, 2, nz));
+    interp_sec(0, &t1, SEC(2, nxg, 1, nyg, 2, nz), &t2, SEC(2, nxg - 1, 1, nyg, 2, nz));
+    for (int i = 2; i <= nx; i++)
+        for (int k = 1; k <= nzg; k++)
+            for (int j = 2; j <= nyg - 1; j++)
+                F3(t1, i, j, k) = F3(t2, i, j, k) * (F3(*U, i, j, k) - F3(*U, i - 1, j, k));
+    NU_ADD(2.0, t1, 5);
+    for (int k = 2; k <= nzg; k++)
+        for (int j = 1; j <= nyg; j++)
+            for (int i = 1; i <= nx; i++) F3(t0, i, j, k) = F3(*U, i, j, k) - F3(*U, i, j, k - 1);
+    interp_sec(0, &t0, SEC(1, nx, 1, nyg, 2, nzg), &t1, SEC(2, nx, 1, nyg, 2, nzg));
+    interp_sec(2, &t1, SEC(2, nx, 1, nyg, 2, nzg), &t2, SEC(2, nx, 1, nyg, 2, nzg - 1));
+    for (int k = 2; k <= nz; k++)
+        for (int j = 1; j <= nyg; j++)
+            for (int i = 2; i <= nxg - 1; i++)
+                F3(t1, i, j, k) = F3(t2, i, j, k) * (F3(*W, i, j, k) - F3(*W, i, j, k - 1));
+    NU_ADD(2.0, t1, 5);
+    for (int j = 2; j <= nyg; j++)
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 1; i <= nx; i++) F3(t0, i, j, k) = F3(*U, i, j, k) - F3(*U, i, j - 1, k);
+    interp_sec(0, &t0, SEC(1, nx, 2, nyg, 1, nzg), &t1, SEC(2, nx, 2, nyg, 1, nzg));
+    for (int j = 2; j <= nyg; j++)
+        for (int k = 1; k <= nz; k++)
+            for (int i = 1; i <= nxg; i++) F3(t0, i, j, k) = F3(*W, i, j, k) - F3(*W, i, j - 1, k);
+    interp_sec(2, &t0, SEC(1, nxg, 2, nyg, 1, nz), &t2, SEC(1, nxg, 2, nyg, 2, nz));
+    WHOLE(F3(t3, i, j, k) = F3(t1, i, j, k) * F3(t2, i, j, k));
+    interp_sec(1, &t3, SEC(2, nxg - 1, 2, nyg, 2, nzg - 1), &t1, SEC(2, nxg - 1, 2, nyg - 1, 2, nzg - 1));
+    NU_ADD(2.0, t1, 5);
+
+    /* 2 (d_hat_i V)(d_hat_i W) S23: subgrid.f90:835-866 */
+    for (int j = 2; j <= nyg; j++)
+        for (int k = 1; k <= nz; k++)
+            for (int i = 1; i <= nxg; i++) F3(t0, i, j, k) = F3(*W, i, j, k) - F3(*W, i, j - 1, k);
+    interp_sec(2, &t0, SEC(1, nxg, 2, nyg, 1, nz), &t1, SEC(1, nxg, 2, nyg, 2, nz));
+    interp_sec(1, &t1, SEC(1, nxg, 2, nyg, 2, nz), &t2, SEC(1, nxg, 2, nyg - 1, 2, nz));
+    for (int j = 2; j <= ny; j++)
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 2; i <= nxg - 1; i++)
+                F3(t1, i, j, k) = F3(t2, i, j, k) * (F3(*V, i, j, k) - F3(*V, i, j - 1, k));
+    NU_ADD(2.0, t1, 6);
+    for (int k = 2; k <= nzg; k++)
+        for (int j = 1; j <= ny; j++)
+            for (int i = 1; i <= nxg; i++) F3(t0, i, j, k) = F3(*V, i, j, k) - F3(*V, i, j, k - 1);
+    interp_sec(1, &t0, SEC(1, nxg, 1, ny, 2, nzg), &t1, SEC(1, nxg, 2, ny, 2, nzg));
+    interp_sec(2, &t1, SEC(1, nxg, 2, ny, 2, nzg), &t2, SEC(1, nxg, 2, ny, 2, nzg - 1));
+    for (int k = 2; k <= nz; k++)
+        for (int j = 2; j <= nyg - 1; j++)
+            for (int i = 1; i <= nxg; i++)
+                F3(t1, i, j, k) = F3(t2, i, j, k) * (F3(*W, i, j, k) - F3(*W, i, j, k - 1));
+    NU_ADD(2.0, t1, 6);
+    for (int i = 2; i <= nxg; i++)
+        for (int k = 1; k <= nzg; k++)
+            for (int j = 1; j <= ny; j++) F3(t0, i, j, k) = F3(*V, i, j, k) - F3(*V, i - 1, j, k);
+    interp_sec(1, &t0, SEC(2, nxg, 1, ny, 1, nzg), &t1, SEC(2, nxg, 2, ny, 1, nzg));
+    for (int i = 2; i <= nxg; i++)
+        for (int k = 1; k <= nz; k++)
+            for (int j = 1; j <= nyg; j++) F3(t0, i, j, k) = F3(*W, i, j, k) - F3(*W, i - 1, j, k);
+    interp_sec(2, &t0, SEC(2, nxg, 1, nyg, 1, nz), &t2, SEC(2, nxg, 1, nyg, 2, nz));
+    WHOLE(F3(t3, i, j, k) = F3(t1, i, j, k) * F3(t2, i, j, k));
+    interp_sec(0, &t3, SEC(2, nxg, 2, nyg - 1, 2, nzg - 1), &t1, SEC(2, nxg - 1, 2, nyg - 1, 2, nzg - 1));
+    NU_ADD(2.0, t1, 6);
+#undef NU_ADD
+#undef NU_ADD1
+#undef WHOLE
+
+    /* quotient and clipping (NaN -> 0), subgrid.f90:868-871 */
+    int nan_can = 0;
+    for (int k = 1; k <= nzg; k++)
+        for (int j = 1; j <= nyg; j++)
+            for (int i = 1; i <= nxg; i++) {
+                double v = -C * F3(*nt, i, j, k) / F3(t4, i, j, k);
+                if (v != v && i >= 2 && i <= nxg - 2 && j >= 2 && j <= nyg - 1 && k >= 2 && k <= nzg - 2) nan_can++;
+                F3(*nt, i, j, k) = v > 0.0 ? v : 0.0;
+            }
+    o->amd_nan_canonical = nan_can;
+    /* subgrid.f90:873-876 (one slab: the interior-plane update is the wrap) */
+    periodic_x(nt, 2, nx, nxg, 1);
+    periodic_z(nt, 4, nz, nzg, 1);
+    if (o->p.Dirichlet_nu_t == 1) {
+        dirichlet_y(nt, 2, ny, nyg);
+    } else if (o->p.Dirichlet_nu_t == 0) {
+        neumann_y(nt, 2, ny, nyg);
+    } else if (o->p.Dirichlet_nu_t == 2) {
+        double g = 2.0 * 0.38 * pow(o->dPdx, 0.5) * (y[2] - y[1]) / 2.0;
+        for (int k = 1; k <= nzg; k++)
+            for (int i = 1; i <= nxg; i++) {
+                F3(*nt, i, 1, k) = -F3(*nt, i, 2, k) + g;
+                F3(*nt, i, nyg, k) = -F3(*nt, i, nyg - 1, k) + g;
+            }
+    }
+    /* subgrid.f90:877-879: rows 1 and nyg of avg_nu_t are left as they were */
+    for (int j = 2; j <= nyg - 1; j++) {
+        double s = 0.0;
+        for (int k = 2; k <= nzg - 2; k++)
+            for (int i = 2; i <= nxg - 2; i++) s += F3(*nt, i, j, k);
+        F3(o->avg_nu_t, 1, j, 1) = s / (double)((nxg - 3) * (nzg - 3));
+    }
+    for (int q = 0; q < 5; q++) fa_free(tt[q]);
+}
+#undef AMD_LOOP
+
 void cfo_compute_eddy_viscosity(cfo *o) {
     /* subgrid.f90:23-47 */
     if (o->p.LES_model == 2) {
         sgs_dynamic_smagorinsky(o);
+    } else if (o->p.LES_model == 3) {
+        sgs_amd(o);
     } else if (o->p.LES_model == 0) {
         for (size_t q = 0; q < fa_size(&o->nu_t); q++) o->nu_t.p[q] = 0.0;
         for (size_t q = 0; q < fa_size(&o->avg_nu_t); q++) o->avg_nu_t.p[q] = 0.0;

@@ -112,3 +112,16 @@ def test_statistics_text_file_known_answer(tmp_path):
     assert got == want
     assert cf.statistics_file_name("  run/out  ", 200, 1000) == "run/out.1200.stats.txt"
     assert cf.statistics_file_name("o", 123456789, 0) == "o.********.stats.txt"
+
+
+def test_create_rejects_unsupported_models_without_gpu_work():
+    """LES_model 1 (constant Smagorinsky) and an AMD wall rule other than
+    0, 1, 2 are refused before any device work."""
+    import pytest
+    import channelflow as cf
+    from channelflow import grids
+    x, y, z = grids.channel_grid(10, 9, 8)
+    with pytest.raises(cf.CfError, match="LES_model must be"):
+        cf.Channel(x, y, z, LES_model=1)
+    with pytest.raises(cf.CfError, match="Dirichlet_nu_t must be"):
+        cf.Channel(x, y, z, LES_model=3, Dirichlet_nu_t=3)

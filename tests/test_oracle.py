@@ -284,3 +284,124 @@ def test_pressure_solves_discrete_poisson(check):
     assert np.array_equal(P[nxg - 2], P[1])
     assert np.array_equal(P[1:nxg - 1, :, nzg - 2], P[1:nxg - 1, :, 1])
     assert abs(P[1:-1, 0, 1:-1] - P[1:-1, 1, 1:-1]).max() > 1e-6 * abs(P).max()
+
+
+def amd_point_formula(o, U, V, W):
+    """sgs_AMD (subgrid.f90:639-871) at the canonical cells as one formula per
+    cell: the reference's section operations (interpolate_x/y/z of squared or
+    plain differences of partly set temporaries) reduced by hand to the cell's
+    3x3x3 neighbourhood.  Returns (-C num/den clipped, den)."""
+    nxg, nyg, nzg = U.shape[0] + 1, U.shape[1], U.shape[2]
+    P = lambda a: np.r_[np.nan, a]  # 1-based coordinates
+    x, y, z, xg, yg, zg = (P(o.array(n)) for n in ("x", "y", "z", "xg", "yg", "zg"))
+    i = np.arange(2, nxg - 1)[:, None, None]
+    j = np.arange(2, nyg)[None, :, None]
+    k = np.arange(2, nzg - 1)[None, None, :]
+    F = lambda a, di=0, dj=0, dk=0: a[1 + di:nxg - 2 + di, 1 + dj:nyg - 1 + dj, 1 + dk:nzg - 2 + dk]
+    h = 0.5
+    s11 = (F(U) - F(U, -1)) / (x[i] - x[i - 1])
+    s22 = (F(V) - F(V, 0, -1)) / (y[j] - y[j - 1])
+    s33 = (F(W) - F(W, 0, 0, -1)) / (z[k] - z[k - 1])
+    e4 = lambda a, b: h * ((F(U, a - 1, b) - F(U, a - 1, b - 1)) / (yg[j + b] - yg[j + b - 1]) +
+                           (F(V, a, b - 1) - F(V, a - 1, b - 1)) / (xg[i + a] - xg[i + a - 1]))
+    e5 = lambda a, b: h * ((F(U, a - 1, 0, b) - F(U, a - 1, 0, b - 1)) / (zg[k + b] - zg[k + b - 1]) +
+                           (F(W, a, 0, b - 1) - F(W, a - 1, 0, b - 1)) / (xg[i + a] - xg[i + a - 1]))
+    e6 = lambda a, b: h * ((F(V, 0, a - 1, b) - F(V, 0, a - 1, b - 1)) / (zg[k + b] - zg[k + b - 1]) +
+                           (F(W, 0, a, b - 1) - F(W, 0, a - 1, b - 1)) / (yg[j + a] - yg[j + a - 1]))
+    s12 = 0.25 * (e4(0, 0) + e4(1, 0) + e4(0, 1) + e4(1, 1))
+    s13 = 0.25 * (e5(0, 0) + e5(1, 0) + e5(0, 1) + e5(1, 1))
+    s23 = 0.25 * (e6(0, 0) + e6(1, 0) + e6(0, 1) + e6(1, 1))
+    # differences: dU_y(a, b) = U(i+a, j+b) - U(i+a, j+b-1) etc.
+    dUx = lambda a=0, b=0, c=0: F(U, a, b, c) - F(U, a - 1, b, c)
+    dUy = lambda a=0, b=0, c=0: F(U, a, b, c) - F(U, a, b - 1, c)
+    dUz = lambda a=0, b=0, c=0: F(U, a, b, c) - F(U, a, b, c - 1)
+    dVx = lambda a=0, b=0, c=0: F(V, a, b, c) - F(V, a - 1, b, c)
+    dVy = lambda a=0, b=0, c=0: F(V, a, b, c) - F(V, a, b - 1, c)
+    dVz = lambda a=0, b=0, c=0: F(V, a, b, c) - F(V, a, b, c - 1)
+    dWx = lambda a=0, b=0, c=0: F(W, a, b, c) - F(W, a - 1, b, c)
+    dWy = lambda a=0, b=0, c=0: F(W, a, b, c) - F(W, a, b - 1, c)
+    dWz = lambda a=0, b=0, c=0: F(W, a, b, c) - F(W, a, b, c - 1)
+    av = lambda p, q: h * (p + q)
+    # U: faces i-1, i; y faces j, j+1 / z faces k, k+1
+    uy = lambda f: av(av(f(-1, 0, 0), f(0, 0, 0)), av(f(-1, 1, 0), f(0, 1, 0)))
+    uz = lambda f: av(av(f(-1, 0, 0), f(0, 0, 0)), av(f(-1, 0, 1), f(0, 0, 1)))
+    # V: x faces i, i+1 with y rows j-1, j (y first) / z faces k, k+1 (y first)
+    vx = lambda f: av(av(f(0, -1, 0), f(0, 0, 0)), av(f(1, -1, 0), f(1, 0, 0)))
+    vz = lambda f: av(av(f(0, -1, 0), f(0, 0, 0)), av(f(0, -1, 1), f(0, 0, 1)))
+    # W: x faces i, i+1 with z rows k-1, k (z first) / y faces j, j+1 (z first)
+    wx = lambda f: av(av(f(0, 0, -1), f(0, 0, 0)), av(f(1, 0, -1), f(1, 0, 0)))
+    wy = lambda f: av(av(f(0, 0, -1), f(0, 0, 0)), av(f(0, 1, -1), f(0, 1, 0)))
+    sq = lambda d: (lambda a, b, c: d(a, b, c) ** 2)
+    dyg = lambda b: yg[j + b] - yg[j + b - 1]
+    dzg = lambda c: zg[k + c] - zg[k + c - 1]
+    dxg = lambda a: xg[i + a] - xg[i + a - 1]
+    den = dUx() ** 2 / (x[i] - x[i - 1]) ** 2
+    den = den + uy(lambda a, b, c: dUy(a, b, c) ** 2 / dyg(b) ** 2)
+    den = den + uz(lambda a, b, c: dUz(a, b, c) ** 2 / dzg(c) ** 2)
+    den = den + dVy() ** 2 / (y[j] - y[j - 1]) ** 2
+    den = den + vx(lambda a, b, c: dVx(a, b, c) ** 2 / dxg(a) ** 2)
+    den = den + vz(lambda a, b, c: dVz(a, b, c) ** 2 / dzg(c) ** 2)
+    den = den + dWz() ** 2 / (z[k] - z[k - 1]) ** 2
+    den = den + wx(lambda a, b, c: dWx(a, b, c) ** 2 / dxg(a) ** 2)
+    den = den + wy(lambda a, b, c: dWy(a, b, c) ** 2 / dyg(b) ** 2)
+    num = dUx() ** 2 * s11
+    num = num + uy(sq(dUy)) * s11
+    num = num + uz(sq(dUz)) * s11
+    num = num + dVy() ** 2 * s22
+    num = num + vx(sq(dVx)) * s22
+    num = num + vz(sq(dVz)) * s22
+    num = num + dWz() ** 2 * s33
+    num = num + wx(sq(dWx)) * s33
+    num = num + wy(sq(dWy)) * s33
+    num = num + 2.0 * (av(av(dVx(0, -1), dVx()), av(dVx(1, -1), dVx(1))) * dUx()) * s12
+    num = num + 2.0 * (av(av(dUy(-1), dUy()), av(dUy(-1, 1), dUy(0, 1))) * dVy()) * s12
+    num = num + 2.0 * av(av(dUz(-1), dUz()) * av(dVz(0, -1), dVz()), av(dUz(-1, 0, 1), dUz(0, 0, 1)) *
+                         av(dVz(0, -1, 1), dVz(0, 0, 1))) * s12
+    num = num + 2.0 * (av(av(dWx(0, 0, -1), dWx()), av(dWx(1, 0, -1), dWx(1))) * dUx()) * s13
+    num = num + 2.0 * (av(av(dUz(-1), dUz()), av(dUz(-1, 0, 1), dUz(0, 0, 1))) * dWz()) * s13
+    num = num + 2.0 * av(av(dUy(-1), dUy()) * av(dWy(0, 0, -1), dWy()), av(dUy(-1, 1), dUy(0, 1)) *
+                         av(dWy(0, 1, -1), dWy(0, 1))) * s13
+    num = num + 2.0 * (av(av(dWy(0, 0, -1), dWy()), av(dWy(0, 1, -1), dWy(0, 1))) * dVy()) * s23
+    num = num + 2.0 * (av(av(dVz(0, -1), dVz()), av(dVz(0, -1, 1), dVz(0, 0, 1))) * dWz()) * s23
+    num = num + 2.0 * av(av(dVx(0, -1), dVx()) * av(dWx(0, 0, -1), dWx()), av(dVx(1, -1), dVx(1)) *
+                         av(dWx(1, 0, -1), dWx(1))) * s23
+    with np.errstate(invalid="ignore", divide="ignore"):
+        v = -0.3 * num / den
+    return np.where(v > 0, v, 0.0), den
+
+
+@pytest.mark.parametrize("check,dirichlet", [(True, 0), (False, 1), (False, 2)])
+def test_amd_matches_point_formula(check, dirichlet):
+    """The oracle's sgs_AMD (section operations of subgrid.f90:639-881 on
+    NaN-filled temporaries) against the per-cell formula: the canonical cells
+    agree to round-off and take nothing from an unset temporary; ghosts
+    follow the periodic copies and the wall rule; avg_nu_t is the canonical
+    plane mean; the model is Galilean invariant away from the walls."""
+    from oracle import Oracle
+    nx, ny, nz = 18, 17, 14
+    case = channel_case(nx, ny, nz, stretch=1.5, les=3)
+    case["prm"]["Dirichlet_nu_t"] = dirichlet
+    o = Oracle(case["x"], case["y"], case["z"], case["prm"], check=check)
+    o.set_fields(case["U"], case["V"], case["W"])
+    o.apply_boundary_conditions()
+    o.compute_eddy_viscosity()
+    assert o.scalar("amd_nan_canonical") == 0
+    f = o.fields()
+    nt = o.array("nu_t")
+    want, den = amd_point_formula(o, f["U"], f["V"], f["W"])
+    assert (den > 0).all()
+    can = nt[1:nx - 1, 1:ny, 1:nz - 1]
+    assert abs(can - want).max() <= 1e-14 * abs(want).max()
+    assert (want > 0).any() and (want == 0).any()
+    nxg, nyg, nzg = nx + 1, ny + 1, nz + 1
+    assert np.array_equal(nt[0], nt[nxg - 3]) and np.array_equal(nt[nxg - 2], nt[1]) and np.array_equal(nt[nxg - 1], nt[2])
+    assert np.array_equal(nt[:, 1:-1, 0], nt[:, 1:-1, nzg - 3]) and np.array_equal(nt[:, 1:-1, nzg - 2], nt[:, 1:-1, 1])
+    g = 2 * 0.38 * o.scalar("dPdx") ** 0.5 * (case["y"][1] - case["y"][0]) / 2 if dirichlet == 2 else 0.0
+    sgn = 1.0 if dirichlet == 0 else -1.0
+    assert abs(nt[:, 0, :] - (sgn * nt[:, 1, :] + g)).max() <= 1e-15
+    avg = o.array("avg_nu_t").ravel()
+    assert abs(avg[1:-1] - can.mean(axis=(0, 2))).max() <= 1e-15 * abs(can).max()
+    o.set_fields(f["U"] + 0.7, f["V"], f["W"] - 0.3)
+    o.apply_boundary_conditions()
+    o.compute_eddy_viscosity()
+    assert abs(o.array("nu_t")[:, 2:-2, :] - nt[:, 2:-2, :]).max() <= 1e-12 * abs(nt).max()

@@ -302,3 +302,61 @@ def test_statistics_and_text_file(tmp_path):
     rows = np.array([[float(l[15 * c:15 * (c + 1)]) for c in range(7)] for l in lines[1:-1]])
     want = np.stack([o.array("y")] + [so[q * ny:(q + 1) * ny] for q in (0, 3, 4, 5, 6, 8)], axis=1)
     assert abs(rows - want).max() <= 5.1e-9
+
+
+@pytest.mark.parametrize("which,dirichlet,wall", [("small", 0, 0), ("small", 1, 0), ("small", 2, 0),
+                                                  ("config1", 0, 0), ("small", 0, 3)])
+def test_eddy_viscosity_amd(which, dirichlet, wall):
+    """sgs_AMD (subgrid.f90:639-881): nu_t everywhere (ghosts included) and the
+    plane means avg_nu_t(2..nyg-1) against the oracle."""
+    extra = dict(stretch=0.0, wall=3, retau=2000.0, profile="plug") if wall else {}
+    case = channel_case(*CASES[which], les=3, **extra)
+    case["prm"]["Dirichlet_nu_t"] = dirichlet
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    o.compute_eddy_viscosity(); ch.compute_eddy_viscosity()
+    assert o.scalar("amd_nan_canonical") == 0
+    f, g = o.fields(), ch.download()
+    assert_close(g["nu_t"], f["nu_t"], 1e-12, "nu_t")
+    assert (f["nu_t"] > 0).mean() > 0.2
+    assert_close(ch.avg_nu_t()[1:-1], o.array("avg_nu_t").ravel()[1:-1], 1e-12, "avg_nu_t")
+
+
+@pytest.mark.parametrize("which,wall", [("small", 0), ("config1", 0), ("small", 3)])
+def test_ten_steps_amd(which, wall):
+    """Ten RK3 steps with the AMD model, fast path against the oracle."""
+    extra = dict(stretch=0.0, wall=3, retau=2000.0, profile="plug") if wall else {}
+    case = channel_case(*CASES[which], les=3, **extra)
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    ch.set_fixed_dt(case["dt"])
+    for _ in range(10):
+        o.compute_dt()
+        o.time_step_rk3()
+    ch.time_step_rk3(10)
+    errs = compare_fields(o, ch, 1e-10, names=("U", "V", "W", "P", "nu_t"), what="10 AMD steps")
+    _, dabs = ch.check_divergence()
+    assert dabs <= 1e-10, dabs
+    print(which, wall, errs)
+
+
+def test_amd_split_precision_short_horizon():
+    """AMD in the split (FP32 + compensated state) path against FP64 after ten
+    steps."""
+    import channelflow as cf
+    case = channel_case(*CASES["config1"], les=3)
+    out = []
+    for prec in (cf.PREC_FP64, cf.PREC_SPLIT):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=prec, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        ch.set_fixed_dt(case["dt"])
+        ch.time_step_rk3(10)
+        out.append(ch.download())
+        ch.close()
+    for n in ("U", "V", "W", "nu_t"):
+        e = rel_err(out[1][n], out[0][n])
+        assert e < (1e-4 if n != "nu_t" else 1e-3), (n, e)
