@@ -10,6 +10,7 @@ no CPU fallback: a missing or unloadable library raises immediately.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import os
 import re
 
@@ -33,7 +34,7 @@ class CfParams(C.Structure):
         ("Retau_int", C.c_int), ("x_mass_cte", C.c_int), ("y_mass_cte", C.c_int),
         ("LES_model", C.c_int), ("iwall_model", C.c_int), ("Dirichlet_nu_t", C.c_int), ("jref_eqwm", C.c_int),
         ("precision", C.c_int), ("eqwm_ncv", C.c_int), ("eqwm_stretch", C.c_double), ("sgs_recompute", C.c_int),
-        ("dsm_unfused", C.c_int),
+        ("dsm_unfused", C.c_int), ("cfl_corrected", C.c_int),
     ]
 
 
@@ -99,6 +100,7 @@ def load(build_if_missing: bool = True):
     L.cf_get_stream.argtypes = [vp]
     L.cf_get_stream.restype = vp
     L.cf_compute_statistics.argtypes = [vp, dp]
+    L.cf_output_monitor.argtypes = [vp, dp]
     L.cf_profile_steps.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, dp, ip, ip]
     L.cf_read_input_parameters.argtypes = [C.c_char_p, C.POINTER(CfParams), ip, C.c_char_p, C.c_char_p, ip, ip]
     L.cf_read_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp]
@@ -298,6 +300,61 @@ class Channel:
         path = statistics_file_name(fileout, istep, nstep_init)
         write_statistics(path, self.scalars()["t"], self.params.nu, self.nx, self.ny, self.nz, istep, self.y, stats)
         return path
+
+    def monitor(self) -> dict:
+        """The reductions of output_monitor (monitor.f90:28-52)."""
+        out = np.zeros(9)
+        self._check(self.L.cf_output_monitor(self.h, _dp(out)))
+        keys = ["meanU", "meanV", "meanW", "maxU", "maxV", "maxW", "meanNut", "maxNut", "max_divergence"]
+        return dict(zip(keys, out.tolist()))
+
+    def output_monitor(self, istep: int, retau: float = float("nan"), qflow=(float("nan"), float("nan")),
+                       elapsed: float = float("nan"), file=None) -> dict:
+        """Prints the block of output_monitor (monitor.f90:20-150) for this
+        step; Retau and the mass flows are the last statistics' values, as in
+        the reference.  Returns the reductions."""
+        import sys
+        m = self.monitor()
+        sc = self.scalars()
+        p = self.params
+        f = file or sys.stdout
+        w = lambda label, v: print(f" {label}{v}", file=f)
+        w("step number :", istep)
+        w("time        :", sc["t"])
+        w("time step   :", sc["dt"])
+        print(" ", file=f)
+        w("Retau:      :", retau)
+        print(" ", file=f)
+        w("Maximum U   :", m["maxU"])
+        w("Maximum V   :", m["maxV"])
+        w("Maximum W   :", m["maxW"])
+        w("Mean U      :", m["meanU"])
+        w("Mean V      :", m["meanV"])
+        w("Mean W      :", m["meanW"])
+        if p.LES_model > 0:
+            print(" ", file=f)
+            w("Maximum nu_t: ", m["maxNut"])
+            w("Average nu_t: ", m["meanNut"])
+        print(" ", file=f)
+        w("Mean mass flow in x         :", qflow[0])
+        w("Mean mass flow in y         :", qflow[1])
+        w("Mean pressure gradient in x :", sc["dPdx"])
+        w("Mean pressure gradient in y :", sc["dPdy"])
+        w("Spanwise rotation Omega_z   :", p.Rossby_plus * math.sqrt(p.dPdx) / 2.0)  # input_output.f90:83-84
+        print(" ", file=f)
+        if p.iwall_model == 3:
+            n_nan, n_iter = self.eqwm_counters()
+            w("Wall model     : ", "Equilibrium wall model (Larsson)")
+            w("      jref     : ", p.jref_eqwm)
+            w("      NaN eqwm : ", n_nan)
+            w("      Max iter : ", n_iter)
+        else:
+            w("No wall model", "")
+        print(" ", file=f)
+        w("Maximum divergence          :", m["max_divergence"])
+        w("Elapsed time (s)            :", elapsed)
+        w("------------------------------------------------------", "")
+        return m
 
     # ------------------------------------------------------------ fast path
     def time_step_rk3(self, nsteps: int = 1, sync: bool = True):

@@ -521,7 +521,9 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     ctx->red_n = std::max({ctx->nzg + 8, ctx->nxg + ctx->nyg + ctx->nzg + 16, (ctx->nzg - 2) * cdiv(ctx->nyg - 2, 16) + 16});
     CF_CUDA(cudaMalloc(&ctx->d_red, (size_t)ctx->red_n * sizeof(double)));
     {
-        std::vector<double> inf((size_t)ctx->nxg + ctx->nyg + ctx->nzg + 6, INFINITY);
+        // per-index extrema of |u| for compute_dt: minima start at +inf,
+        // the maxima of the corrected rule at 0
+        std::vector<double> inf((size_t)ctx->nxg + ctx->nyg + ctx->nzg + 6, p->cfl_corrected ? 0.0 : INFINITY);
         CF_CUDA(cudaMalloc(&ctx->d_dtmin, inf.size() * sizeof(double)));
         CF_CUDA(cudaMemcpy(ctx->d_dtmin, inf.data(), inf.size() * sizeof(double), cudaMemcpyHostToDevice));
     }
@@ -987,7 +989,7 @@ static int enqueue_step(cf_ctx *ctx) {
     const int X = ctx->cur;
     const int a = (X + 1) % 3, b = (X + 2) % 3;
     ctx->old = X;
-    TRY(launch_dt<T>(ctx, X));  // main.f90:71
+    TRY(launch_dt<T>(ctx, X, true));  // main.f90:71; t = to + dt of the step
     // substep 1 (time_integration.f90:100-115)
     TRY(eddy(ctx, X));
     if (ctx->prm.iwall_model == 3) {
@@ -1083,6 +1085,42 @@ extern "C" int cf_synchronize(cf_ctx *ctx) {
 
 extern "C" void *cf_get_stream(cf_ctx *ctx) { return ctx ? (void *)ctx->st : nullptr; }
 extern "C" int cf_launches_per_step(cf_ctx *ctx) { return ctx ? ctx->step_launches : 0; }
+
+extern "C" int cf_output_monitor(cf_ctx *ctx, double *out) {
+    // monitor.f90:28-52 with the reference's normalisations
+    if (!ctx || !out) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    const int np = ctx->nzg - 2;
+    double *d;
+    CF_CUDA(cudaMalloc(&d, (size_t)8 * np * sizeof(double)));
+    int rc = DISPATCH(launch_monitor<double>(ctx, ctx->cur, d), launch_monitor<float>(ctx, ctx->cur, d));
+    if (rc) { cudaFree(d); return rc; }
+    std::vector<double> r((size_t)8 * np);
+    cudaError_t e = cudaMemcpyAsync(r.data(), d, r.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->st);
+    cudaFree(d);
+    if (e != cudaSuccess) return cf_fail(ctx, CF_ERR_CUDA, std::string("monitor: ") + cudaGetErrorString(e));
+    double sum[4] = {0, 0, 0, 0}, mx[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    for (int k = 0; k < np; k++)
+        for (int q = 0; q < 4; q++) {
+            sum[q] += r[(size_t)8 * k + q];
+            mx[q] = std::max(mx[q], r[(size_t)8 * k + 4 + q]);
+        }
+    const double cells = (double)(ctx->nx - 1) * (ctx->ny - 1) * (ctx->nz - 1);  // nxm nym nzm (monitor.f90:74-76)
+    const double all = (double)ctx->nxg * ctx->nyg * ctx->nzg;                   // nxg nyg nzg (monitor.f90:81)
+    out[0] = sum[0] / cells;
+    out[1] = sum[1] / cells;
+    out[2] = sum[2] / cells;
+    out[3] = mx[0];
+    out[4] = mx[1];
+    out[5] = mx[2];
+    out[6] = sum[3] / all;
+    out[7] = mx[3];
+    double dmax = 0.0;
+    TRY(cf_check_divergence(ctx, &dmax, nullptr));
+    out[8] = dmax;
+    return CF_OK;
+}
 
 extern "C" int cf_compute_statistics(cf_ctx *ctx, double *out) {
     // statistics.f90:43-159 with the reference's normalisations

@@ -264,10 +264,11 @@ template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only
 template <typename T> int launch_mass_apply(cf_ctx *ctx, int buf, int mode, bool ghosts = false); // add ds->lmax[2], dPdx = it/dt (ghosts: whole array, as the BCs would)
-template <typename T> int launch_dt(cf_ctx *ctx, int buf);
+template <typename T> int launch_dt(cf_ctx *ctx, int buf, bool advance_t = false);  // advance_t: t += dt (fast path)
 template <typename T> int launch_eqwm(cf_ctx *ctx, int buf);
 template <typename T> int launch_copy_state(cf_ctx *ctx, int src, int dst);
 template <typename T> int launch_stats(cf_ctx *ctx, int buf, double *d_out);
+template <typename T> int launch_monitor(cf_ctx *ctx, int buf, double *d_out);  // (nzg-2) x 8 plane partials
 
 // Called after every kernel launch.  Counts launches while a step is being
 // captured, and in a profiling pass records an event after each launch: on

@@ -1034,8 +1034,13 @@ __device__ __forceinline__ void atomic_min_pos(double *a, double v) {
     // non-negative doubles order like their bit patterns
     atomicMin((unsigned long long *)a, (unsigned long long)__double_as_longlong(v));
 }
+__device__ __forceinline__ void atomic_max_pos(double *a, double v) {
+    atomicMax((unsigned long long *)a, (unsigned long long)__double_as_longlong(v));
+}
 
-template <typename T>
+// CORR: the corrected convective limit of cf_params.cfl_corrected, which
+// needs the maxima of |u| per index instead (same blocks and atomics)
+template <typename T, bool CORR>
 __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, double *mu,
                                                 double *mv, double *mw) {
     // block (x: 256 x indices, y: JR rows, z: KR planes), thread = x index i:
@@ -1048,14 +1053,16 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
     __shared__ T wsm[8][KR];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
     const int i = 2 + blockIdx.x * 256 + threadIdx.x, j0 = 2 + blockIdx.y * JR, k0 = 2 + blockIdx.z * KR;
-    T umin = T(INFINITY);
+    const T init = CORR ? T(0) : T(INFINITY);
+    auto ext = [](T a, T b) { return CORR ? fmax(a, b) : fmin(a, b); };
+    T umin = init;
     T vmin[JR];
 #pragma unroll
-    for (int r = 0; r < JR; r++) vmin[r] = T(INFINITY);
+    for (int r = 0; r < JR; r++) vmin[r] = init;
 #pragma unroll
     for (int kk = 0; kk < KR; kk++) {
         const int k = k0 + kk;
-        T wmin = T(INFINITY);
+        T wmin = init;
         if (k <= nzg - 1 && i <= nxg - 1) {
             T u[JR], v[JR], w[JR];
 #pragma unroll
@@ -1067,36 +1074,40 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
             }
 #pragma unroll
             for (int r = 0; r < JR; r++) {
-                umin = fmin(umin, fabs(u[r]));
-                vmin[r] = fmin(vmin[r], fabs(v[r]));
-                wmin = fmin(wmin, fabs(w[r]));
+                umin = ext(umin, fabs(u[r]));
+                vmin[r] = ext(vmin[r], fabs(v[r]));
+                wmin = ext(wmin, fabs(w[r]));
             }
         }
-        for (int o = 16; o > 0; o >>= 1) wmin = fmin(wmin, __shfl_down_sync(0xffffffff, wmin, o));
+        for (int o = 16; o > 0; o >>= 1) wmin = ext(wmin, __shfl_down_sync(0xffffffff, wmin, o));
         if (lane == 0) wsm[wp][kk] = wmin;
     }
 #pragma unroll
     for (int r = 0; r < JR; r++) {
         T v = vmin[r];
-        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_down_sync(0xffffffff, v, o));
+        for (int o = 16; o > 0; o >>= 1) v = ext(v, __shfl_down_sync(0xffffffff, v, o));
         if (lane == 0) vsm[wp][r] = v;
     }
-    if (i <= nxg - 1) atomic_min_pos(&mu[i], (double)umin);
+    auto put = [](double *a, double v) {
+        if (CORR) atomic_max_pos(a, v);
+        else atomic_min_pos(a, v);
+    };
+    if (i <= nxg - 1) put(&mu[i], (double)umin);
     __syncthreads();
     const int nw = blockDim.x >> 5;
     if (threadIdx.x < JR) {
         const int j = j0 + threadIdx.x;
         if (j <= nyg - 1) {
             T m = vsm[0][threadIdx.x];
-            for (int q = 1; q < nw; q++) m = fmin(m, vsm[q][threadIdx.x]);
-            atomic_min_pos(&mv[j], (double)m);
+            for (int q = 1; q < nw; q++) m = ext(m, vsm[q][threadIdx.x]);
+            put(&mv[j], (double)m);
         }
     } else if (threadIdx.x >= 32 && threadIdx.x < 32 + KR) {
         const int kk = threadIdx.x - 32, k = k0 + kk;
         if (k <= nzg - 1) {
             T m = wsm[0][kk];
-            for (int q = 1; q < nw; q++) m = fmin(m, wsm[q][kk]);
-            atomic_min_pos(&mw[k], (double)m);
+            for (int q = 1; q < nw; q++) m = ext(m, wsm[q][kk]);
+            put(&mw[k], (double)m);
         }
     }
 }
@@ -1104,37 +1115,41 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
 
 // The maxima dx/min|u| per direction (one quotient per thread: FP64
 // divisions are slow here, so they run side by side), dt, and the minima
-// reset to +inf for the next call.
+// reset to +inf for the next call.  corr: the minima dx/max|u| instead, the
+// maxima reset to 0.
 __global__ void __launch_bounds__(1024) k_dt_final(double *mu, double *mv, double *mw, Geo g, DevScal *ds, double CFL,
-                                                   double dt_vis) {
+                                                   double dt_vis, int corr, int advance_t) {
     __shared__ double sh[3][32];
     const int nxi = g.nxg - 2, nyi = g.nyg - 2, nzi = g.nzg - 2;
-    double l[3] = {0.0, 0.0, 0.0};
+    const double init = corr ? INFINITY : 0.0;
+    auto ext = [corr](double a, double b) { return corr ? fmin(a, b) : fmax(a, b); };
+    double l[3] = {init, init, init};
     for (int t = threadIdx.x; t < nxi + nyi + nzi; t += blockDim.x) {
         if (t < nxi) {
             const int i = t + 2;
-            l[0] = fmax(l[0], (g.xg[i + 1] - g.xg[i]) / mu[i]);
+            l[0] = ext(l[0], (g.xg[i + 1] - g.xg[i]) / mu[i]);
         } else if (t < nxi + nyi) {
             const int j = t - nxi + 2;
-            l[1] = fmax(l[1], (g.yg[j + 1] - g.yg[j]) / mv[j]);
+            l[1] = ext(l[1], (g.yg[j + 1] - g.yg[j]) / mv[j]);
         } else {
             const int k = t - nxi - nyi + 2;
-            l[2] = fmax(l[2], (g.zg[k + 1] - g.zg[k]) / mw[k]);
+            l[2] = ext(l[2], (g.zg[k + 1] - g.zg[k]) / mw[k]);
         }
     }
 #pragma unroll
     for (int d = 0; d < 3; d++)
-        for (int o = 16; o > 0; o >>= 1) l[d] = fmax(l[d], __shfl_down_sync(0xffffffff, l[d], o));
+        for (int o = 16; o > 0; o >>= 1) l[d] = ext(l[d], __shfl_down_sync(0xffffffff, l[d], o));
     const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
     if ((threadIdx.x & 31) == 0) { sh[0][w] = l[0]; sh[1][w] = l[1]; sh[2][w] = l[2]; }
     __syncthreads();
-    for (int t = threadIdx.x; t < g.nxg + 2; t += blockDim.x) mu[t] = INFINITY;
-    for (int t = threadIdx.x; t < g.nyg + 2; t += blockDim.x) mv[t] = INFINITY;
-    for (int t = threadIdx.x; t < g.nzg + 2; t += blockDim.x) mw[t] = INFINITY;
+    const double reset = corr ? 0.0 : INFINITY;
+    for (int t = threadIdx.x; t < g.nxg + 2; t += blockDim.x) mu[t] = reset;
+    for (int t = threadIdx.x; t < g.nyg + 2; t += blockDim.x) mv[t] = reset;
+    for (int t = threadIdx.x; t < g.nzg + 2; t += blockDim.x) mw[t] = reset;
     if (threadIdx.x != 0) return;
     double lU = sh[0][0], lV = sh[1][0], lW = sh[2][0];
     for (int q = 1; q < nw; q++) {
-        lU = fmax(lU, sh[0][q]); lV = fmax(lV, sh[1][q]); lW = fmax(lW, sh[2][q]);
+        lU = ext(lU, sh[0][q]); lV = ext(lV, sh[1][q]); lW = ext(lW, sh[2][q]);
     }
     double du = CFL * lU, dv = CFL * lV, dw = CFL * lW;
     double dt_conv = fmin(du, fmin(dv, dw));
@@ -1144,23 +1159,29 @@ __global__ void __launch_bounds__(1024) k_dt_final(double *mu, double *mv, doubl
     if (ds->fixed_dt > 0) dt = ds->fixed_dt;
     ds->dt = dt;
     ds->dtf = (float)dt;
+    // the step's t = to + rk_t(3) dt, rk_t(3) = 1 (time_integration.f90:146);
+    // nothing in the step reads t
+    if (advance_t) ds->t = ds->t + dt;
     ds->lmax[0] = lU;
     ds->lmax[1] = lV;
 }
 
 template <typename T>
-int launch_dt(cf_ctx *ctx, int b) {
+int launch_dt(cf_ctx *ctx, int b, bool advance_t) {
     // minima start at +inf: set at context creation and reset by k_dt_final
     double *mu = ctx->d_dtmin, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
-    k_dt_min<T><<<dim3(cdiv(ctx->nxg - 2, 256), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2)), 256, 0, ctx->st>>>(
-        make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
-        make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg), ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
+    const dim3 grd(cdiv(ctx->nxg - 2, 256), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2));
+    const Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
+                 W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    if (ctx->prm.cfl_corrected) k_dt_min<T, true><<<grd, 256, 0, ctx->st>>>(U, V, W, ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
+    else k_dt_min<T, false><<<grd, 256, 0, ctx->st>>>(U, V, W, ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
     count_launch(ctx, "k_dt_min");
     double CFL = ctx->prm.CFL;
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
            vw = CFL * pow(ctx->dzmin, 2.0) / ctx->prm.nu;
     double dt_vis = fmin(vu, fmin(vv, vw));
-    k_dt_final<<<1, 1024, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis);
+    k_dt_final<<<1, 1024, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis, ctx->prm.cfl_corrected ? 1 : 0,
+                                        advance_t ? 1 : 0);
     count_launch(ctx, "k_dt_final");
     CF_CUDA(cudaGetLastError());
     return 0;
@@ -1169,9 +1190,6 @@ int launch_dt(cf_ctx *ctx, int b) {
 // ---------------------------------------------------------------------------
 // check_divergence, projection.f90:234-256 (signed max from 0, and max |div|)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void atomic_max_pos(double *a, double v) {
-    atomicMax((unsigned long long *)a, (unsigned long long)__double_as_longlong(v));
-}
 
 template <typename T>
 __global__ void k_div(Fld<T> U, Fld<T> V, Fld<T> W, Geo g, double *out) {
@@ -1242,7 +1260,7 @@ int check_bc(cf_ctx *ctx, int b, bool *ok) {
     template int launch_mass_flow<T>(cf_ctx *, int, int, bool);      \
     template int launch_mass_value<T>(cf_ctx *, int, int);           \
     template int launch_mass_apply<T>(cf_ctx *, int, int, bool);     \
-    template int launch_dt<T>(cf_ctx *, int);                        \
+    template int launch_dt<T>(cf_ctx *, int, bool);                  \
     template int launch_div_check<T>(cf_ctx *, int, double *);
 INST(double)
 INST(float)

@@ -109,5 +109,67 @@ int launch_stats(cf_ctx *ctx, int b, double *d_out) {
     return 0;
 }
 
+// ---------------------------------------------------------------------------
+// output_monitor reductions (monitor.f90:28-50): per interior plane k the sums
+// and maxima of U(2:nx-1, 2:nyg-1, k), V(2:nxg-1, 2:ny-1, k),
+// W(2:nxg-1, 2:nyg-1, k) (k <= nz-1) and nu_t(2:nxg-1, 2:nyg-1, k); the host
+// adds the planes in order.  out[8 (k-2) + q]: q = 0..3 sums, 4..7 maxima.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double bmax(double v, double *sh) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffff, v, o));
+    int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) sh[w] = v;
+    __syncthreads();
+    double r = -INFINITY;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) r = fmax(r, sh[q]);
+    __syncthreads();
+    return r;
+}
+
+template <typename T>
+__global__ void k_monitor(Geo g, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, double *out) {
+    __shared__ double sh[32];
+    const int k = blockIdx.x + 2;
+    double s[4] = {0, 0, 0, 0}, m[4] = {-INFINITY, -INFINITY, -INFINITY, -INFINITY};
+    auto scan = [&](const Fld<T> &F, int i1, int j1, int q) {
+        const int ni = i1 - 1;
+        const long n = (long)ni * (j1 - 1);
+        for (long t = threadIdx.x; t < n; t += blockDim.x) {
+            const int i = (int)(t % ni) + 2, j = (int)(t / ni) + 2;
+            const double v = (double)F(i, j, k);
+            s[q] += v;
+            m[q] = fmax(m[q], v);
+        }
+    };
+    scan(U, g.nx - 1, g.nyg - 1, 0);
+    scan(V, g.nxg - 1, g.ny - 1, 1);
+    if (k <= g.nz - 1) scan(W, g.nxg - 1, g.nyg - 1, 2);
+    scan(nt, g.nxg - 1, g.nyg - 1, 3);
+    for (int q = 0; q < 4; q++) {
+        const double a = bsum(s[q], sh);
+        const double b = bmax(m[q], sh);
+        if (threadIdx.x == 0) {
+            out[8 * (k - 2) + q] = a;
+            out[8 * (k - 2) + 4 + q] = b;
+        }
+    }
+}
+
+template <typename T>
+int launch_monitor(cf_ctx *ctx, int b, double *d_out) {
+    if (int rc = launch_nut_materialize<T>(ctx)) return rc;
+    Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
+    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+    k_monitor<T><<<ctx->nzg - 2, 256, 0, ctx->st>>>(ctx->geo, U, V, W, nt, d_out);
+    count_launch(ctx, "k_monitor");
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template int launch_monitor<double>(cf_ctx *, int, double *);
+template int launch_monitor<float>(cf_ctx *, int, double *);
 template int launch_stats<double>(cf_ctx *, int, double *);
 template int launch_stats<float>(cf_ctx *, int, double *);

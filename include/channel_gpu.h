@@ -46,9 +46,10 @@ typedef struct {
     int Retau_int;         /* mass-flow rescale flag (initialization.f90:433)   */
     int x_mass_cte;        /* 0 fixed dPdx, 1 constant mass flow, 2 centre-line */
     int y_mass_cte;        /* 1 constant mass flow in y                         */
-    int LES_model;         /* 0 none, 2 dynamic Smagorinsky                     */
+    int LES_model;         /* 0 none, 2 dynamic Smagorinsky, 3 AMD              */
     int iwall_model;       /* 0 no-slip walls, 3 equilibrium wall model         */
-    int Dirichlet_nu_t;    /* ghost rule for nu_t: 1 Dirichlet, 0 Neumann       */
+    int Dirichlet_nu_t;    /* ghost rule for nu_t: 1 Dirichlet, 0 Neumann, 2 (AMD
+                              only) -nu_t(2) + 0.38 dPdx^(1/2) (y(2)-y(1))       */
     int jref_eqwm;         /* eqwm matching index                               */
     /* library options (not in input_parameters) */
     int precision;         /* CF_PREC_FP64 or CF_PREC_SPLIT                     */
@@ -59,6 +60,11 @@ typedef struct {
                               0: reuse the first one (bit-identical inputs)      */
     int dsm_unfused;       /* 1: evaluate the dynamic Smagorinsky model with the
                               multi-pass kernels even where the fused pass applies */
+    int cfl_corrected;     /* 1: convective limit of compute_dt with the minimum
+                              over cells of spacing/|u| (the reference takes the
+                              maximum, time_integration.f90:191-201, which leaves
+                              only the viscous limit and the 5e-3 cap); 0: as the
+                              reference (default) */
 } cf_params;
 
 /* Fills p with the defaults of the library (reference values where the
@@ -160,6 +166,13 @@ int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double
  * dU/dy at the bottom and top walls, and the wall averages of nu_t
  * (9*ny + 8 values). */
 int cf_compute_statistics(cf_ctx *ctx, double *out);
+/* The reductions of output_monitor (monitor.f90:20-52) on the current
+ * fields: out[9] = mean U, V, W over the interior ranges divided by
+ * (nx-1)(ny-1)(nz-1), max U, V, W, mean nu_t (interior sum divided by
+ * (nx+1)(ny+1)(nz+1)), max nu_t, and check_divergence's max (signed)
+ * divergence.  The printing itself is the caller's (channelflow's
+ * Channel.output_monitor mirrors it). */
+int cf_output_monitor(cf_ctx *ctx, double *out);
 
 /* ---- input_parameters file and snapshot format ----------------------- */
 /* Parses the reference's input_parameters text (input_output.f90:29-81).

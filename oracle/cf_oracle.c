@@ -1977,6 +1977,44 @@ void cfo_time_step_rk3(cfo *o) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* output_monitor reductions, monitor.f90:28-52, 74-81: out[9] = mean U, V, */
+/* W, max U, V, W, mean nu_t, max nu_t, max divergence.  Fortran Sum and     */
+/* Maxval over column-major sections.                                        */
+/* ------------------------------------------------------------------------ */
+static void sum_max(fa *F, int i1, int j1, int k1, double *sum, double *mx) {
+    double s = 0.0, m = -INFINITY;
+    for (int k = 2; k <= k1; k++)
+        for (int j = 2; j <= j1; j++)
+            for (int i = 2; i <= i1; i++) {
+                double v = F3(*F, i, j, k);
+                s += v;
+                if (v > m) m = v;
+            }
+    *sum = s;
+    *mx = m;
+}
+
+void cfo_output_monitor(cfo *o, double *out) {
+    int nx = o->nx, ny = o->ny, nz = o->nz, nxg = o->nxg, nyg = o->nyg, nzg = o->nzg;
+    double su, sv, sw, sn, mu, mv, mw, mn;
+    sum_max(&o->U, nx - 1, nyg - 1, nzg - 1, &su, &mu);
+    sum_max(&o->V, nxg - 1, ny - 1, nzg - 1, &sv, &mv);
+    sum_max(&o->W, nxg - 1, nyg - 1, nz - 1, &sw, &mw);
+    sum_max(&o->nu_t, nxg - 1, nyg - 1, nzg - 1, &sn, &mn);
+    double cells = (double)(nx - 1) * (double)(ny - 1) * (double)(nz - 1);
+    out[0] = su / cells;
+    out[1] = sv / cells;
+    out[2] = sw / cells;
+    out[3] = mu;
+    out[4] = mv;
+    out[5] = mw;
+    out[6] = sn / ((double)nxg * (double)nyg * (double)nzg);
+    out[7] = mn;
+    double mabs;
+    out[8] = cfo_check_divergence(o, &mabs);
+}
+
+/* ------------------------------------------------------------------------ */
 /* compute_statistics, statistics.f90:43-159.                                */
 /* out layout: 9 profiles of length ny (Umean, Vmean, Wmean, U2, V2, W2, UV,  */
 /* Pmean, P2mean) then utau, Retau, Qflow_x, Qflow_y, dUdy_b, dUdy_t,        */

@@ -83,6 +83,7 @@ double cfo_compute_dPx_for_constant_mass_flow(cfo *o); /* mass_flow.f90:103   */
 double cfo_compute_mean_mass_flow_U(cfo *o);       /* mass_flow.f90:25         */
 double cfo_compute_mean_mass_flow_V(cfo *o);       /* mass_flow.f90:61         */
 void cfo_compute_statistics(cfo *o, double *out);  /* statistics.f90:43-155    */
+void cfo_output_monitor(cfo *o, double *out);       /* monitor.f90:28-52        */
 
 /* Third-party arithmetic restated for pinning tests. */
 void cfo_fft(double *re_im, int n, int sign);      /* complex DFT, FFTW sign   */

@@ -70,6 +70,7 @@ def lib(check: bool = False):
             getattr(L, name).restype = C.c_double
             getattr(L, name).argtypes = [vp]
         L.cfo_compute_statistics.argtypes = [vp, dp]
+        L.cfo_output_monitor.argtypes = [vp, dp]
         L.cfo_fft.argtypes = [dp, C.c_int, C.c_int]
         L.cfo_zgtsv.restype = C.c_int
         L.cfo_zgtsv.argtypes = [C.c_int, dp, dp, dp, dp]
@@ -166,6 +167,11 @@ class Oracle:
         m = C.c_double()
         s = self.L.cfo_check_divergence(self.h, C.byref(m))
         return s, m.value
+
+    def output_monitor(self):
+        out = np.zeros(9)
+        self.L.cfo_output_monitor(self.h, _dp(out))
+        return out
 
     def statistics(self):
         out = np.zeros(9 * self.ny + 8)

@@ -405,3 +405,23 @@ def test_amd_matches_point_formula(check, dirichlet):
     o.apply_boundary_conditions()
     o.compute_eddy_viscosity()
     assert abs(o.array("nu_t")[:, 2:-2, :] - nt[:, 2:-2, :]).max() <= 1e-12 * abs(nt).max()
+
+
+def test_monitor_reductions_match_numpy():
+    """output_monitor (monitor.f90:28-52, 74-81) in the oracle against numpy
+    on the same sections and normalisations."""
+    nx, ny, nz = 18, 17, 14
+    case = channel_case(nx, ny, nz)
+    o = oracle_for(case)
+    o.apply_boundary_conditions()
+    o.compute_eddy_viscosity()
+    m = o.output_monitor()
+    f = o.fields()
+    U, V, W, nt = f["U"], f["V"], f["W"], f["nu_t"]
+    cells = (nx - 1) * (ny - 1) * (nz - 1)
+    secs = [U[1:nx - 1, 1:ny, 1:nz], V[1:nx, 1:ny - 1, 1:nz], W[1:nx, 1:ny, 1:nz - 1], nt[1:nx, 1:ny, 1:nz]]
+    want = [secs[0].sum() / cells, secs[1].sum() / cells, secs[2].sum() / cells, secs[0].max(), secs[1].max(),
+            secs[2].max(), secs[3].sum() / ((nx + 1) * (ny + 1) * (nz + 1)), secs[3].max()]
+    for q in range(8):
+        assert abs(m[q] - want[q]) <= 1e-13 * max(1.0, abs(want[q])), (q, m[q], want[q])
+    assert m[8] == o.check_divergence()[0]

@@ -360,3 +360,76 @@ def test_amd_split_precision_short_horizon():
     for n in ("U", "V", "W", "nu_t"):
         e = rel_err(out[1][n], out[0][n])
         assert e < (1e-4 if n != "nu_t" else 1e-3), (n, e)
+
+
+def test_monitor_reductions(capsys):
+    """output_monitor (monitor.f90:20-150) after five steps: means to
+    round-off, maxima exactly, and the printed block."""
+    case = channel_case(*CASES["config1"])
+    o, ch = make_pair(case)
+    for a in (o, ch):
+        a.apply_boundary_conditions()
+    ch.set_fixed_dt(case["dt"])
+    for _ in range(5):
+        o.compute_dt()
+        o.time_step_rk3()
+    ch.time_step_rk3(5)
+    mo = o.output_monitor()
+    mg = ch.output_monitor(5)
+    g = [mg[k] for k in ("meanU", "meanV", "meanW", "maxU", "maxV", "maxW", "meanNut", "maxNut", "max_divergence")]
+    for q in (0, 1, 2, 6):
+        assert abs(g[q] - mo[q]) <= 1e-12 * max(abs(mo[q]), 1e-3), (q, g[q], mo[q])
+    f = o.fields()
+    for q, n in ((3, "U"), (4, "V"), (5, "W"), (7, "nu_t")):
+        assert abs(g[q] - mo[q]) <= 1e-10 * abs(f[n]).max(), (q, g[q], mo[q])
+    assert abs(g[8] - mo[8]) <= 1e-10
+    text = capsys.readouterr().out
+    assert "Maximum nu_t:" in text and "Maximum divergence" in text and "step number :5" in text
+    assert ch.scalars()["t"] == o.scalar("t") > 0  # t = to + dt per step, summed alike
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-15), (1, 1e-6)])
+def test_corrected_cfl_option(precision, tol):
+    """cfl_corrected = 1: dt = min(CFL min over cells of spacing/|u|, the
+    viscous limit, 5e-3), computed here with numpy on the same fields with
+    the ranges of time_integration.f90:191-197; the default keeps the
+    reference's rule (viscous limit or cap)."""
+    import channelflow as cf
+    case = channel_case(*CASES["config1"])
+    ch0 = cf.Channel(case["x"], case["y"], case["z"], precision=precision, **dict(case["prm"], CFL=0.5))
+    ch0.upload(case["U"], case["V"], case["W"])
+    ch0.apply_boundary_conditions()
+    dt_ref = ch0.compute_dt()
+    g = ch0.download()
+    ch0.close()
+    xg = np.r_[np.nan, grids_centres(case["x"])]
+    yg = np.r_[np.nan, grids_centres(case["y"])]
+    zg = np.r_[np.nan, grids_centres(case["z"])]
+    nx, ny, nz = len(case["x"]), len(case["y"]), len(case["z"])
+    nxg, nyg, nzg = nx + 1, ny + 1, nz + 1
+
+    def conv(U, V, W):
+        with np.errstate(divide="ignore"):
+            lu = ((xg[3:nxg + 1] - xg[2:nxg])[:, None, None] / np.abs(U[1:nxg - 1, 1:nyg - 1, 1:nzg - 1])).min()
+            lv = ((yg[3:nyg + 1] - yg[2:nyg])[None, :, None] / np.abs(V[1:nxg - 1, 1:nyg - 1, 1:nzg - 1])).min()
+            lw = ((zg[3:nzg + 1] - zg[2:nzg])[None, None, :] / np.abs(W[1:nxg - 1, 1:nyg - 1, 1:nzg - 1])).min()
+        return 0.5 * min(lu, lv, lw)
+
+    scale = conv(g["U"], g["V"], g["W"]) / (0.5 * dt_ref)  # convective limit at half the reference's dt
+    U, V, W = (case[k] * scale for k in ("U", "V", "W"))
+    ch = cf.Channel(case["x"], case["y"], case["z"], precision=precision, **dict(case["prm"], CFL=0.5, cfl_corrected=1))
+    ch.upload(U, V, W)
+    ch.apply_boundary_conditions()
+    for _ in range(2):  # the second call checks the reset of the per-index maxima
+        dt = ch.compute_dt()
+        f = ch.download()
+        want = min(conv(f["U"], f["V"], f["W"]), dt_ref)
+        assert abs(dt - want) <= tol * want, (dt, want)
+    assert dt < 0.6 * dt_ref
+    ch.close()
+
+
+def grids_centres(f):
+    """Ghost-extended centre grid of initialization.f90:169-195 (nf + 1 values)."""
+    from channelflow import grids
+    return grids.centres(np.asarray(f))
