@@ -197,6 +197,51 @@ def cpu_baseline(wl, steps, threads):
     return nc * steps / dt, dt
 
 
+def stats_run(wl, steps, every, device):
+    """The long-run comparison of the split path against the FP64 path: both
+    advanced `steps` steps from the same seeded field, the statistics of
+    compute_statistics (statistics.f90:43-159) sampled every `every` steps over
+    the second half and time-averaged; mean U+, the u, v, w RMS and the uv
+    Reynolds stress profiles of the split run against the FP64 run."""
+    import numpy as np
+    import channelflow as cf
+    ny = wl["ny"]
+    out = {}
+    for name, prec in (("fp64", cf.PREC_FP64), ("split", cf.PREC_SPLIT)):
+        ch, init = make_channel(wl, prec, device, seed=1)
+        acc, tail, n = np.zeros(9 * ny), np.zeros(8), 0
+        t0 = time.perf_counter()
+        done = 0
+        while done < steps:
+            k = min(every, steps - done)
+            ch.time_step_rk3(k)
+            done += k
+            if done > steps // 2:
+                s = ch.statistics()
+                acc += s[:9 * ny]
+                tail += s[9 * ny:]
+                n += 1
+        wall = time.perf_counter() - t0
+        m, tl = acc / n, tail / n
+        U, V, W, U2, V2, W2, UV = (m[q * ny:(q + 1) * ny] for q in range(7))
+        utau = tl[0]
+        out[name] = dict(Uplus=U / utau, urms=np.sqrt(np.maximum(U2 - U * U, 0.0)),
+                         vrms=np.sqrt(np.maximum(V2 - V * V, 0.0)), wrms=np.sqrt(np.maximum(W2 - W * W, 0.0)),
+                         uv=UV - U * V, utau=utau, retau=tl[1], samples=n, seconds=wall,
+                         finite=bool(np.isfinite(ch.download()["U"]).all()))
+        ch.close()
+    a, b = out["split"], out["fp64"]
+    err = {k: float(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k]))) for k in ("Uplus", "urms", "vrms", "wrms", "uv")}
+    line = {"stats_run": {"workload": wl["name"], "steps": steps, "sample_every": every,
+                          "samples": b["samples"], "window": "second half",
+                          "error_split_vs_fp64 (max|a-b| / max|b|)": err,
+                          "utau": {"fp64": b["utau"], "split": a["utau"]},
+                          "retau": {"fp64": b["retau"], "split": a["retau"]},
+                          "wall_seconds": {"fp64": b["seconds"], "split": a["seconds"]},
+                          "finite": a["finite"] and b["finite"]}}
+    print(json.dumps(line))
+
+
 def run_reference(args, wl, rank, world):
     """Reference arm: the reference's CPU path (its C restatement; the Fortran
     reference needs ifort/MPI/FFTW, absent here) on all host threads."""
@@ -401,9 +446,15 @@ def main():
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     ap.add_argument("--kernel-table", action="store_true",
                     help="with --profile-steps: also print per-kernel event times of two more steps")
+    ap.add_argument("--stats-run", type=int, default=0,
+                    help="only run the long-run statistics comparison of the split and FP64 paths over N steps")
+    ap.add_argument("--stats-every", type=int, default=10)
     args = ap.parse_args()
     rank, world, local = dist_info()
     wl = WORKLOADS[args.workload]
+    if args.stats_run:
+        stats_run(wl, args.stats_run, args.stats_every, local)
+        return
     if args.profile_steps:
         import channelflow as cf
         ch, _ = make_channel(wl, cf.PREC_SPLIT if args.precision == "split" else cf.PREC_FP64, local, seed=1)
