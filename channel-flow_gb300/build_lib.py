@@ -22,7 +22,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-rel
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-I", os.path.join(ROOT, "include")]
 
 CU_SOURCES = ["cf_api.cu", "k_core.cu", "k_dsm.cu", "k_dsm_fused.cu", "k_poisson.cu", "k_eqwm.cu", "k_stats.cu",
-              "k_noalloc.cu", "k_amd.cu"]
+              "k_noalloc.cu", "k_amd.cu", "k_wmlp.cu"]
 CXX_SOURCES = ["io.cpp"]
 
 

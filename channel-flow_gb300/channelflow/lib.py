@@ -356,6 +356,22 @@ class Channel:
         w("------------------------------------------------------", "")
         return m
 
+    def set_wall_mlp(self, net, judge_every: int = 100):
+        """Serves the wall stress of the equilibrium wall model from a trained
+        channelflow.wallmlp.WallMLP (eqwm outside its envelope); every
+        `judge_every` wall-model calls eqwm also runs and the network's error
+        is recorded (wall_mlp_log).  None detaches it."""
+        from . import wallmlp
+        wallmlp._bind()
+        self._wall_net = net  # keeps the network alive while it serves
+        self._check(self.L.cf_set_wall_mlp(self.h, None if net is None else net.h, judge_every))
+
+    def wall_mlp_log(self) -> dict:
+        out = np.zeros(5)
+        self._check(self.L.cf_get_wall_mlp_log(self.h, _dp(out)))
+        return dict(calls=int(out[0]), max_rel_err=out[1], mean_rel_err=out[2], served=int(out[3]),
+                    fallback=int(out[4]))
+
     # ------------------------------------------------------------ fast path
     def time_step_rk3(self, nsteps: int = 1, sync: bool = True):
         self._check(self.L.cf_time_step_rk3(self.h, nsteps, 1 if sync else 0))

@@ -548,7 +548,8 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
                     ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->tri_l32, ctx->tri_ru32,
                     ctx->tri_du32, ctx->tri_flag, ctx->tri_list, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
                     ctx->wtemp1, ctx->wtemp2, ctx->eq_grid, ctx->eq_zst, ctx->eq_xst, ctx->eq_zw, ctx->eq_xw, ctx->ds,
-                    ctx->d_red, ctx->d_dtmin, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage};
+                    ctx->d_red, ctx->d_dtmin, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage,
+                    ctx->wm_u, ctx->wm_tau, ctx->wm_tau_eq, ctx->wm_log, ctx->wm_inside, ctx->wm_calls};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     for (int b = 0; b < 3; b++) {

@@ -213,6 +213,12 @@ struct cf_ctx {
     // wall model
     double *alpha_x = nullptr, *alpha_z = nullptr, *alpha_zt = nullptr, *tau0 = nullptr;
     double *wtemp1 = nullptr, *wtemp2 = nullptr;   // W at jref: z-interp (nxg,2,nzg), x-interp (nx,2,nzg)
+    // learned wall stress (cf_set_wall_mlp): the network, per wall point u_les,
+    // stress, envelope flag and the judged eqwm stress; call counter and log
+    struct cf_mlp *wmlp = nullptr;
+    double *wm_u = nullptr, *wm_tau = nullptr, *wm_tau_eq = nullptr, *wm_log = nullptr;
+    int *wm_inside = nullptr, *wm_calls = nullptr;
+    int wm_judge_every = 0;
     double *eq_grid = nullptr;                      // y_cv(1..ncv), y_fa(1..ncv+1)
     int *eq_zst = nullptr, *eq_xst = nullptr;       // stencil indices
     double *eq_zw = nullptr, *eq_xw = nullptr;      // stencil weights
@@ -266,6 +272,7 @@ template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // 
 template <typename T> int launch_mass_apply(cf_ctx *ctx, int buf, int mode, bool ghosts = false); // add ds->lmax[2], dPdx = it/dt (ghosts: whole array, as the BCs would)
 template <typename T> int launch_dt(cf_ctx *ctx, int buf, bool advance_t = false);  // advance_t: t += dt (fast path)
 template <typename T> int launch_eqwm(cf_ctx *ctx, int buf);
+int wall_mlp_infer(cf_ctx *ctx, int npts, double h_wm, double nu);  // network stress of every wall point
 template <typename T> int launch_copy_state(cf_ctx *ctx, int src, int dst);
 template <typename T> int launch_stats(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_monitor(cf_ctx *ctx, int buf, double *d_out);  // (nzg-2) x 8 plane partials

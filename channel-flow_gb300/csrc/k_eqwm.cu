@@ -32,12 +32,68 @@ struct EqParams {
     double nu, h_wm, tau_mean;
 };
 
+// |u| at the matching row of wall point t = (i, wall, k) (wallmodel.f90:
+// 597-612): U there and W moved to the U location by interpolate_x_2nd of
+// temp_1; returns u_les and, through Uv / wv, the two components.
+struct WallPt {
+    int i, w, k, jj;
+    long toff;
+};
+__device__ __forceinline__ WallPt wall_point(long t, const EqParams &ep) {
+    WallPt p;
+    p.i = (int)(t % ep.nx) + 1;
+    const long r = t / ep.nx;
+    p.w = (int)(r % 2);
+    p.k = (int)(r / 2) + 1;
+    p.jj = p.w == 0 ? ep.jref : ep.nyg - ep.jref + 1;
+    p.toff = (long)(p.i - 1) + (long)ep.nx * (p.w + 2L * (p.k - 1));
+    return p;
+}
+__device__ __forceinline__ double wall_ules(const WallPt &p, const EqParams &ep, const Fld<double> &Ud, const float *Uf32,
+                                            int use_f32, int sy, int sz, const double *t1, const int *xst,
+                                            const double *xw, double *Uv_out, double *wv_out) {
+    const int xj = xst[p.i];
+    const double *c = xw + 3 * p.i;
+    const double *row = t1 + (long)ep.nxg * (p.w + 2L * (p.k - 1)) - 1;
+    const double wv = c[0] * row[xj - 1] + c[1] * row[xj] + c[2] * row[xj + 1];
+    const long uoff = (long)(p.i - 1) + (long)sy * (p.jj - 1) + (long)sz * (p.k - 1);
+    const double Uv = use_f32 ? (double)Uf32[uoff] : Ud.p[uoff];
+    *Uv_out = Uv;
+    *wv_out = wv;
+    return sqrt(Uv * Uv + wv * wv);
+}
+
+// u_les of every wall point (the input of the learned wall stress)
+__global__ void k_wm_ules(const Fld<double> Ud, const float *Uf32, int use_f32, int sy, int sz, const double *t1,
+                          const int *xst, const double *xw, EqParams ep, double *ules) {
+    const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long)ep.nx * ep.nzg * 2) return;
+    const WallPt p = wall_point(t, ep);
+    double Uv, wv;
+    ules[p.toff] = wall_ules(p, ep, Ud, Uf32, use_f32, sy, sz, t1, xst, xw, &Uv, &wv);
+}
+
+// Learned-stress state of the wall model: the network's stress and envelope
+// flag per point, the call counter and judging period, the judged eqwm
+// stress.  mode 0: eqwm everywhere (the reference).
+struct WmState {
+    const double *tau_nn;
+    const int *inside;
+    const int *calls;
+    int judge_every;
+    int mode;
+    double *tau_eq;
+};
+
 // solve_u_eqwm (eqwm.f90:90-223) inline, grid in shared memory:
 // yfa[1..ncv+1], idcv[i] = 1/(y_cv(i+1)-y_cv(i)) (i = 1..ncv-1),
 // rw = 1/(y_cv(1)-y_fa(1)); grid[1..ncv] = y_cv, grid[ncv+1..2ncv+1] = y_fa.
+// With the learned stress (mode 1) the network's value stands for the solve
+// at points inside its training envelope; on judged calls the solve runs for
+// every point and its result is kept in tau_eq for the error record.
 __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32, int sy, int sz, const double *t1,
                            const int *xst, const double *xw, const double *grid, EqParams ep, const double *nut,
-                           int nut_f32, double *tau0, double *alpha_x, double *alpha_zt, int *counters) {
+                           int nut_f32, double *tau0, double *alpha_x, double *alpha_zt, int *counters, WmState wm) {
     extern __shared__ double sg[];
     const int ncv = ep.ncv;
     // grid: yfa[1..ncv+1], idcv[1..ncv-1], rw
@@ -50,67 +106,64 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
     long npts = (long)ep.nx * ep.nzg * 2;
     if (t >= npts) return;
-    int i = (int)(t % ep.nx) + 1;
-    long r = t / ep.nx;
-    int w = (int)(r % 2);
-    int k = (int)(r / 2) + 1;
+    const WallPt pt = wall_point(t, ep);
+    const int i = pt.i, w = pt.w, k = pt.k;
     const int nxg = ep.nxg, nyg = ep.nyg;
-    int jj = w == 0 ? ep.jref : nyg - ep.jref + 1;
-    // W at the U location (interpolate_x_2nd of temp_1)
-    int xj = xst[i];
-    const double *c = xw + 3 * i;
-    const double *row = t1 + (long)nxg * (w + 2L * (k - 1)) - 1;
-    double wv = c[0] * row[xj - 1] + c[1] * row[xj] + c[2] * row[xj + 1];
-    long uoff = (long)(i - 1) + (long)sy * (jj - 1) + (long)sz * (k - 1);
-    double Uv = use_f32 ? (double)Uf32[uoff] : Ud.p[uoff];
-    double u_les = sqrt(Uv * Uv + wv * wv);
-    // solve_u_eqwm(u_les, nu, 1.0, yg(jref), ncv, stretch, tau, iter, tau_in)
-    const double kappa = 0.41, Aplus = 17.0, tol = 0.0000001, mu_lam = ep.nu, rho = 1.0;
-    const int max_iter = 100;
-    double tau_lam = mu_lam * u_les / ep.h_wm;
-    long toff = (long)(i - 1) + (long)ep.nx * (w + 2L * (k - 1));
+    double Uv, wv;
+    const double u_les = wall_ules(pt, ep, Ud, Uf32, use_f32, sy, sz, t1, xst, xw, &Uv, &wv);
+    const long toff = pt.toff;
+    const bool served = wm.mode == 1 && wm.inside[toff] != 0;
+    const bool judge = wm.mode == 1 && wm.judge_every > 0 && (*wm.calls % wm.judge_every) == 0;
     double tau = tau0[toff];
-    int iter = 0;
-    while (true) {
-        double tau_prev = tau;
-        double nu_eq = mu_lam / rho;
-        double utau = sqrt(tau / rho);
-        double c1 = rho * kappa * utau;
-        double al = u_les, be = 0.0;
-        double yf = yfa[ncv];
-        double D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
-        double mu_up = mu_lam + c1 * yf * (D * D);
-        for (int q = ncv - 1; q >= 2; q--) {
-            yf = yfa[q];
-            D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
-            double mu_q = mu_lam + c1 * yf * (D * D);
-            double sup = mu_up * idcv[q];
-            double sub = mu_q * idcv[q - 1];
-            double m = -1.0 * (sup + sub) + sup * be;
-            double rm = 1.0 / m;
-            al = -sup * al * rm;
-            be = -sub * rm;
-            mu_up = mu_q;
+    if (!served || judge) {
+        // solve_u_eqwm(u_les, nu, 1.0, yg(jref), ncv, stretch, tau, iter, tau_in)
+        const double kappa = 0.41, Aplus = 17.0, tol = 0.0000001, mu_lam = ep.nu, rho = 1.0;
+        const int max_iter = 100;
+        double tau_lam = mu_lam * u_les / ep.h_wm;
+        int iter = 0;
+        while (true) {
+            double tau_prev = tau;
+            double nu_eq = mu_lam / rho;
+            double utau = sqrt(tau / rho);
+            double c1 = rho * kappa * utau;
+            double al = u_les, be = 0.0;
+            double yf = yfa[ncv];
+            double D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
+            double mu_up = mu_lam + c1 * yf * (D * D);
+            for (int q = ncv - 1; q >= 2; q--) {
+                yf = yfa[q];
+                D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
+                double mu_q = mu_lam + c1 * yf * (D * D);
+                double sup = mu_up * idcv[q];
+                double sub = mu_q * idcv[q - 1];
+                double m = -1.0 * (sup + sub) + sup * be;
+                double rm = 1.0 / m;
+                al = -sup * al * rm;
+                be = -sub * rm;
+                mu_up = mu_q;
+            }
+            double sup = mu_up * idcv[1];
+            double diag = -1.0 * (sup + mu_lam * rw);
+            double x1 = -sup * al / (diag + sup * be);
+            tau = mu_lam * (x1 - 0.0) * rw;
+            int done = 0;
+            if (fabs((tau - tau_prev) / tau_lam) < tol) done = 1;
+            if (done == 0) iter = iter + 1;
+            if (iter > max_iter) done = 1;
+            if (done) break;
         }
-        double sup = mu_up * idcv[1];
-        double diag = -1.0 * (sup + mu_lam * rw);
-        double x1 = -sup * al / (diag + sup * be);
-        tau = mu_lam * (x1 - 0.0) * rw;
-        int done = 0;
-        if (fabs((tau - tau_prev) / tau_lam) < tol) done = 1;
-        if (done == 0) iter = iter + 1;
-        if (iter > max_iter) done = 1;
-        if (done) break;
+        // wallmodel.f90:620-640
+        if (isnan(tau)) {
+            atomicAdd(&counters[0], 1);
+            tau = ep.tau_mean;
+        }
+        if (iter == 100) {
+            tau = ep.tau_mean;
+            atomicAdd(&counters[1], 1);
+        }
+        if (judge) wm.tau_eq[toff] = tau;
     }
-    // wallmodel.f90:620-640
-    if (isnan(tau)) {
-        atomicAdd(&counters[0], 1);
-        tau = ep.tau_mean;
-    }
-    if (iter == 100) {
-        tau = ep.tau_mean;
-        atomicAdd(&counters[1], 1);
-    }
+    if (served) tau = wm.tau_nn[toff];
     tau0[toff] = tau;
     double tx = tau * Uv / u_les, tz = tau * wv / u_les;
     int ja = w == 0 ? 1 : nyg, jb = w == 0 ? 2 : nyg - 1;
@@ -122,6 +175,50 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
     double nu_t_ik = 0.5 * (0.5 * (NT(i, ja) + NT(i + 1, ja)) + 0.5 * (NT(i, jb) + NT(i + 1, jb)));
     alpha_x[toff] = tx / (ep.nu + nu_t_ik);
     alpha_zt[toff] = tz / (ep.nu + nu_t_ik);
+}
+
+// The error record of judged calls: max and mean |tau_nn/tau_eq - 1| over
+// the points the network served, their count and the fallback count; every
+// call advances the call counter.  One block.
+__global__ void __launch_bounds__(1024) k_wm_judge(long npts, const double *tau_nn, const int *inside,
+                                                  const double *tau_eq, int *calls, int judge_every, double *log) {
+    __shared__ double sm[3][32];
+    const bool judge = judge_every > 0 && (*calls % judge_every) == 0;
+    if (judge) {
+        double mx = 0.0, sum = 0.0, cnt = 0.0;
+        for (long t = threadIdx.x; t < npts; t += blockDim.x) {
+            if (!inside[t]) continue;
+            const double e = fabs(tau_nn[t] / tau_eq[t] - 1.0);
+            mx = fmax(mx, e);
+            sum += e;
+            cnt += 1.0;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+            sum += __shfl_down_sync(0xffffffffu, sum, o);
+            cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            sm[0][threadIdx.x >> 5] = mx;
+            sm[1][threadIdx.x >> 5] = sum;
+            sm[2][threadIdx.x >> 5] = cnt;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int q = 1; q < (int)(blockDim.x >> 5); q++) {
+                mx = fmax(mx, sm[0][q]);
+                sum += sm[1][q];
+                cnt += sm[2][q];
+            }
+            log[0] = (double)(*calls + 1);
+            log[1] = mx;
+            log[2] = cnt > 0 ? sum / cnt : 0.0;
+            log[3] = cnt;
+            log[4] = (double)npts - cnt;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *calls = *calls + 1;
 }
 
 // alpha_z: 4-point average of alpha_z_temp and its copies (wallmodel.f90:656-664)
@@ -159,11 +256,30 @@ int launch_eqwm(cf_ctx *ctx, int b) {
     long npts = (long)nx * nzg * 2;
     size_t sh = (size_t)(2 * ep.ncv + 4) * sizeof(double);
     Fld<double> Ud = make_fld<double>(ctx->U[b], nx, nyg);
+    WmState wm = {};
+    if (ctx->wmlp) {
+        // the learned stress of every point, then the solve where it does not serve
+        k_wm_ules<<<cdiv(npts, 256), 256, 0, ctx->st>>>(Ud, (const float *)ctx->U[b], sizeof(T) == 4, nx, nx * nyg,
+                                                        ctx->wtemp1, ctx->eq_xst, ctx->eq_xw, ep, ctx->wm_u);
+        count_launch(ctx, "k_wm_ules");
+        if (int rc = wall_mlp_infer(ctx, (int)npts, ep.h_wm, ep.nu)) return rc;
+        wm.tau_nn = ctx->wm_tau;
+        wm.inside = ctx->wm_inside;
+        wm.calls = ctx->wm_calls;
+        wm.judge_every = ctx->wm_judge_every;
+        wm.mode = 1;
+        wm.tau_eq = ctx->wm_tau_eq;
+    }
     k_eq_solve<<<cdiv(npts, 128), 128, sh, ctx->st>>>(Ud, (const float *)ctx->U[b], sizeof(T) == 4, nx, nx * nyg,
                                                      ctx->wtemp1, ctx->eq_xst, ctx->eq_xw, ctx->eq_grid, ep,
                                                      (const double *)ctx->nut, sizeof(T) == 4, ctx->tau0, ctx->alpha_x,
-                                                     ctx->alpha_zt, (int *)ctx->d_red);
+                                                     ctx->alpha_zt, (int *)ctx->d_red, wm);
     count_launch(ctx, "k_eq_solve");
+    if (ctx->wmlp) {
+        k_wm_judge<<<1, 1024, 0, ctx->st>>>(npts, ctx->wm_tau, ctx->wm_inside, ctx->wm_tau_eq, ctx->wm_calls,
+                                            ctx->wm_judge_every, ctx->wm_log);
+        count_launch(ctx, "k_wm_judge");
+    }
     k_eq_alphaz<<<dim3(cdiv(nxg, 128), nz, 2), 128, 0, ctx->st>>>(ctx->alpha_zt, ctx->alpha_z, nx, nxg, nz, nzg);
     count_launch(ctx, "k_eq_alphaz");
     CF_CUDA(cudaGetLastError());

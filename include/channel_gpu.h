@@ -199,6 +199,63 @@ int cf_write_statistics(const char *path, double t, double nu, int nx, int ny, i
  * (input_output.f90:557-558); fails when it needs more than cap bytes. */
 int cf_statistics_file_name(const char *fileout, int istep, int nstep_init, char *name, int cap);
 
+/* ---- learned wall-stress model ----------------------------------------
+ * A 3 -> 64 -> 64 -> 1 tanh network standing in for the equilibrium wall
+ * model's ODE solve (solve_u_eqwm, eqwm.f90:90-223, called per wall point at
+ * wallmodel.f90:621): inputs log(u_les), log(matching height), log(nu),
+ * output log(tau_w h / (nu u_les)) (the stress over its laminar value), all
+ * normalised with the training set's mean and standard deviation.  BF16 weights, FP32 accumulation; the 64 x 64 layer of
+ * the inference runs on the tensor cores.  No counterpart in the reference.
+ * Device pointers throughout; every call is ordered on `stream` (NULL: the
+ * legacy default stream). */
+typedef struct cf_mlp cf_mlp;
+enum { CF_MLP_NPARAM = 4481 };
+/* eqwm solve per sample: u, h, nu (n each) -> tau (and the Picard passes,
+ * may be NULL); ODE grid of ncv cells with stretching `stretch`, warm start
+ * tau_init; the reference's non-convergence rule (101 passes) is reported in
+ * iters, not replaced. */
+int cf_eqwm_solve_batch(int n, const double *u, const double *h, const double *nu, int ncv, double stretch,
+                        double tau_init, double *tau, int *iters, void *stream);
+/* A network with seeded (Xavier-uniform) weights for eqwm with (ncv, stretch). */
+int cf_mlp_create(int seed, int ncv, double stretch, cf_mlp **out);
+int cf_mlp_destroy(cf_mlp *m);
+/* Sets the normalisation and the training envelope from a training set
+ * (means and standard deviations of the three input logs and the target,
+ * per-input min and max of the logs). */
+int cf_mlp_fit_normalisation(cf_mlp *m, int n, const double *u, const double *h, const double *nu,
+                             const double *tau, void *stream);
+/* Mini-batch Adam on mean((y - target)^2): `epochs` passes over n
+ * samples in batches of `batch` (a multiple of 128) with a seeded
+ * permutation per epoch, step size lr decayed by cosine to lr/100.
+ * loss_out (epochs values, may be NULL): mean batch loss per epoch. */
+int cf_mlp_train(cf_mlp *m, int n, const double *u, const double *h, const double *nu, const double *tau, int epochs,
+                 int batch, double lr, int seed, double *loss_out, void *stream);
+/* Gradient of the batch loss over samples 0..n-1 (n a multiple of 128) at
+ * the current parameters, into grad (CF_MLP_NPARAM doubles, device). */
+int cf_mlp_gradient(cf_mlp *m, int n, const double *u, const double *h, const double *nu, const double *tau,
+                    double *grad, double *loss, void *stream);
+/* tau = network(u, h, nu); use_tensor_cores 0 runs the same arithmetic on
+ * the FP32 pipes (the cross-check).  inside (may be NULL): 1 where all three
+ * inputs lie within the training envelope. */
+int cf_mlp_predict(cf_mlp *m, int n, const double *u, const double *h, const double *nu, double *tau, int *inside,
+                   int use_tensor_cores, void *stream);
+/* FP32 master parameters (CF_MLP_NPARAM floats, host) and the normalisation
+ * (8 doubles: means, standard deviations) and envelope (6 doubles: min, max
+ * of the three input logs). */
+int cf_mlp_get(cf_mlp *m, float *params, double *norm, double *envelope);
+int cf_mlp_set(cf_mlp *m, const float *params, const double *norm, const double *envelope);
+/* Uses the network for the wall stress of ctx's equilibrium wall model
+ * (iwall_model 3): points whose inputs fall outside the envelope, and all
+ * points when m is NULL, keep the eqwm solve.  Every `judge_every` calls of
+ * the wall model (0: never) the eqwm solve also runs for all points and the
+ * relative error of the network against it is recorded.  ctx's eqwm_ncv and
+ * eqwm_stretch must be those m was trained for.  m must outlive its use. */
+int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int judge_every);
+/* The last judgement: out[5] = wall-model calls so far, max and mean
+ * |tau_mlp - tau_eqwm|/tau_eqwm over the points the network served, points
+ * served, points that fell back to eqwm. */
+int cf_get_wall_mlp_log(cf_ctx *ctx, double *out);
+
 /* ---- divergence check without device allocation ---------------------- */
 /* No counterpart in the reference: the arithmetic is check_divergence
  * (projection.f90:234-256), as in cf_check_divergence, but on caller-owned

@@ -1535,6 +1535,11 @@ static double solve_u_eqwm(double umag_les, double mu_lam, double rho_eq, double
     return tau_wall;
 }
 
+double cfo_solve_u_eqwm(double umag_les, double nu, double h_wm, int ncv, double stretch, double tau_in, int *iter) {
+    /* one wall point of wallmodel.f90:621 (rho = 1) */
+    return solve_u_eqwm(umag_les, nu, 1.0, h_wm, ncv, stretch, iter, tau_in);
+}
+
 /* interpolate_z_2nd (interpolation.f90:188-252) for u(1:n1,1,1:ny) -> ui(1:n1,1,1:n3) */
 static void interp_z_2nd(const double *y, int ny, const fa *u, const double *yi, int n3, fa *ui) {
     int n1 = (int)u->n[0];

@@ -84,6 +84,10 @@ double cfo_compute_mean_mass_flow_U(cfo *o);       /* mass_flow.f90:25         *
 double cfo_compute_mean_mass_flow_V(cfo *o);       /* mass_flow.f90:61         */
 void cfo_compute_statistics(cfo *o, double *out);  /* statistics.f90:43-155    */
 void cfo_output_monitor(cfo *o, double *out);       /* monitor.f90:28-52        */
+/* solve_u_eqwm (eqwm.f90:90-223) for one point: u_les, nu, matching height,
+ * ODE cells and stretching, warm-start stress; returns tau_w, *iter the
+ * Picard passes (101 = not converged). */
+double cfo_solve_u_eqwm(double umag_les, double nu, double h_wm, int ncv, double stretch, double tau_in, int *iter);
 
 /* Third-party arithmetic restated for pinning tests. */
 void cfo_fft(double *re_im, int n, int sign);      /* complex DFT, FFTW sign   */

@@ -71,6 +71,9 @@ def lib(check: bool = False):
             getattr(L, name).argtypes = [vp]
         L.cfo_compute_statistics.argtypes = [vp, dp]
         L.cfo_output_monitor.argtypes = [vp, dp]
+        L.cfo_solve_u_eqwm.restype = C.c_double
+        L.cfo_solve_u_eqwm.argtypes = [C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, C.c_double,
+                                       C.POINTER(C.c_int)]
         L.cfo_fft.argtypes = [dp, C.c_int, C.c_int]
         L.cfo_zgtsv.restype = C.c_int
         L.cfo_zgtsv.argtypes = [C.c_int, dp, dp, dp, dp]
@@ -177,3 +180,11 @@ class Oracle:
         out = np.zeros(9 * self.ny + 8)
         self.L.cfo_compute_statistics(self.h, _dp(out))
         return out
+
+
+def solve_u_eqwm(u, nu, h, ncv, stretch, tau_in):
+    """eqwm.f90:90-223 for one point (the oracle's restatement): (tau_w, iterations)."""
+    L = lib()
+    it = C.c_int()
+    t = L.cfo_solve_u_eqwm(float(u), float(nu), float(h), int(ncv), float(stretch), float(tau_in), C.byref(it))
+    return t, it.value
