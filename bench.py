@@ -39,6 +39,12 @@ WORKLOADS = {
                   retau=550.0, stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar"),
     "re550_amd": dict(name="LES Re_tau=550, 192x128x192, AMD, no-slip, constant mass flow", nx=194, ny=129, nz=194,
                       retau=550.0, stretch=1.5, les=3, wall=0, jref=3, ncv=100, profile="laminar"),
+    "re5200_wmlp": dict(name="WMLES Re_tau=5200, 512x128x512, DSM + learned wall stress (eqwm fallback, ncv 30), "
+                             "uniform y, matched at 0.1 delta", nx=514, ny=129, nz=514, retau=5200.0, stretch=0.0, les=2,
+                        wall=3, jref=8, ncv=30, profile="plug", mlp=True),
+    "re5200_eqwm": dict(name="WMLES Re_tau=5200, 512x128x512, DSM + eqwm (ncv 30), uniform y, matched at 0.1 delta",
+                        nx=514, ny=129, nz=514, retau=5200.0, stretch=0.0, les=2, wall=3, jref=8, ncv=30,
+                        profile="plug"),
     "re180": dict(name="Re_tau=180, 64x64x64, DSM, no-slip, constant mass flow", nx=66, ny=65, nz=66, retau=180.0,
                   stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar"),
     "re2000_eqwm": dict(name="WMLES Re_tau=2000, 256x96x256, DSM + eqwm (ncv 30), uniform y", nx=258, ny=97, nz=258,
@@ -153,6 +159,34 @@ def dist_info():
     return rank, world, local
 
 
+_NET = {}
+
+
+def wall_net(wl, device):
+    """The learned wall stress of a workload that uses it: trained once per
+    process on 2^20 eqwm-labelled samples with the project's own kernels."""
+    key = (wl["ncv"], device)
+    if key not in _NET:
+        import torch
+        from channelflow import wallmlp
+        dev = torch.device("cuda", device)
+        t0 = time.perf_counter()
+        u, h, nu, tau = wallmlp.training_set(1 << 20, seed=5200, device=dev, ncv=wl["ncv"], stretch=1.10)
+        t1 = time.perf_counter()
+        net = wallmlp.WallMLP(seed=3, ncv=wl["ncv"], stretch=1.10)
+        net.fit_normalisation(u, h, nu, tau)
+        loss = net.train(u, h, nu, tau, epochs=8, batch=512, lr=3e-3, seed=0)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        ut, ht, nt, tt = wallmlp.training_set(1 << 16, seed=5201, device=dev, ncv=wl["ncv"], stretch=1.10,
+                                              **wallmlp.OPERATING)
+        err = (net.predict(ut, ht, nt) / tt - 1).abs()
+        _NET[key] = (net, {"samples": int(u.numel()), "label_seconds": t1 - t0, "train_seconds": t2 - t1,
+                           "final_loss": float(loss[-1]), "heldout_max_rel_err": float(err.max()),
+                           "heldout_mean_rel_err": float(err.mean())})
+    return _NET[key]
+
+
 def make_channel(wl, precision, device, seed, cfl=0.5):
     import channelflow as cf
     from channelflow import grids
@@ -162,6 +196,8 @@ def make_channel(wl, precision, device, seed, cfl=0.5):
     prm = dict(nu=nu, CFL=cfl, dPdx=(wl["retau"] * nu) ** 2, LES_model=wl["les"], iwall_model=wl["wall"],
                x_mass_cte=1, jref_eqwm=wl["jref"], eqwm_ncv=wl["ncv"], precision=precision)
     ch = cf.Channel(x, y, z, device=device, **prm)
+    if wl.get("mlp"):
+        ch.set_wall_mlp(wall_net(wl, device)[0], judge_every=100)
     ch.upload(U, V, W)
     ch.init_mass_flow()
     ch.apply_boundary_conditions()
@@ -425,6 +461,10 @@ def run_ours(args, wl, rank, world, local):
             "gpu_launches": launches,
             "clocks": clocks,
         }
+        if wl.get("mlp"):
+            net_info = dict(wall_net(wl, dev)[1])
+            net_info["judged_in_run"] = ch.wall_mlp_log()
+            line["wall_mlp"] = net_info
         print(json.dumps(line), flush=True)
     ch.close()
     ch64.close()

@@ -792,10 +792,11 @@ int wall_mlp_infer(cf_ctx *ctx, int npts, double h_wm, double nu) {
     (void)h_wm;
     (void)nu;
     // wm_log[6], wm_log[7] hold the matching height and the viscosity
-    return mlp_predict_tc(ctx->wmlp, npts, ctx->wm_u, ctx->wm_log + 6, 0, ctx->wm_log + 7, 0, ctx->wm_tau,
-                          ctx->wm_inside, ctx->st)
-               ? cf_fail(ctx, CF_ERR_CUDA, "learned wall stress: " + ctx->wmlp->err)
-               : 0;
+    if (mlp_predict_tc(ctx->wmlp, npts, ctx->wm_u, ctx->wm_log + 6, 0, ctx->wm_log + 7, 0, ctx->wm_tau,
+                       ctx->wm_inside, ctx->st))
+        return cf_fail(ctx, CF_ERR_CUDA, "learned wall stress: " + ctx->wmlp->err);
+    count_launch(ctx, "k_mlp_infer_tc");
+    return 0;
 }
 
 extern "C" int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int judge_every) {
