@@ -278,6 +278,120 @@ def stats_run(wl, steps, every, device):
     print(json.dumps(line))
 
 
+ENSEMBLE = {"name": "ensemble of 16 channels: 6x(64x64x64), 6x(96x64x96), 4x(128x96x128), Re_tau from "
+                    "{180, 395, 550}, DSM, no-slip, constant mass flow", "members": [(66, 65, 66)] * 6 +
+            [(98, 65, 98)] * 6 + [(130, 97, 130)] * 4}
+
+
+def ensemble_members(precision, device):
+    """The 16 members: own seed, own Re_tau (seeded draw from 180, 395, 550),
+    own perturbed laminar field and mass-flow target."""
+    import numpy as np
+    import channelflow as cf
+    rng = np.random.default_rng(16)
+    out = []
+    for q, (nx, ny, nz) in enumerate(ENSEMBLE["members"]):
+        retau = float(rng.choice([180.0, 395.0, 550.0]))
+        wl = dict(nx=nx, ny=ny, nz=nz, retau=retau, stretch=1.5, les=2, wall=0, jref=3, ncv=100, profile="laminar")
+        ch, _ = make_channel(wl, precision, device, seed=100 + q)
+        out.append((ch, retau))
+    return out
+
+
+def run_ensemble(args, rank, world, local):
+    """The ensemble workload: every member advanced by one ensemble step per
+    step (one CUDA graph with a branch per member), against the same members
+    stepped one after another on their own streams."""
+    import numpy as np
+    import torch
+    import channelflow as cf
+    dev = local
+    torch.cuda.set_device(dev)
+    mem = ensemble_members(cf.PREC_SPLIT, dev)
+    chans = [m[0] for m in mem]
+    nc = sum((c.nx - 2) * (c.ny - 1) * (c.nz - 2) for c in chans)
+    ens = cf.Ensemble(chans)
+    ens.step(args.warmup)
+    strm = torch.cuda.ExternalStream(ens.stream(), device=torch.device("cuda", dev))
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev)
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(strm)
+    ens.step(args.steps, sync=False)
+    e1.record(strm)
+    e1.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    value = world * nc * args.steps / (ms / 1e3)
+    # the same members stepped one after another (each its own graph)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for c in chans:
+        c.time_step_rk3(args.steps, sync=True)
+    seq = time.perf_counter() - t0
+    # end to end: every member's fields up from and back to pinned host arrays each step
+    pinned = []
+    for c in chans:
+        d = c.download()
+        bufs = {}
+        for k in ("U", "V", "W"):
+            t = torch.empty(int(np.prod(c.shapes[k])), dtype=torch.float64, pin_memory=True)
+            bufs[k] = t.numpy().reshape(c.shapes[k], order="F")
+            bufs[k][...] = d[k]
+        pinned.append(bufs)
+    ke = max(2, min(args.steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        for c, b in zip(chans, pinned):
+            c.upload(b["U"], b["V"], b["W"])
+        ens.step(1, sync=False)
+        for c, b in zip(chans, pinned):
+            c.download_into(U=b["U"], V=b["V"], W=b["W"])
+    torch.cuda.synchronize()
+    te = time.perf_counter() - t0
+    nbytes = sum(8 * sum(int(np.prod(c.shapes[k])) for k in ("U", "V", "W")) for c in chans)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        # one member of each grid through the CPU oracle, scaled by the member counts
+        thr = os.cpu_count() or 1
+        tot_s, tot_c = 0.0, 0
+        for nx, ny, nz, cnt in ((66, 65, 66, 6), (98, 65, 98, 6), (130, 97, 130, 4)):
+            wl = dict(nx=nx, ny=ny, nz=nz, retau=395.0, stretch=1.5, les=2, wall=0, jref=3, ncv=100,
+                      profile="laminar")
+            v, sec = cpu_baseline(wl, 1, thr)
+            cells = (nx - 2) * (ny - 1) * (nz - 2)
+            tot_s += cnt * cells / v
+            tot_c += cnt * cells
+        cpu = {"value": tot_c / tot_s, "unit": UNIT, "cores": thr, "kind": "port",
+               "sample": "one RK3 step of one member of each grid (C restatement of the reference CPU path, "
+                         "OpenMP), the ensemble's time as the members' sum"}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 (split)", "data": "synthetic (16 seeded perturbed laminar fields)",
+            "config": {"workload": ENSEMBLE["name"], "members": len(chans), "grid_points": nc,
+                       "retau": [m[1] for m in mem], "precision": "split",
+                       "graph": "one CUDA graph per ensemble step, a branch per member",
+                       "l2": "members' working set (~2.5 GB) larger than L2; no flush needed"},
+            "sequential_members": {"value": world * nc * args.steps / seq, "ms_per_step": 1e3 * seq / args.steps,
+                                   "how": "each member's own graph, one member after another"},
+            "ensemble_over_sequential": (world * nc * args.steps / seq and value / (world * nc * args.steps / seq)),
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * nc * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                    "d2h_bytes_per_step": nbytes, "steps": ke,
+                    "path": "cf_upload_fields x16 + cf_ensemble_step + cf_download_fields x16, pinned host buffers"},
+            "gpu_launches": ens.launches_per_step() * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    ens.close()
+    for c in chans:
+        c.close()
+
+
 def run_reference(args, wl, rank, world):
     """Reference arm: the reference's CPU path (its C restatement; the Fortran
     reference needs ifort/MPI/FFTW, absent here) on all host threads."""
@@ -478,7 +592,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="re550", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="re550", choices=sorted(WORKLOADS) + ["ensemble16"])
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
@@ -491,6 +605,14 @@ def main():
     ap.add_argument("--stats-every", type=int, default=10)
     args = ap.parse_args()
     rank, world, local = dist_info()
+    if args.workload == "ensemble16":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference arm is timed on the "
+                                  "single-channel workloads"}))
+            return
+        run_ensemble(args, rank, world, local)
+        return
     wl = WORKLOADS[args.workload]
     if args.stats_run:
         stats_run(wl, args.stats_run, args.stats_every, local)

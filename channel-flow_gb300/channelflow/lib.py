@@ -431,6 +431,52 @@ class Channel:
             self.apply_boundary_conditions()
 
 
+class Ensemble:
+    """Independent channels advanced together: one CUDA graph per ensemble
+    step with a branch per member (cf_ensemble_*).  The members stay usable
+    as Channel objects between steps."""
+
+    def __init__(self, members):
+        self.L = load()
+        L = self.L
+        vp = C.c_void_p
+        L.cf_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(vp)]
+        L.cf_ensemble_destroy.argtypes = [vp]
+        L.cf_ensemble_step.argtypes = [vp, C.c_int, C.c_int]
+        L.cf_ensemble_stream.argtypes = [vp]
+        L.cf_ensemble_stream.restype = vp
+        L.cf_ensemble_launches_per_step.argtypes = [vp]
+        self.members = list(members)
+        arr = (vp * len(self.members))(*[m.h.value for m in self.members])
+        h = vp()
+        rc = L.cf_ensemble_create(len(self.members), arr, C.byref(h))
+        if rc != 0:
+            raise CfError(L.cf_last_error(None).decode() or f"cf_ensemble_create failed ({rc})")
+        self.h = h
+
+    def step(self, nsteps: int = 1, sync: bool = True):
+        rc = self.L.cf_ensemble_step(self.h, nsteps, 1 if sync else 0)
+        if rc != 0:
+            raise CfError(self.L.cf_last_error(None).decode() or f"cf_ensemble_step failed ({rc})")
+
+    def stream(self) -> int:
+        return self.L.cf_ensemble_stream(self.h)
+
+    def launches_per_step(self) -> int:
+        return self.L.cf_ensemble_launches_per_step(self.h)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.L.cf_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def read_input_parameters(path: str):
     """Parses an input_parameters file (input_output.f90:21-133)."""
     L = load()

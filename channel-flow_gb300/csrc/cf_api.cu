@@ -1241,3 +1241,153 @@ extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *na
     *n_names = n;
     return CF_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Ensembles: independent channels (any mix of grids and parameters) advanced
+// together.  One step of the whole ensemble is one CUDA graph: a fork from
+// the ensemble's stream to every member's stream, each member's step
+// sequence on its own branch, a join back.  The graph is captured once per
+// combination of the members' buffer rotations and replayed; the members
+// run concurrently on the GPU, so small grids fill it together.
+// ---------------------------------------------------------------------------
+#include <map>
+
+struct cf_ensemble {
+    std::vector<cf_ctx *> m;
+    int dev = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    std::map<std::vector<int>, std::pair<cudaGraphExec_t, std::vector<int>>> graphs;  // rotation -> (graph, next)
+    int launches = 0;
+    std::string err;
+};
+
+static thread_local std::string g_ens_err;
+static int ens_fail(cf_ensemble *e, int code, const std::string &msg) {
+    if (e) e->err = msg;
+    g_ens_err = msg;
+    g_last_error = msg;
+    return code;
+}
+#define ENS_CUDA(call)                                                                                  \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) return ens_fail(e, CF_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" int cf_ensemble_create(int n, cf_ctx *const *members, cf_ensemble **out) {
+    cf_ensemble *e = nullptr;
+    if (!out || n < 1 || !members) return ens_fail(e, CF_ERR_INVALID, "cf_ensemble_create: bad argument");
+    *out = nullptr;
+    for (int q = 0; q < n; q++) {
+        if (!members[q]) return ens_fail(e, CF_ERR_INVALID, "cf_ensemble_create: null member");
+        if (members[q]->dev != members[0]->dev)
+            return ens_fail(e, CF_ERR_INVALID, "cf_ensemble_create: members on different devices");
+        for (int r = 0; r < q; r++)
+            if (members[r] == members[q]) return ens_fail(e, CF_ERR_INVALID, "cf_ensemble_create: repeated member");
+    }
+    e = new cf_ensemble();
+    e->m.assign(members, members + n);
+    e->dev = members[0]->dev;
+    cudaSetDevice(e->dev);
+    cudaError_t ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
+    e->join.assign(n, nullptr);
+    for (int q = 0; q < n && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&e->join[q], cudaEventDisableTiming);
+    if (ce != cudaSuccess) {
+        int rc = ens_fail(e, CF_ERR_CUDA, std::string("cf_ensemble_create: ") + cudaGetErrorString(ce));
+        cf_ensemble_destroy(e);
+        return rc;
+    }
+    *out = e;
+    return CF_OK;
+}
+
+extern "C" int cf_ensemble_destroy(cf_ensemble *e) {
+    if (!e) return CF_OK;
+    cudaSetDevice(e->dev);
+    if (e->st) cudaStreamSynchronize(e->st);
+    for (auto &kv : e->graphs) cudaGraphExecDestroy(kv.second.first);
+    for (auto ev : e->join)
+        if (ev) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->st) cudaStreamDestroy(e->st);
+    delete e;
+    return CF_OK;
+}
+
+extern "C" int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync) {
+    if (!e) return ens_fail(e, CF_ERR_INVALID, "null ensemble");
+    ENS_CUDA(cudaSetDevice(e->dev));
+    const int n = (int)e->m.size();
+    for (int s = 0; s < nsteps; s++) {
+        // members whose ghosts are not yet filled take their first step alone
+        // (as cf_time_step_rk3 does), ordered after the ensemble's work
+        bool eager = false;
+        for (cf_ctx *c : e->m)
+            if (!c->state_periodic && c->prm.iwall_model == 0) eager = true;
+        if (eager) {
+            ENS_CUDA(cudaEventRecord(e->fork, e->st));
+            for (int q = 0; q < n; q++) {
+                cf_ctx *c = e->m[q];
+                ENS_CUDA(cudaStreamWaitEvent(c->st, e->fork, 0));
+                if (int rc = cf_time_step_rk3(c, 1, 0)) return ens_fail(e, rc, "member step: " + c->err);
+                ENS_CUDA(cudaEventRecord(e->join[q], c->st));
+                ENS_CUDA(cudaStreamWaitEvent(e->st, e->join[q], 0));
+            }
+            continue;
+        }
+        std::vector<int> key(n);
+        for (int q = 0; q < n; q++) key[q] = e->m[q]->cur;
+        auto it = e->graphs.find(key);
+        if (it == e->graphs.end()) {
+            cudaGraph_t g;
+            for (cf_ctx *c : e->m) {
+                c->launches = 0;
+                c->counting = true;
+            }
+            ENS_CUDA(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+            int rc = 0;
+            cudaError_t ce = cudaEventRecord(e->fork, e->st);
+            for (int q = 0; q < n && !rc && ce == cudaSuccess; q++) {
+                cf_ctx *c = e->m[q];
+                ce = cudaStreamWaitEvent(c->st, e->fork, 0);
+                if (ce == cudaSuccess) rc = step_eager(c);
+                if (!rc && ce == cudaSuccess) ce = cudaEventRecord(e->join[q], c->st);
+                if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(e->st, e->join[q], 0);
+            }
+            cudaError_t ee = cudaStreamEndCapture(e->st, &g);
+            std::vector<int> next(n);
+            int total = 0;
+            for (int q = 0; q < n; q++) {
+                cf_ctx *c = e->m[q];
+                c->counting = false;
+                next[q] = c->cur;
+                c->cur = key[q];
+                total += c->launches;
+            }
+            if (rc) return ens_fail(e, rc, "capture of a member step failed");
+            if (ce != cudaSuccess) return ens_fail(e, CF_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ce));
+            if (ee != cudaSuccess) return ens_fail(e, CF_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ee));
+            cudaGraphExec_t x;
+            ENS_CUDA(cudaGraphInstantiate(&x, g, 0));
+            ENS_CUDA(cudaGraphDestroy(g));
+            e->launches = total;
+            it = e->graphs.emplace(key, std::make_pair(x, next)).first;
+        }
+        ENS_CUDA(cudaGraphLaunch(it->second.first, e->st));
+        for (int q = 0; q < n; q++) {
+            e->m[q]->cur = it->second.second[q];
+            e->m[q]->old = e->m[q]->cur;
+        }
+    }
+    // the members' own streams see the ensemble's work before anything they do next
+    ENS_CUDA(cudaEventRecord(e->fork, e->st));
+    for (cf_ctx *c : e->m) ENS_CUDA(cudaStreamWaitEvent(c->st, e->fork, 0));
+    if (sync) ENS_CUDA(cudaStreamSynchronize(e->st));
+    return CF_OK;
+}
+
+extern "C" void *cf_ensemble_stream(cf_ensemble *e) { return e ? (void *)e->st : nullptr; }
+extern "C" int cf_ensemble_launches_per_step(cf_ensemble *e) { return e ? e->launches : 0; }

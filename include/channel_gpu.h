@@ -256,6 +256,24 @@ int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int judge_every);
  * served, points that fell back to eqwm. */
 int cf_get_wall_mlp_log(cf_ctx *ctx, double *out);
 
+/* ---- ensembles of independent channels ---------------------------------
+ * Members are contexts created by cf_create (any grids and parameters, one
+ * device) and stay owned by the caller.  cf_ensemble_step advances every
+ * member by nsteps steps of cf_time_step_rk3; one step of the ensemble is
+ * one CUDA graph with a branch per member, replayed (captured again only for
+ * a new combination of the members' buffer rotations), so the members run
+ * concurrently.  The ensemble's stream orders the work; the members' streams
+ * are made to wait for it before the call returns.  A member must not be
+ * used on its own while an ensemble step is in flight.  No counterpart in the
+ * reference. */
+typedef struct cf_ensemble cf_ensemble;
+int cf_ensemble_create(int n, cf_ctx *const *members, cf_ensemble **out);
+int cf_ensemble_destroy(cf_ensemble *e);
+int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync);
+void *cf_ensemble_stream(cf_ensemble *e);
+/* Kernel launches one ensemble step holds (all members). */
+int cf_ensemble_launches_per_step(cf_ensemble *e);
+
 /* ---- divergence check without device allocation ---------------------- */
 /* No counterpart in the reference: the arithmetic is check_divergence
  * (projection.f90:234-256), as in cf_check_divergence, but on caller-owned
