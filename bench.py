@@ -310,6 +310,13 @@ def run_ensemble(args, rank, world, local):
     mem = ensemble_members(cf.PREC_SPLIT, dev)
     chans = [m[0] for m in mem]
     nc = sum((c.nx - 2) * (c.ny - 1) * (c.nz - 2) for c in chans)
+    tuned = None
+    if args.autotune:
+        # each grid shape picks its own chunking on its own warmed-up state
+        tuned = []
+        for c in chans:
+            c.time_step_rk3(1)
+            tuned.append(c.autotune(reps=2))
     ens = cf.Ensemble(chans)
     ens.step(args.warmup)
     strm = torch.cuda.ExternalStream(ens.stream(), device=torch.device("cuda", dev))
@@ -375,6 +382,8 @@ def run_ensemble(args, rank, world, local):
             "config": {"workload": ENSEMBLE["name"], "members": len(chans), "grid_points": nc,
                        "retau": [m[1] for m in mem], "precision": "split",
                        "graph": "one CUDA graph per ensemble step, a branch per member",
+                       "autotune": None if tuned is None else sorted({(t["rhs_chunks"], t["dsm_chunk_len"])
+                                                                     for t in tuned}),
                        "l2": "members' working set (~2.5 GB) larger than L2; no flush needed"},
             "sequential_members": {"value": world * nc * args.steps / seq, "ms_per_step": 1e3 * seq / args.steps,
                                    "how": "each member's own graph, one member after another"},
@@ -455,6 +464,7 @@ def run_ours(args, wl, rank, world, local):
     ncmp = max(args.warmup, 3)
     ch.time_step_rk3(ncmp)
     ch64.time_step_rk3(ncmp)
+    tuned = ch.autotune(reps=3) if args.autotune else None
     s32, s64 = ch.statistics(), ch64.statistics()
     ny = wl["ny"]
     prof_err = {}
@@ -563,7 +573,7 @@ def run_ours(args, wl, rank, world, local):
                        "precision": "split", "dt_rule": "reference compute_dt (CFL 0.5 -> 5e-3 cap)",
                        "l2": "working set (~1 GB) larger than L2 (129 MB); no flush needed",
                        "replicas": world, "graph": "one CUDA graph per step",
-                       "sgs_recompute": True},
+                       "sgs_recompute": True, "autotune": tuned},
             "fp64": {"value": v64, "ms_per_step": ms64 / k64, "steps": k64},
             "split_over_fp64": value / v64,
             "stats_err_vs_fp64": {"steps": ncmp, **prof_err},
@@ -600,6 +610,8 @@ def main():
     ap.add_argument("--precision", default="split", choices=["split", "fp64"])
     ap.add_argument("--kernel-table", action="store_true",
                     help="with --profile-steps: also print per-kernel event times of two more steps")
+    ap.add_argument("--autotune", type=int, default=1,
+                    help="1: tune the z-chunk counts of the marching kernels on the warmed-up state (cf_autotune)")
     ap.add_argument("--stats-run", type=int, default=0,
                     help="only run the long-run statistics comparison of the split and FP64 paths over N steps")
     ap.add_argument("--stats-every", type=int, default=10)

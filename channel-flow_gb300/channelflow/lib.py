@@ -356,6 +356,15 @@ class Channel:
         w("------------------------------------------------------", "")
         return m
 
+    def autotune(self, reps: int = 3) -> dict:
+        """cf_autotune: times every admissible z-chunk count of the marching
+        kernels on the current state and keeps the fastest."""
+        self.L.cf_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        out = np.zeros(6)
+        self._check(self.L.cf_autotune(self.h, reps, _dp(out)))
+        return dict(rhs_chunks=int(out[0]), rhs_us=out[1], dsm_chunk_len=int(out[2]), dsm_us=out[3],
+                    amd_chunks=int(out[4]), amd_us=out[5])
+
     def set_wall_mlp(self, net, judge_every: int = 100):
         """Serves the wall stress of the equilibrium wall model from a trained
         channelflow.wallmlp.WallMLP (eqwm outside its envelope); every

@@ -513,6 +513,7 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     }
     size_t nch = std::max({(size_t)ctx->dsm_nblk, nch_fused, (size_t)cdiv(amd_parts, 2)});
     CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));
+    ctx->dsm_part_nch = nch;
     // avg_nu_t (1..nyg) in FP64, followed by an FP32 copy
     CF_CUDA(cudaMalloc(&ctx->avg_nu_t, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
     CF_CUDA(cudaMemset(ctx->avg_nu_t, 0, (size_t)(2 * ctx->nyg + 4) * sizeof(double)));
@@ -1391,3 +1392,111 @@ extern "C" int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync) {
 
 extern "C" void *cf_ensemble_stream(cf_ensemble *e) { return e ? (void *)e->st : nullptr; }
 extern "C" int cf_ensemble_launches_per_step(cf_ensemble *e) { return e ? e->launches : 0; }
+
+// ---------------------------------------------------------------------------
+// Autotuner: the z-chunk counts of the marching kernels (fused right-hand
+// side, fused dynamic Smagorinsky pass, AMD pass) chosen by timing every
+// admissible candidate on the current state, instead of the analytic wave
+// plans of cf_create.  The timed launches are the step's own (the RK update
+// of substep 1 into a scratch buffer, the eddy viscosity of the current
+// state), so the state is unchanged; the captured steps are dropped.
+// ---------------------------------------------------------------------------
+template <typename T>
+static int tune_t(cf_ctx *ctx, int reps, double *rep) {
+    cudaEvent_t e0, e1;
+    CF_CUDA(cudaEventCreate(&e0));
+    CF_CUDA(cudaEventCreate(&e1));
+    auto timed = [&](auto &&launch, double *us) -> int {
+        if (int rc = launch()) return rc;  // warm-up
+        CF_CUDA(cudaEventRecord(e0, ctx->st));
+        for (int q = 0; q < reps; q++)
+            if (int rc = launch()) return rc;
+        CF_CUDA(cudaEventRecord(e1, ctx->st));
+        CF_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CF_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        *us = 1e3 * ms / reps;
+        return 0;
+    };
+    const int X = ctx->cur, a = (X + 1) % 3, old = ctx->old;
+    const int nzp = ctx->nzp;
+    int rc = 0;
+    // fused right-hand side + RK update (substep 1, X -> a)
+    {
+        ctx->old = X;
+        const int keep = ctx->rhs_nkc;
+        double best = 1e300;
+        int best_n = keep;
+        int last_len = -1;
+        for (int nn = 1; nn <= std::max(1, nzp / 4) && !rc; nn++) {
+            const int len = cdiv(nzp, nn);
+            if (len == last_len) continue;
+            last_len = len;
+            ctx->rhs_nkc = nn;
+            double us = 0;
+            rc = timed([&] { return launch_rhs_update<T>(ctx, 1, X, a); }, &us);
+            if (!rc && us < best) { best = us; best_n = nn; }
+        }
+        ctx->rhs_nkc = rc ? keep : best_n;
+        ctx->old = old;
+        rep[0] = ctx->rhs_nkc;
+        rep[1] = best;
+    }
+    // the eddy-viscosity pass
+    if (!rc && ctx->prm.LES_model == 2 && ctx->use_fused_dsm && ctx->prm.iwall_model == 0 && ctx->state_periodic) {
+        const int keep = ctx->dsm_kc;
+        const int ntx = cdiv(ctx->nxp, sizeof(T) == 4 ? 32 : 16);
+        double best = 1e300;
+        int best_kc = keep, last_len = -1;
+        for (int nn = cdiv(nzp, DSM_ZMAX_HOST); nn <= std::max(1, nzp / 4) && !rc; nn++) {
+            const int len = cdiv(nzp, nn);
+            if (len == last_len || (size_t)ntx * cdiv(nzp, len) > ctx->dsm_part_nch) continue;
+            last_len = len;
+            ctx->dsm_kc = len;
+            double us = 0;
+            rc = timed([&] { return launch_dsm<T>(ctx, X); }, &us);
+            if (!rc && us < best) { best = us; best_kc = len; }
+        }
+        ctx->dsm_kc = rc ? keep : best_kc;
+        if (!rc) rc = launch_dsm<T>(ctx, X);  // the current state's eddy viscosity with the chosen plan
+        rep[2] = ctx->dsm_kc;
+        rep[3] = best;
+    } else if (!rc && ctx->prm.LES_model == 3) {
+        const int keep = ctx->amd_nkc;
+        double best = 1e300;
+        int best_n = keep, last_len = -1;
+        for (int nn = 1; nn <= std::max(1, nzp / 4) && !rc; nn++) {
+            const int len = cdiv(nzp, nn);
+            if (len == last_len || (size_t)amd_partials_for(ctx, nn) > 2 * ctx->dsm_part_nch) continue;
+            last_len = len;
+            ctx->amd_nkc = nn;
+            double us = 0;
+            rc = timed([&] { return launch_amd<T>(ctx, X); }, &us);
+            if (!rc && us < best) { best = us; best_n = nn; }
+        }
+        ctx->amd_nkc = rc ? keep : best_n;
+        if (!rc) rc = launch_amd<T>(ctx, X);
+        rep[4] = ctx->amd_nkc;
+        rep[5] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+extern "C" int cf_autotune(cf_ctx *ctx, int reps, double *report) {
+    if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
+    if (reps < 1) return cf_fail(ctx, CF_ERR_INVALID, "reps must be >= 1");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    double rep[6] = {(double)ctx->rhs_nkc, 0, (double)ctx->dsm_kc, 0, (double)ctx->amd_nkc, 0};
+    TRY(DISPATCH(tune_t<double>(ctx, reps, rep), tune_t<float>(ctx, reps, rep)));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    for (auto &g : ctx->graphs)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    if (report) std::copy(rep, rep + 6, report);
+    return CF_OK;
+}

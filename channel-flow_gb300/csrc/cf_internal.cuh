@@ -188,6 +188,7 @@ struct cf_ctx {
     bool use_rhs3 = true;              // one fused RHS + update launch per substep
     int rhs_nkc = 1;                   // z chunks of the fused RHS
     int amd_nkc = 1;                   // z chunks of the AMD pass
+    size_t dsm_part_nch = 0;           // plane-partial slots per row allocated in dsm_part
     int amd_nparts = 0;                // partial sums per row of the last AMD pass
     bool amd_avg_pending = false;      // avg_nu_t not yet formed from them
     bool state_periodic = false;       // U, V, W satisfy the periodic/no-slip ghost identities
@@ -266,6 +267,8 @@ template <typename T> int launch_pressure(cf_ctx *ctx, int buf);  // actual pres
 template <typename T> int launch_amd(cf_ctx *ctx, int buf);  // AMD eddy viscosity (subgrid.f90:639)
 void amd_plan(int esz, int nxp, int nym, int nzp, int sms, int *nkc, int *nparts);  // z chunks of the AMD pass
 int launch_avg_nu_t_flush(cf_ctx *ctx);  // AMD plane means of the last pass, if not formed yet
+int amd_partials_for(cf_ctx *ctx, int nkc);  // plane partials per row of an AMD pass with nkc z chunks
+constexpr int DSM_ZMAX_HOST = 256;           // planes per z chunk of the fused DSM pass at most
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only

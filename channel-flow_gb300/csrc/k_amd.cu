@@ -311,6 +311,8 @@ int launch_amd(cf_ctx *ctx, int b) {
     return 0;
 }
 
+int amd_partials_for(cf_ctx *ctx, int nkc) { return cdiv(ctx->nxp, AMD_TX) * cdiv(ctx->nzp, cdiv(ctx->nzp, nkc)); }
+
 int launch_avg_nu_t_flush(cf_ctx *ctx) {
     if (!ctx->amd_avg_pending) return 0;
     k_amd_avg<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, ctx->amd_nparts, ctx->nyg,

@@ -48,7 +48,7 @@ struct RGeo {  // reciprocal spacings, 1-based like the coordinates
 };
 
 // planes per z chunk at most (their z spacings sit in static shared memory)
-constexpr int DSM_ZMAX = 256;
+constexpr int DSM_ZMAX = DSM_ZMAX_HOST;
 
 template <typename T, int TX, int TY>
 struct DsmSmem {

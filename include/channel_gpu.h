@@ -160,6 +160,15 @@ int cf_launches_per_step(cf_ctx *ctx);
 int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
                      int *n_names);
 
+/* Empirical tuning of the z-chunk counts of the marching kernels (fused
+ * right-hand side, fused dynamic Smagorinsky pass or AMD pass) on the
+ * current state: every admissible count is timed (reps launches each, CUDA
+ * events) and the fastest kept; the state is unchanged.  report (6 doubles,
+ * may be NULL): chosen right-hand-side chunks and its microseconds, chosen
+ * DSM chunk length and its microseconds, chosen AMD chunks and its
+ * microseconds (0 where not tuned).  Call after at least one step. */
+int cf_autotune(cf_ctx *ctx, int reps, double *report);
+
 /* ---- statistics (statistics.f90:22-171) ------------------------------ */
 /* out: 9 profiles of length ny (Umean, Vmean, Wmean, U2mean, V2mean, W2mean,
  * UVmean, Pmean, P2mean) followed by utau, Retau, Qflow_x, Qflow_y,

@@ -473,3 +473,36 @@ def test_ensemble_members_match_single_runs():
         ens.close()
         for m in members:
             m.close()
+
+
+@pytest.mark.parametrize("les", [2, 3])
+def test_autotune_keeps_the_state(les):
+    """cf_autotune on a running channel: the chosen chunk counts are
+    admissible, the timed launches leave the state as it was, and the run
+    continues to the same fields up to the order of the plane sums."""
+    import channelflow as cf
+    case = channel_case(*CASES["config1"], les=les)
+    runs = []
+    for tune in (False, True):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_FP64, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        ch.set_fixed_dt(case["dt"])
+        ch.time_step_rk3(2)
+        if tune:
+            before = ch.download()
+            rep = ch.autotune(reps=2)
+            after = ch.download()
+            for n in ("U", "V", "W"):
+                assert np.array_equal(before[n], after[n]), n
+            assert rep["rhs_chunks"] >= 1 and rep["rhs_us"] > 0
+            if les == 2:
+                assert 1 <= rep["dsm_chunk_len"] <= 64 and rep["dsm_us"] > 0
+            else:
+                assert rep["amd_chunks"] >= 1 and rep["amd_us"] > 0
+        ch.time_step_rk3(3)
+        runs.append(ch.download())
+        ch.close()
+    for n in ("U", "V", "W", "nu_t"):
+        assert rel_err(runs[1][n], runs[0][n]) < 1e-12, n
