@@ -94,7 +94,6 @@ static int alloc_all(cf_ctx *ctx) {
     TRY(alloc<T>(ctx, &ctx->F[0][2], ctx->nW));
     if (ctx->prm.LES_model == 2) {
         TRY(alloc<T>(ctx, &ctx->dsm_q, 16 * ctx->nCan));
-        TRY(alloc<T>(ctx, &ctx->dsm_lf, 12 * ctx->nCan));
         TRY(alloc<T>(ctx, &ctx->Uf, ctx->nU));
         TRY(alloc<T>(ctx, &ctx->Vf, ctx->nV));
         TRY(alloc<T>(ctx, &ctx->Wf, ctx->nW));
@@ -545,7 +544,7 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
     for (auto e : ctx->pev) cudaEventDestroy(e);
     for (auto &g : ctx->graphs)
         if (g) cudaGraphExecDestroy(g);
-    void *ptrs[] = {ctx->nut, ctx->P, ctx->dsm_q, ctx->dsm_lf, ctx->Uf, ctx->Vf, ctx->Wf, ctx->dsm_part, ctx->avg_nu_t,
+    void *ptrs[] = {ctx->nut, ctx->P, ctx->dsm_q, ctx->Uf, ctx->Vf, ctx->Wf, ctx->dsm_part, ctx->avg_nu_t,
                     ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->tri_l32, ctx->tri_ru32,
                     ctx->tri_du32, ctx->tri_flag, ctx->tri_list, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
                     ctx->wtemp1, ctx->wtemp2, ctx->eq_grid, ctx->eq_zst, ctx->eq_xst, ctx->eq_zw, ctx->eq_xw, ctx->ds,

@@ -113,15 +113,21 @@ __host__ __device__ __forceinline__ int wrapc(int i, int np) {
 
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
-// compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual indices.
+// compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual
+// indices.  FP64 divides by the spacings as the reference does; FP32 (the
+// split path) multiplies by the stored reciprocal spacings rc.
 template <typename T>
-__device__ __forceinline__ void sij_point(const GeoT<T> &g, const Fld<T> &U, const Fld<T> &V, const Fld<T> &W, int i,
-                                          int j, int k, T s[6], T &S) {
+__device__ __forceinline__ void sij_point(const GeoT<T> &g, const RcpT<T> &rc, const Fld<T> &U, const Fld<T> &V,
+                                          const Fld<T> &W, int i, int j, int k, T s[6], T &S) {
     const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg;
     const T h = T(0.5), q = T(0.25);
-    s[0] = (U(i, j, k) - U(i - 1, j, k)) / (x[i] - x[i - 1]);
-    s[1] = (V(i, j, k) - V(i, j - 1, k)) / (y[j] - y[j - 1]);
-    s[2] = (W(i, j, k) - W(i, j, k - 1)) / (z[k] - z[k - 1]);
+    auto quo = [&](T a, const T *c, const T *r, int e) -> T {
+        if constexpr (sizeof(T) == 8) return a / (c[e] - c[e - 1]);
+        else return a * r[e];
+    };
+    s[0] = quo(U(i, j, k) - U(i - 1, j, k), x, rc.dx, i);
+    s[1] = quo(V(i, j, k) - V(i, j - 1, k), y, rc.dy, j);
+    s[2] = quo(W(i, j, k) - W(i, j, k - 1), z, rc.dz, k);
     T e4[2][2], e5[2][2], e6[2][2];
 #pragma unroll
     for (int a = 0; a < 2; a++)
@@ -129,13 +135,13 @@ __device__ __forceinline__ void sij_point(const GeoT<T> &g, const Fld<T> &U, con
         for (int b = 0; b < 2; b++) {
             int ii = i + a, jj = j + b, kk = k + b;
             // edge values at (ii, jj, k), (ii, j, kk), (i, j+a, k+b)
-            e4[a][b] = h * ((U(ii - 1, jj, k) - U(ii - 1, jj - 1, k)) / (yg[jj] - yg[jj - 1]) +
-                            (V(ii, jj - 1, k) - V(ii - 1, jj - 1, k)) / (xg[ii] - xg[ii - 1]));
-            e5[a][b] = h * ((U(ii - 1, j, kk) - U(ii - 1, j, kk - 1)) / (zg[kk] - zg[kk - 1]) +
-                            (W(ii, j, kk - 1) - W(ii - 1, j, kk - 1)) / (xg[ii] - xg[ii - 1]));
+            e4[a][b] = h * (quo(U(ii - 1, jj, k) - U(ii - 1, jj - 1, k), yg, rc.dyg, jj) +
+                            quo(V(ii, jj - 1, k) - V(ii - 1, jj - 1, k), xg, rc.dxg, ii));
+            e5[a][b] = h * (quo(U(ii - 1, j, kk) - U(ii - 1, j, kk - 1), zg, rc.dzg, kk) +
+                            quo(W(ii, j, kk - 1) - W(ii - 1, j, kk - 1), xg, rc.dxg, ii));
             int j6 = j + a, k6 = k + b;
-            e6[a][b] = h * ((V(i, j6 - 1, k6) - V(i, j6 - 1, k6 - 1)) / (zg[k6] - zg[k6 - 1]) +
-                            (W(i, j6, k6 - 1) - W(i, j6 - 1, k6 - 1)) / (yg[j6] - yg[j6 - 1]));
+            e6[a][b] = h * (quo(V(i, j6 - 1, k6) - V(i, j6 - 1, k6 - 1), zg, rc.dzg, k6) +
+                            quo(W(i, j6, k6 - 1) - W(i, j6 - 1, k6 - 1), yg, rc.dyg, j6));
         }
     s[3] = q * (e4[0][0] + e4[1][0] + e4[0][1] + e4[1][1]);
     s[4] = q * (e5[0][0] + e5[1][0] + e5[0][1] + e5[1][1]);
@@ -177,7 +183,6 @@ struct cf_ctx {
     void *F[3][3] = {};                // [slot 0..2][comp]
     // eddy viscosity
     void *dsm_q = nullptr;             // 16 canonical arrays
-    void *dsm_lf = nullptr;            // 12 canonical arrays (L and hat(|S|Sij))
     void *Uf = nullptr, *Vf = nullptr, *Wf = nullptr;
     double *dsm_part = nullptr;        // plane partial sums
     double *avg_nu_t = nullptr;        // (nyg) device

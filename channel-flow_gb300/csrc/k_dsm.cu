@@ -8,10 +8,11 @@
 // i = 2..nxg-1, k = 2..nzg-1 like the reference, i.e. the duplicate column
 // i = nxg-1 and row k = nzg-1 (copies of i = 2, k = 2) are counted twice;
 // here that is a weight 2 on the canonical column/row 2.
+#include <algorithm>
+
 #include "cf_internal.cuh"
 
 enum { Q_UC = 0, Q_VC, Q_WC, Q_UU, Q_VV, Q_WW, Q_UV, Q_UW, Q_VW, Q_SS1, Q_SS2, Q_SS3, Q_SS4, Q_SS5, Q_SS6, Q_S, NQ };
-enum { L_1 = 0, L_6 = 5, FSS_1 = 6, NLF = 12 };
 
 struct Can {
     int nxp, nym, nzp;
@@ -23,7 +24,7 @@ struct Can {
 
 // Stage A: centre velocities, products and |S| S_ij at canonical centres.
 template <typename T>
-__global__ void k_dsm_a(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, T *q, Can c) {
+__global__ void k_dsm_a(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, T *q, Can c) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
     int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
     int k = blockIdx.z + 2;
@@ -44,7 +45,7 @@ __global__ void k_dsm_a(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, T *q, Can c) {
     q[o + Q_UW * n] = uc * wc;
     q[o + Q_VW * n] = vc * wc;
     T s[6], S;
-    sij_point<T>(g, U, V, W, i, j, k, s, S);
+    sij_point<T>(g, rc, U, V, W, i, j, k, s, S);
 #pragma unroll
     for (int a = 0; a < 6; a++) q[o + (Q_SS1 + a) * n] = S * s[a];
     q[o + Q_S * n] = S;
@@ -77,22 +78,101 @@ __device__ __forceinline__ T filt_can(const T *q, const Can &c, int nyg, int i, 
     return acc;
 }
 
-// Stage B: L_ij = hat(ui uj) - hat(ui) hat(uj) and hat(|S| S_ij).
+// Stages B and D: L_ij = hat(ui uj) - hat(ui) hat(uj) and hat(|S| S_ij)
+// (the filter of 15 canonical quantities), then M_ij = 4 |S(Uf)| S_ij(Uf) -
+// hat(|S| S_ij) and the plane partial sums of L.M and M.M
+// (subgrid.f90:429-513).  A block owns a DB_X x DB_Y tile of (i, j) and
+// marches along z over a chunk of planes: each plane of the 15 quantities
+// (tile plus one halo cell, periodic in x, rows clamped to the interior) is
+// staged in shared memory, every thread forms the x-y filter at its point and
+// spreads it over the z accumulators of planes r-1, r, r+1 (weights 1/6,
+// 2/3, 1/6), so that plane r-1 is complete once plane r is in.  The filtered
+// velocities Uf, Vf, Wf (stage C) are read at their actual indices.  The
+// plane sums count the duplicate column and plane as weight 2 on i = 2 and
+// k = 2 (the reference's loops run over i = 2..nxg-1, k = 2..nzg-1).
+constexpr int DB_X = 32, DB_Y = 8, DB_NQ = 15;
+
 template <typename T>
-__global__ void k_dsm_b(const T *q, T *lf, Can c, int nx, int nyg) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
-    int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
-    int k = blockIdx.z + 2;
-    if (i > nx - 1 || j > nyg - 1) return;
-    long o = c(i, j, k), n = c.n;
-    T fu = filt_can<T>(q + Q_UC * n, c, nyg, i, j, k);
-    T fv = filt_can<T>(q + Q_VC * n, c, nyg, i, j, k);
-    T fw = filt_can<T>(q + Q_WC * n, c, nyg, i, j, k);
-    const T fa[6] = {fu, fv, fw, fu, fu, fv}, fb[6] = {fu, fv, fw, fv, fw, fw};
+__global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, GeoT<T> g, RcpT<T> rc, Fld<T> Uf,
+                                                      Fld<T> Vf, Fld<T> Wf, Can c, int nyg, int kc_len, double *part,
+                                                      int nchunk) {
+    constexpr int SX = DB_X + 2, SY = DB_Y + 2, NP = SX * SY;
+    __shared__ T pl[DB_NQ][NP];
+    __shared__ double red[2][DB_X * DB_Y];
+    const int tx = threadIdx.x % DB_X, ty = threadIdx.x / DB_X;
+    const int i0 = 2 + blockIdx.x * DB_X, j0 = 2 + blockIdx.y * DB_Y;
+    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, c.nzp + 1);
+    const int i = i0 + tx, j = j0 + ty;
+    const bool own = i <= c.nxp + 1 && j <= nyg - 1;
+    const long n = c.n;
+    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
+    // y weights of this row (one-sided at rows 2 and nyg-1)
+    T wm = f6, w0 = f23, wp = f6;
+    if (j == 2) { wm = T(0); wp = f13; }
+    else if (j == nyg - 1) { wm = f13; wp = T(0); }
+    const T fw[3] = {f6, f23, f6};
+    T accp[DB_NQ], accc[DB_NQ];  // planes r-1 (two contributions in) and r (one)
 #pragma unroll
-    for (int a = 0; a < 6; a++) lf[o + (L_1 + a) * n] = filt_can<T>(q + (Q_UU + a) * n, c, nyg, i, j, k) - fa[a] * fb[a];
+    for (int qq = 0; qq < DB_NQ; qq++) accp[qq] = accc[qq] = T(0);
+    double sl = 0.0, smm = 0.0;
+    for (int r = kb - 1; r <= ke + 1; r++) {
+        const int rc_ = wrapn(r, c.nzp);
+        __syncthreads();  // the previous plane is no longer read
+        for (int e = threadIdx.x; e < NP; e += DB_X * DB_Y) {
+            const int sy = e / SX, sx = e - sy * SX;
+            // columns past the domain's last halo are never read: clamp them in range
+            const int ii = wrapn(min(i0 + sx - 1, c.nxp + 2), c.nxp), jj = min(max(j0 + sy - 1, 2), nyg - 1);
+            const long o = c(ii, jj, rc_);
 #pragma unroll
-    for (int a = 0; a < 6; a++) lf[o + (FSS_1 + a) * n] = filt_can<T>(q + (Q_SS1 + a) * n, c, nyg, i, j, k);
+            for (int qq = 0; qq < DB_NQ; qq++) pl[qq][e] = q[o + qq * n];
+        }
+        __syncthreads();
+        if (!own) continue;
+        const int e = (ty + 1) * SX + tx + 1;
+        T fq[DB_NQ];
+#pragma unroll
+        for (int qq = 0; qq < DB_NQ; qq++) {
+            T a = T(0);
+#pragma unroll
+            for (int d = -1; d <= 1; d++)
+                a += fw[d + 1] * (wm * pl[qq][e + d - SX] + w0 * pl[qq][e + d] + wp * pl[qq][e + d + SX]);
+            fq[qq] = accp[qq] + f6 * a;  // plane r-1, complete
+            accp[qq] = accc[qq] + f23 * a;
+            accc[qq] = f6 * a;
+        }
+        const int k = r - 1;
+        if (k < kb) continue;
+        // M from S_ij of the filtered velocities (fil_size**2 = 4, subgrid.f90:156, 463)
+        T sf[6], Sf;
+        sij_point<T>(g, rc, Uf, Vf, Wf, i, j, k, sf, Sf);
+        const T fu = fq[0], fv = fq[1], fwv = fq[2];
+        const T pa[6] = {fu, fv, fwv, fu, fu, fv}, pb[6] = {fu, fv, fwv, fv, fwv, fwv};
+        T L[6], M[6];
+#pragma unroll
+        for (int a = 0; a < 6; a++) {
+            L[a] = fq[3 + a] - pa[a] * pb[a];
+            M[a] = T(4) * Sf * sf[a] - fq[9 + a];
+        }
+        const T lm = (L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + T(2) * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]));
+        const T mm = (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + T(2) * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]));
+        const double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
+        sl += wgt * (double)lm;
+        smm += wgt * (double)mm;
+    }
+    // plane partials of this block for row j: the sum over the tile's DB_X threads of the row
+    red[0][threadIdx.x] = sl;
+    red[1][threadIdx.x] = smm;
+    __syncthreads();
+    if (tx == 0 && j <= nyg - 1) {
+        double a = 0.0, b = 0.0;
+        for (int t = 0; t < DB_X; t++) {
+            a += red[0][ty * DB_X + t];
+            b += red[1][ty * DB_X + t];
+        }
+        const long chunk = (long)blockIdx.z * gridDim.x + blockIdx.x;
+        part[((long)(j - 2) * nchunk + chunk) * 2] = a;
+        part[((long)(j - 2) * nchunk + chunk) * 2 + 1] = b;
+    }
 }
 
 // Stage C: filtered velocities Uf, Vf, Wf (subgrid.f90:431-445) at every
@@ -126,47 +206,6 @@ __global__ void k_dsm_c(Fld<T> A, Fld<T> Af, int n1, int n2, int n3, int nxp, in
         acc += fw[a + 1] * sz;
     }
     Af(i, j, k) = acc;
-}
-
-// Stage D: M_ij, L.M and M.M with the plane partial sums.
-// Grid: x = chunks of the (i,k) plane, y = j.
-template <typename T>
-__global__ void k_dsm_d(GeoT<T> g, Fld<T> Uf, Fld<T> Vf, Fld<T> Wf, const T *lf, Can c, double *part, int nchunk) {
-    __shared__ double shl[32], shm[32];
-    int j = blockIdx.y + 2;
-    long nik = (long)c.nxp * c.nzp;
-    double sl = 0.0, sm = 0.0;
-    for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < nik; t += (long)gridDim.x * blockDim.x) {
-        int i = (int)(t % c.nxp) + 2, k = (int)(t / c.nxp) + 2;
-        long o = c(i, j, k), n = c.n;
-        T s[6], S;
-        sij_point<T>(g, Uf, Vf, Wf, i, j, k, s, S);
-        const T fs2 = T(4);  // fil_size**2, fil_size = 2 (subgrid.f90:156)
-        T M[6], L[6];
-#pragma unroll
-        for (int a = 0; a < 6; a++) {
-            M[a] = fs2 * S * s[a] - lf[o + (FSS_1 + a) * n];
-            L[a] = lf[o + (L_1 + a) * n];
-        }
-        T lm = (L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + T(2) * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]));
-        T mm = (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + T(2) * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]));
-        double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
-        sl += wgt * (double)lm;
-        sm += wgt * (double)mm;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        sl += __shfl_down_sync(0xffffffff, sl, o);
-        sm += __shfl_down_sync(0xffffffff, sm, o);
-    }
-    int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { shl[w] = sl; shm[w] = sm; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int q = 0; q < (int)(blockDim.x >> 5); q++) { a += shl[q]; b += shm[q]; }
-        part[((long)(j - 2) * nchunk + blockIdx.x) * 2] = a;
-        part[((long)(j - 2) * nchunk + blockIdx.x) * 2 + 1] = b;
-    }
 }
 
 // Stage E: avg_nu_t(j) = <LM>/<MM> (subgrid.f90:516-518) and its ghosts.
@@ -274,12 +313,11 @@ int launch_dsm(cf_ctx *ctx, int b) {
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
     Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
-    T *q = (T *)ctx->dsm_q, *lf = (T *)ctx->dsm_lf;
+    T *q = (T *)ctx->dsm_q;
+    const RcpT<T> rc = rcp_of<T>(ctx);
     dim3 grdc(cdiv(ctx->nxp, 32), cdiv(ctx->nym, 4), ctx->nzp);
-    k_dsm_a<T><<<grdc, blk, 0, ctx->st>>>(g, U, V, W, q, c);
+    k_dsm_a<T><<<grdc, blk, 0, ctx->st>>>(g, rc, U, V, W, q, c);
     count_launch(ctx, "k_dsm_a");
-    k_dsm_b<T><<<grdc, blk, 0, ctx->st>>>(q, lf, c, ctx->nx, ctx->nyg);
-    count_launch(ctx, "k_dsm_b");
     Fld<T> Uf = make_fld<T>(ctx->Uf, ctx->nx, ctx->nyg);
     Fld<T> Vf = make_fld<T>(ctx->Vf, ctx->nxg, ctx->ny);
     Fld<T> Wf = make_fld<T>(ctx->Wf, ctx->nxg, ctx->nyg);
@@ -287,9 +325,20 @@ int launch_dsm(cf_ctx *ctx, int b) {
     k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->ny, 4), ctx->nzg), blk, 0, ctx->st>>>(V, Vf, ctx->nxg, ctx->ny, ctx->nzg, ctx->nxp, ctx->nzp);
     k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nz), blk, 0, ctx->st>>>(W, Wf, ctx->nxg, ctx->nyg, ctx->nz, ctx->nxp, ctx->nzp);
     count_launch(ctx, "k_dsm_c"); count_launch(ctx, "k_dsm_c"); count_launch(ctx, "k_dsm_c");
-    int nchunk = ctx->dsm_nblk;
-    k_dsm_d<T><<<dim3(nchunk, ctx->nym), 256, 0, ctx->st>>>(g, Uf, Vf, Wf, lf, c, ctx->dsm_part, nchunk);
-    count_launch(ctx, "k_dsm_d");
+    int nchunk;
+    {
+        // z chunks: about two waves of 256-thread tiles, within the plane-partial slots
+        const int ntx = cdiv(ctx->nxp, DB_X);
+        const long tiles = (long)ntx * cdiv(ctx->nym, DB_Y);
+        long nkc = std::max(1L, std::min((long)ctx->nzp / 4, (2L * 152 * 4 + tiles - 1) / tiles));
+        nkc = std::max(1L, std::min(nkc, (long)ctx->dsm_part_nch / ntx));
+        const int kc_len = cdiv(ctx->nzp, nkc);
+        const int nz_chunks = cdiv(ctx->nzp, kc_len);
+        nchunk = ntx * nz_chunks;
+        k_dsm_b<T><<<dim3(ntx, cdiv(ctx->nym, DB_Y), nz_chunks), DB_X * DB_Y, 0, ctx->st>>>(
+            q, g, rc, Uf, Vf, Wf, c, ctx->nyg, kc_len, ctx->dsm_part, nchunk);
+        count_launch(ctx, "k_dsm_b");
+    }
     k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
     count_launch(ctx, "k_dsm_e");
     Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);

@@ -126,13 +126,16 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
             double nu_eq = mu_lam / rho;
             double utau = sqrt(tau / rho);
             double c1 = rho * kappa * utau;
+            // y utau / nu / A+ of eqwm.f90:134-136 with the per-pass factor
+            // formed once (two FP64 divisions less per cell)
+            const double cd = utau / nu_eq / Aplus;
             double al = u_les, be = 0.0;
             double yf = yfa[ncv];
-            double D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
+            double D = 1.0 - exp(-(yf * cd));
             double mu_up = mu_lam + c1 * yf * (D * D);
             for (int q = ncv - 1; q >= 2; q--) {
                 yf = yfa[q];
-                D = 1.0 - exp(-1.0 * yf * utau / nu_eq / Aplus);
+                D = 1.0 - exp(-(yf * cd));
                 double mu_q = mu_lam + c1 * yf * (D * D);
                 double sup = mu_up * idcv[q];
                 double sub = mu_q * idcv[q - 1];

@@ -71,13 +71,14 @@ __global__ void k_eqwm_batch(int n, const double *u, const double *h, const doub
         const double tau_prev = tw;
         const double utau = sqrt(tw);
         const double c1 = kappa * utau;
+        const double cd = utau / mu_lam / Aplus;
         double al = u_les, be = 0.0;
         double yf = ufa[ncv] * h_wm;
-        double D = 1.0 - exp(-1.0 * yf * utau / mu_lam / Aplus);
+        double D = 1.0 - exp(-(yf * cd));
         double mu_up = mu_lam + c1 * yf * (D * D);
         for (int q = ncv - 1; q >= 2; q--) {
             yf = ufa[q] * h_wm;
-            D = 1.0 - exp(-1.0 * yf * utau / mu_lam / Aplus);
+            D = 1.0 - exp(-(yf * cd));
             const double mu_q = mu_lam + c1 * yf * (D * D);
             const double sup = mu_up / (ucv[q + 1] * h_wm - ucv[q] * h_wm);
             const double sub = mu_q / (ucv[q] * h_wm - ucv[q - 1] * h_wm);
