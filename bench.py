@@ -73,12 +73,10 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
         "k_amd": 4 * nC * es,
         # 3 velocity components in, |S| Sij (6), products (6), centre velocities (3), |S| out
         "k_dsm_a": (3 + 16) * nC * es,
-        # 15 filtered inputs, 12 outputs
-        "k_dsm_b": (15 + 12) * nC * es,
+        # 15 filtered quantities and Uf, Vf, Wf in (L, M and the plane sums formed in place)
+        "k_dsm_b": (15 + 3) * nC * es,
         # one velocity component in and out
         "k_dsm_c": 2 * nC * es,
-        # Uf, Vf, Wf and 12 L/hat(|S|Sij) arrays in
-        "k_dsm_d": (3 + 12) * nC * es,
         "k_dsm_f": 2 * nC * es,
         # U, V, W, nu_t, Uo (+ lo), F1 in; out + F1 (substep 1 of 3 stores it)
         # one component: U, V, W, nu_t, Uo (+ its low word) and F1 in, the new
