@@ -315,7 +315,7 @@ def run_ensemble(args, rank, world, local):
         for c in chans:
             c.time_step_rk3(1)
             tuned.append(c.autotune(reps=2))
-    ens = cf.Ensemble(chans)
+    ens = cf.Ensemble(chans, batched_tri=True)
     ens.step(args.warmup)
     strm = torch.cuda.ExternalStream(ens.stream(), device=torch.device("cuda", dev))
     torch.cuda.synchronize()
@@ -379,7 +379,8 @@ def run_ensemble(args, rank, world, local):
             "vs_baseline": None, "dtype": "f32+f64 (split)", "data": "synthetic (16 seeded perturbed laminar fields)",
             "config": {"workload": ENSEMBLE["name"], "members": len(chans), "grid_points": nc,
                        "retau": [m[1] for m in mem], "precision": "split",
-                       "graph": "one CUDA graph per ensemble step, a branch per member",
+                       "graph": "one CUDA graph per ensemble step, a branch per member; the tridiagonal "
+                                "systems of all members in one FP64 launch per substep",
                        "autotune": None if tuned is None else sorted({(t["rhs_chunks"], t["dsm_chunk_len"])
                                                                      for t in tuned}),
                        "l2": "members' working set (~2.5 GB) larger than L2; no flush needed"},

@@ -442,13 +442,15 @@ class Channel:
 
 class Ensemble:
     """Independent channels advanced together: one CUDA graph per ensemble
-    step with a branch per member (cf_ensemble_*).  The members stay usable
-    as Channel objects between steps."""
+    step with a branch per member (cf_ensemble_*), the tridiagonal systems of
+    all members solved by one FP64 launch per substep (batched_tri).  The
+    members stay usable as Channel objects between steps."""
 
-    def __init__(self, members):
+    def __init__(self, members, batched_tri: bool = True):
         self.L = load()
         L = self.L
         vp = C.c_void_p
+        L.cf_ensemble_set_batched_tri.argtypes = [vp, C.c_int]
         L.cf_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(vp)]
         L.cf_ensemble_destroy.argtypes = [vp]
         L.cf_ensemble_step.argtypes = [vp, C.c_int, C.c_int]
@@ -462,6 +464,7 @@ class Ensemble:
         if rc != 0:
             raise CfError(L.cf_last_error(None).decode() or f"cf_ensemble_create failed ({rc})")
         self.h = h
+        L.cf_ensemble_set_batched_tri(h, 1 if batched_tri else 0)
 
     def step(self, nsteps: int = 1, sync: bool = True):
         rc = self.L.cf_ensemble_step(self.h, nsteps, 1 if sync else 0)

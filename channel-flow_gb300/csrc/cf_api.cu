@@ -985,43 +985,61 @@ extern "C" int cf_check_divergence(cf_ctx *ctx, double *maxdiv, double *maxabs) 
 // ---------------------------------------------------------------------------
 // fast path: compute_dt + compute_time_step_RK3 + mass-flow forcing
 // ---------------------------------------------------------------------------
+// One step in four segments separated by the three tridiagonal solves of
+// the projections: segment s ends with the forward transforms of substep
+// s+1's projection, segment s+1 starts with its inverse transforms.  A single
+// channel runs its own solve at the end of each segment (tri = true); an
+// ensemble runs one solve for all its members between the segments.
 template <typename T>
-static int enqueue_step(cf_ctx *ctx) {
-    const int X = ctx->cur;
-    const int a = (X + 1) % 3, b = (X + 2) % 3;
-    ctx->old = X;
-    TRY(launch_dt<T>(ctx, X, true));  // main.f90:71; t = to + dt of the step
-    // substep 1 (time_integration.f90:100-115)
-    TRY(eddy(ctx, X));
-    if (ctx->prm.iwall_model == 3) {
-        TRY(wall_model(ctx, X));
-        if (ctx->prm.sgs_recompute) TRY(eddy(ctx, X));
-    } else if (ctx->prm.sgs_recompute) {
+static int enqueue_seg(cf_ctx *ctx, int seg, bool tri) {
+    const int fwd = POISSON_FWD | (tri ? POISSON_TRI : 0);
+    const bool canon = true;
+    if (seg == 0) {
+        const int X = ctx->cur;
+        ctx->seg_base = X;
+        const int a = (X + 1) % 3;
+        ctx->old = X;
+        TRY(launch_dt<T>(ctx, X, true));  // main.f90:71; t = to + dt of the step
+        // substep 1 (time_integration.f90:100-115)
         TRY(eddy(ctx, X));
+        if (ctx->prm.iwall_model == 3) {
+            TRY(wall_model(ctx, X));
+            if (ctx->prm.sgs_recompute) TRY(eddy(ctx, X));
+        } else if (ctx->prm.sgs_recompute) {
+            TRY(eddy(ctx, X));
+        }
+        // substeps 1 and 2 hold intermediate stages: the split path keeps a low
+        // word only for u^n and the new state of substep 3.  The boundary
+        // conditions between the RK update and the projection
+        // (time_integration.f90:113) are not launched: the projection reads
+        // only interior values plus the periodic neighbours below the first
+        // interior index, which it takes through the wrap, and the update
+        // itself reproduces the periodic duplicate columns bit for bit; the
+        // call after the projection fills every ghost.
+        TRY(launch_rhs_update<T>(ctx, 1, X, a));
+        ctx->cur = a;
+        return launch_projection<T>(ctx, a, true, false, canon, fwd);
     }
-    // substeps 1 and 2 hold intermediate stages: the split path keeps a low
-    // word only for u^n and the new state of substep 3.  The boundary
-    // conditions between the RK update and the projection
-    // (time_integration.f90:113) are not launched: the projection reads
-    // only interior values plus the periodic neighbours below the first
-    // interior index, which it takes through the wrap, and the update itself
-    // reproduces the periodic duplicate columns bit for bit; the call after
-    // the projection fills every ghost.
-    TRY(launch_rhs_update<T>(ctx, 1, X, a));
-    ctx->cur = a;
-    TRY(launch_projection<T>(ctx, a, true, false, true));
-    TRY(launch_bc<T>(ctx, a, false));
-    // substep 2 (:118-131)
-    TRY(eddy(ctx, a));
-    TRY(launch_rhs_update<T>(ctx, 2, a, b));
-    ctx->cur = b;
-    TRY(launch_projection<T>(ctx, b, false, false, true));
-    TRY(launch_bc<T>(ctx, b, false));
-    // substep 3 (:134-150)
-    TRY(eddy(ctx, b));
-    TRY(launch_rhs_update<T>(ctx, 3, b, a));
-    ctx->cur = a;
-    TRY(launch_projection<T>(ctx, a, false, true, true));
+    const int X = ctx->seg_base, a = (X + 1) % 3, b = (X + 2) % 3;
+    if (seg == 1) {
+        TRY(launch_projection<T>(ctx, a, true, false, canon, POISSON_INV));
+        TRY(launch_bc<T>(ctx, a, false));
+        // substep 2 (:118-131)
+        TRY(eddy(ctx, a));
+        TRY(launch_rhs_update<T>(ctx, 2, a, b));
+        ctx->cur = b;
+        return launch_projection<T>(ctx, b, false, false, canon, fwd);
+    }
+    if (seg == 2) {
+        TRY(launch_projection<T>(ctx, b, false, false, canon, POISSON_INV));
+        TRY(launch_bc<T>(ctx, b, false));
+        // substep 3 (:134-150)
+        TRY(eddy(ctx, b));
+        TRY(launch_rhs_update<T>(ctx, 3, b, a));
+        ctx->cur = a;
+        return launch_projection<T>(ctx, a, false, true, canon, fwd);
+    }
+    TRY(launch_projection<T>(ctx, a, false, true, canon, POISSON_INV));
     TRY(launch_bc<T>(ctx, a));
     // mass-flow forcing (:153-171); with no-slip walls the correction is
     // added to the ghosts as apply_boundary_conditions would propagate it
@@ -1036,6 +1054,16 @@ static int enqueue_step(cf_ctx *ctx) {
     }
     ctx->old = a;
     return 0;
+}
+
+template <typename T>
+static int enqueue_step(cf_ctx *ctx) {
+    for (int seg = 0; seg < 4; seg++) TRY(enqueue_seg<T>(ctx, seg, true));
+    return 0;
+}
+
+static int step_seg(cf_ctx *ctx, int seg, bool tri) {
+    return DISPATCH(enqueue_seg<double>(ctx, seg, tri), enqueue_seg<float>(ctx, seg, tri));
 }
 
 static int step_eager(cf_ctx *ctx) { return DISPATCH(enqueue_step<double>(ctx), enqueue_step<float>(ctx)); }
@@ -1255,6 +1283,10 @@ extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *na
 struct cf_ensemble {
     std::vector<cf_ctx *> m;
     int dev = 0;
+    bool batched_tri = true;          // one FP64 launch for every member's tridiagonal systems
+    TriMember *dtab = nullptr;        // device table of the members' systems
+    double2 *scratch = nullptr;       // FP64 elimination scratch of every member
+    long total_modes = 0;             // blocks of the batched launch
     cudaStream_t st = nullptr;
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> join;
@@ -1295,12 +1327,42 @@ extern "C" int cf_ensemble_create(int n, cf_ctx *const *members, cf_ensemble **o
     if (ce == cudaSuccess) ce = cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming);
     e->join.assign(n, nullptr);
     for (int q = 0; q < n && ce == cudaSuccess; q++) ce = cudaEventCreateWithFlags(&e->join[q], cudaEventDisableTiming);
+    if (ce == cudaSuccess) {
+        std::vector<TriMember> tab(n);
+        long first = 0, sc = 0;
+        for (int q = 0; q < n; q++) {
+            tab[q] = tri_member(members[q]);
+            tab[q].first = first;
+            first += tri_batch_blocks(tab[q].NM);
+            sc += (long)tab[q].nym * tab[q].NM;
+        }
+        e->total_modes = first;  // blocks of the batched launch
+        ce = cudaMalloc(&e->scratch, (size_t)sc * sizeof(double2));
+        long off = 0;
+        for (int q = 0; q < n && ce == cudaSuccess; q++) {
+            tab[q].scratch = e->scratch + off;
+            off += (long)tab[q].nym * tab[q].NM;
+        }
+        if (ce == cudaSuccess) ce = cudaMalloc(&e->dtab, n * sizeof(TriMember));
+        if (ce == cudaSuccess) ce = cudaMemcpy(e->dtab, tab.data(), n * sizeof(TriMember), cudaMemcpyHostToDevice);
+    }
     if (ce != cudaSuccess) {
         int rc = ens_fail(e, CF_ERR_CUDA, std::string("cf_ensemble_create: ") + cudaGetErrorString(ce));
         cf_ensemble_destroy(e);
         return rc;
     }
     *out = e;
+    return CF_OK;
+}
+
+extern "C" int cf_ensemble_set_batched_tri(cf_ensemble *e, int on) {
+    if (!e) return ens_fail(e, CF_ERR_INVALID, "null ensemble");
+    if (e->batched_tri != (on != 0)) {
+        ENS_CUDA(cudaStreamSynchronize(e->st));
+        for (auto &kv : e->graphs) cudaGraphExecDestroy(kv.second.first);
+        e->graphs.clear();
+    }
+    e->batched_tri = on != 0;
     return CF_OK;
 }
 
@@ -1312,6 +1374,8 @@ extern "C" int cf_ensemble_destroy(cf_ensemble *e) {
     for (auto ev : e->join)
         if (ev) cudaEventDestroy(ev);
     if (e->fork) cudaEventDestroy(e->fork);
+    if (e->dtab) cudaFree(e->dtab);
+    if (e->scratch) cudaFree(e->scratch);
     if (e->st) cudaStreamDestroy(e->st);
     delete e;
     return CF_OK;
@@ -1343,23 +1407,38 @@ extern "C" int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync) {
         auto it = e->graphs.find(key);
         if (it == e->graphs.end()) {
             cudaGraph_t g;
+            int total_tri = 0;
             for (cf_ctx *c : e->m) {
                 c->launches = 0;
                 c->counting = true;
             }
             ENS_CUDA(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
             int rc = 0;
-            cudaError_t ce = cudaEventRecord(e->fork, e->st);
-            for (int q = 0; q < n && !rc && ce == cudaSuccess; q++) {
-                cf_ctx *c = e->m[q];
-                ce = cudaStreamWaitEvent(c->st, e->fork, 0);
-                if (ce == cudaSuccess) rc = step_eager(c);
-                if (!rc && ce == cudaSuccess) ce = cudaEventRecord(e->join[q], c->st);
-                if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(e->st, e->join[q], 0);
+            cudaError_t ce = cudaSuccess;
+            // with the batched solve the members' steps run in four segments,
+            // the tridiagonal systems of all of them solved between segments
+            const int nseg = e->batched_tri ? 4 : 1;
+            for (int seg = 0; seg < nseg && !rc && ce == cudaSuccess; seg++) {
+                ce = cudaEventRecord(e->fork, e->st);
+                for (int q = 0; q < n && !rc && ce == cudaSuccess; q++) {
+                    cf_ctx *c = e->m[q];
+                    ce = cudaStreamWaitEvent(c->st, e->fork, 0);
+                    if (ce == cudaSuccess) {
+                        if (e->batched_tri) rc = step_seg(c, seg, false);
+                        else
+                            for (int s2 = 0; s2 < 4 && !rc; s2++) rc = step_seg(c, s2, true);
+                    }
+                    if (!rc && ce == cudaSuccess) ce = cudaEventRecord(e->join[q], c->st);
+                    if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(e->st, e->join[q], 0);
+                }
+                if (!rc && ce == cudaSuccess && e->batched_tri && seg < 3) {
+                    rc = launch_tri_batch(e->st, e->dtab, n, e->total_modes);
+                    total_tri++;
+                }
             }
             cudaError_t ee = cudaStreamEndCapture(e->st, &g);
             std::vector<int> next(n);
-            int total = 0;
+            int total = total_tri;
             for (int q = 0; q < n; q++) {
                 cf_ctx *c = e->m[q];
                 c->counting = false;

@@ -193,6 +193,7 @@ struct cf_ctx {
     bool use_rhs3 = true;              // one fused RHS + update launch per substep
     int rhs_nkc = 1;                   // z chunks of the fused RHS
     int amd_nkc = 1;                   // z chunks of the AMD pass
+    int seg_base = 0;                  // buffer a step in segments started from
     size_t dsm_part_nch = 0;           // plane-partial slots per row allocated in dsm_part
     int amd_nparts = 0;                // partial sums per row of the last AMD pass
     bool amd_avg_pending = false;      // avg_nu_t not yet formed from them
@@ -267,7 +268,24 @@ template <typename T> int launch_nut_zero(cf_ctx *ctx);
 template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut if held lazily
 // canon: project the canonical cells only (the boundary conditions that
 // follow rewrite the periodic duplicates)
-template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true, bool canon = false);
+// one channel's tridiagonal systems for the batched solve of an ensemble
+struct TriMember {
+    void *spec;                          // spectrum [row][mode], complex of the state's precision
+    const double *m, *rd, *du, *dl;      // zgtsv factors [row][mode]
+    const unsigned char *piv;
+    double2 *scratch;                    // FP64 [row][mode] of the eliminated right-hand side
+    int nym, esz;
+    long NM, first;                      // modes, first block of the member in the launch
+};
+TriMember tri_member(const cf_ctx *ctx);
+long tri_batch_blocks(long NM);
+int launch_tri_batch(cudaStream_t st, const TriMember *dtab, int nmem, long total_blocks);
+
+// Poisson phases (forward transforms, tridiagonal solves, inverse transforms
+// and the projection)
+enum { POISSON_FWD = 1, POISSON_TRI = 2, POISSON_INV = 4, POISSON_ALL = 7 };
+template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true, bool canon = false,
+                                            int phases = POISSON_ALL);
 template <typename T> int launch_pressure(cf_ctx *ctx, int buf);  // actual pressure into P (pressure.f90:21)
 template <typename T> int launch_amd(cf_ctx *ctx, int buf);  // AMD eddy viscosity (subgrid.f90:639)
 void amd_plan(int esz, int nxp, int nym, int nzp, int sms, int *nkc, int *nparts);  // z chunks of the AMD pass

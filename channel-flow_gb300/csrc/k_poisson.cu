@@ -425,6 +425,95 @@ __global__ void __launch_bounds__(32) k_tri_mode(typename C2<T>::t *__restrict__
 
 static size_t tri_mode_smem(int nym) { return (size_t)nym * (6 * sizeof(double) + 1); }
 
+// The tridiagonal systems of many channels in one launch (ensembles): the
+// FP64 replay of k_tri_mode (zgtsv's elimination with its recorded pivots)
+// with one thread per (member, mode).  Modes of a member are adjacent in
+// memory ([row][mode]), so a warp's loads of one row are coalesced; warps
+// never straddle members (each member's modes start a new 32-block).  The
+// eliminated right-hand side is kept in FP64 scratch [row][mode], so FP32
+// spectra (split-path members) are solved in FP64 throughout and FP64
+// members bit for bit as k_tri_mode.
+constexpr int TRI_BATCH_T = 64;
+
+__global__ void __launch_bounds__(TRI_BATCH_T) k_tri_batch(const TriMember *__restrict__ tab, int nmem) {
+    const long gb = blockIdx.x;
+    int lo = 0, hi = nmem - 1;
+    while (lo < hi) {  // last member whose first block <= gb
+        const int mid = (lo + hi + 1) >> 1;
+        if (tab[mid].first <= gb) lo = mid;
+        else hi = mid - 1;
+    }
+    const TriMember t = tab[lo];
+    const long mo = (gb - t.first) * TRI_BATCH_T + threadIdx.x, NM = t.NM;
+    if (mo >= NM) return;
+    const int nym = t.nym;
+    double2 *sc = t.scratch;
+    auto rd_spec = [&](long o) -> double2 {
+        if (t.esz == 4) {
+            const float2 v = ((const float2 *)t.spec)[o];
+            return make_double2(v.x, v.y);
+        }
+        return ((const double2 *)t.spec)[o];
+    };
+    double2 r0 = rd_spec(mo);
+    for (int q = 0; q < nym - 1; q++) {
+        const long o = (long)q * NM + mo;
+        double2 nx = rd_spec(o + NM);
+        const double m = t.m[o];
+        if (t.piv[o]) {
+            sc[o] = nx;
+            nx = make_double2(r0.x - m * nx.x, r0.y - m * nx.y);
+        } else {
+            sc[o] = r0;
+            nx = make_double2(nx.x - m * r0.x, nx.y - m * r0.y);
+        }
+        r0 = nx;
+    }
+    const long ol = (long)(nym - 1) * NM + mo;
+    double x1r = r0.x * t.rd[ol], x1i = r0.y * t.rd[ol], x2r = 0.0, x2i = 0.0;
+    auto wr_spec = [&](long o, double a, double b) {
+        if (t.esz == 4) ((float2 *)t.spec)[o] = make_float2((float)a, (float)b);
+        else ((double2 *)t.spec)[o] = make_double2(a, b);
+    };
+    wr_spec(ol, x1r, x1i);
+    for (int q = nym - 2; q >= 0; q--) {
+        const long o = (long)q * NM + mo;
+        const double2 b = sc[o];
+        const double du = t.du[o], dl = t.dl[o], rdq = t.rd[o];
+        const double yr = (b.x - du * x1r - dl * x2r) * rdq;
+        const double yi = (b.y - du * x1i - dl * x2i) * rdq;
+        wr_spec(o, yr, yi);
+        x2r = x1r;
+        x2i = x1i;
+        x1r = yr;
+        x1i = yi;
+    }
+}
+
+TriMember tri_member(const cf_ctx *ctx) {
+    TriMember t;
+    const long NM = (long)ctx->nzp * ctx->nxh;
+    const size_t nf = (size_t)ctx->nym * NM;
+    t.spec = ctx->spec;
+    t.m = ctx->tri_fac;
+    t.rd = ctx->tri_fac + nf;
+    t.du = ctx->tri_fac + 2 * nf;
+    t.dl = ctx->tri_fac + 3 * nf;
+    t.piv = ctx->tri_piv;
+    t.nym = ctx->nym;
+    t.esz = ctx->esz;
+    t.NM = NM;
+    t.first = 0;
+    return t;
+}
+
+long tri_batch_blocks(long NM) { return (NM + TRI_BATCH_T - 1) / TRI_BATCH_T; }
+
+int launch_tri_batch(cudaStream_t st, const TriMember *dtab, int nmem, long total_blocks) {
+    k_tri_batch<<<(unsigned)total_blocks, TRI_BATCH_T, 0, st>>>(dtab, nmem);
+    return cudaGetLastError() == cudaSuccess ? 0 : CF_ERR_CUDA;
+}
+
 
 // Split path, one launch for every mode.
 //  * Blocks nlist.. : MB modes whose elimination never pivots, one thread each
@@ -897,11 +986,12 @@ static size_t smem_pairs(int n, int LP) {
 
 // phi = Laplacian^-1 div(U, V, W) on the canonical cells: the forward
 // transforms with the divergence fused, the per-mode tridiagonal solves and
-// the inverse transforms (projection.f90:40-120).  U, V, W have the extents
+// the inverse transforms (projection.f90:40-120), each phase on request (an
+// ensemble solves the tridiagonal systems of all its members in one launch).  U, V, W have the extents
 // of the velocity fields; only their canonical cells, the x and z neighbours
 // below them (read through the periodic wrap) and the wall rows of V are read.
 template <typename T>
-static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
+static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) {
     typedef typename C2<T>::t C;
     GeoT<T> g = geo_of<T>(ctx);
     C *spec = (C *)ctx->spec;
@@ -936,6 +1026,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
 #define CF_FFTZF(N) CF_FFTZ(N, twzf)
 #define CF_FFTZB(N) CF_FFTZ(N, twzb)
 #define CF_INVX(N) case N: k_inv_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale); break;
+    if (phases & POISSON_FWD) {
     // forward x (divergence fused)
     switch (nxp) {
         CF_FFT_SIZES(CF_FWDX)
@@ -948,6 +1039,8 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
         default: k_fft_z<T, 0><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, twzf, (int)nlines, nh, LB);
     }
     count_launch(ctx, "k_fft_z");
+    }
+    if (phases & POISSON_TRI) {
     // tridiagonal
     const long NM = (long)nzp * nh;
     TriFac tf;
@@ -981,6 +1074,8 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
         k_tri_mode<T><<<(unsigned)NM, 32, tri_mode_smem(nym), ctx->st>>>(spec, tf, nym, NM, nullptr);
         count_launch(ctx, "k_tri_mode");
     }
+    }
+    if (phases & POISSON_INV) {
     // inverse z
     switch (nzp) {
         CF_FFT_SIZES(CF_FFTZB)
@@ -994,6 +1089,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
         default: k_inv_x<T, 0><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale);
     }
     count_launch(ctx, "k_inv_x");
+    }
 #undef CF_FWDX
 #undef CF_FFTZ
 #undef CF_FFTZF
@@ -1004,12 +1100,13 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W) {
 }
 
 template <typename T>
-int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon) {
+int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon, int phases) {
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
     Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
-    if (int rc = poisson_solve<T>(ctx, U, V, W)) return rc;
+    if (int rc = poisson_solve<T>(ctx, U, V, W, phases & POISSON_ALL)) return rc;
+    if (!(phases & POISSON_INV)) return 0;  // projection after the inverse transforms
     T *phi = (T *)ctx->phi;
     const int nxp = ctx->nxp, nzp = ctx->nzp, nym = ctx->nym;
     // projection
@@ -1124,7 +1221,7 @@ int launch_pressure(cf_ctx *ctx, int b) {
     Fld<T> Fw = make_fld<T>(ctx->F[0][2], ctx->nxg, ctx->nyg);
     k_zero_vwall<T><<<dim3(cdiv(ctx->nxg, 128), ctx->nzg), 128, 0, ctx->st>>>(Fv, ctx->nxg, ctx->ny, ctx->nzg);
     count_launch(ctx, "k_zero_vwall");
-    if (int rc = poisson_solve<T>(ctx, Fu, Fv, Fw)) return rc;
+    if (int rc = poisson_solve<T>(ctx, Fu, Fv, Fw, POISSON_ALL)) return rc;
     if (int rc = launch_avg_nu_t_flush(ctx)) return rc;
     const double *y = ctx->hy.data(), *yg = ctx->hyg.data();  // 1-based
     const int ny = ctx->ny, nyg = ctx->nyg;
@@ -1163,7 +1260,7 @@ int fft_setup_attrs() {
     return 0;
 }
 
-template int launch_projection<double>(cf_ctx *, int, bool, bool, bool);
-template int launch_projection<float>(cf_ctx *, int, bool, bool, bool);
+template int launch_projection<double>(cf_ctx *, int, bool, bool, bool, int);
+template int launch_projection<float>(cf_ctx *, int, bool, bool, bool, int);
 template int launch_pressure<double>(cf_ctx *, int);
 template int launch_pressure<float>(cf_ctx *, int);

@@ -282,6 +282,12 @@ int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync);
 void *cf_ensemble_stream(cf_ensemble *e);
 /* Kernel launches one ensemble step holds (all members). */
 int cf_ensemble_launches_per_step(cf_ensemble *e);
+/* 1 (default): the members' steps run in four segments and the tridiagonal
+ * systems of all members -- every (member, kx, kz) mode -- are solved by one
+ * FP64 launch between segments (split-path members then get FP64 solves of
+ * their FP32 spectra); 0: each member solves its own systems inside its
+ * branch, bit for bit as cf_time_step_rk3. */
+int cf_ensemble_set_batched_tri(cf_ensemble *e, int on);
 
 /* ---- divergence check without device allocation ---------------------- */
 /* No counterpart in the reference: the arithmetic is check_divergence

@@ -435,9 +435,13 @@ def grids_centres(f):
     return grids.centres(np.asarray(f))
 
 
-def test_ensemble_members_match_single_runs():
+@pytest.mark.parametrize("batched", [False, True])
+def test_ensemble_members_match_single_runs(batched):
     """Three channels of different grids, models and wall treatments advanced
-    as one ensemble give bit for bit the fields of each advanced alone."""
+    as one ensemble give bit for bit the fields of each advanced alone; with
+    the batched FP64 tridiagonal solve the FP64 members still do (the same
+    replay), the split-path members agree to the precision of their FP32
+    solves."""
     import channelflow as cf
     specs = [dict(dims=(18, 17, 18), seed=3), dict(dims=(34, 33, 26), seed=4, les=3),
              dict(dims=(26, 17, 22), seed=5, stretch=0.0, wall=3, retau=2000.0, profile="plug")]
@@ -462,14 +466,18 @@ def test_ensemble_members_match_single_runs():
             alone.append(ch.download())
             ch.close()
         members = [make(case, prec) for case in cases]
-        ens = cf.Ensemble(members)
+        ens = cf.Ensemble(members, batched_tri=batched)
         ens.step(2)
         ens.step(4)
         assert ens.launches_per_step() > 3 * 20
         for m, ref in zip(members, alone):
             got = m.download()
             for n in ("U", "V", "W", "P", "nu_t"):
-                assert np.array_equal(got[n], ref[n]), (prec, n)
+                if prec == cf.PREC_FP64 or not batched:
+                    assert np.array_equal(got[n], ref[n]), (prec, n)
+                else:  # the pseudo-pressure carries the FP32 solve's error directly
+                    tol = {"P": 2e-3, "nu_t": 1e-4}.get(n, 1e-5)
+                    assert rel_err(got[n], ref[n]) < tol, (prec, n, rel_err(got[n], ref[n]))
         ens.close()
         for m in members:
             m.close()
