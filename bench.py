@@ -195,7 +195,7 @@ def make_channel(wl, precision, device, seed, cfl=0.5):
                x_mass_cte=1, jref_eqwm=wl["jref"], eqwm_ncv=wl["ncv"], precision=precision)
     ch = cf.Channel(x, y, z, device=device, **prm)
     if wl.get("mlp"):
-        ch.set_wall_mlp(wall_net(wl, device)[0], judge_every=100)
+        ch.set_wall_mlp(wall_net(wl, device)[0], check_every=100)
     ch.upload(U, V, W)
     ch.init_mass_flow()
     ch.apply_boundary_conditions()
@@ -586,7 +586,7 @@ def run_ours(args, wl, rank, world, local):
         }
         if wl.get("mlp"):
             net_info = dict(wall_net(wl, dev)[1])
-            net_info["judged_in_run"] = ch.wall_mlp_log()
+            net_info["checked_in_run"] = ch.wall_mlp_log()
             line["wall_mlp"] = net_info
         print(json.dumps(line), flush=True)
     ch.close()

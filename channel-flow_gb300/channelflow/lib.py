@@ -365,15 +365,15 @@ class Channel:
         return dict(rhs_chunks=int(out[0]), rhs_us=out[1], dsm_chunk_len=int(out[2]), dsm_us=out[3],
                     amd_chunks=int(out[4]), amd_us=out[5])
 
-    def set_wall_mlp(self, net, judge_every: int = 100):
+    def set_wall_mlp(self, net, check_every: int = 100):
         """Serves the wall stress of the equilibrium wall model from a trained
         channelflow.wallmlp.WallMLP (eqwm outside its envelope); every
-        `judge_every` wall-model calls eqwm also runs and the network's error
+        `check_every` wall-model calls eqwm also runs and the network's error
         is recorded (wall_mlp_log).  None detaches it."""
         from . import wallmlp
         wallmlp._bind()
         self._wall_net = net  # keeps the network alive while it serves
-        self._check(self.L.cf_set_wall_mlp(self.h, None if net is None else net.h, judge_every))
+        self._check(self.L.cf_set_wall_mlp(self.h, None if net is None else net.h, check_every))
 
     def wall_mlp_log(self) -> dict:
         out = np.zeros(5)

@@ -65,7 +65,7 @@ def eqwm_solve_batch(u, h, nu, ncv=30, stretch=1.10, tau_init=1e-3, iters=False)
     return (tau, it) if iters else tau
 
 
-# The operating range the network is judged on: channels at Re_tau 500-10000
+# The operating range the network is checked on: channels at Re_tau 500-10000
 # matched at 0.04-0.2 half-heights, instantaneous u_les within about +-25 % of
 # the log law.  The training distribution (the defaults of training_inputs)
 # extends it on every side, so that the operating range lies inside the

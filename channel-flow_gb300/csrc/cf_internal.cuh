@@ -221,11 +221,11 @@ struct cf_ctx {
     double *alpha_x = nullptr, *alpha_z = nullptr, *alpha_zt = nullptr, *tau0 = nullptr;
     double *wtemp1 = nullptr, *wtemp2 = nullptr;   // W at jref: z-interp (nxg,2,nzg), x-interp (nx,2,nzg)
     // learned wall stress (cf_set_wall_mlp): the network, per wall point u_les,
-    // stress, envelope flag and the judged eqwm stress; call counter and log
+    // stress, envelope flag and the checked eqwm stress; call counter and log
     struct cf_mlp *wmlp = nullptr;
     double *wm_u = nullptr, *wm_tau = nullptr, *wm_tau_eq = nullptr, *wm_log = nullptr;
     int *wm_inside = nullptr, *wm_calls = nullptr;
-    int wm_judge_every = 0;
+    int wm_check_every = 0;
     double *eq_grid = nullptr;                      // y_cv(1..ncv), y_fa(1..ncv+1)
     int *eq_zst = nullptr, *eq_xst = nullptr;       // stencil indices
     double *eq_zw = nullptr, *eq_xw = nullptr;      // stencil weights

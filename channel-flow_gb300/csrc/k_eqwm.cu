@@ -74,13 +74,13 @@ __global__ void k_wm_ules(const Fld<double> Ud, const float *Uf32, int use_f32, 
 }
 
 // Learned-stress state of the wall model: the network's stress and envelope
-// flag per point, the call counter and judging period, the judged eqwm
+// flag per point, the call counter and checking period, the checked eqwm
 // stress.  mode 0: eqwm everywhere (the reference).
 struct WmState {
     const double *tau_nn;
     const int *inside;
     const int *calls;
-    int judge_every;
+    int check_every;
     int mode;
     double *tau_eq;
 };
@@ -89,7 +89,7 @@ struct WmState {
 // yfa[1..ncv+1], idcv[i] = 1/(y_cv(i+1)-y_cv(i)) (i = 1..ncv-1),
 // rw = 1/(y_cv(1)-y_fa(1)); grid[1..ncv] = y_cv, grid[ncv+1..2ncv+1] = y_fa.
 // With the learned stress (mode 1) the network's value stands for the solve
-// at points inside its training envelope; on judged calls the solve runs for
+// at points inside its training envelope; on checked calls the solve runs for
 // every point and its result is kept in tau_eq for the error record.
 __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32, int sy, int sz, const double *t1,
                            const int *xst, const double *xw, const double *grid, EqParams ep, const double *nut,
@@ -113,9 +113,9 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
     const double u_les = wall_ules(pt, ep, Ud, Uf32, use_f32, sy, sz, t1, xst, xw, &Uv, &wv);
     const long toff = pt.toff;
     const bool served = wm.mode == 1 && wm.inside[toff] != 0;
-    const bool judge = wm.mode == 1 && wm.judge_every > 0 && (*wm.calls % wm.judge_every) == 0;
+    const bool check = wm.mode == 1 && wm.check_every > 0 && (*wm.calls % wm.check_every) == 0;
     double tau = tau0[toff];
-    if (!served || judge) {
+    if (!served || check) {
         // solve_u_eqwm(u_les, nu, 1.0, yg(jref), ncv, stretch, tau, iter, tau_in)
         const double kappa = 0.41, Aplus = 17.0, tol = 0.0000001, mu_lam = ep.nu, rho = 1.0;
         const int max_iter = 100;
@@ -164,7 +164,7 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
             tau = ep.tau_mean;
             atomicAdd(&counters[1], 1);
         }
-        if (judge) wm.tau_eq[toff] = tau;
+        if (check) wm.tau_eq[toff] = tau;
     }
     if (served) tau = wm.tau_nn[toff];
     tau0[toff] = tau;
@@ -180,14 +180,14 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
     alpha_zt[toff] = tz / (ep.nu + nu_t_ik);
 }
 
-// The error record of judged calls: max and mean |tau_nn/tau_eq - 1| over
+// The error record of checked calls: max and mean |tau_nn/tau_eq - 1| over
 // the points the network served, their count and the fallback count; every
 // call advances the call counter.  One block.
-__global__ void __launch_bounds__(1024) k_wm_judge(long npts, const double *tau_nn, const int *inside,
-                                                  const double *tau_eq, int *calls, int judge_every, double *log) {
+__global__ void __launch_bounds__(1024) k_wm_audit(long npts, const double *tau_nn, const int *inside,
+                                                  const double *tau_eq, int *calls, int check_every, double *log) {
     __shared__ double sm[3][32];
-    const bool judge = judge_every > 0 && (*calls % judge_every) == 0;
-    if (judge) {
+    const bool check = check_every > 0 && (*calls % check_every) == 0;
+    if (check) {
         double mx = 0.0, sum = 0.0, cnt = 0.0;
         for (long t = threadIdx.x; t < npts; t += blockDim.x) {
             if (!inside[t]) continue;
@@ -269,7 +269,7 @@ int launch_eqwm(cf_ctx *ctx, int b) {
         wm.tau_nn = ctx->wm_tau;
         wm.inside = ctx->wm_inside;
         wm.calls = ctx->wm_calls;
-        wm.judge_every = ctx->wm_judge_every;
+        wm.check_every = ctx->wm_check_every;
         wm.mode = 1;
         wm.tau_eq = ctx->wm_tau_eq;
     }
@@ -279,9 +279,9 @@ int launch_eqwm(cf_ctx *ctx, int b) {
                                                      ctx->alpha_zt, (int *)ctx->d_red, wm);
     count_launch(ctx, "k_eq_solve");
     if (ctx->wmlp) {
-        k_wm_judge<<<1, 1024, 0, ctx->st>>>(npts, ctx->wm_tau, ctx->wm_inside, ctx->wm_tau_eq, ctx->wm_calls,
-                                            ctx->wm_judge_every, ctx->wm_log);
-        count_launch(ctx, "k_wm_judge");
+        k_wm_audit<<<1, 1024, 0, ctx->st>>>(npts, ctx->wm_tau, ctx->wm_inside, ctx->wm_tau_eq, ctx->wm_calls,
+                                            ctx->wm_check_every, ctx->wm_log);
+        count_launch(ctx, "k_wm_audit");
     }
     k_eq_alphaz<<<dim3(cdiv(nxg, 128), nz, 2), 128, 0, ctx->st>>>(ctx->alpha_zt, ctx->alpha_z, nx, nxg, nz, nzg);
     count_launch(ctx, "k_eq_alphaz");

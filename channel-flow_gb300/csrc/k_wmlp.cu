@@ -800,10 +800,10 @@ int wall_mlp_infer(cf_ctx *ctx, int npts, double h_wm, double nu) {
     return 0;
 }
 
-extern "C" int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int judge_every) {
+extern "C" int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int check_every) {
     if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
     if (ctx->prm.iwall_model != 3) return cf_fail(ctx, CF_ERR_INVALID, "the learned wall stress needs iwall_model 3");
-    if (judge_every < 0) return cf_fail(ctx, CF_ERR_INVALID, "judge_every must be >= 0");
+    if (check_every < 0) return cf_fail(ctx, CF_ERR_INVALID, "check_every must be >= 0");
     if (m && (m->ncv != ctx->prm.eqwm_ncv || std::fabs(m->stretch - ctx->prm.eqwm_stretch) > 1e-12))
         return cf_fail(ctx, CF_ERR_INVALID, "the network was trained for another eqwm grid (eqwm_ncv, eqwm_stretch)");
     CF_CUDA(cudaSetDevice(ctx->dev));
@@ -823,7 +823,7 @@ extern "C" int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int judge_every) {
         CF_CUDA(cudaMemset(ctx->wm_calls, 0, sizeof(int)));
     }
     ctx->wmlp = m;
-    ctx->wm_judge_every = judge_every;
+    ctx->wm_check_every = check_every;
     // the captured steps do not contain the new sequence
     for (auto &g : ctx->graphs)
         if (g) {

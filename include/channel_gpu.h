@@ -255,12 +255,12 @@ int cf_mlp_get(cf_mlp *m, float *params, double *norm, double *envelope);
 int cf_mlp_set(cf_mlp *m, const float *params, const double *norm, const double *envelope);
 /* Uses the network for the wall stress of ctx's equilibrium wall model
  * (iwall_model 3): points whose inputs fall outside the envelope, and all
- * points when m is NULL, keep the eqwm solve.  Every `judge_every` calls of
+ * points when m is NULL, keep the eqwm solve.  Every `check_every` calls of
  * the wall model (0: never) the eqwm solve also runs for all points and the
  * relative error of the network against it is recorded.  ctx's eqwm_ncv and
  * eqwm_stretch must be those m was trained for.  m must outlive its use. */
-int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int judge_every);
-/* The last judgement: out[5] = wall-model calls so far, max and mean
+int cf_set_wall_mlp(cf_ctx *ctx, cf_mlp *m, int check_every);
+/* The last check: out[5] = wall-model calls so far, max and mean
  * |tau_mlp - tau_eqwm|/tau_eqwm over the points the network served, points
  * served, points that fell back to eqwm. */
 int cf_get_wall_mlp_log(cf_ctx *ctx, double *out);

@@ -130,7 +130,7 @@ def test_training_reaches_two_percent_and_tensor_cores_match():
 def test_learned_stress_in_the_wall_model():
     """A trained network serving the wall stress of the equilibrium wall model
     (channel with eqwm, Re_tau 2000): ten fast-path steps stay close to the
-    eqwm run, the judged error stays within 2 %, and points outside the
+    eqwm run, the checked error stays within 2 %, and points outside the
     envelope fall back to eqwm."""
     import torch
     import channelflow as cf
@@ -149,7 +149,7 @@ def test_learned_stress_in_the_wall_model():
         ch.init_mass_flow()
         ch.apply_boundary_conditions()
         if use:
-            ch.set_wall_mlp(net, judge_every=5)
+            ch.set_wall_mlp(net, check_every=5)
         ch.set_fixed_dt(case["dt"])
         ch.time_step_rk3(10)
         out[use] = ch.download()
@@ -220,7 +220,7 @@ def test_points_outside_the_envelope_fall_back_to_eqwm():
         ch.init_mass_flow()
         ch.apply_boundary_conditions()
         if use:
-            ch.set_wall_mlp(net, judge_every=1)
+            ch.set_wall_mlp(net, check_every=1)
         ch.set_fixed_dt(case["dt"])
         ch.time_step_rk3(3)
         out[use] = ch.download()
