@@ -53,8 +53,8 @@ constexpr int DSM_ZMAX = DSM_ZMAX_HOST;
 template <typename T, int TX, int TY>
 struct DsmSmem {
     static constexpr int RX = TX + 4, RY = TY + 4, QX = TX + 2, QY = TY + 2;
-    static constexpr int NR = 9 * RX * RY, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY;
-    static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ) * sizeof(T);
+    static constexpr int NR = 9 * RX * RY, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY, NC = 16 * QX * TY;
+    static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ + NC) * sizeof(T);
 };
 
 // resident blocks per SM the pass is compiled for (three blocks at 80
@@ -73,6 +73,7 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
     T *F = G + SM::NG;          // [slot 3][field 3][QY][QX]
     typedef typename PairT<T>::t PT;
     PT *Qs = (PT *)(F + SM::NF);  // [8 pairs][QY][QX]
+    PT *Cs = Qs + SM::NQ / 2;     // [8 pairs][TY][QX]: Q filtered in y
     const T *rdx = (const T *)rgv.rdx, *rdxg = (const T *)rgv.rdxg, *rdy = (const T *)rgv.rdy,
             *rdyg = (const T *)rgv.rdyg, *rdz = (const T *)rgv.rdz, *rdzg = (const T *)rgv.rdzg;
     const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0), h = T(0.5), qq = T(0.25);
@@ -86,6 +87,7 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
     auto GS = [&](int slot, int f, int sy, int sx) -> T & { return G[((slot * 3 + f) * QY + sy) * QX + sx]; };
     auto FS = [&](int slot, int f, int sy, int sx) -> T & { return F[((slot * 3 + f) * QY + sy) * QX + sx]; };
     auto QS = [&](int p, int sy, int sx) -> PT & { return Qs[(p * QY + sy) * QX + sx]; };
+    auto CS = [&](int p, int oy, int sx) -> PT & { return Cs[(p * TY + oy) * QX + sx]; };
 
     // y filter weights of a row in [lo, hi] (one-sided at the ends)
     auto yw = [&](int j, int lo, int hi, T &wm, T &w0, T &wp) {
@@ -261,23 +263,39 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
             }
         }
         __syncthreads();
+        if (r >= kb) {
+            // -- y filter of Q(r-1), one (pair, column) of the region per
+            // task: the column's QY values are read once and give the TY
+            // filtered rows (one-sided at the wall rows j = 2 and nyg-1)
+            for (int t = tid; t < 8 * QX; t += NTH) {
+                const int q = t / QX, sx = t - q * QX;
+                PT col[QY];
+#pragma unroll
+                for (int s = 0; s < QY; s++) col[s] = QS(q, s, sx);
+#pragma unroll
+                for (int oy = 0; oy < TY; oy++) {
+                    const int j = j0 + oy;
+                    T wm, w0, wp;
+                    yw(j, 2, nyg - 1, wm, w0, wp);
+                    const PT cm = j > 2 ? col[oy] : col[oy + 1], cp = j < nyg - 1 ? col[oy + 2] : col[oy + 1];
+                    PT c = pmul(psplat(w0), col[oy + 1]);
+                    c = pfma(psplat(wm), cm, c);
+                    c = pfma(psplat(wp), cp, c);
+                    CS(q, oy, sx) = c;
+                }
+            }
+            __syncthreads();
+        }
         if (r >= kb && own) {
-            // -- x-y filter of Q(r-1) at the own point, spread over planes r-2, r-1, r
-            T wm, w0, wp;
-            yw(jo, 2, nyg - 1, wm, w0, wp);
+            // -- x filter of the y-filtered Q(r-1) at the own point, spread
+            // over planes r-2, r-1, r
             const int sx = tx + 1, sy = ty + 1;
-            const int dm = jo > 2 ? -1 : 0, dp = jo < nyg - 1 ? 1 : 0;
-            const PT pwm = psplat(wm), pw0 = psplat(w0), pwp = psplat(wp), pf6 = psplat(f6), pf23 = psplat(f23);
+            const PT pf6 = psplat(f6), pf23 = psplat(f23);
 #pragma unroll
             for (int q = 0; q < 8; q++) {
                 PT a = psplat(T(0));
 #pragma unroll
-                for (int d = -1; d <= 1; d++) {
-                    PT c = pmul(pw0, QS(q, sy, sx + d));
-                    c = pfma(pwm, QS(q, sy + dm, sx + d), c);
-                    c = pfma(pwp, QS(q, sy + dp, sx + d), c);
-                    a = pfma(psplat(fw[d + 1]), c, a);
-                }
+                for (int d = -1; d <= 1; d++) a = pfma(psplat(fw[d + 1]), CS(q, ty, sx + d), a);
                 acc[P1][q] = pfma(pf6, a, acc[P1][q]);   // plane r-2 (last contribution)
                 acc[P2][q] = pfma(pf23, a, acc[P2][q]);  // plane r-1
                 acc[PH][q] = pmul(pf6, a);               // plane r (first contribution; the slot held plane r-3)
