@@ -263,33 +263,91 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
             }
         }
         __syncthreads();
+        // R(r-2) (slot P1) was last read by Q(r-1): R(r+1) takes its place
+        // (visible after the next barrier)
+        if (r + 1 <= re) commit(P1);
+        // S_ij of Uf, Vf, Wf at the output plane k = r-2 (from F(r-3) [PH],
+        // F(r-2) [P1], F(r-1) [P2]) and |S| of Q(r-1) at the own point, read
+        // before the barrier: the next step overwrites F(r-3) and Q
+        T sf[6], Sf = T(0), Snew = T(0);
+#pragma unroll
+        for (int q = 0; q < 6; q++) sf[q] = T(0);
         if (r >= kb) {
             // -- y filter of Q(r-1), one (pair, column) of the region per
             // task: the column's QY values are read once and give the TY
-            // filtered rows (one-sided at the wall rows j = 2 and nyg-1)
+            // filtered rows (one-sided at the wall rows j = 2 and nyg-1).
+            // Tasks 0 .. 8 TX - 1 take columns 0 .. TX - 1 of one pair per
+            // TX lanes; the last 16 take columns TX and TX + 1.
+            const bool inner = j0 > 2 && j0 + TY - 1 < nyg - 1;
             for (int t = tid; t < 8 * QX; t += NTH) {
-                const int q = t / QX, sx = t - q * QX;
+                int q, sx;
+                if (t < 8 * TX) { q = t / TX; sx = t - q * TX; }
+                else { q = (t - 8 * TX) >> 1; sx = TX + ((t - 8 * TX) & 1); }
                 PT col[QY];
 #pragma unroll
                 for (int s = 0; s < QY; s++) col[s] = QS(q, s, sx);
+                if (inner) {
+                    const PT pf6 = psplat(f6), pf23 = psplat(f23);
 #pragma unroll
-                for (int oy = 0; oy < TY; oy++) {
-                    const int j = j0 + oy;
-                    T wm, w0, wp;
-                    yw(j, 2, nyg - 1, wm, w0, wp);
-                    const PT cm = j > 2 ? col[oy] : col[oy + 1], cp = j < nyg - 1 ? col[oy + 2] : col[oy + 1];
-                    PT c = pmul(psplat(w0), col[oy + 1]);
-                    c = pfma(psplat(wm), cm, c);
-                    c = pfma(psplat(wp), cp, c);
-                    CS(q, oy, sx) = c;
+                    for (int oy = 0; oy < TY; oy++) {
+                        PT c = pmul(pf23, col[oy + 1]);
+                        c = pfma(pf6, col[oy], c);
+                        c = pfma(pf6, col[oy + 2], c);
+                        CS(q, oy, sx) = c;
+                    }
+                } else {
+#pragma unroll
+                    for (int oy = 0; oy < TY; oy++) {
+                        const int j = j0 + oy;
+                        T wm, w0, wp;
+                        yw(j, 2, nyg - 1, wm, w0, wp);
+                        const PT cm = j > 2 ? col[oy] : col[oy + 1], cp = j < nyg - 1 ? col[oy + 2] : col[oy + 1];
+                        PT c = pmul(psplat(w0), col[oy + 1]);
+                        c = pfma(psplat(wm), cm, c);
+                        c = pfma(psplat(wp), cp, c);
+                        CS(q, oy, sx) = c;
+                    }
                 }
             }
-            __syncthreads();
+            if (own) {
+                const int sx = tx + 1, sy = ty + 1;
+                Snew = QS(7, sy, sx).y;
+                if (r >= kb + 2) {
+                    const int k = r - 2;
+                    auto uf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 0, sy + dj, sx + di); };
+                    auto vf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 1, sy + dj, sx + di); };
+                    auto wf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 2, sy + dj, sx + di); };
+                    const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
+                    const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
+                    const T rz = gsz[0][k - rs], rzg0 = gsz[1][k - rs], rzg1 = gsz[2][k - rs];
+                    T s0 = (uf(0, 0, 0) - uf(-1, 0, 0)) * rx0;
+                    T s1 = (vf(0, 0, 0) - vf(0, -1, 0)) * ry0;
+                    T s2 = (wf(0, 0, 0) - wf(0, 0, -1)) * rz;
+                    T s3 = T(0), s4 = T(0), s5 = T(0);
+#pragma unroll
+                    for (int a = 0; a < 2; a++)
+#pragma unroll
+                        for (int b = 0; b < 2; b++) {
+                            const T rxa = a ? rxg1 : rxg0, ryb = b ? ryg1 : ryg0, rzb = b ? rzg1 : rzg0, rya = a ? ryg1 : ryg0;
+                            s3 += h * ((uf(a - 1, b, 0) - uf(a - 1, b - 1, 0)) * ryb + (vf(a, b - 1, 0) - vf(a - 1, b - 1, 0)) * rxa);
+                            s4 += h * ((uf(a - 1, 0, b) - uf(a - 1, 0, b - 1)) * rzb + (wf(a, 0, b - 1) - wf(a - 1, 0, b - 1)) * rxa);
+                            s5 += h * ((vf(0, a - 1, b) - vf(0, a - 1, b - 1)) * rzb + (wf(0, a, b - 1) - wf(0, a - 1, b - 1)) * rya);
+                        }
+                    s3 *= qq; s4 *= qq; s5 *= qq;
+                    Sf = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
+                              T(4) * s5 * s5);
+                    sf[0] = s0; sf[1] = s1; sf[2] = s2; sf[3] = s3; sf[4] = s4; sf[5] = s5;
+                }
+            }
         }
+        __syncthreads();
+        // No barrier closes the step: the next step's first writes (G(r+1)
+        // over G(r-2), F(r) over F(r-3), Q(r)) touch nothing read below, and
+        // the filtered columns are rewritten only after its first barrier.
         if (r >= kb && own) {
             // -- x filter of the y-filtered Q(r-1) at the own point, spread
             // over planes r-2, r-1, r
-            const int sx = tx + 1, sy = ty + 1;
+            const int sx = tx + 1;
             const PT pf6 = psplat(f6), pf23 = psplat(f23);
 #pragma unroll
             for (int q = 0; q < 8; q++) {
@@ -301,32 +359,9 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
                 acc[PH][q] = pmul(pf6, a);               // plane r (first contribution; the slot held plane r-3)
             }
             if (r >= kb + 2) {
-                // -- output plane k = r-2: S_ij of Uf, Vf, Wf from F(r-3) [PH], F(r-2) [P1], F(r-1) [P2]
-                const int k = r - 2, kcn = wrapn(k, nzp);
-                auto uf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 0, sy + dj, sx + di); };
-                auto vf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 1, sy + dj, sx + di); };
-                auto wf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 2, sy + dj, sx + di); };
-                const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
-                const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
-                const T rz = gsz[0][k - rs], rzg0 = gsz[1][k - rs], rzg1 = gsz[2][k - rs];
-                T s0 = (uf(0, 0, 0) - uf(-1, 0, 0)) * rx0;
-                T s1 = (vf(0, 0, 0) - vf(0, -1, 0)) * ry0;
-                T s2 = (wf(0, 0, 0) - wf(0, 0, -1)) * rz;
-                T s3 = T(0), s4 = T(0), s5 = T(0);
-#pragma unroll
-                for (int a = 0; a < 2; a++)
-#pragma unroll
-                    for (int b = 0; b < 2; b++) {
-                        const T rxa = a ? rxg1 : rxg0, ryb = b ? ryg1 : ryg0, rzb = b ? rzg1 : rzg0, rya = a ? ryg1 : ryg0;
-                        s3 += h * ((uf(a - 1, b, 0) - uf(a - 1, b - 1, 0)) * ryb + (vf(a, b - 1, 0) - vf(a - 1, b - 1, 0)) * rxa);
-                        s4 += h * ((uf(a - 1, 0, b) - uf(a - 1, 0, b - 1)) * rzb + (wf(a, 0, b - 1) - wf(a - 1, 0, b - 1)) * rxa);
-                        s5 += h * ((vf(0, a - 1, b) - vf(0, a - 1, b - 1)) * rzb + (wf(0, a, b - 1) - wf(0, a - 1, b - 1)) * rya);
-                    }
-                s3 *= qq; s4 *= qq; s5 *= qq;
-                T Sf = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
-                            T(4) * s5 * s5);
+                // -- output plane k = r-2
+                const int kcn = wrapn(r - 2, nzp);
                 const T fs2 = T(4);  // fil_size**2 (subgrid.f90:156, 463)
-                const T sf[6] = {s0, s1, s2, s3, s4, s5};
                 // filtered quantities of plane r-2 in the order uc vc wc uu vv ww uv uw vw |S|S11..|S|S23
                 T fq[15];
 #pragma unroll
@@ -351,11 +386,8 @@ __global__ void __launch_bounds__(TX *TY, DsmMinB<T>::v) k_dsm_fused(Fld<T> U, F
                 smm += wgt * mm;
                 Sout[(long)(io - 2) + (long)nxp * ((jo - 2) + (long)(nyg - 2) * (kcn - 2))] = Sprev;
             }
-            Sprev = QS(7, sy, sx).y;  // |S| at plane r-1 for the next output
+            Sprev = Snew;  // |S| at plane r-1 for the next output
         }
-        // R(r-2) (slot P1) was last read by Q(r-1): R(r+1) takes its place
-        if (r + 1 <= re) commit(P1);
-        __syncthreads();
     };
     fetch(rs);
     commit(0);
