@@ -521,11 +521,31 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     ctx->red_n = std::max({ctx->nzg + 8, ctx->nxg + ctx->nyg + ctx->nzg + 16, (ctx->nzg - 2) * cdiv(ctx->nyg - 2, 16) + 16});
     CF_CUDA(cudaMalloc(&ctx->d_red, (size_t)ctx->red_n * sizeof(double)));
     {
-        // per-index extrema of |u| for compute_dt: minima start at +inf,
-        // the maxima of the corrected rule at 0
-        std::vector<double> inf((size_t)ctx->nxg + ctx->nyg + ctx->nzg + 6, p->cfl_corrected ? 0.0 : INFINITY);
-        CF_CUDA(cudaMalloc(&ctx->d_dtmin, inf.size() * sizeof(double)));
-        CF_CUDA(cudaMemcpy(ctx->d_dtmin, inf.data(), inf.size() * sizeof(double), cudaMemcpyHostToDevice));
+        // per-index extrema of |u| for compute_dt, in the state's
+        // precision: minima start at +inf, the maxima of the corrected rule
+        // at 0
+        const size_t n = (size_t)ctx->nxg + ctx->nyg + ctx->nzg + 6;
+        CF_CUDA(cudaMalloc(&ctx->d_dtmin, n * sizeof(double)));
+        if (ctx->esz == 8) {
+            std::vector<double> inf(n, p->cfl_corrected ? 0.0 : INFINITY);
+            CF_CUDA(cudaMemcpy(ctx->d_dtmin, inf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        } else {
+            std::vector<float> inf(n, p->cfl_corrected ? 0.0f : INFINITY);
+            CF_CUDA(cudaMemcpy(ctx->d_dtmin, inf.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+        }
+    }
+    {
+        // mass_flow.f90:116-123 as sum_j c_j sum_i U_ij: c_j = the two half
+        // intervals next to row j, split into float hi + lo for the split path
+        std::vector<float2> c((size_t)ctx->nyg + 2, make_float2(0.f, 0.f));
+        const std::vector<double> &yg = ctx->hyg;
+        for (int j = 2; j <= ctx->nyg - 1; j++) {
+            const double cj = (j >= 3 ? 0.5 * (yg[j] - yg[j - 1]) : 0.0) + (j <= ctx->nyg - 2 ? 0.5 * (yg[j + 1] - yg[j]) : 0.0);
+            c[j].x = (float)cj;
+            c[j].y = (float)(cj - (double)c[j].x);
+        }
+        CF_CUDA(cudaMalloc(&ctx->d_mass_c, c.size() * sizeof(float2)));
+        CF_CUDA(cudaMemcpy(ctx->d_mass_c, c.data(), c.size() * sizeof(float2), cudaMemcpyHostToDevice));
     }
     CF_CUDA(cudaMalloc(&ctx->ds, sizeof(DevScal)));
     TRY(push_scal(ctx));
@@ -548,7 +568,7 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
                     ctx->phi, ctx->spec, ctx->d_tri, ctx->d_tw, ctx->tri_fac, ctx->tri_piv, ctx->tri_l32, ctx->tri_ru32,
                     ctx->tri_du32, ctx->tri_flag, ctx->tri_list, ctx->alpha_x, ctx->alpha_z, ctx->alpha_zt, ctx->tau0,
                     ctx->wtemp1, ctx->wtemp2, ctx->eq_grid, ctx->eq_zst, ctx->eq_xst, ctx->eq_zw, ctx->eq_xw, ctx->ds,
-                    ctx->d_red, ctx->d_dtmin, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage,
+                    ctx->d_red, ctx->d_dtmin, ctx->d_mass_c, ctx->d_geo, ctx->d_geo_f, ctx->d_rgeo, ctx->d_rgeo_f, ctx->stage,
                     ctx->wm_u, ctx->wm_tau, ctx->wm_tau_eq, ctx->wm_log, ctx->wm_inside, ctx->wm_calls};
     for (void *q : ptrs)
         if (q) cudaFree(q);

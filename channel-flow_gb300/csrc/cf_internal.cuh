@@ -100,6 +100,14 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
     hi = s + e;
     lo = e - (hi - s);
 }
+// (hi, lo) += (bh, bl), both float-float
+__device__ __forceinline__ void ff_add2(float &hi, float &lo, float bh, float bl) {
+    float s, e;
+    two_sum(hi, bh, s, e);
+    e += lo + bl;
+    hi = s + e;
+    lo = e - (hi - s);
+}
 
 // periodic index for i in [2 - np, 2 np + 1] (compares only)
 __host__ __device__ __forceinline__ int wrapn(int i, int np) { return i < 2 ? i + np : (i > np + 1 ? i - np : i); }
@@ -235,6 +243,7 @@ struct cf_ctx {
     DevScal *ds = nullptr;
     double *d_red = nullptr;           // reduction scratch
     double *d_dtmin = nullptr;         // compute_dt minima per x, y, z index (+inf between calls)
+    float2 *d_mass_c = nullptr;        // trapezoid weight of row j as float hi + lo (split path)
     int red_n = 0;
     // staging for transfers
     double *stage = nullptr;

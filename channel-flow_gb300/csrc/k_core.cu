@@ -397,7 +397,7 @@ __device__ __forceinline__ void rk_apply(T r, T f1, T uo, T uolo, bool has_lo, i
 
 // mode: 0 = store F(slot); 1 = fused update from Uo with F1 (s = 1 stores F1)
 template <typename T, int COMP>
-__global__ void k_rhs(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds, T nu, T Om,
+__global__ void k_rhs(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt, const DevScal *ds, T nu, T Om, int rot,
                       Fld<T> out, Fld<T> F1, Fld<T> Uo, Fld<T> Uolo, Fld<T> Unlo, int mode, int s, RkCoef rk,
                       int i1, int j1, int k1) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
@@ -405,7 +405,6 @@ __global__ void k_rhs(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T
     int k = blockIdx.z + 2;
     if (i > i1 || j > j1 || k > k1) return;
     T r;
-    const bool rot = fabs((double)Om) > 1e-6;
     if (COMP == 0) r = rhs_u_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdx<T>(ds), Om, rot, i, j, k);
     else if (COMP == 1) r = rhs_v_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, Om, rot, i, j, k);
     else r = rhs_w_point<T, Fld<T>>(g, rc, U, V, W, nt, nu, ds_dpdz<T>(ds), i, j, k);
@@ -462,10 +461,11 @@ static int rhs_launch(cf_ctx *ctx, int comp, int src, int mode, int s, int slot,
     Fld<T> Unlo = make_fld<T>(unlo, n1, n2);
     dim3 blk(32, 4, 1), grd(cdiv(i1 - 1, 32), cdiv(j1 - 1, 4), k1 - 1);
     T nu = (T)ctx->prm.nu, Om = (T)ctx->omega_z;
+    const int rot = fabs(ctx->omega_z) > 1e-6;  // equations.f90:169, 334
     RkCoef rk = rk_coefs();
-    if (comp == 0) k_rhs<T, 0><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
-    else if (comp == 1) k_rhs<T, 1><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
-    else k_rhs<T, 2><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    if (comp == 0) k_rhs<T, 0><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, rot, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    else if (comp == 1) k_rhs<T, 1><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, rot, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
+    else k_rhs<T, 2><<<grd, blk, 0, ctx->st>>>(g, rcp_of<T>(ctx), U, V, W, nt, ctx->ds, nu, Om, rot, out, F1, Uo, Uolo, Unlo, mode, s, rk, i1, j1, k1);
     count_launch(ctx, "k_rhs");
     CF_CUDA(cudaGetLastError());
     return 0;
@@ -513,9 +513,9 @@ template <typename T> struct RhsMinB { static constexpr int v = sizeof(T) == 4 ?
 
 template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
-                                                     NutSrc<T> ns, const DevScal *ds, T nu, T Om, Trio<T> out,
+                                                     NutSrc<T> ns, const DevScal *ds, T nu, T Om, int rot, Trio<T> out,
                                                      Trio<T> F1, Trio<T> Uo, Trio<T> Uolo, Trio<T> Unlo, int s,
-                                                     RkCoef rk, int kc_len, int ilim, int klim) {
+                                                     T ca, T cb, int kc_len, int ilim, int klim) {
     constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
     __shared__ T ring[3][4][NP];  // [plane slot][field U V W nu_t][tile]
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxg = g.nxg, nyg = g.nyg, nzg = g.nzg;
@@ -524,9 +524,6 @@ __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int i = i0 + tx, j = j0 + ty;
     const T dt = ds_dt<T>(ds), dPdx = ds_dpdx<T>(ds), dPdz = ds_dpdz<T>(ds);
-    const T ca = T(s == 1 ? rk.c[1][1] : (s == 2 ? rk.c[2][1] : rk.c[3][1]));
-    const T cb = T(s == 1 ? 0.0 : (s == 2 ? rk.c[2][2] : rk.c[3][3]));
-    const bool rot = fabs((double)Om) > 1e-6;
     // the tile's x and y reciprocal spacings and interpolation weights, and
     // the chunk's z reciprocal spacings, in shared memory; gl and rcs index
     // them with the global 1-based indices
@@ -692,6 +689,7 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
     int ntx = cdiv(ilim - 1, TX), nty = cdiv(ctx->nyg - 2, TY);
     int nkc = std::max(ctx->rhs_nkc > 0 ? ctx->rhs_nkc : 1, cdiv(ctx->nzp, RHS_ZMAX));
     int kc_len = cdiv(klim - 1, nkc);
+    const RkCoef rk = rk_coefs();  // F1 and r weights of substep s, rounded to T
     NutSrc<T> ns = {};
     if (ctx->nut_lazy) {
         ns.S = (const T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
@@ -702,7 +700,9 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
         ns.dirichlet = ctx->prm.Dirichlet_nu_t == 1;
     }
     k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(klim - 1, kc_len)), TX * TY, 0, ctx->st>>>(
-        g, rcp_of<T>(ctx), U, V, W, nt, ns, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, out, F1, Uo, Uolo, Unlo, s, rk_coefs(), kc_len,
+        g, rcp_of<T>(ctx), U, V, W, nt, ns, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, fabs(ctx->omega_z) > 1e-6 ? 1 : 0, out, F1, Uo,
+        Uolo, Unlo, s, T(s == 1 ? rk.c[1][1] : (s == 2 ? rk.c[2][1] : rk.c[3][1])),
+        T(s == 1 ? 0.0 : (s == 2 ? rk.c[2][2] : rk.c[3][3])), kc_len,
         ilim, klim);
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
@@ -853,6 +853,66 @@ __global__ void __launch_bounds__(256) k_mass_partial(Fld<T> U, const double *yg
     }
 }
 
+// mode 1 in the split path, with no FP64 instruction per row or warp (each
+// is dozens of times the cost of an FP32 one on this part): the row sum over
+// i in float-float, times c_j held as float hi + lo, accumulated per warp and
+// per block in float-float; one float-float partial per block.
+__global__ void __launch_bounds__(256) k_mass_partial_ff(Fld<float> U, const float2 *cj, int nx, int nyg, float2 *part) {
+    __shared__ float2 sh[8];
+    const int k = blockIdx.x + 2, j0 = 2 + blockIdx.y * MASS_JR;
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float ah = 0.f, al = 0.f;
+    for (int r = wp; r < MASS_JR; r += nw) {
+        const int j = j0 + r;
+        if (j > nyg - 1) break;
+        float hi = 0.f, lo = 0.f;
+#pragma unroll 8
+        for (int i = lane + 2; i <= nx - 1; i += 32) ff_add(hi, lo, U(i, j, k));
+        for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
+            ff_add(hi, lo, oh);
+            lo += ol;
+        }
+        // lane 0: (hi + lo) * (c.x + c.y), the product's rounding error
+        // recovered by an FMA
+        const float2 c = cj[j];
+        const float p = c.x * hi;
+        const float e = fmaf(c.x, hi, -p) + (c.x * lo + c.y * hi);
+        ff_add2(ah, al, p, e);
+    }
+    if (lane == 0) sh[wp] = make_float2(ah, al);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float h = 0.f, l = 0.f;
+        for (int q = 0; q < nw; q++) ff_add2(h, l, sh[q].x, sh[q].y);
+        part[blockIdx.x * gridDim.y + blockIdx.y] = make_float2(h, l);
+    }
+}
+
+// its final: the float-float partials summed in a fixed order (lane-strided,
+// warp tree, block tree), the correction of mode 1 in FP64 by one thread
+__global__ void __launch_bounds__(256) k_mass_final_ff(const float2 *part, int n, DevScal *ds, double norm) {
+    __shared__ float2 sh[8];
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    float h = 0.f, l = 0.f;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) ff_add2(h, l, part[q].x, part[q].y);
+    for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_down_sync(0xffffffffu, h, o), ol = __shfl_down_sync(0xffffffffu, l, o);
+        ff_add2(h, l, oh, ol);
+    }
+    if (lane == 0) sh[wp] = make_float2(h, l);
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    h = 0.f;
+    l = 0.f;
+    for (int q = 0; q < nw; q++) ff_add2(h, l, sh[q].x, sh[q].y);
+    const double s = (double)h + (double)l;
+    ds->mass_sum = s;
+    const double corr = ds->Qflow_x_0 - s / norm;
+    ds->lmax[2] = corr;  // scratch slot: correction before division by dt
+    ds->corrf = (float)corr;
+}
+
 // mode 2: centre-line sum (mass_flow.f90:203-204), planes k = 1..nzg-2
 template <typename T>
 __global__ void k_ucl_partial(Fld<T> U, int nx, int jc, double *part) {
@@ -957,6 +1017,16 @@ static int mass_partial(cf_ctx *ctx, int b, int mode) {
     double *part = ctx->d_red;
     int nb = ctx->nzg - 2;
     double norm;
+    if (mode == 1 && sizeof(T) == 4) {
+        const int njc = cdiv(ctx->nyg - 2, MASS_JR);
+        k_mass_partial_ff<<<dim3(nb, njc), 256, 0, ctx->st>>>(make_fld<float>(ctx->U[b], ctx->nx, ctx->nyg),
+                                                               ctx->d_mass_c, ctx->nx, ctx->nyg, (float2 *)part);
+        count_launch(ctx, "k_mass_partial");
+        k_mass_final_ff<<<1, 256, 0, ctx->st>>>((const float2 *)part, nb * njc, ctx->ds, ctx->mass_norm);
+        count_launch(ctx, "k_mass_final");
+        CF_CUDA(cudaGetLastError());
+        return 0;
+    }
     if (mode == 1) {
         const int njc = cdiv(ctx->nyg - 2, MASS_JR);
         k_mass_partial<T><<<dim3(nb, njc), 256, 0, ctx->st>>>(make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), ctx->geo.yg,
@@ -1039,15 +1109,18 @@ __device__ __forceinline__ void atomic_max_pos(double *a, double v) {
 }
 
 // CORR: the corrected convective limit of cf_params.cfl_corrected, which
-// needs the maxima of |u| per index instead (same blocks and atomics)
+// needs the maxima of |u| per index instead (same blocks and atomics).  The
+// extrema are kept in the state's precision: FP32 ones as the bit patterns of
+// non-negative floats (which order like unsigned integers) with 32-bit
+// atomics, FP64 ones as 64-bit patterns; widening a float to double is exact,
+// so the quotients of the finaliser do not depend on the storage.
 template <typename T, bool CORR>
-__global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, double *mu,
-                                                double *mv, double *mw) {
+__global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, T *mu, T *mv,
+                                                T *mw) {
     // block (x: 256 x indices, y: JR rows, z: KR planes), thread = x index i:
     // min |U| per i over the block's rows
     // and planes, min |V| per row, min |W| per plane; all loads of a plane's
-    // rows are issued together.  One global atomic per index per block;
-    // minima in the state's precision, widened exactly.
+    // rows are issued together.  One global atomic per index per block.
     constexpr int JR = 16, KR = 2;
     __shared__ T vsm[8][JR];
     __shared__ T wsm[8][KR];
@@ -1088,11 +1161,16 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
         for (int o = 16; o > 0; o >>= 1) v = ext(v, __shfl_down_sync(0xffffffff, v, o));
         if (lane == 0) vsm[wp][r] = v;
     }
-    auto put = [](double *a, double v) {
-        if (CORR) atomic_max_pos(a, v);
-        else atomic_min_pos(a, v);
+    auto put = [](T *a, T v) {
+        if constexpr (sizeof(T) == 4) {
+            if (CORR) atomicMax((unsigned *)a, __float_as_uint(v));
+            else atomicMin((unsigned *)a, __float_as_uint(v));
+        } else {
+            if (CORR) atomic_max_pos(a, v);
+            else atomic_min_pos(a, v);
+        }
     };
-    if (i <= nxg - 1) put(&mu[i], (double)umin);
+    if (i <= nxg - 1) put(&mu[i], umin);
     __syncthreads();
     const int nw = blockDim.x >> 5;
     if (threadIdx.x < JR) {
@@ -1100,57 +1178,71 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
         if (j <= nyg - 1) {
             T m = vsm[0][threadIdx.x];
             for (int q = 1; q < nw; q++) m = ext(m, vsm[q][threadIdx.x]);
-            put(&mv[j], (double)m);
+            put(&mv[j], m);
         }
     } else if (threadIdx.x >= 32 && threadIdx.x < 32 + KR) {
         const int kk = threadIdx.x - 32, k = k0 + kk;
         if (k <= nzg - 1) {
             T m = wsm[0][kk];
             for (int q = 1; q < nw; q++) m = ext(m, wsm[q][kk]);
-            put(&mw[k], (double)m);
+            put(&mw[k], m);
         }
     }
 }
 
 
-// The maxima dx/min|u| per direction (one quotient per thread: FP64
-// divisions are slow here, so they run side by side), dt, and the minima
-// reset to +inf for the next call.  corr: the minima dx/max|u| instead, the
-// maxima reset to 0.
-__global__ void __launch_bounds__(1024) k_dt_final(double *mu, double *mv, double *mw, Geo g, DevScal *ds, double CFL,
-                                                   double dt_vis, int corr, int advance_t) {
-    __shared__ double sh[3][32];
+// The maxima dx/min|u| per direction (one FP64 quotient per thread), dt, and
+// the minima reset to +inf for the next call.  corr: the minima dx/max|u|
+// instead, the maxima reset to 0.  The quotients are non-negative, so their
+// extrema are taken on the 64-bit patterns with integer compares (FP64
+// max/min chains are slow on this part); a NaN quotient is skipped like
+// fmax/fmin skip it.
+template <typename T>
+__global__ void __launch_bounds__(1024) k_dt_final(T *mu, T *mv, T *mw, Geo g, DevScal *ds, double CFL, double dt_vis,
+                                                   int corr, int advance_t) {
+    typedef unsigned long long u64;
+    __shared__ u64 sh[3][32];
     const int nxi = g.nxg - 2, nyi = g.nyg - 2, nzi = g.nzg - 2;
-    const double init = corr ? INFINITY : 0.0;
-    auto ext = [corr](double a, double b) { return corr ? fmin(a, b) : fmax(a, b); };
-    double l[3] = {init, init, init};
+    const u64 pinf = 0x7FF0000000000000ull;
+    const u64 init = corr ? pinf : 0ull;
+    auto ext = [corr](u64 a, u64 b) { return corr ? (a < b ? a : b) : (a > b ? a : b); };
+    auto key = [init, pinf](double q) {
+        const u64 b = (u64)__double_as_longlong(q);
+        return b > pinf ? init : b;
+    };
+    u64 l[3] = {init, init, init};
     for (int t = threadIdx.x; t < nxi + nyi + nzi; t += blockDim.x) {
         if (t < nxi) {
             const int i = t + 2;
-            l[0] = ext(l[0], (g.xg[i + 1] - g.xg[i]) / mu[i]);
+            l[0] = ext(l[0], key((g.xg[i + 1] - g.xg[i]) / (double)mu[i]));
         } else if (t < nxi + nyi) {
             const int j = t - nxi + 2;
-            l[1] = ext(l[1], (g.yg[j + 1] - g.yg[j]) / mv[j]);
+            l[1] = ext(l[1], key((g.yg[j + 1] - g.yg[j]) / (double)mv[j]));
         } else {
             const int k = t - nxi - nyi + 2;
-            l[2] = ext(l[2], (g.zg[k + 1] - g.zg[k]) / mw[k]);
+            l[2] = ext(l[2], key((g.zg[k + 1] - g.zg[k]) / (double)mw[k]));
         }
     }
 #pragma unroll
     for (int d = 0; d < 3; d++)
         for (int o = 16; o > 0; o >>= 1) l[d] = ext(l[d], __shfl_down_sync(0xffffffff, l[d], o));
-    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sh[0][w] = l[0]; sh[1][w] = l[1]; sh[2][w] = l[2]; }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { sh[0][w] = l[0]; sh[1][w] = l[1]; sh[2][w] = l[2]; }
     __syncthreads();
-    const double reset = corr ? 0.0 : INFINITY;
+    const T reset = corr ? T(0) : T(INFINITY);
     for (int t = threadIdx.x; t < g.nxg + 2; t += blockDim.x) mu[t] = reset;
     for (int t = threadIdx.x; t < g.nyg + 2; t += blockDim.x) mv[t] = reset;
     for (int t = threadIdx.x; t < g.nzg + 2; t += blockDim.x) mw[t] = reset;
-    if (threadIdx.x != 0) return;
-    double lU = sh[0][0], lV = sh[1][0], lW = sh[2][0];
-    for (int q = 1; q < nw; q++) {
-        lU = ext(lU, sh[0][q]); lV = ext(lV, sh[1][q]); lW = ext(lW, sh[2][q]);
+    if (w != 0) return;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        u64 x = lane < nw ? sh[d][lane] : init;
+        for (int o = 16; o > 0; o >>= 1) x = ext(x, __shfl_down_sync(0xffffffff, x, o));
+        l[d] = x;
     }
+    if (lane != 0) return;
+    const double lU = __longlong_as_double((long long)l[0]), lV = __longlong_as_double((long long)l[1]),
+                 lW = __longlong_as_double((long long)l[2]);
     double du = CFL * lU, dv = CFL * lV, dw = CFL * lW;
     double dt_conv = fmin(du, fmin(dv, dw));
     double dt = fmin(dt_conv, dt_vis);
@@ -1168,8 +1260,9 @@ __global__ void __launch_bounds__(1024) k_dt_final(double *mu, double *mv, doubl
 
 template <typename T>
 int launch_dt(cf_ctx *ctx, int b, bool advance_t) {
-    // minima start at +inf: set at context creation and reset by k_dt_final
-    double *mu = ctx->d_dtmin, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
+    // extrema start at +inf (0 for the corrected rule): set at context
+    // creation and reset by k_dt_final; stored in the state's precision
+    T *mu = (T *)ctx->d_dtmin, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
     const dim3 grd(cdiv(ctx->nxg - 2, 256), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2));
     const Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
                  W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
@@ -1180,8 +1273,8 @@ int launch_dt(cf_ctx *ctx, int b, bool advance_t) {
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
            vw = CFL * pow(ctx->dzmin, 2.0) / ctx->prm.nu;
     double dt_vis = fmin(vu, fmin(vv, vw));
-    k_dt_final<<<1, 1024, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis, ctx->prm.cfl_corrected ? 1 : 0,
-                                        advance_t ? 1 : 0);
+    k_dt_final<T><<<1, 1024, 0, ctx->st>>>(mu, mv, mw, ctx->geo, ctx->ds, CFL, dt_vis, ctx->prm.cfl_corrected ? 1 : 0,
+                                           advance_t ? 1 : 0);
     count_launch(ctx, "k_dt_final");
     CF_CUDA(cudaGetLastError());
     return 0;

@@ -239,6 +239,40 @@ __global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, in
         }
     }
 }
+// The same from float-float partials (L.M hi, lo, M.M hi, lo) of the one-pass
+// FP32 kernel: the sums in float-float, FP64 only for lane 0's quotient.
+__global__ void k_dsm_e_ff(const float4 *part, int nchunk, int nyg, double *avg, int dirichlet) {
+    const int lane = threadIdx.x & 31;
+    const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) + 2;
+    if (j > nyg - 1) return;
+    float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
+    for (int q = lane; q < nchunk; q += 32) {
+        const float4 v = part[(long)(j - 2) * nchunk + q];
+        ff_add2(ah, al, v.x, v.y);
+        ff_add2(bh, bl, v.z, v.w);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const float a1 = __shfl_down_sync(0xffffffffu, ah, o), a2 = __shfl_down_sync(0xffffffffu, al, o);
+        const float b1 = __shfl_down_sync(0xffffffffu, bh, o), b2 = __shfl_down_sync(0xffffffffu, bl, o);
+        ff_add2(ah, al, a1, a2);
+        ff_add2(bh, bl, b1, b2);
+    }
+    if (lane == 0) {
+        float *af = (float *)(avg + nyg + 2);  // FP32 copy for the split path
+        const double c = ((double)ah + (double)al) / ((double)bh + (double)bl);
+        avg[j] = c;
+        af[j] = (float)c;
+        if (j == 2) {
+            avg[1] = dirichlet ? -c : c;
+            af[1] = (float)avg[1];
+        }
+        if (j == nyg - 1) {
+            avg[nyg] = dirichlet ? -c : c;
+            af[nyg] = (float)avg[nyg];
+        }
+    }
+}
+
 // Stage F: nu_t = max(-0.5 C(j) |S|, 0) everywhere, periodic copies and the
 // wall ghost rule (subgrid.f90:521-536).
 template <typename T>
@@ -302,7 +336,11 @@ int launch_dsm(cf_ctx *ctx, int b) {
         int rc = launch_dsm_fused<T>(ctx, b);
         if (rc) return rc;
         int nch = ctx->dsm_nchunk_fused;
-        k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir);
+        if (sizeof(T) == 4)  // float-float partials of the FP32 kernel
+            k_dsm_e_ff<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>((const float4 *)ctx->dsm_part, nch, ctx->nyg,
+                                                                ctx->avg_nu_t, dir);
+        else
+            k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir);
         count_launch(ctx, "k_dsm_e");
         ctx->nut_lazy = true;  // nu_t = max(-C(j)|S|/2, 0) is formed by its readers
         CF_CUDA(cudaGetLastError());

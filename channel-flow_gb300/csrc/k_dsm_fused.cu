@@ -401,6 +401,24 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
         if (r + 2 <= re) step(r + 2, c2);
     }
     // plane partials of this block for row jo: reduce over the TX threads of the row
+    if constexpr (sizeof(T) == 4 && TX == 32) {
+        // one warp per row: a float-float shuffle tree (FP64 instructions are
+        // dozens of times the cost of FP32 ones on this part); lane 0 writes
+        // (L.M hi, lo, M.M hi, lo)
+        float ah = own ? (float)sl : 0.f, al = 0.f, bh = own ? (float)smm : 0.f, bl = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a1 = __shfl_down_sync(0xffffffffu, ah, o), a2 = __shfl_down_sync(0xffffffffu, al, o);
+            const float b1 = __shfl_down_sync(0xffffffffu, bh, o), b2 = __shfl_down_sync(0xffffffffu, bl, o);
+            ff_add2(ah, al, a1, a2);
+            ff_add2(bh, bl, b1, b2);
+        }
+        if (tx == 0 && jo <= nyg - 1) {
+            const int chunk = blockIdx.x * gridDim.z + blockIdx.z;
+            ((float4 *)part)[(long)(jo - 2) * nchunk + chunk] = make_float4(ah, al, bh, bl);
+        }
+        return;
+    }
     __syncthreads();
     double *red = (double *)sm_raw;  // 2 * TX * TY doubles fit in the R ring
     red[2 * tid] = own ? (double)sl : 0.0;

@@ -793,7 +793,7 @@ static size_t tri_split_smem(int nym) {
 // ---------------------------------------------------------------------------
 template <typename T, int N>
 __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const typename C2<T>::t *tw_g, int nym, int nzp,
-                        int LP, double scale) {
+                        int LP, T scale) {
     typedef typename C2<T>::t C;
     extern __shared__ unsigned char smraw[];
     C *sm = (C *)smraw;
@@ -834,8 +834,8 @@ __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const
     long base0 = (long)n * (jj + (long)nym * kk), base1 = (long)n * (jj + (long)nym * (kk + 1));
 #pragma unroll
     for (int q = tid; q < (N > 0 ? N : n); q += (N > 0 ? fft_x_threads(N) : G)) {
-        phi[base0 + q] = r[q].x * T(scale);
-        phi[base1 + q] = r[q].y * T(scale);
+        phi[base0 + q] = r[q].x * scale;
+        phi[base1 + q] = r[q].y * scale;
     }
 }
 
@@ -960,7 +960,7 @@ __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ul
 // interior cell (projection.f90:129-137, 144-162); KP planes per thread.
 template <typename T>
 __global__ void __launch_bounds__(128) k_store_p(Fld<T> P, const T *__restrict__ phi, PhiView pv, const DevScal *ds,
-                                                 double c11, int nxg, int nyg, int nzg) {
+                                                 T c11, int nxg, int nyg, int nzg) {
     constexpr int KP = PROJ_KP;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -973,7 +973,7 @@ __global__ void __launch_bounds__(128) k_store_p(Fld<T> P, const T *__restrict__
         const int kc = min(max(k0 + q, 2), nzg - 1);
         v[q] = k0 + q <= nzg ? phi[pv(ic, jc, kc)] : T(0);
     }
-    const T den = ds_dt<T>(ds) * T(c11);
+    const T den = ds_dt<T>(ds) * c11;
 #pragma unroll
     for (int q = 0; q < KP; q++)
         if (k0 + q <= nzg) P(i, j, k0 + q) = v[q] / den;
@@ -1083,7 +1083,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
     }
     count_launch(ctx, "k_fft_z");
     // inverse x
-    const double scale = 1.0 / ((double)nxp * (double)nzp);
+    const T scale = T(1.0 / ((double)nxp * (double)nzp));
     switch (nxp) {
         CF_FFT_SIZES(CF_INVX)
         default: k_inv_x<T, 0><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale);
