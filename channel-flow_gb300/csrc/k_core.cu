@@ -506,10 +506,11 @@ struct NutSrc {
 
 // planes per z chunk of the fused RHS (its z spacings sit in shared memory)
 constexpr int RHS_ZMAX = 256;
-// resident blocks per SM the fused RHS is compiled for: three in FP32 (80
-// registers; the kernel waits on shared-memory and arithmetic latency, so
-// more warps pay), two in FP64
-template <typename T> struct RhsMinB { static constexpr int v = sizeof(T) == 4 ? 3 : 2; };
+// resident blocks per SM the fused RHS is compiled for: two (128 registers).
+// With u, v and w computed before any store, the shared-memory reads common
+// to them are issued once but more values stay live: at three blocks (80
+// registers) the FP32 kernel spills and runs 25 % slower.
+template <typename T> struct RhsMinB { static constexpr int v = 2; };
 
 template <typename T, int TX, int TY>
 __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
@@ -638,18 +639,16 @@ __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<
         aU.i0 = aV.i0 = aW.i0 = aN.i0 = i0;
         aU.j0 = aV.j0 = aW.j0 = aN.j0 = j0;
         aU.kc = aV.kc = aW.kc = aN.kc = k;
-        if (cu) {
-            T r = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, rot, i, j, k);
-            rk_apply<T>(r, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, ca, cb, dt);
-        }
-        if (cv) {
-            T r = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, rot, i, j, k);
-            rk_apply<T>(r, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, ca, cb, dt);
-        }
-        if (cw) {
-            T r = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k);
-            rk_apply<T>(r, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, ca, cb, dt);
-        }
+        // the three right-hand sides first, every thread (the ring holds the
+        // tile and its halo, so the reads stay inside it; points outside the
+        // field are not stored): with no store between them the shared-memory
+        // reads common to u, v and w are issued once
+        const T ru = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, rot, i, j, k);
+        const T rv = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, rot, i, j, k);
+        const T rw = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k);
+        if (cu) rk_apply<T>(ru, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, ca, cb, dt);
+        if (cv) rk_apply<T>(rv, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, ca, cb, dt);
+        if (cw) rk_apply<T>(rw, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, ca, cb, dt);
         __syncthreads();            // plane k-1 no longer read
         if (k + 1 <= ke) commit(sm1);  // plane k+2 into the freed slot
         __syncthreads();
