@@ -98,8 +98,41 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
     return tab.get(kernel)
 
 
+class _Nvml:
+    """Reads the SM clock and the clock-event reasons of one GPU through
+    libnvidia-ml (read-only queries)."""
+
+    SM = 1  # NVML_CLOCK_SM
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index: int):
+        import ctypes as C
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = C.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(index), C.byref(self.h)) != 0:
+            raise RuntimeError("no NVML device %d" % index)
+        self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = C.c_uint()
+        self.max_mhz = float(mx.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, self.SM, C.byref(mx)) == 0 else None
+
+    def sample(self):
+        C = self.C
+        clk, r = C.c_uint(), C.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, self.SM, C.byref(clk)) != 0:
+            return None
+        self.reasons_fn(self.h, C.byref(r))
+        return float(clk.value), int(r.value)
+
+
 class ClockSampler:
-    """Samples nvidia-smi clocks and throttle reasons while running."""
+    """Samples the SM clock and throttle reasons while running: NVML polled
+    about every millisecond from a thread (so that even a timed region of a
+    few tens of milliseconds holds many samples), nvidia-smi at 200 ms when
+    NVML cannot be loaded."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -109,8 +142,20 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.nvml = None
+        self.samples = []
+        self.running = False
 
     def start(self):
+        try:
+            self.nvml = _Nvml(self.gpu)
+            self.nvml.sample()
+            self.running = True
+            self.thread = threading.Thread(target=self._poll, daemon=True)
+            self.thread.start()
+            return
+        except Exception:
+            self.nvml = None
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
@@ -120,11 +165,25 @@ class ClockSampler:
         except Exception:
             self.proc = None
 
+    def _poll(self):
+        while self.running:
+            s = self.nvml.sample()
+            if s is not None:
+                self.samples.append(s)
+            time.sleep(0.001)
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def stop(self) -> dict:
+        if self.nvml is not None:
+            self.running = False
+            self.thread.join(timeout=5)
+            sm = [c for c, _ in self.samples]
+            reasons = sorted({n for _, r in self.samples for bit, n in _Nvml.BITS.items() if r & bit})
+            return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": self.nvml.max_mhz,
+                    "reasons": reasons, "samples": len(sm), "source": "nvml"}
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -147,7 +206,7 @@ class ClockSampler:
                 if v.lower().startswith("active"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi"}
 
 
 def dist_info():
