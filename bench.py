@@ -98,6 +98,31 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
     return tab.get(kernel)
 
 
+def host_link(nbytes: int, dev: int) -> dict:
+    """The host link's rate for the e2e bytes: plain pinned copies of nbytes
+    each way (copy engine, CUDA events), and the per-step floor they set."""
+    import torch
+    h = torch.empty(nbytes // 8, dtype=torch.float64, pin_memory=True)
+    d = torch.empty(nbytes // 8, dtype=torch.float64, device=f"cuda:{dev}")
+    e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+    for _ in range(2):
+        d.copy_(h, non_blocking=True)
+        h.copy_(d, non_blocking=True)
+    torch.cuda.synchronize()
+    reps = 3
+    e0.record()
+    for _ in range(reps):
+        d.copy_(h, non_blocking=True)
+    e1.record()
+    for _ in range(reps):
+        h.copy_(d, non_blocking=True)
+    e2.record()
+    e2.synchronize()
+    up, down = e0.elapsed_time(e1) / reps, e1.elapsed_time(e2) / reps
+    return {"link_h2d_gbs": nbytes / up / 1e6, "link_d2h_gbs": nbytes / down / 1e6,
+            "link_floor_ms_per_step": up + down}
+
+
 class _Nvml:
     """Reads the SM clock and the clock-event reasons of one GPU through
     libnvidia-ml (read-only queries)."""
@@ -447,9 +472,10 @@ def run_ensemble(args, rank, world, local):
                                    "how": "each member's own graph, one member after another"},
             "ensemble_over_sequential": (world * nc * args.steps / seq and value / (world * nc * args.steps / seq)),
             "cpu_baseline": cpu,
-            "e2e": {"value": world * nc * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-                    "d2h_bytes_per_step": nbytes, "steps": ke,
-                    "path": "cf_upload_fields x16 + cf_ensemble_step + cf_download_fields x16, pinned host buffers"},
+            "e2e": dict({"value": world * nc * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+                         "d2h_bytes_per_step": nbytes, "steps": ke,
+                         "path": "cf_upload_fields x16 + cf_ensemble_step + cf_download_fields x16, pinned host buffers"},
+                        **host_link(nbytes, dev)),
             "gpu_launches": ens.launches_per_step() * args.steps,
             "clocks": clocks,
         }
@@ -609,6 +635,7 @@ def run_ours(args, wl, rank, world, local):
     nbytes = 8 * sum(int(np.prod(shp[k])) for k in ("U", "V", "W"))
     e2e = {"value": world * nc * ke / te, "unit": UNIT, "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
            "steps": ke, "path": "cf_upload_fields + cf_time_step_rk3 + cf_download_fields, pinned host buffers"}
+    e2e.update(host_link(nbytes, dev))
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
