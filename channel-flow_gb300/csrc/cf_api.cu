@@ -9,6 +9,7 @@
 
 int fft_setup_attrs();
 int dsm_fused_setup();
+int dsm_b_setup();
 int dsm_fused_plan(int esz, int nxp, int nym, int nzp, int sms, int *kc, size_t *nchunk);
 
 static thread_local std::string g_last_error;  // failures without a context
@@ -493,6 +494,7 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
         int dev_sms = 152;
         cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device);
         dsm_fused_setup();
+        dsm_b_setup();
         dsm_fused_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms, &ctx->dsm_kc, &nch_fused);
         ctx->use_fused_dsm = !p->dsm_unfused;
         // fused RHS: 32 x 8 column tiles, z chunks for ~4 resident blocks per SM

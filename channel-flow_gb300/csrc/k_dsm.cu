@@ -92,12 +92,31 @@ __device__ __forceinline__ T filt_can(const T *q, const Can &c, int nyg, int i, 
 // k = 2 (the reference's loops run over i = 2..nxg-1, k = 2..nzg-1).
 constexpr int DB_X = 32, DB_Y = 8, DB_NQ = 15;
 
+// asynchronous global -> shared copies of single elements (the plane gather
+// of the next z plane runs while the current one is filtered)
+template <int B>
+__device__ __forceinline__ void cp_async_elem(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(s), "l"(gmem), "n"(B) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+// dynamic shared memory of k_dsm_b: two planes of the 15 quantities
+template <typename T>
+constexpr size_t dsm_b_smem() { return (size_t)2 * DB_NQ * (DB_X + 2) * (DB_Y + 2) * sizeof(T); }
+
 template <typename T>
 __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, GeoT<T> g, RcpT<T> rc, Fld<T> Uf,
                                                       Fld<T> Vf, Fld<T> Wf, Can c, int nyg, int kc_len, double *part,
                                                       int nchunk) {
     constexpr int SX = DB_X + 2, SY = DB_Y + 2, NP = SX * SY;
-    __shared__ T pl[DB_NQ][NP];
+    extern __shared__ __align__(16) unsigned char dsmb_raw[];
+    T *plb = (T *)dsmb_raw;  // [2 planes][DB_NQ][NP]
+    // the plane filtered in y, rows of the tile (FP32: within 48 KB of static
+    // shared memory with the plane; the FP64 kernel filters from the plane)
+    constexpr bool COLS = sizeof(T) == 4;
+    __shared__ T cl[COLS ? DB_NQ : 1][DB_Y][SX];
     __shared__ double red[2][DB_X * DB_Y];
     const int tx = threadIdx.x % DB_X, ty = threadIdx.x / DB_X;
     const int i0 = 2 + blockIdx.x * DB_X, j0 = 2 + blockIdx.y * DB_Y;
@@ -106,36 +125,70 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
     const bool own = i <= c.nxp + 1 && j <= nyg - 1;
     const long n = c.n;
     const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
-    // y weights of this row (one-sided at rows 2 and nyg-1)
-    T wm = f6, w0 = f23, wp = f6;
-    if (j == 2) { wm = T(0); wp = f13; }
-    else if (j == nyg - 1) { wm = f13; wp = T(0); }
     const T fw[3] = {f6, f23, f6};
     T accp[DB_NQ], accc[DB_NQ];  // planes r-1 (two contributions in) and r (one)
 #pragma unroll
     for (int qq = 0; qq < DB_NQ; qq++) accp[qq] = accc[qq] = T(0);
+    // plane sums of this thread: FP64 in the FP64 path, float-float in the
+    // split path (an FP64 instruction per cell costs dozens of FP32 ones here)
     double sl = 0.0, smm = 0.0;
-    for (int r = kb - 1; r <= ke + 1; r++) {
+    float slh = 0.f, sll = 0.f, smh = 0.f, sml = 0.f;
+    // gather of plane r (tile plus one halo cell, periodic in x, rows clamped
+    // to the interior) into buffer b, as one group of asynchronous copies
+    auto issue = [&](int r, int b) {
         const int rc_ = wrapn(r, c.nzp);
-        __syncthreads();  // the previous plane is no longer read
         for (int e = threadIdx.x; e < NP; e += DB_X * DB_Y) {
             const int sy = e / SX, sx = e - sy * SX;
             // columns past the domain's last halo are never read: clamp them in range
             const int ii = wrapn(min(i0 + sx - 1, c.nxp + 2), c.nxp), jj = min(max(j0 + sy - 1, 2), nyg - 1);
             const long o = c(ii, jj, rc_);
 #pragma unroll
-            for (int qq = 0; qq < DB_NQ; qq++) pl[qq][e] = q[o + qq * n];
+            for (int qq = 0; qq < DB_NQ; qq++) cp_async_elem<sizeof(T)>(plb + (b * DB_NQ + qq) * NP + e, q + o + qq * n);
+        }
+        cp_async_commit();
+    };
+    issue(kb - 1, 0);
+    for (int r = kb - 1; r <= ke + 1; r++) {
+        const int cur = (r - (kb - 1)) & 1;
+        T(*pl)[NP] = (T(*)[NP])(plb + cur * DB_NQ * NP);
+        __syncthreads();  // plane r-1 (the other buffer) is no longer read
+        if (r + 1 <= ke + 1) {
+            issue(r + 1, cur ^ 1);
+            cp_async_wait<1>();  // this thread's copies of plane r are done
+        } else {
+            cp_async_wait<0>();
+        }
+        __syncthreads();  // and every thread's
+        // y filter, one (quantity, column) per task: the column's SY values
+        // give the DB_Y filtered rows (one-sided at rows 2 and nyg-1)
+        if constexpr (COLS) {
+        for (int t = threadIdx.x; t < DB_NQ * SX; t += DB_X * DB_Y) {
+            const int qq = t / SX, sx = t - qq * SX;
+            T col[SY];
+#pragma unroll
+            for (int sy = 0; sy < SY; sy++) col[sy] = pl[qq][sy * SX + sx];
+#pragma unroll
+            for (int oy = 0; oy < DB_Y; oy++) {
+                const int jr = j0 + oy;
+                const T rm = jr == 2 ? T(0) : (jr == nyg - 1 ? f13 : f6), rp = jr == 2 ? f13 : (jr == nyg - 1 ? T(0) : f6);
+                cl[qq][oy][sx] = rm * col[oy] + f23 * col[oy + 1] + rp * col[oy + 2];
+            }
         }
         __syncthreads();
+        }
         if (!own) continue;
+        // y weights of this row for the FP64 kernel (one-sided at rows 2 and nyg-1)
+        const T wm = j == 2 ? T(0) : (j == nyg - 1 ? f13 : f6), wp = j == 2 ? f13 : (j == nyg - 1 ? T(0) : f6);
         const int e = (ty + 1) * SX + tx + 1;
         T fq[DB_NQ];
 #pragma unroll
         for (int qq = 0; qq < DB_NQ; qq++) {
             T a = T(0);
 #pragma unroll
-            for (int d = -1; d <= 1; d++)
-                a += fw[d + 1] * (wm * pl[qq][e + d - SX] + w0 * pl[qq][e + d] + wp * pl[qq][e + d + SX]);
+            for (int d = -1; d <= 1; d++) {
+                if constexpr (COLS) a += fw[d + 1] * cl[qq][ty][tx + 1 + d];
+                else a += fw[d + 1] * (wm * pl[qq][e + d - SX] + f23 * pl[qq][e + d] + wp * pl[qq][e + d + SX]);
+            }
             fq[qq] = accp[qq] + f6 * a;  // plane r-1, complete
             accp[qq] = accc[qq] + f23 * a;
             accc[qq] = f6 * a;
@@ -155,9 +208,32 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
         }
         const T lm = (L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + T(2) * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]));
         const T mm = (M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + T(2) * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]));
-        const double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
-        sl += wgt * (double)lm;
-        smm += wgt * (double)mm;
+        if constexpr (sizeof(T) == 4) {
+            const float wgt = (i == 2 ? 2.f : 1.f) * (k == 2 ? 2.f : 1.f);  // exact: lm, mm times 1, 2 or 4
+            ff_add(slh, sll, wgt * lm);
+            ff_add(smh, sml, wgt * mm);
+        } else {
+            const double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
+            sl += wgt * (double)lm;
+            smm += wgt * (double)mm;
+        }
+    }
+    if constexpr (sizeof(T) == 4) {
+        // one warp per row (DB_X = 32): float-float shuffle tree, lane 0
+        // writes (L.M hi, lo, M.M hi, lo)
+        if (!own) slh = sll = smh = sml = 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a1 = __shfl_down_sync(0xffffffffu, slh, o), a2 = __shfl_down_sync(0xffffffffu, sll, o);
+            const float b1 = __shfl_down_sync(0xffffffffu, smh, o), b2 = __shfl_down_sync(0xffffffffu, sml, o);
+            ff_add2(slh, sll, a1, a2);
+            ff_add2(smh, sml, b1, b2);
+        }
+        if (tx == 0 && j <= nyg - 1) {
+            const long chunk = (long)blockIdx.z * gridDim.x + blockIdx.x;
+            ((float4 *)part)[(long)(j - 2) * nchunk + chunk] = make_float4(slh, sll, smh, sml);
+        }
+        return;
     }
     // plane partials of this block for row j: the sum over the tile's DB_X threads of the row
     red[0][threadIdx.x] = sl;
@@ -373,11 +449,15 @@ int launch_dsm(cf_ctx *ctx, int b) {
         const int kc_len = cdiv(ctx->nzp, nkc);
         const int nz_chunks = cdiv(ctx->nzp, kc_len);
         nchunk = ntx * nz_chunks;
-        k_dsm_b<T><<<dim3(ntx, cdiv(ctx->nym, DB_Y), nz_chunks), DB_X * DB_Y, 0, ctx->st>>>(
+        k_dsm_b<T><<<dim3(ntx, cdiv(ctx->nym, DB_Y), nz_chunks), DB_X * DB_Y, dsm_b_smem<T>(), ctx->st>>>(
             q, g, rc, Uf, Vf, Wf, c, ctx->nyg, kc_len, ctx->dsm_part, nchunk);
         count_launch(ctx, "k_dsm_b");
     }
-    k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
+    if (sizeof(T) == 4)  // float-float partials of the FP32 kernel
+        k_dsm_e_ff<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>((const float4 *)ctx->dsm_part, nchunk, ctx->nyg,
+                                                            ctx->avg_nu_t, dir);
+    else
+        k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
     count_launch(ctx, "k_dsm_e");
     Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
     k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(nt, q + Q_S * c.n, ctx->avg_nu_t, c,
@@ -393,3 +473,11 @@ template int launch_nut_zero<double>(cf_ctx *);
 template int launch_nut_materialize<double>(cf_ctx *);
 template int launch_nut_materialize<float>(cf_ctx *);
 template int launch_nut_zero<float>(cf_ctx *);
+
+// shared-memory opt-in of the multi-pass filter kernel (two planes in dynamic
+// shared memory; called at context creation)
+int dsm_b_setup() {
+    cudaFuncSetAttribute(k_dsm_b<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm_b_smem<float>());
+    cudaFuncSetAttribute(k_dsm_b<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm_b_smem<double>());
+    return 0;
+}
