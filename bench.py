@@ -76,7 +76,7 @@ def algorithmic_bytes(kernel: str, c, es: int) -> float | None:
         # 15 filtered quantities and Uf, Vf, Wf in (L, M and the plane sums formed in place)
         "k_dsm_b": (15 + 3) * nC * es,
         # one velocity component in and out
-        "k_dsm_c": 2 * nC * es,
+        "k_dsm_c_t": 2 * nC * es,
         "k_dsm_f": 2 * nC * es,
         # U, V, W, nu_t, Uo (+ lo), F1 in; out + F1 (substep 1 of 3 stores it)
         # one component: U, V, W, nu_t, Uo (+ its low word) and F1 in, the new

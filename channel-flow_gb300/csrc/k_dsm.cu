@@ -253,35 +253,79 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
 
 // Stage C: filtered velocities Uf, Vf, Wf (subgrid.f90:431-445) at every
 // element of their arrays; ghost and duplicate elements take the value of the
-// canonical element (the periodic fills of subgrid.f90:448-458).
-// xc/zc: 1 if the field sits at x/z centres; y one-sided at rows 1 and n2.
+// canonical element (the periodic fills of subgrid.f90:448-458); y one-sided
+// at rows 1 and n2.  A z-marching tile kernel: a block owns a 32 x 8 tile of
+// (canonical i, j), one raw plane (tile plus one halo cell) in shared memory,
+// the next plane's loads in flight in registers while the current one is
+// filtered in x and y, the z filter over a register ring of three filtered
+// planes; each canonical value is stored to every element that wraps to it.
+// (The x-y filter is taken before the z filter, the reverse of the order of
+// a 27-point loop over x outermost: the results agree to rounding.)
 template <typename T>
-__global__ void k_dsm_c(Fld<T> A, Fld<T> Af, int n1, int n2, int n3, int nxp, int nzp) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    int k = blockIdx.z + 1;
-    if (i > n1 || j > n2) return;
-    int is = wrapc(i, nxp), ks = wrapc(k, nzp);
+__global__ void __launch_bounds__(256) k_dsm_c_t(Fld<T> A, Fld<T> Af, int n1, int n2, int n3, int nxp, int nzp,
+                                                 int kc_len) {
+    constexpr int TX = 32, TY = 8, SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
+    __shared__ T pl[NP];
+    const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
+    const int is0 = 2 + blockIdx.x * TX, j0 = 1 + blockIdx.y * TY;
+    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, nzp + 1);
+    const int is = is0 + tx, j = j0 + ty;
+    const bool own = is <= nxp + 1 && j <= n2;
     const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
     T wm, w0, wp;
     if (j == 1) { wm = T(0); w0 = f23; wp = f13; }
     else if (j == n2) { wm = f13; w0 = f23; wp = T(0); }
     else { wm = f6; w0 = f23; wp = f6; }
-    int jm = j > 1 ? j - 1 : j, jp = j < n2 ? j + 1 : j;
-    const T fw[3] = {f6, f23, f6};
-    T acc = T(0);
+    // rows 0 and n2+1 of the tile read row 1 and n2 (their weight is 0);
+    // columns past the array are never read by an owned point: clamped
+    int eidx[NL];
 #pragma unroll
-    for (int a = -1; a <= 1; a++) {
-        T sz = T(0);
-#pragma unroll
-        for (int b = -1; b <= 1; b++) {
-            int ii = is + a, kk = ks + b;
-            T yv = wm * A(ii, jm, kk) + w0 * A(ii, j, kk) + wp * A(ii, jp, kk);
-            sz += fw[b + 1] * yv;
-        }
-        acc += fw[a + 1] * sz;
+    for (int q = 0; q < NL; q++) {
+        const int e = threadIdx.x + q * NT, sy = e / SX, sx = e - sy * SX;
+        const int ii = min(is0 - 1 + sx, n1), jj = min(max(j0 - 1 + sy, 1), n2);
+        eidx[q] = e < NP ? A.idx(ii, jj, 1) : -1;
     }
-    Af(i, j, k) = acc;
+    T pre[NL];
+    auto fetch = [&](int k) {
+#pragma unroll
+        for (int q = 0; q < NL; q++) pre[q] = eidx[q] >= 0 ? A.p[eidx[q] + (long)A.sz * (k - 1)] : T(0);
+    };
+    T g2 = T(0), g1 = T(0);  // x-y filtered planes p-2, p-1 at the own point
+    fetch(kb - 1);
+    for (int p = kb - 1; p <= ke + 1; p++) {
+        __syncthreads();  // the previous plane is no longer read
+#pragma unroll
+        for (int q = 0; q < NL; q++)
+            if (eidx[q] >= 0) pl[threadIdx.x + q * NT] = pre[q];
+        __syncthreads();
+        if (p + 1 <= ke + 1) fetch(p + 1);
+        if (!own) continue;
+        const int e = (ty + 1) * SX + tx + 1;
+        T g = T(0);
+#pragma unroll
+        for (int a = -1; a <= 1; a++) {
+            const T fa = a == 0 ? f23 : f6;
+            g += fa * (wm * pl[e + a - SX] + w0 * pl[e + a] + wp * pl[e + a + SX]);
+        }
+        if (p >= kb + 1) {
+            const int ks = p - 1;
+            const T v = f6 * g2 + f23 * g1 + f6 * g;
+            // every element (i, j, k) with wrapc(i) = is, wrapc(k) = ks
+#pragma unroll
+            for (int di = -1; di <= 1; di++) {
+                const int i = is + di * nxp;
+                if (i < 1 || i > n1) continue;
+#pragma unroll
+                for (int dk = -1; dk <= 1; dk++) {
+                    const int k = ks + dk * nzp;
+                    if (k < 1 || k > n3) continue;
+                    Af(i, j, k) = v;
+                }
+            }
+        }
+        g2 = g1;
+        g1 = g;
+    }
 }
 
 // Stage E: avg_nu_t(j) = <LM>/<MM> (subgrid.f90:516-518) and its ghosts.
@@ -435,10 +479,14 @@ int launch_dsm(cf_ctx *ctx, int b) {
     Fld<T> Uf = make_fld<T>(ctx->Uf, ctx->nx, ctx->nyg);
     Fld<T> Vf = make_fld<T>(ctx->Vf, ctx->nxg, ctx->ny);
     Fld<T> Wf = make_fld<T>(ctx->Wf, ctx->nxg, ctx->nyg);
-    k_dsm_c<T><<<dim3(cdiv(ctx->nx, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(U, Uf, ctx->nx, ctx->nyg, ctx->nzg, ctx->nxp, ctx->nzp);
-    k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->ny, 4), ctx->nzg), blk, 0, ctx->st>>>(V, Vf, ctx->nxg, ctx->ny, ctx->nzg, ctx->nxp, ctx->nzp);
-    k_dsm_c<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nz), blk, 0, ctx->st>>>(W, Wf, ctx->nxg, ctx->nyg, ctx->nz, ctx->nxp, ctx->nzp);
-    count_launch(ctx, "k_dsm_c"); count_launch(ctx, "k_dsm_c"); count_launch(ctx, "k_dsm_c");
+    {
+        // z chunks of 16 canonical planes
+        const int kc = 16, nkc = cdiv(ctx->nzp, kc), ntx = cdiv(ctx->nxp, 32);
+        k_dsm_c_t<T><<<dim3(ntx, cdiv(ctx->nyg, 8), nkc), 256, 0, ctx->st>>>(U, Uf, ctx->nx, ctx->nyg, ctx->nzg, ctx->nxp, ctx->nzp, kc);
+        k_dsm_c_t<T><<<dim3(ntx, cdiv(ctx->ny, 8), nkc), 256, 0, ctx->st>>>(V, Vf, ctx->nxg, ctx->ny, ctx->nzg, ctx->nxp, ctx->nzp, kc);
+        k_dsm_c_t<T><<<dim3(ntx, cdiv(ctx->nyg, 8), nkc), 256, 0, ctx->st>>>(W, Wf, ctx->nxg, ctx->nyg, ctx->nz, ctx->nxp, ctx->nzp, kc);
+    }
+    count_launch(ctx, "k_dsm_c_t"); count_launch(ctx, "k_dsm_c_t"); count_launch(ctx, "k_dsm_c_t");
     int nchunk;
     {
         // z chunks: about two waves of 256-thread tiles, within the plane-partial slots
