@@ -30,6 +30,7 @@ __global__ void k_eq_zinterp_t(Fld<T> W, int jref, int nxg, int nyg, int nzg, co
 struct EqParams {
     int ncv, jref, nx, nxg, nyg, nzg;
     double nu, h_wm, tau_mean;
+    int mixed;  // split path: FP32 Picard passes before the FP64 ones
 };
 
 // |u| at the matching row of wall point t = (i, wall, k) (wallmodel.f90:
@@ -96,11 +97,17 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
                            int nut_f32, double *tau0, double *alpha_x, double *alpha_zt, int *counters, WmState wm) {
     extern __shared__ double sg[];
     const int ncv = ep.ncv;
-    // grid: yfa[1..ncv+1], idcv[1..ncv-1], rw
+    // grid: yfa[1..ncv+1], idcv[1..ncv-1], rw; FP32 copies after them
     double *yfa = sg, *idcv = sg + ncv + 2;
-    for (int q = threadIdx.x; q < ncv + 2; q += blockDim.x) yfa[q] = q >= 1 && q <= ncv + 1 ? grid[ncv + q] : 0.0;
-    for (int q = threadIdx.x; q < ncv + 1; q += blockDim.x)
+    float *yfa32 = (float *)(idcv + ncv + 1), *idcv32 = yfa32 + ncv + 2;
+    for (int q = threadIdx.x; q < ncv + 2; q += blockDim.x) {
+        yfa[q] = q >= 1 && q <= ncv + 1 ? grid[ncv + q] : 0.0;
+        yfa32[q] = (float)yfa[q];
+    }
+    for (int q = threadIdx.x; q < ncv + 1; q += blockDim.x) {
         idcv[q] = (q >= 1 && q <= ncv - 1) ? 1.0 / (grid[q + 1] - grid[q]) : 0.0;
+        idcv32[q] = (float)idcv[q];
+    }
     __syncthreads();
     const double rw = 1.0 / (grid[1] - grid[ncv + 1]);
     long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -121,6 +128,45 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
         const int max_iter = 100;
         double tau_lam = mu_lam * u_les / ep.h_wm;
         int iter = 0;
+        if (ep.mixed) {
+            // Split path: the same Picard passes in FP32 (at most 50) until
+            // the change is below 1e-5 of tau (FP32 resolves about 1e-7), the
+            // unconverged ones counted like FP64 passes; the FP64 passes
+            // below then start next to the fixed point and reach the
+            // reference's criterion after a few passes, instead of all of
+            // them in FP64 (each FP64 pass costs dozens of FP32 ones here).
+            // A non-finite or non-positive FP32 result starts the FP64
+            // passes from the initial tau instead.
+            const float mu32 = (float)mu_lam, ul32 = (float)u_les, rw32 = (float)rw;
+            const float c0 = (float)(rho * kappa), cdf = (float)(1.0 / (mu_lam / rho) / Aplus);
+            float t = (float)tau;
+            int it = 0;
+            while (it < 50) {
+                const float tp = t, ut = sqrtf(t), c1 = c0 * ut, cd = ut * cdf;
+                float al = ul32, be = 0.f, yf = yfa32[ncv];
+                float D = 1.f - __expf(-(yf * cd));
+                float mu_up = mu32 + c1 * yf * (D * D);
+                for (int q = ncv - 1; q >= 2; q--) {
+                    yf = yfa32[q];
+                    D = 1.f - __expf(-(yf * cd));
+                    const float mu_q = mu32 + c1 * yf * (D * D);
+                    const float sup = mu_up * idcv32[q], sub = mu_q * idcv32[q - 1];
+                    const float rm = 1.f / (-(sup + sub) + sup * be);
+                    al = -sup * al * rm;
+                    be = -sub * rm;
+                    mu_up = mu_q;
+                }
+                const float sup = mu_up * idcv32[1];
+                const float x1 = -sup * al / (-(sup + mu32 * rw32) + sup * be);
+                t = mu32 * x1 * rw32;
+                if (fabsf(t - tp) < 1e-5f * fabsf(t)) break;
+                it++;
+            }
+            if (isfinite(t) && t > 0.f) {
+                tau = (double)t;
+                iter = it;
+            }
+        }
         while (true) {
             double tau_prev = tau;
             double nu_eq = mu_lam / rho;
@@ -255,9 +301,10 @@ int launch_eqwm(cf_ctx *ctx, int b) {
     ep.nu = ctx->prm.nu;
     ep.h_wm = ctx->hyg[ep.jref];
     ep.tau_mean = ctx->hs.tau_mean_eqwm;
+    ep.mixed = sizeof(T) == 4;
     CF_CUDA(cudaMemsetAsync(ctx->d_red, 0, 2 * sizeof(int), ctx->st));
     long npts = (long)nx * nzg * 2;
-    size_t sh = (size_t)(2 * ep.ncv + 4) * sizeof(double);
+    size_t sh = (size_t)(2 * ep.ncv + 4) * (sizeof(double) + sizeof(float));
     Fld<double> Ud = make_fld<double>(ctx->U[b], nx, nyg);
     WmState wm = {};
     if (ctx->wmlp) {
