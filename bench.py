@@ -289,9 +289,11 @@ def make_channel(wl, precision, device, seed, cfl=0.5):
     return ch, (x, y, z, U, V, W, prm)
 
 
-def cpu_baseline(wl, steps, threads):
+def cpu_baseline(wl, steps, threads, target_s=12.0):
     """The CPU oracle (C restatement of the reference CPU path, OpenMP) on the
-    same workload: `steps` full RK3 steps after one untimed step."""
+    same workload: `steps` full RK3 steps after one untimed step; steps = 0
+    takes as many as fill about `target_s` seconds at the untimed step's pace
+    (at most 50)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     from oracle import Oracle
     from channelflow import grids
@@ -304,7 +306,10 @@ def cpu_baseline(wl, steps, threads):
     o.set_fields(U, V, W)
     o.init_mass_flow()
     o.apply_boundary_conditions()
+    t0 = time.perf_counter()
     o.compute_dt(); o.time_step_rk3()
+    if steps <= 0:
+        steps = max(1, min(50, int(math.ceil(target_s / max(time.perf_counter() - t0, 1e-3)))))
     t0 = time.perf_counter()
     for _ in range(steps):
         o.compute_dt()
@@ -312,7 +317,7 @@ def cpu_baseline(wl, steps, threads):
     dt = time.perf_counter() - t0
     o.close()
     nc = (wl["nx"] - 2) * (wl["ny"] - 1) * (wl["nz"] - 2)
-    return nc * steps / dt, dt
+    return nc * steps / dt, dt, steps
 
 
 def stats_run(wl, steps, every, device):
@@ -445,17 +450,19 @@ def run_ensemble(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu:
         # one member of each grid through the CPU oracle, scaled by the member counts
         thr = os.cpu_count() or 1
-        tot_s, tot_c = 0.0, 0
+        tot_s, tot_c, sample = 0.0, 0, []
         for nx, ny, nz, cnt in ((66, 65, 66, 6), (98, 65, 98, 6), (130, 97, 130, 4)):
             wl = dict(nx=nx, ny=ny, nz=nz, retau=395.0, stretch=1.5, les=2, wall=0, jref=3, ncv=100,
                       profile="laminar")
-            v, sec = cpu_baseline(wl, 1, thr)
+            v, sec, nst = cpu_baseline(wl, 0, thr, target_s=4.0)
             cells = (nx - 2) * (ny - 1) * (nz - 2)
             tot_s += cnt * cells / v
             tot_c += cnt * cells
+            sample.append(f"{nst} steps of {nx}x{ny}x{nz} ({sec:.1f} s)")
         cpu = {"value": tot_c / tot_s, "unit": UNIT, "cores": thr, "kind": "port",
-               "sample": "one RK3 step of one member of each grid (C restatement of the reference CPU path, "
-                         "OpenMP), the ensemble's time as the members' sum"}
+               "sample": "RK3 steps of one member of each grid: " + ", ".join(sample) +
+                         " (C restatement of the reference CPU path, OpenMP), the ensemble's time as the "
+                         "members' sum"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -641,9 +648,9 @@ def run_ours(args, wl, rank, world, local):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         thr = os.cpu_count() or 1
-        cv, csec = cpu_baseline(wl, args.cpu_steps, thr)
+        cv, csec, cst = cpu_baseline(wl, args.cpu_steps, thr)
         cpu = {"value": cv, "unit": UNIT, "cores": thr, "kind": "port",
-               "sample": f"{args.cpu_steps} full RK3 steps of the same workload after 1 untimed step "
+               "sample": f"{cst} full RK3 steps of the same workload after 1 untimed step "
                          f"({csec:.1f} s; C restatement of the reference CPU path, OpenMP)"}
 
     launches = ch.launches_per_step() * args.steps
@@ -688,7 +695,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="re550", choices=sorted(WORKLOADS) + ["ensemble16"])
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=0,
+                    help="steps of the CPU baseline (0: as many as fill about 12 s)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="only run N steps of the split path after one warm-up step (for ncu)")
