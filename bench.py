@@ -605,16 +605,26 @@ def run_ours(args, wl, rank, world, local):
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     ab = algorithmic_bytes(dom, ch, 4)
     avg_s = dom_ms / dom_n / 1e3
-    traffic = None
+    traffic, wavefronts = None, None
     try:
         tj = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
         traffic = tj.get(wl["name"], {}).get(dom)
+        wavefronts = tj.get(wl["name"], {}).get(dom + ":smem_wavefronts")
     except Exception:
         pass
     roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak, "peak_source": peak_src,
             "achieved": (ab / avg_s / 1e9) if ab else None, "frac": (ab / avg_s / 1e9 / hbm_peak) if ab else None,
             "traffic": traffic, "avg_launch_ms": avg_s * 1e3, "launches_per_step": dom_n / 2,
             "share_of_step": dom_ms / tot if tot else None}
+    if wavefronts:
+        # the bound the kernel actually meets: shared-memory wavefronts of one
+        # launch (ncu) at one per clock per SM, at the clock sampled above
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        mhz = clocks.get("sm_mhz") or 2070.0
+        floor_s = wavefronts / sms / (mhz * 1e6)
+        roof["smem_bound"] = {"wavefronts_per_launch": wavefronts, "floor_ms": floor_s * 1e3,
+                              "frac": floor_s / avg_s, "how": "ncu l1tex__data_pipe_lsu_wavefronts_mem_shared.sum "
+                              "of one launch / (SMs x SM clock)"}
 
     # ---- end to end through the public API with host buffers
     shp = ch.shapes
