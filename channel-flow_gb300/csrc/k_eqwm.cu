@@ -128,6 +128,7 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
         const int max_iter = 100;
         double tau_lam = mu_lam * u_les / ep.h_wm;
         int iter = 0;
+        bool mixed_ok = false;  // the FP32 passes gave the FP64 ones their start
         if (ep.mixed) {
             // Split path: the same Picard passes in FP32 (at most 50) until
             // the change is below 1e-5 of tau (FP32 resolves about 1e-7), the
@@ -165,10 +166,12 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
             if (isfinite(t) && t > 0.f) {
                 tau = (double)t;
                 iter = it;
+                mixed_ok = true;
             }
         }
-        while (true) {
-            double tau_prev = tau;
+        // one FP64 Picard pass of solve_u_eqwm (eqwm.f90:121-205): tau from
+        // the mixing-length viscosity of the previous tau
+        auto pass64 = [&](double tau) -> double {
             double nu_eq = mu_lam / rho;
             double utau = sqrt(tau / rho);
             double c1 = rho * kappa * utau;
@@ -194,7 +197,35 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
             double sup = mu_up * idcv[1];
             double diag = -1.0 * (sup + mu_lam * rw);
             double x1 = -sup * al / (diag + sup * be);
-            tau = mu_lam * (x1 - 0.0) * rw;
+            return mu_lam * (x1 - 0.0) * rw;
+        };
+        bool fin = false;
+        if (ep.mixed && mixed_ok) {
+            // Split path, from the FP32 iterate: two FP64 passes (checked and
+            // counted like the reference's), then Aitken's extrapolation of
+            // the linearly converging sequence; the reference passes below
+            // take it from there to the reference's criterion.
+            const double t0 = tau, t1 = pass64(t0);
+            if (fabs((t1 - t0) / tau_lam) < tol) {
+                tau = t1;
+                fin = true;
+            } else {
+                iter = iter + 1;
+                const double t2 = pass64(t1);
+                if (fabs((t2 - t1) / tau_lam) < tol) {
+                    tau = t2;
+                    fin = true;
+                } else {
+                    iter = iter + 1;
+                    const double d1 = t1 - t0, d2 = t2 - t1, den = d2 - d1;
+                    const double ta = den != 0.0 ? t2 - d2 * d2 / den : t2;
+                    tau = (isfinite(ta) && ta > 0.0) ? ta : t2;
+                }
+            }
+        }
+        while (!fin) {
+            double tau_prev = tau;
+            tau = pass64(tau);
             int done = 0;
             if (fabs((tau - tau_prev) / tau_lam) < tol) done = 1;
             if (done == 0) iter = iter + 1;
