@@ -507,10 +507,11 @@ int launch_dsm(cf_ctx *ctx, int b) {
     else
         k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
     count_launch(ctx, "k_dsm_e");
-    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
-    k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), blk, 0, ctx->st>>>(nt, q + Q_S * c.n, ctx->avg_nu_t, c,
-                                                                                            ctx->nxg, ctx->nyg, ctx->nzg, dir);
-    count_launch(ctx, "k_dsm_f");
+    // stage F (nu_t = max(-C(j)|S|/2, 0) everywhere) is left to the readers,
+    // as after the one-pass kernel: |S| sits in the same canonical slot, the
+    // fused RHS forms nu_t in its loader and the other readers (eqwm,
+    // statistics, downloads) materialise it first
+    ctx->nut_lazy = true;
     CF_CUDA(cudaGetLastError());
     return 0;
 }
