@@ -10,6 +10,7 @@
 int fft_setup_attrs();
 int dsm_fused_setup();
 int dsm_b_setup();
+int dsm_b_plan(int esz, int nxp, int nym, int nzp, int sms);
 int dsm_fused_plan(int esz, int nxp, int nym, int nzp, int sms, int *kc, size_t *nchunk);
 
 static thread_local std::string g_last_error;  // failures without a context
@@ -511,8 +512,10 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
         }
         ctx->rhs_nkc = (int)best;
         if (p->LES_model == 3) amd_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms, &ctx->amd_nkc, &amd_parts);
+        ctx->dsmb_nkc = dsm_b_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms);
     }
-    size_t nch = std::max({(size_t)ctx->dsm_nblk, nch_fused, (size_t)cdiv(amd_parts, 2)});
+    size_t nch = std::max({(size_t)ctx->dsm_nblk, nch_fused, (size_t)cdiv(amd_parts, 2),
+                           (size_t)cdiv(nxp, 32) * (size_t)ctx->dsmb_nkc});
     CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));
     ctx->dsm_part_nch = nch;
     // avg_nu_t (1..nyg) in FP64, followed by an FP32 copy

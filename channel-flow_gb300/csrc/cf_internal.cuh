@@ -198,6 +198,7 @@ struct cf_ctx {
     int dsm_kc = 0;                    // z-chunk length of the fused pass
     int dsm_nchunk_fused = 0;
     bool use_fused_dsm = true;
+    int dsmb_nkc = 0;                  // z chunks of the multi-pass DSM filter kernel
     bool use_rhs3 = true;              // one fused RHS + update launch per substep
     int rhs_nkc = 1;                   // z chunks of the fused RHS
     int amd_nkc = 1;                   // z chunks of the AMD pass

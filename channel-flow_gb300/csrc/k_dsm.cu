@@ -489,11 +489,9 @@ int launch_dsm(cf_ctx *ctx, int b) {
     count_launch(ctx, "k_dsm_c_t"); count_launch(ctx, "k_dsm_c_t"); count_launch(ctx, "k_dsm_c_t");
     int nchunk;
     {
-        // z chunks: about two waves of 256-thread tiles, within the plane-partial slots
+        // z chunks planned at context creation (dsm_b_plan), within the plane-partial slots
         const int ntx = cdiv(ctx->nxp, DB_X);
-        const long tiles = (long)ntx * cdiv(ctx->nym, DB_Y);
-        long nkc = std::max(1L, std::min((long)ctx->nzp / 4, (2L * 152 * 4 + tiles - 1) / tiles));
-        nkc = std::max(1L, std::min(nkc, (long)ctx->dsm_part_nch / ntx));
+        long nkc = std::max(1L, std::min((long)std::max(ctx->dsmb_nkc, 1), (long)ctx->dsm_part_nch / ntx));
         const int kc_len = cdiv(ctx->nzp, nkc);
         const int nz_chunks = cdiv(ctx->nzp, kc_len);
         nchunk = ntx * nz_chunks;
@@ -522,6 +520,27 @@ template int launch_nut_zero<double>(cf_ctx *);
 template int launch_nut_materialize<double>(cf_ctx *);
 template int launch_nut_materialize<float>(cf_ctx *);
 template int launch_nut_zero<float>(cf_ctx *);
+
+// z chunks of the multi-pass filter kernel: the count that minimises (waves
+// of resident blocks) x (planes per chunk + the 2 halo planes a chunk loads
+// again); its plane partials take ceil(nxp / 32) x nkc slots per row
+int dsm_b_plan(int esz, int nxp, int nym, int nzp, int sms) {
+    int per = 1;
+    if (esz == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dsm_b<float>, DB_X * DB_Y, dsm_b_smem<float>());
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dsm_b<double>, DB_X * DB_Y, dsm_b_smem<double>());
+    const long tiles = (long)cdiv(nxp, DB_X) * cdiv(nym, DB_Y), res = (long)(per < 1 ? 1 : per) * sms;
+    long best = 1;
+    double best_cost = 1e300;
+    for (long n = 1; n <= std::max(1L, (long)nzp / 4); n++) {
+        const double waves = (double)((tiles * n + res - 1) / res);
+        const double cost = waves * ((double)cdiv(nzp, n) + 2.0);
+        if (cost < best_cost - 1e-9) {
+            best_cost = cost;
+            best = n;
+        }
+    }
+    return (int)best;
+}
 
 // shared-memory opt-in of the multi-pass filter kernel (two planes in dynamic
 // shared memory; called at context creation)
