@@ -246,11 +246,42 @@ __global__ void k_fwd_x(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>:
     // need not be filled before this kernel
     const int km = k == 2 ? nzp + 1 : k - 1;
     if (active) {
-        if constexpr (sizeof(T) == 4) {
-            // split path: reciprocal spacings instead of divisions
+        if constexpr (sizeof(T) == 4 && N > 0) {
+            // split path, compile-time length: reciprocal spacings instead of
+            // divisions; the loads of XB points are issued before any of them
+            // is used or stored (a shared-memory store would otherwise order
+            // every later load of U, V, W behind it)
+            constexpr int GX = fft_x_threads(N), NPT = N / GX, XB = NPT < 3 ? NPT : 3;
             const float ry = rs.ry[j], rz0 = rs.rz[k], rz1 = rs.rz[k + 1];
+            const int k1 = k + 1;
 #pragma unroll
-            for (int i = tid + 2; i <= (N > 0 ? N : n) + 1; i += (N > 0 ? fft_x_threads(N) : G)) {
+            for (int e0 = 0; e0 < NPT; e0 += XB) {
+                float ua[XB], uam[XB], ub[XB], ubm[XB], va[XB], vam[XB], vb[XB], vbm[XB], wa[XB], wb[XB], wm[XB], rx[XB];
+#pragma unroll
+                for (int b = 0; b < XB; b++) {
+                    const int i = tid + 2 + (e0 + b) * GX, im = i == 2 ? n + 1 : i - 1;
+                    if (e0 + b < NPT) {
+                        rx[b] = rs.rx[i];
+                        ua[b] = U(i, j, k); uam[b] = U(im, j, k); ub[b] = U(i, j, k1); ubm[b] = U(im, j, k1);
+                        va[b] = V(i, j, k); vam[b] = V(i, j - 1, k); vb[b] = V(i, j, k1); vbm[b] = V(i, j - 1, k1);
+                        wa[b] = W(i, j, k); wb[b] = W(i, j, k1); wm[b] = W(i, j, km);
+                    }
+                }
+#pragma unroll
+                for (int b = 0; b < XB; b++) {
+                    if (e0 + b < NPT) {
+                        const int i = tid + 2 + (e0 + b) * GX;
+                        C z;
+                        z.x = (ua[b] - uam[b]) * rx[b] + (va[b] - vam[b]) * ry + (wa[b] - wm[b]) * rz0;
+                        z.y = (ub[b] - ubm[b]) * rx[b] + (vb[b] - vbm[b]) * ry + (wb[b] - wa[b]) * rz1;
+                        a[i - 2] = z;
+                    }
+                }
+            }
+        } else if constexpr (sizeof(T) == 4) {
+            // split path, run-time length
+            const float ry = rs.ry[j], rz0 = rs.rz[k], rz1 = rs.rz[k + 1];
+            for (int i = tid + 2; i <= n + 1; i += G) {
                 const float rx = rs.rx[i];
                 const int k1 = k + 1, im = i == 2 ? n + 1 : i - 1;
                 const float w0 = W(i, j, k), w1 = W(i, j, k1);
@@ -809,10 +840,36 @@ __global__ void k_inv_x(const typename C2<T>::t *spec, T *phi, FftPlan pl, const
         kk = (int)(pair / nym) * 2;
     }
     C *a = sm + (long)lp * 2 * n, *b = a + n;
-    if (active) {
+    if (active && N > 0) {
+        // compile-time length: every load of the thread issued before the
+        // first store to shared memory
+        constexpr int GX = fft_x_threads(N > 0 ? N : 16), NPT = N > 0 ? N / GX : 1;
         const C *s0 = spec + ((long)jj * nzp + kk) * nh, *s1 = spec + ((long)jj * nzp + kk + 1) * nh;
+        C A[NPT], B[NPT];
 #pragma unroll
-        for (int q = tid; q < (N > 0 ? N : n); q += (N > 0 ? fft_x_threads(N) : G)) {
+        for (int e = 0; e < NPT; e++) {
+            const int q = tid + e * GX, src = q < nh ? q : n - q;
+            A[e] = s0[src];
+            B[e] = s1[src];
+        }
+#pragma unroll
+        for (int e = 0; e < NPT; e++) {
+            const int q = tid + e * GX;
+            C a0 = A[e], b0 = B[e];
+            if (q < nh) {
+                if (q == 0 || 2 * q == n) { a0.y = 0; b0.y = 0; }
+            } else {
+                a0 = cconj(a0);
+                b0 = cconj(b0);
+            }
+            C z;  // A + i B
+            z.x = a0.x - b0.y;
+            z.y = a0.y + b0.x;
+            a[q] = z;
+        }
+    } else if (active) {
+        const C *s0 = spec + ((long)jj * nzp + kk) * nh, *s1 = spec + ((long)jj * nzp + kk + 1) * nh;
+        for (int q = tid; q < n; q += G) {
             C A, B;
             if (q < nh) {
                 A = s0[q];
