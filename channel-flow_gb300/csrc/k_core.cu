@@ -865,8 +865,17 @@ __global__ void __launch_bounds__(256) k_mass_partial_ff(Fld<float> U, const flo
         const int j = j0 + r;
         if (j > nyg - 1) break;
         float hi = 0.f, lo = 0.f;
-#pragma unroll 8
-        for (int i = lane + 2; i <= nx - 1; i += 32) ff_add(hi, lo, U(i, j, k));
+        // the row's loads issued MP at a time before they are summed (a
+        // dependent sum per load would wait out the memory latency each time)
+        constexpr int MP = 8;
+        for (int i0 = lane + 2; i0 <= nx - 1; i0 += 32 * MP) {
+            float v[MP];
+#pragma unroll
+            for (int q = 0; q < MP; q++) v[q] = i0 + 32 * q <= nx - 1 ? U(i0 + 32 * q, j, k) : 0.f;
+#pragma unroll
+            for (int q = 0; q < MP; q++)
+                if (i0 + 32 * q <= nx - 1) ff_add(hi, lo, v[q]);
+        }
         for (int o = 16; o > 0; o >>= 1) {
             const float oh = __shfl_down_sync(0xffffffffu, hi, o), ol = __shfl_down_sync(0xffffffffu, lo, o);
             ff_add(hi, lo, oh);
@@ -1116,7 +1125,7 @@ __device__ __forceinline__ void atomic_max_pos(double *a, double v) {
 template <typename T, bool CORR>
 __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, int nxg, int nyg, int nzg, T *mu, T *mv,
                                                 T *mw) {
-    // block (x: 256 x indices, y: JR rows, z: KR planes), thread = x index i:
+    // block (x: up to 256 x indices, y: JR rows, z: KR planes), thread = x index i:
     // min |U| per i over the block's rows
     // and planes, min |V| per row, min |W| per plane; all loads of a plane's
     // rows are issued together.  One global atomic per index per block.
@@ -1124,7 +1133,7 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
     __shared__ T vsm[8][JR];
     __shared__ T wsm[8][KR];
     const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-    const int i = 2 + blockIdx.x * 256 + threadIdx.x, j0 = 2 + blockIdx.y * JR, k0 = 2 + blockIdx.z * KR;
+    const int i = 2 + blockIdx.x * blockDim.x + threadIdx.x, j0 = 2 + blockIdx.y * JR, k0 = 2 + blockIdx.z * KR;
     const T init = CORR ? T(0) : T(INFINITY);
     auto ext = [](T a, T b) { return CORR ? fmax(a, b) : fmin(a, b); };
     T umin = init;
@@ -1179,8 +1188,8 @@ __global__ void __launch_bounds__(256) k_dt_min(Fld<T> U, Fld<T> V, Fld<T> W, in
             for (int q = 1; q < nw; q++) m = ext(m, vsm[q][threadIdx.x]);
             put(&mv[j], m);
         }
-    } else if (threadIdx.x >= 32 && threadIdx.x < 32 + KR) {
-        const int kk = threadIdx.x - 32, k = k0 + kk;
+    } else if (threadIdx.x < JR + KR) {  // JR + KR <= 32: present in a one-warp block too
+        const int kk = threadIdx.x - JR, k = k0 + kk;
         if (k <= nzg - 1) {
             T m = wsm[0][kk];
             for (int q = 1; q < nw; q++) m = ext(m, wsm[q][kk]);
@@ -1262,11 +1271,14 @@ int launch_dt(cf_ctx *ctx, int b, bool advance_t) {
     // extrema start at +inf (0 for the corrected rule): set at context
     // creation and reset by k_dt_final; stored in the state's precision
     T *mu = (T *)ctx->d_dtmin, *mv = mu + ctx->nxg + 2, *mw = mv + ctx->nyg + 2;
-    const dim3 grd(cdiv(ctx->nxg - 2, 256), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2));
+    // blocks as wide as the x range (whole warps, at most 256 threads): no
+    // idle threads, and more of the small blocks resident at once
+    const int bx = std::min(256, 32 * cdiv(ctx->nxg - 2, 32));
+    const dim3 grd(cdiv(ctx->nxg - 2, bx), cdiv(ctx->nyg - 2, 16), cdiv(ctx->nzg - 2, 2));
     const Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg), V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny),
                  W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
-    if (ctx->prm.cfl_corrected) k_dt_min<T, true><<<grd, 256, 0, ctx->st>>>(U, V, W, ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
-    else k_dt_min<T, false><<<grd, 256, 0, ctx->st>>>(U, V, W, ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
+    if (ctx->prm.cfl_corrected) k_dt_min<T, true><<<grd, bx, 0, ctx->st>>>(U, V, W, ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
+    else k_dt_min<T, false><<<grd, bx, 0, ctx->st>>>(U, V, W, ctx->nxg, ctx->nyg, ctx->nzg, mu, mv, mw);
     count_launch(ctx, "k_dt_min");
     double CFL = ctx->prm.CFL;
     double vu = CFL * pow(ctx->dxmin, 2.0) / ctx->prm.nu, vv = CFL * pow(ctx->dymin, 2.0) / ctx->prm.nu,
