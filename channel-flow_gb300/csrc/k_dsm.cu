@@ -152,12 +152,16 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
         const int cur = (r - (kb - 1)) & 1;
         T(*pl)[NP] = (T(*)[NP])(plb + cur * DB_NQ * NP);
         __syncthreads();  // plane r-1 (the other buffer) is no longer read
-        if (r + 1 <= ke + 1) {
-            issue(r + 1, cur ^ 1);
-            cp_async_wait<1>();  // this thread's copies of plane r are done
-        } else {
-            cp_async_wait<0>();
-        }
+        if (r + 1 <= ke + 1) issue(r + 1, cur ^ 1);
+        // S_ij of the filtered velocities at the output plane k = r-1
+        // (fil_size**2 = 4 in M, subgrid.f90:156, 463), read from global
+        // memory while the plane copies are in flight
+        const int k = r - 1;
+        const bool outp = own && k >= kb;
+        T sf[6], Sf = T(0);
+        if (outp) sij_point<T>(g, rc, Uf, Vf, Wf, i, j, k, sf, Sf);
+        if (r + 1 <= ke + 1) cp_async_wait<1>();  // this thread's copies of plane r are done
+        else cp_async_wait<0>();
         __syncthreads();  // and every thread's
         // y filter, one (quantity, column) per task: the column's SY values
         // give the DB_Y filtered rows (one-sided at rows 2 and nyg-1)
@@ -193,11 +197,7 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
             accp[qq] = accc[qq] + f23 * a;
             accc[qq] = f6 * a;
         }
-        const int k = r - 1;
-        if (k < kb) continue;
-        // M from S_ij of the filtered velocities (fil_size**2 = 4, subgrid.f90:156, 463)
-        T sf[6], Sf;
-        sij_point<T>(g, rc, Uf, Vf, Wf, i, j, k, sf, Sf);
+        if (!outp) continue;
         const T fu = fq[0], fv = fq[1], fwv = fq[2];
         const T pa[6] = {fu, fv, fwv, fu, fu, fv}, pb[6] = {fu, fv, fwv, fv, fwv, fwv};
         T L[6], M[6];
