@@ -53,8 +53,9 @@ constexpr int DSM_ZMAX = DSM_ZMAX_HOST;
 template <typename T, int TX, int TY>
 struct DsmSmem {
     static constexpr int RX = TX + 4, RY = TY + 4, QX = TX + 2, QY = TY + 2;
-    static constexpr int NR = 9 * RX * RY, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY, NC = 16 * QX * TY;
-    static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ + NC) * sizeof(T);
+    static constexpr int NR = 9 * RX * RY, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY, NC = 16 * QX * TY,
+                         NY = 3 * QY * RX;
+    static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ + NC + NY) * sizeof(T);
 };
 
 // resident blocks per SM the pass is compiled for (three blocks at 80
@@ -74,6 +75,7 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
     typedef typename PairT<T>::t PT;
     PT *Qs = (PT *)(F + SM::NF);  // [8 pairs][QY][QX]
     PT *Cs = Qs + SM::NQ / 2;     // [8 pairs][TY][QX]: Q filtered in y
+    T *Ry = (T *)(Cs + SM::NC / 2);  // [field 3][QY][RX]: the raw plane filtered in y
     const T *rdx = (const T *)rgv.rdx, *rdxg = (const T *)rgv.rdxg, *rdy = (const T *)rgv.rdy,
             *rdyg = (const T *)rgv.rdyg, *rdz = (const T *)rgv.rdz, *rdzg = (const T *)rgv.rdzg;
     const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0), h = T(0.5), qq = T(0.25);
@@ -88,6 +90,7 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
     auto FS = [&](int slot, int f, int sy, int sx) -> T & { return F[((slot * 3 + f) * QY + sy) * QX + sx]; };
     auto QS = [&](int p, int sy, int sx) -> PT & { return Qs[(p * QY + sy) * QX + sx]; };
     auto CS = [&](int p, int oy, int sx) -> PT & { return Cs[(p * TY + oy) * QX + sx]; };
+    auto YS = [&](int f, int sy, int rx) -> T & { return Ry[(f * QY + sy) * RX + rx]; };
 
     // y filter weights of a row in [lo, hi] (one-sided at the ends)
     auto yw = [&](int j, int lo, int hi, T &wm, T &w0, T &wp) {
@@ -181,6 +184,24 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
         constexpr int PH = decltype(PHc)::value;
         constexpr int P1 = (PH + 1) % 3, P2 = (PH + 2) % 3;
         if (r + 1 <= re) fetch(r + 1);
+        // -- y filter of the raw plane R(r) (slot PH), one (field, raw
+        // column) per task: the column's RY values give the QY rows of the
+        // region (one-sided at rows 1 and jhi); G below is its x filter
+        for (int t = tid; t < 3 * RX; t += NTH) {
+            const int f = t / RX, rx = t - f * RX, jhi = f == 1 ? ny : nyg;
+            T col[RY];
+#pragma unroll
+            for (int q = 0; q < RY; q++) col[q] = RS(PH, f, q, rx);
+#pragma unroll
+            for (int sy = 0; sy < QY; sy++) {
+                const int j = j0 + sy - 1;
+                T wm, w0, wp;
+                yw(j, 1, jhi, wm, w0, wp);
+                const T cm = j > 1 ? col[sy] : col[sy + 1], cp = j < jhi ? col[sy + 2] : col[sy + 1];
+                YS(f, sy, rx) = wm * cm + w0 * col[sy + 1] + wp * cp;
+            }
+        }
+        __syncthreads();
         // G(r), F(r-1) and Q(r-1) at this thread's points of the tile + 1 halo
         // (its own point, and one point of the halo ring for the first
         // 2 QX + 2 TY threads): G and F at a point only need that point's G
@@ -198,15 +219,8 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
                 const int jhi = f == 1 ? ny : nyg;
                 T g = T(0);
                 if (j >= 1 && j <= jhi) {
-                    T wm, w0, wp;
-                    yw(j, 1, jhi, wm, w0, wp);
-                    const int dm = j > 1 ? -1 : 0, dp = j < jhi ? 1 : 0;
 #pragma unroll
-                    for (int a = -1; a <= 1; a++) {
-                        const int rx = sx + 1 + a, ry = sy + 1;
-                        const T yv = wm * RS(PH, f, ry + dm, rx) + w0 * RS(PH, f, ry, rx) + wp * RS(PH, f, ry + dp, rx);
-                        g += fw[a + 1] * yv;
-                    }
+                    for (int a = -1; a <= 1; a++) g += fw[a + 1] * YS(f, sy, sx + 1 + a);
                 }
                 GS(PH, f, sy, sx) = g;
                 gc[f] = g;
