@@ -84,12 +84,15 @@ __device__ __forceinline__ T filt_can(const T *q, const Can &c, int nyg, int i, 
 // (subgrid.f90:429-513).  A block owns a DB_X x DB_Y tile of (i, j) and
 // marches along z over a chunk of planes: each plane of the 15 quantities
 // (tile plus one halo cell, periodic in x, rows clamped to the interior) is
-// staged in shared memory, every thread forms the x-y filter at its point and
-// spreads it over the z accumulators of planes r-1, r, r+1 (weights 1/6,
-// 2/3, 1/6), so that plane r-1 is complete once plane r is in.  The filtered
-// velocities Uf, Vf, Wf (stage C) are read at their actual indices.  The
-// plane sums count the duplicate column and plane as weight 2 on i = 2 and
-// k = 2 (the reference's loops run over i = 2..nxg-1, k = 2..nzg-1).
+// gathered into one of two shared-memory buffers with cp.async while the
+// other is filtered; the FP32 kernel filters it in y by a column pass and in
+// x at its point (the FP64 kernel with a 9-point stencil at its point) and
+// spreads the result over the z accumulators of planes r-1, r, r+1 (weights
+// 1/6, 2/3, 1/6), so that plane r-1 is complete once plane r is in.  The
+// filtered velocities Uf, Vf, Wf (stage C) are read at their actual indices,
+// while the next plane's copies are in flight.  The plane sums (float-float
+// in the FP32 kernel) count the duplicate column and plane as weight 2 on
+// i = 2 and k = 2 (the reference's loops run over i = 2..nxg-1, k = 2..nzg-1).
 constexpr int DB_X = 32, DB_Y = 8, DB_NQ = 15;
 
 // asynchronous global -> shared copies of single elements (the plane gather

@@ -9,11 +9,17 @@
 //   G(p)  U, V, W filtered in x and y on the tile + 1 halo    (plane p)
 //   F(p)  Uf, Vf, Wf = z-filter of G(p-1..p+1)                 (plane p)
 //   Q(p)  centre velocities, their products, |S| S_ij and |S| (plane p, one)
-// The x-y filter of the 15 Q quantities at a thread's own point is spread
-// into z-accumulators held in registers (weights 1/6, 2/3, 1/6 to planes
-// p-1, p, p+1), so L_ij and hat(|S| S_ij) of plane k are complete once Q(k+1)
-// has been filtered; M_ij then needs S_ij of Uf, Vf, Wf at k, i.e. F(k-1..k+1).
+// Both x-y filters are separable passes: a column pass per (field or pair,
+// column) filters R(p) and Q(p) in y (each column read once for all its
+// rows), and each point takes the x filter of three filtered columns.  The
+// x-y filtered 15 Q quantities at a thread's own point are spread into
+// z-accumulators held in registers (weights 1/6, 2/3, 1/6 to planes p-1, p,
+// p+1), so L_ij and hat(|S| S_ij) of plane k are complete once Q(k+1) has
+// been filtered; M_ij then needs S_ij of Uf, Vf, Wf at k, i.e. F(k-1..k+1).
 // With raw plane r entering the ring, the block therefore emits plane r-2.
+// Three barriers per plane: after the raw column pass, after G/F/Q, after
+// the Q column pass (with the next raw plane committed and the strain of the
+// filtered velocities read before it).
 //
 // The halo is read through the periodic wrap, which reproduces the
 // reference's periodic copies whenever U, V, W are themselves periodic in x
