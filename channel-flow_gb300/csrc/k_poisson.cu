@@ -933,7 +933,7 @@ __device__ __forceinline__ void proj_update(const Fld<T> &F, const Fld<T> &Flo, 
 
 // KP consecutive planes per thread: every load of the thread is issued
 // before the first store (the fields may alias as far as the compiler knows).
-constexpr int PROJ_KP = 4;
+constexpr int PROJ_KP = 2;
 
 // ilim, klim: last x and z index projected (nxg-1 and nzg-1 for the full
 // interior; nxp+1 and nzp+1 for the canonical cells only)
