@@ -320,49 +320,155 @@ def cpu_baseline(wl, steps, threads, target_s=12.0):
     return nc * steps / dt, dt, steps
 
 
-def stats_run(wl, steps, every, device):
-    """The long-run comparison of the split path against the FP64 path: both
-    advanced `steps` steps from the same seeded field, the statistics of
-    compute_statistics (statistics.f90:43-159) sampled every `every` steps over
-    the second half and time-averaged; mean U+, the u, v, w RMS and the uv
-    Reynolds stress profiles of the split run against the FP64 run."""
+def long_run_stats(wl):
+    """The committed result of the long-run split-vs-FP64 statistics
+    comparison on developed turbulence for this workload (bench.py
+    --stats-run with --stats-develop; about two minutes of FP64 steps, so it
+    is not rerun by every bench invocation), or None."""
+    try:
+        tab = json.load(open(os.path.join(ROOT, "profiles", "stats_long_run.json")))
+    except Exception:
+        return None
+    r = tab.get(wl["name"])
+    if not r:
+        return None
+    keep = ("steps", "develop_steps", "retau", "error_split_vs_fp64 (max|a-b| / max|b|)",
+            "error_fp64_perturbed_vs_fp64 (floor)", "command", "measured")
+    return {k: r[k] for k in keep if k in r}
+
+
+def channel_from_fields(wl, precision, device, fields, dPdx, cfl=0.5):
+    """A channel of the workload's parameters started from given fields (a
+    snapshot) with the given mean pressure gradient; its constant mass flow is
+    the fields' own."""
+    import channelflow as cf
+    from channelflow import grids
+    x, y, z, U, V, W = fields
+    nu = grids.dean_nu(wl["retau"])
+    prm = dict(nu=nu, CFL=cfl, dPdx=(wl["retau"] * nu) ** 2, LES_model=wl["les"], iwall_model=wl["wall"],
+               x_mass_cte=1, jref_eqwm=wl["jref"], eqwm_ncv=wl["ncv"], precision=precision)
+    ch = cf.Channel(x, y, z, device=device, **prm)
+    ch.upload(U, V, W)
+    ch.init_mass_flow()
+    ch.apply_boundary_conditions()
+    ch.set_scalars(dt=5e-3, rk_step=1, dPdx=dPdx)
+    return ch
+
+
+def profiles_of(mean, tail, ny):
+    """Mean U+, u, v, w RMS and the uv Reynolds stress from time-averaged
+    compute_statistics vectors (statistics.f90:43-118)."""
+    import numpy as np
+    U, V, W, U2, V2, W2, UV = (mean[q * ny:(q + 1) * ny] for q in range(7))
+    utau = tail[0]
+    return dict(Uplus=U / utau, urms=np.sqrt(np.maximum(U2 - U * U, 0.0)),
+                vrms=np.sqrt(np.maximum(V2 - V * V, 0.0)), wrms=np.sqrt(np.maximum(W2 - W * W, 0.0)),
+                uv=UV - U * V, utau=float(utau), retau=float(tail[1]))
+
+
+def sample_run(ch, steps, every, ny):
+    """Advances `steps` steps and time-averages compute_statistics sampled
+    every `every` steps over the second half."""
+    import numpy as np
+    acc, tail, n = np.zeros(9 * ny), np.zeros(8), 0
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        k = min(every, steps - done)
+        ch.time_step_rk3(k)
+        done += k
+        if done > steps // 2:
+            s = ch.statistics()
+            acc += s[:9 * ny]
+            tail += s[9 * ny:]
+            n += 1
+    out = profiles_of(acc / n, tail / n, ny)
+    out.update(samples=n, seconds=time.perf_counter() - t0, finite=bool(np.isfinite(ch.download()["U"]).all()))
+    return out
+
+
+PROFILE_KEYS = ("Uplus", "urms", "vrms", "wrms", "uv")
+
+
+def profile_errors(a, b):
+    import numpy as np
+    return {k: float(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k]))) for k in PROFILE_KEYS}
+
+
+def stats_run(wl, steps, every, device, develop=0, perturb=6e-8, seed=1):
+    """The long-run comparison of the split path against the FP64 path.
+
+    develop > 0: the turbulent initial field (power-law mean plus large-scale
+    modes) is advanced `develop` steps with the split path until the flow is
+    turbulent (Re_tau is recorded along the way), written to and read back
+    from a snapshot file in the reference's format, and three runs start from
+    it: the FP64 path, the split path, and the FP64 path from the same field
+    with every value perturbed by a relative `perturb` (the size of FP32
+    rounding) -- the last one measures how far two FP64 runs that start a
+    rounding error apart drift in the same window, the floor any precision
+    change meets once the flow is chaotic.  develop = 0: both paths start from
+    the seeded laminar field (no developed turbulence).
+    Each run advances `steps` steps and time-averages compute_statistics
+    (statistics.f90:43-159) sampled every `every` steps over the second half;
+    mean U+, the u, v, w RMS and the uv Reynolds stress profiles are
+    compared as max|a - b| / max|b|."""
+    import tempfile
     import numpy as np
     import channelflow as cf
     ny = wl["ny"]
-    out = {}
-    for name, prec in (("fp64", cf.PREC_FP64), ("split", cf.PREC_SPLIT)):
-        ch, init = make_channel(wl, prec, device, seed=1)
-        acc, tail, n = np.zeros(9 * ny), np.zeros(8), 0
+    line = {"workload": wl["name"], "steps": steps, "sample_every": every, "window": "second half"}
+    if develop > 0:
+        wl_t = dict(wl, profile="turbulent")
+        ch, init = make_channel(wl_t, cf.PREC_SPLIT, device, seed=seed)
+        hist = []
         t0 = time.perf_counter()
         done = 0
-        while done < steps:
-            k = min(every, steps - done)
+        while done < develop:
+            k = min(1000, develop - done)
             ch.time_step_rk3(k)
             done += k
-            if done > steps // 2:
-                s = ch.statistics()
-                acc += s[:9 * ny]
-                tail += s[9 * ny:]
-                n += 1
-        wall = time.perf_counter() - t0
-        m, tl = acc / n, tail / n
-        U, V, W, U2, V2, W2, UV = (m[q * ny:(q + 1) * ny] for q in range(7))
-        utau = tl[0]
-        out[name] = dict(Uplus=U / utau, urms=np.sqrt(np.maximum(U2 - U * U, 0.0)),
-                         vrms=np.sqrt(np.maximum(V2 - V * V, 0.0)), wrms=np.sqrt(np.maximum(W2 - W * W, 0.0)),
-                         uv=UV - U * V, utau=utau, retau=tl[1], samples=n, seconds=wall,
-                         finite=bool(np.isfinite(ch.download()["U"]).all()))
+            s = ch.statistics()
+            hist.append([done, round(float(s[9 * ny + 1]), 2)])
+        dev_s = time.perf_counter() - t0
+        f = ch.download()
+        dPdx = ch.scalars()["dPdx"]
         ch.close()
-    a, b = out["split"], out["fp64"]
-    err = {k: float(np.max(np.abs(a[k] - b[k])) / np.max(np.abs(b[k]))) for k in ("Uplus", "urms", "vrms", "wrms", "uv")}
-    line = {"stats_run": {"workload": wl["name"], "steps": steps, "sample_every": every,
-                          "samples": b["samples"], "window": "second half",
-                          "error_split_vs_fp64 (max|a-b| / max|b|)": err,
-                          "utau": {"fp64": b["utau"], "split": a["utau"]},
-                          "retau": {"fp64": b["retau"], "split": a["retau"]},
-                          "wall_seconds": {"fp64": b["seconds"], "split": a["seconds"]},
-                          "finite": a["finite"] and b["finite"]}}
-    print(json.dumps(line))
+        x, y, z = init[:3]
+        with tempfile.TemporaryDirectory() as td:
+            path = os.path.join(td, "developed.bin")
+            cf.write_snapshot(path, x, y, z, f["U"], f["V"], f["W"], f["P"], f["nu_t"])
+            fields = cf.read_snapshot(path, len(x), len(y), len(z))
+        assert all(np.array_equal(fields[3 + q], f[k]) for q, k in enumerate("UVW"))
+        line["develop"] = {"steps": develop, "precision": "split", "initial_field": "turbulent",
+                           "retau_every_1000_steps": hist, "seconds": dev_s}
+        runs = {}
+        for name, prec in (("fp64", cf.PREC_FP64), ("split", cf.PREC_SPLIT), ("fp64_perturbed", cf.PREC_FP64)):
+            flds = fields
+            if name == "fp64_perturbed":
+                rng = np.random.default_rng(seed + 100)
+                flds = fields[:3] + tuple(np.asfortranarray(a * (1.0 + perturb * (2.0 * rng.random(a.shape) - 1.0)))
+                                          for a in fields[3:])
+            c = channel_from_fields(wl, prec, device, flds, dPdx)
+            runs[name] = sample_run(c, steps, every, ny)
+            c.close()
+        b = runs["fp64"]
+        line["error_split_vs_fp64 (max|a-b| / max|b|)"] = profile_errors(runs["split"], b)
+        line["error_fp64_perturbed_vs_fp64 (floor)"] = profile_errors(runs["fp64_perturbed"], b)
+        line["perturbation"] = perturb
+    else:
+        runs = {}
+        for name, prec in (("fp64", cf.PREC_FP64), ("split", cf.PREC_SPLIT)):
+            ch, init = make_channel(wl, prec, device, seed=seed)
+            runs[name] = sample_run(ch, steps, every, ny)
+            ch.close()
+        line["error_split_vs_fp64 (max|a-b| / max|b|)"] = profile_errors(runs["split"], runs["fp64"])
+    line["samples"] = runs["fp64"]["samples"]
+    line["utau"] = {k: r["utau"] for k, r in runs.items()}
+    line["retau"] = {k: r["retau"] for k, r in runs.items()}
+    line["wall_seconds"] = {k: r["seconds"] for k, r in runs.items()}
+    line["finite"] = all(r["finite"] for r in runs.values())
+    line["profiles"] = {k: {q: [float(v) for v in r[q]] for q in PROFILE_KEYS} for k, r in runs.items()}
+    print(json.dumps({"stats_run": line}))
 
 
 ENSEMBLE = {"name": "ensemble of 16 channels: 6x(64x64x64), 6x(96x64x96), 4x(128x96x128), Re_tau from "
@@ -591,8 +697,10 @@ def run_ours(args, wl, rank, world, local):
     ms64 = timed(ch64, k64, stream64)
     v64 = world * nc * k64 / (ms64 / 1e3)
 
-    # ---- per-kernel device time (eager pass with an event after every launch)
-    prof = ch.profile_steps(2)
+    # ---- per-kernel device time: two steps, each captured as one graph with
+    # an event-record node after every kernel and launched like the timed
+    # step graphs
+    prof = ch.profile_steps(2, graph=True)
     tot = sum(v[0] for v in prof.values())
     top = sorted(prof.items(), key=lambda kv: -kv[1][0])
     dom, (dom_ms, dom_n) = top[0]
@@ -615,7 +723,10 @@ def run_ours(args, wl, rank, world, local):
     roof = {"kernel": dom, "bound": "hbm", "unit": "GB/s", "peak": hbm_peak, "peak_source": peak_src,
             "achieved": (ab / avg_s / 1e9) if ab else None, "frac": (ab / avg_s / 1e9 / hbm_peak) if ab else None,
             "traffic": traffic, "avg_launch_ms": avg_s * 1e3, "launches_per_step": dom_n / 2,
-            "share_of_step": dom_ms / tot if tot else None}
+            "share_of_step": dom_ms / tot if tot else None,
+            "timing": "CUDA events captured as graph nodes around each launch of two graph-launched steps",
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one ncu launch of this kernel on "
+                              "this workload (profiles/traffic.json)"}
     if wavefronts:
         # the bound the kernel actually meets: shared-memory wavefronts of one
         # launch (ncu) at one per clock per SM, at the clock sampled above
@@ -678,7 +789,10 @@ def run_ours(args, wl, rank, world, local):
                        "sgs_recompute": True, "autotune": tuned},
             "fp64": {"value": v64, "ms_per_step": ms64 / k64, "steps": k64},
             "split_over_fp64": value / v64,
-            "stats_err_vs_fp64": {"steps": ncmp, **prof_err},
+            "short_horizon_err_vs_fp64": {"steps": ncmp, "what": "profile errors after a few steps from the same "
+                                          "field; the long-run gate on developed turbulence is long_run_stats",
+                                          **prof_err},
+            "long_run_stats": long_run_stats(wl),
             "hbm_frac_step": value / world * BYTES_PER_PT_STEP["split"] / (hbm_peak * 1e9),
             "roofline": roof,
             "kernels_ms_per_step": {k: round(v[0] / 2, 4) for k, v in top[:10]},
@@ -718,6 +832,9 @@ def main():
     ap.add_argument("--stats-run", type=int, default=0,
                     help="only run the long-run statistics comparison of the split and FP64 paths over N steps")
     ap.add_argument("--stats-every", type=int, default=10)
+    ap.add_argument("--stats-develop", type=int, default=0,
+                    help="with --stats-run: first develop turbulence from the turbulent initial field for N split "
+                         "steps, then compare FP64, split and a perturbed FP64 run from it")
     args = ap.parse_args()
     rank, world, local = dist_info()
     if args.workload == "ensemble16":
@@ -730,7 +847,7 @@ def main():
         return
     wl = WORKLOADS[args.workload]
     if args.stats_run:
-        stats_run(wl, args.stats_run, args.stats_every, local)
+        stats_run(wl, args.stats_run, args.stats_every, local, develop=args.stats_develop)
         return
     if args.profile_steps:
         import channelflow as cf
@@ -739,7 +856,7 @@ def main():
         ch.time_step_rk3(args.profile_steps)
         print(json.dumps({"profile_steps": args.profile_steps, "launches_per_step": ch.launches_per_step()}))
         if args.kernel_table:
-            prof = ch.profile_steps(2)
+            prof = ch.profile_steps(2, graph=True)
             tot = sum(v[0] for v in prof.values())
             for k, (ms, n) in sorted(prof.items(), key=lambda kv: -kv[1][0]):
                 print(f"{k:16s} {n / 2:5.1f}/step {1e3 * ms / 2:9.1f} us/step {100 * ms / tot:5.1f}%"

@@ -86,7 +86,10 @@ def seeded_fields(x, y, z, seed: int = 1, amp: float = 0.1, profile: str = "lami
                   bulk: float = 1.0):
     """Perturbed initial velocity in the reference layout.
 
-    profile 'laminar': U = 1.5*bulk*y(2-y) at the U centres; 'plug': U = bulk.
+    profile 'laminar': U = 1.5*bulk*y(2-y) at the U centres; 'plug': U = bulk;
+    'turbulent': the 1/7 power-law profile of bulk velocity `bulk` plus
+    large-scale wall-vanishing Fourier modes (see turbulent_modes), a field
+    that becomes turbulent within a few tens of time units.
     Uniform i.i.d. noise in [-amp, amp]*bulk on U, V, W (PCG64, seeded), then
     the periodic and no-slip ghost fills.  A projection (done by the solver)
     makes the field divergence-free."""
@@ -96,6 +99,9 @@ def seeded_fields(x, y, z, seed: int = 1, amp: float = 0.1, profile: str = "lami
     yg = centres(np.asarray(y))
     if profile == "laminar":
         prof = 1.5 * bulk * yg * (2.0 - yg)
+    elif profile == "turbulent":
+        eta = np.clip(1.0 - np.abs(1.0 - yg / (0.5 * (y[-1] - y[0]))), 0.0, 1.0)
+        prof = bulk * (8.0 / 7.0) * eta ** (1.0 / 7.0)
     else:
         prof = np.full_like(yg, bulk)
     U = np.asfortranarray(np.broadcast_to(prof[None, :, None], s["U"]).copy())
@@ -103,8 +109,44 @@ def seeded_fields(x, y, z, seed: int = 1, amp: float = 0.1, profile: str = "lami
     V = np.asfortranarray(amp * bulk * (2.0 * rng.random(s["V"]) - 1.0))
     W = np.asfortranarray(amp * bulk * (2.0 * rng.random(s["W"]) - 1.0))
     U = np.asfortranarray(U)
+    if profile == "turbulent":
+        dU, dV, dW = turbulent_modes(x, y, z, rng, bulk)
+        U += dU; V += dV; W += dW
     apply_bcs_noslip(U, V, W)
     return U, V, W
+
+
+def turbulent_modes(x, y, z, rng, bulk: float = 1.0, amp_u: float = 0.25, amp_vw: float = 0.12):
+    """Large-scale perturbations that trip a channel into turbulence: a sum of
+    Fourier modes with streamwise wavenumbers 0..3 and spanwise 1..4 (and
+    oblique ones), random phases, wall-normal shape (1 - eta^2)^2 (eta the
+    distance from the centre plane over the half height), so that every mode
+    vanishes at both walls.  Streamwise rolls (kx = 0) in V, W lift up streaks
+    in U; the oblique modes break them.  Returned on the U, V, W staggered
+    positions; the projection that follows removes their divergence."""
+    x, y, z = (np.asarray(a, dtype=np.float64) for a in (x, y, z))
+    nx, ny, nz = len(x), len(y), len(z)
+    Lx, Lz = x[nx - 2] - x[0], z[nz - 2] - z[0]
+    h = 0.5 * (y[-1] - y[0])
+    xg, yg, zg = centres(x), centres(y), centres(z)
+
+    def shape(yy):
+        eta = (yy - y[0]) / h - 1.0
+        return np.where(np.abs(eta) < 1.0, (1.0 - eta * eta) ** 2, 0.0)
+
+    modes = [(kx, kz) for kx in range(0, 4) for kz in range(1, 5)] + [(kx, 0) for kx in range(1, 4)]
+    out = []
+    for (xs, ys, zs), a in (((x, yg, zg), amp_u), ((xg, y, zg), amp_vw), ((xg, yg, z), amp_vw)):
+        f = np.zeros((len(xs), len(ys), len(zs)))
+        wy = shape(ys)
+        for kx, kz in modes:
+            c = rng.standard_normal() / math.sqrt(len(modes))
+            ph = rng.random() * 2 * math.pi
+            ax = 2 * math.pi * kx * (xs - x[0]) / Lx
+            az = 2 * math.pi * kz * (zs - z[0]) / Lz
+            f += c * np.cos(ax[:, None, None] + az[None, None, :] + ph) * wy[None, :, None]
+        out.append(np.asfortranarray(a * bulk * f))
+    return out
 
 
 def dean_nu(retau: float) -> float:
