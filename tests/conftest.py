@@ -31,6 +31,25 @@ def assert_close(a, b, tol, what=""):
     return e
 
 
+def pointwise_rel_err(a, b, floor=1e-6):
+    """max over points of |a-b| / max(|b|, floor*max|b|): the relative error
+    of every value, values below `floor` of the array's largest measured
+    against that floor (an exact zero has no relative error)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    den = np.maximum(np.abs(b), floor * np.max(np.abs(b)))
+    if not np.any(den > 0):
+        return float(np.max(np.abs(a - b)))
+    den = np.where(den > 0, den, 1.0)
+    return float(np.max(np.abs(a - b) / den))
+
+
+def assert_pointwise(a, b, tol, what="", floor=1e-6):
+    e = pointwise_rel_err(a, b, floor)
+    assert e <= tol, f"{what}: pointwise relative error {e:.3e} > {tol:.1e} (floor {floor:.0e} of max)"
+    return e
+
+
 def channel_case(nx, ny, nz, retau=180.0, stretch=1.5, les=2, wall=0, dt=2e-3, seed=1, mass=1, jref=3,
                  profile="laminar", ncv=100):
     """A seeded channel: face grids, oracle/library parameter dicts, fields."""
