@@ -1295,6 +1295,13 @@ int launch_dt(cf_ctx *ctx, int b, bool advance_t) {
 // check_divergence, projection.f90:234-256 (signed max from 0, and max |div|)
 // ---------------------------------------------------------------------------
 
+// A NaN divergence in any cell makes both results NaN (a blown-up field is
+// reported as such; fmax alone would drop it).  The NaN is the positive
+// quiet one, whose bit pattern orders above +Inf for atomic_max_pos.
+__device__ __forceinline__ double nan_max(double a, double b) {
+    return (isnan(a) || isnan(b)) ? __longlong_as_double(0x7FF8000000000000LL) : fmax(a, b);
+}
+
 template <typename T>
 __global__ void k_div(Fld<T> U, Fld<T> V, Fld<T> W, Geo g, double *out) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
@@ -1305,12 +1312,12 @@ __global__ void k_div(Fld<T> U, Fld<T> V, Fld<T> W, Geo g, double *out) {
         d = ((double)U(i, j, k) - (double)U(i - 1, j, k)) / (g.x[i] - g.x[i - 1]) +
             ((double)V(i, j, k) - (double)V(i, j - 1, k)) / (g.y[j] - g.y[j - 1]) +
             ((double)W(i, j, k) - (double)W(i, j, k - 1)) / (g.z[k] - g.z[k - 1]);
-        a = fabs(d);
-        d = fmax(d, 0.0);
+        a = nan_max(fabs(d), 0.0);
+        d = nan_max(d, 0.0);
     }
     for (int o = 16; o > 0; o >>= 1) {
-        d = fmax(d, __shfl_down_sync(0xffffffff, d, o));
-        a = fmax(a, __shfl_down_sync(0xffffffff, a, o));
+        d = nan_max(d, __shfl_down_sync(0xffffffff, d, o));
+        a = nan_max(a, __shfl_down_sync(0xffffffff, a, o));
     }
     if (((threadIdx.x + threadIdx.y * blockDim.x) & 31) == 0) {
         atomic_max_pos(&out[0], d);

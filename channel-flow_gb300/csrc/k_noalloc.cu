@@ -15,9 +15,10 @@
 //   div = (U(i)-U(i-1))/(x(i)-x(i-1)) + (V(j)-V(j-1))/(y(j)-y(j-1))
 //       + (W(k)-W(k-1))/(z(k)-z(k-1))
 // and the results max(0, max div) (the reference's Max starting from 0) and
-// max |div|.  The reduction is two-stage and deterministic: one block per
-// interior z plane writes that plane's two maxima to the scratch, then one
-// block reduces the planes.
+// max |div|; a NaN divergence in any cell makes both results NaN.  The
+// reduction is two-stage and deterministic: one block per interior z plane
+// writes that plane's two maxima to the scratch, then one block reduces the
+// planes.
 #include <mutex>
 
 #include "cf_internal.cuh"
@@ -30,10 +31,15 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
 double *g_planes_ptr[kMaxDevices] = {};  // device address of g_div_planes, per device
 
+// max that keeps a NaN (fmax would drop it)
+__device__ __forceinline__ double nan_max(double a, double b) {
+    return (isnan(a) || isnan(b)) ? __longlong_as_double(0x7FF8000000000000LL) : fmax(a, b);
+}
+
 __device__ __forceinline__ void block_max2(double &d, double &a, double *sh) {
     for (int o = 16; o > 0; o >>= 1) {
-        d = fmax(d, __shfl_down_sync(0xffffffffu, d, o));
-        a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
+        d = nan_max(d, __shfl_down_sync(0xffffffffu, d, o));
+        a = nan_max(a, __shfl_down_sync(0xffffffffu, a, o));
     }
     const int t = threadIdx.x + threadIdx.y * blockDim.x, nw = (blockDim.x * blockDim.y) >> 5;
     if ((t & 31) == 0) {
@@ -45,8 +51,8 @@ __device__ __forceinline__ void block_max2(double &d, double &a, double *sh) {
         d = t < nw ? sh[2 * t] : 0.0;
         a = t < nw ? sh[2 * t + 1] : 0.0;
         for (int o = 16; o > 0; o >>= 1) {
-            d = fmax(d, __shfl_down_sync(0xffffffffu, d, o));
-            a = fmax(a, __shfl_down_sync(0xffffffffu, a, o));
+            d = nan_max(d, __shfl_down_sync(0xffffffffu, d, o));
+            a = nan_max(a, __shfl_down_sync(0xffffffffu, a, o));
         }
     }
 }
@@ -71,8 +77,8 @@ __global__ void __launch_bounds__(256) k_div_planes(int nx, int ny, int nz, cons
             const double v = (Uk[(i - 1) + (size_t)nx * (j - 1)] - Uk[(i - 2) + (size_t)nx * (j - 1)]) / (x[i - 1] - x[i - 2]) +
                              (Vk[(i - 1) + (size_t)nxg * (j - 1)] - Vk[(i - 1) + (size_t)nxg * (j - 2)]) / dy +
                              (Wk[(i - 1) + (size_t)nxg * (j - 1)] - Wm[(i - 1) + (size_t)nxg * (j - 1)]) / dz;
-            d = fmax(d, v);
-            a = fmax(a, fabs(v));
+            d = nan_max(d, v);
+            a = nan_max(a, fabs(v));
         }
     }
     block_max2(d, a, sh);
@@ -87,8 +93,8 @@ __global__ void __launch_bounds__(256) k_div_planes_final(int nplanes, const dou
     __shared__ double sh[16];
     double d = 0.0, a = 0.0;
     for (int p = threadIdx.x; p < nplanes; p += blockDim.x) {
-        d = fmax(d, planes[2 * p]);
-        a = fmax(a, planes[2 * p + 1]);
+        d = nan_max(d, planes[2 * p]);
+        a = nan_max(a, planes[2 * p + 1]);
     }
     block_max2(d, a, sh);
     if (threadIdx.x == 0) {

@@ -65,3 +65,28 @@ def test_noalloc_divergence_matches_context_entry_point():
         assert abs(got[0] - ref_div) <= 1e-14 * ref_abs, (call, got, ref_div)
         assert abs(got[1] - ref_abs) <= 1e-14 * ref_abs, (call, got, ref_abs)
     ch.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_and_context_report_a_nan_divergence():
+    """A NaN in one interior cell makes both results of both divergence
+    checks NaN (a blown-up field is not reported as a finite maximum)."""
+    import torch
+    import channelflow as cf
+    L, f = _bind()
+    case = channel_case(18, 17, 18, seed=9)
+    case["U"][5, 6, 7] = math.nan
+    ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_FP64, **case["prm"])
+    ch.upload(case["U"], case["V"], case["W"])
+    assert all(math.isnan(v) for v in ch.check_divergence())
+    ch.close()
+    dev = torch.device("cuda:0")
+    flat = {k: torch.from_numpy(np.ravel(case[k], order="F").copy()).to(dev) for k in ("U", "V", "W", "x", "y", "z")}
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    nx, ny, nz = len(case["x"]), len(case["y"]), len(case["z"])
+    rc = f(nx, ny, nz, *(flat[k].data_ptr() for k in ("U", "V", "W", "x", "y", "z")), out.data_ptr(),
+           stream.cuda_stream)
+    assert rc == 0, L.cf_last_error(None).decode()
+    stream.synchronize()
+    assert np.isnan(out.cpu().numpy()).all()
