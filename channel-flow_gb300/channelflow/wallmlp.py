@@ -35,6 +35,8 @@ def _bind():
     L.cf_mlp_set.argtypes = [vp, fp, dp, dp]
     L.cf_set_wall_mlp.argtypes = [vp, vp, C.c_int]
     L.cf_get_wall_mlp_log.argtypes = [vp, dp]
+    L.cf_mlp_wait_expired.argtypes = [vp, ip]
+    L.cf_mlp_test_skip_mma.argtypes = [vp, C.c_int]
     L._wmlp_bound = True
     return L
 
@@ -149,6 +151,19 @@ class WallMLP:
         _check(self.L, self.L.cf_mlp_predict(self.h, u.numel(), _ptr(u), _ptr(h), _ptr(nu), _ptr(tau), _ptr(ins),
                                               1 if tensor_cores else 0, _stream(u)), "cf_mlp_predict")
         return (tau, ins) if inside else tau
+
+    def wait_expired(self) -> bool:
+        """True when a tensor-core inference since the last call gave up
+        waiting for its MMA (its unfinished samples were left to eqwm); clears
+        the record."""
+        e = C.c_int()
+        _check(self.L, self.L.cf_mlp_wait_expired(self.h, C.byref(e)), "cf_mlp_wait_expired")
+        return bool(e.value)
+
+    def test_skip_mma(self, on: bool):
+        """Test hook: the tensor-core inference issues no MMA, so its bounded
+        waits run out."""
+        _check(self.L, self.L.cf_mlp_test_skip_mma(self.h, 1 if on else 0), "cf_mlp_test_skip_mma")
 
     def get(self):
         p = np.zeros(NPARAM, dtype=np.float32)

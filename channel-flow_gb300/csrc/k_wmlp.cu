@@ -365,7 +365,18 @@ __device__ __forceinline__ uint4 pack8_bf16(const float *v) {
     return q;
 }
 
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+// a wait gives up after TC_WAIT_NS nanoseconds or TC_WAIT_LIMIT polls,
+// whichever comes first (a completed MMA arrives within microseconds)
+constexpr uint64_t TC_WAIT_NS = 1000000000ull;
+
 __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t phase) {
+    const uint64_t t0 = global_ns();
     for (long it = 0; it < TC_WAIT_LIMIT; it++) {
         uint32_t ok;
         asm volatile(
@@ -376,6 +387,7 @@ __device__ __forceinline__ bool mbar_wait(uint32_t addr, uint32_t phase) {
             : "r"(addr), "r"(phase)
             : "memory");
         if (ok) return true;
+        if ((it & 63) == 63 && global_ns() - t0 > TC_WAIT_NS) return false;
     }
     return false;
 }
@@ -393,7 +405,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v) {
 
 __global__ void __launch_bounds__(TC_M) k_mlp_infer_tc(const float *__restrict__ wm, MlpNorm nm, int n, const double *u,
                                                        const double *h, int hs, const double *nu, int ns, double *tau,
-                                                       int *inside, int *err) {
+                                                       int *inside, int *err, int skip_mma) {
     extern __shared__ unsigned char tc_raw[];
     // 1024-byte alignment of the tiles (the swizzle pattern is anchored to it)
     const uint32_t raw = smem_u32(tc_raw);
@@ -447,7 +459,7 @@ __global__ void __launch_bounds__(TC_M) k_mlp_infer_tc(const float *__restrict__
         }
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         __syncthreads();
-        if (tid == 0) {
+        if (tid == 0 && !skip_mma) {
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 #pragma unroll
             for (int kk = 0; kk < TC_K / 16; kk++) {
@@ -463,11 +475,23 @@ __global__ void __launch_bounds__(TC_M) k_mlp_infer_tc(const float *__restrict__
                          : "memory");
         }
         const bool ok = mbar_wait(mbar, phase);
-        phase ^= 1u;
         if (__syncthreads_or(!ok)) {
+            // The commit did not arrive in time.  Record it, give the MMA of
+            // this tile (if one was issued) a second bounded wait before its
+            // tensor memory is freed below, and mark every sample of this
+            // block's remaining tiles as not served, so that a caller that
+            // falls back outside the envelope (the wall model) solves eqwm
+            // there.
             if (tid == 0) atomicExch(err, 1);
+            if (!ok) mbar_wait(mbar, phase);
+            if (inside)
+                for (int t2 = tile; t2 < ntiles; t2 += gridDim.x) {
+                    const long s2 = (long)t2 * TC_M + tid;
+                    if (s2 < n) inside[s2] = 0;
+                }
             break;
         }
+        phase ^= 1u;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         float acc[TC_N];
         const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
@@ -498,6 +522,7 @@ __global__ void __launch_bounds__(TC_M) k_mlp_infer_tc(const float *__restrict__
 struct cf_mlp {
     int dev = 0, ncv = 0, sms = 152;
     int *derr = nullptr;  // set by a tensor-core wait that expired
+    int test_skip_mma = 0;  // test hook: the inference issues no MMA, so its waits expire
     double stretch = 0.0;
     float *w = nullptr, *m1 = nullptr, *m2 = nullptr, *part = nullptr;
     double *lpart = nullptr, *unit = nullptr;
@@ -752,7 +777,10 @@ extern "C" int cf_mlp_predict(cf_mlp *m, int n, const double *u, const double *h
         int e = 0;
         MLP_CUDA(cudaMemcpyAsync(&e, m->derr, sizeof(int), cudaMemcpyDeviceToHost, st));
         MLP_CUDA(cudaStreamSynchronize(st));
-        if (e) return mlp_fail(m, CF_ERR_CUDA, "cf_mlp_predict: a tensor-core wait expired");
+        if (e) {
+            MLP_CUDA(cudaMemsetAsync(m->derr, 0, sizeof(int), st));
+            return mlp_fail(m, CF_ERR_CUDA, "cf_mlp_predict: a tensor-core wait expired");
+        }
     } else {
         k_mlp_infer_cc<<<cdiv(n, 128), 128, 0, st>>>(m->w, norm_of(m), n, u, h, 1, nu, 1, tau, inside);
     }
@@ -782,8 +810,23 @@ int mlp_predict_tc(cf_mlp *m, int n, const double *u, const double *h, int hs, c
     const int ntiles = cdiv(n, TC_M);
     const int grid = std::min(ntiles, m->sms * 4);
     k_mlp_infer_tc<<<grid, TC_M, sizeof(TcSmem) + 1024, st>>>(m->w, norm_of(m), n, u, h, hs, nu, ns, tau, inside,
-                                                              m->derr);
+                                                              m->derr, m->test_skip_mma);
     return 0;
+}
+
+extern "C" int cf_mlp_wait_expired(cf_mlp *m, int *expired) {
+    if (!m || !expired) return mlp_fail(m, CF_ERR_INVALID, "cf_mlp_wait_expired: null argument");
+    MLP_CUDA(cudaSetDevice(m->dev));
+    MLP_CUDA(cudaDeviceSynchronize());
+    MLP_CUDA(cudaMemcpy(expired, m->derr, sizeof(int), cudaMemcpyDeviceToHost));
+    MLP_CUDA(cudaMemset(m->derr, 0, sizeof(int)));
+    return CF_OK;
+}
+
+extern "C" int cf_mlp_test_skip_mma(cf_mlp *m, int on) {
+    if (!m) return mlp_fail(m, CF_ERR_INVALID, "cf_mlp_test_skip_mma: null network");
+    m->test_skip_mma = on ? 1 : 0;
+    return CF_OK;
 }
 
 // ---------------------------------------------------------------------------

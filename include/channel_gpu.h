@@ -253,6 +253,16 @@ int cf_mlp_predict(cf_mlp *m, int n, const double *u, const double *h, const dou
  * of the three input logs). */
 int cf_mlp_get(cf_mlp *m, float *params, double *norm, double *envelope);
 int cf_mlp_set(cf_mlp *m, const float *params, const double *norm, const double *envelope);
+/* 1 in *expired when a tensor-core inference of m since the last call gave up
+ * waiting for its MMA (each wait is bounded: 1 s, then a second bounded wait
+ * before the kernel frees its tensor memory); the record is then cleared.
+ * Samples of the tiles not finished are marked outside the envelope, so that
+ * the wall model solves eqwm for them.  Synchronises the device. */
+int cf_mlp_wait_expired(cf_mlp *m, int *expired);
+/* Test hook: on = 1 makes the tensor-core inference issue no MMA, so that its
+ * bounded waits run out (about 2 s per launch) -- the path above is exercised
+ * without faulting anything.  0 (default) restores normal inference. */
+int cf_mlp_test_skip_mma(cf_mlp *m, int on);
 /* Uses the network for the wall stress of ctx's equilibrium wall model
  * (iwall_model 3): points whose inputs fall outside the envelope, and all
  * points when m is NULL, keep the eqwm solve.  Every `check_every` calls of

@@ -230,3 +230,44 @@ def test_points_outside_the_envelope_fall_back_to_eqwm():
     assert log["calls"] == 3 and log["served"] == 0 and log["fallback"] == 18 * 19 * 2
     for n in ("U", "V", "W", "P", "nu_t"):
         assert np.array_equal(out[True][n], out[False][n]), n
+
+
+@pytest.mark.gpu
+def test_expired_tensor_core_wait_falls_back_to_eqwm():
+    """With the test hook that makes the tensor-core inference issue no MMA,
+    every bounded wait runs out: the kernel records it, frees its tensor
+    memory and leaves all its samples to eqwm, so the step is bit-identical to
+    the eqwm run; the record clears, and normal inference serves again."""
+    import torch
+    import channelflow as cf
+    from channelflow import wallmlp
+    from conftest import channel_case
+    dev = torch.device("cuda:0")
+    u, h, nu, tau = _data(1 << 15, 43, dev)
+    net = wallmlp.WallMLP(seed=7, ncv=30, stretch=1.10)
+    net.fit_normalisation(u, h, nu, tau)
+    case = channel_case(18, 17, 18, stretch=0.0, wall=3, retau=2000.0, profile="plug", jref=3, ncv=30)
+    out = {}
+    for use in (False, True):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_FP64, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        if use:
+            ch.set_wall_mlp(net, check_every=1)
+            net.test_skip_mma(True)
+        ch.set_fixed_dt(case["dt"])
+        ch.time_step_rk3(1)
+        out[use] = ch.download()
+        if use:
+            log = ch.wall_mlp_log()
+            assert net.wait_expired()
+            assert not net.wait_expired()  # the record was cleared
+            net.test_skip_mma(False)
+            ch.time_step_rk3(1)
+            assert not net.wait_expired()
+            assert ch.wall_mlp_log()["served"] > 0
+        ch.close()
+    assert log["calls"] == 1 and log["served"] == 0 and log["fallback"] == 18 * 19 * 2
+    for n in ("U", "V", "W", "P", "nu_t"):
+        assert np.array_equal(out[True][n], out[False][n]), n
