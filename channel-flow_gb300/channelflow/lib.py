@@ -102,6 +102,7 @@ def load(build_if_missing: bool = True):
     L.cf_compute_statistics.argtypes = [vp, dp]
     L.cf_output_monitor.argtypes = [vp, dp]
     L.cf_profile_steps.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, dp, ip, ip]
+    L.cf_profile_graph_steps.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, dp, ip, ip]
     L.cf_read_input_parameters.argtypes = [C.c_char_p, C.POINTER(CfParams), ip, C.c_char_p, C.c_char_p, ip, ip]
     L.cf_read_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp]
     L.cf_write_snapshot.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp, dp, dp, dp]
@@ -397,15 +398,18 @@ class Channel:
     def launches_per_step(self) -> int:
         return self.L.cf_launches_per_step(self.h)
 
-    def profile_steps(self, nsteps: int = 1) -> dict:
+    def profile_steps(self, nsteps: int = 1, graph: bool = False) -> dict:
         """Per-kernel device time (ms, summed) and launch counts over nsteps
-        eager steps, from CUDA events on the context's stream."""
+        steps, from CUDA events on the context's stream: eager steps, or
+        (graph=True) each step captured with the events as graph nodes and
+        launched as one graph."""
         mx = 64
         names = C.create_string_buffer(48 * mx)
         ms = np.zeros(mx)
         cnt = (C.c_int * mx)()
         n = C.c_int()
-        self._check(self.L.cf_profile_steps(self.h, nsteps, mx, names, _dp(ms), cnt, C.byref(n)))
+        fn = self.L.cf_profile_graph_steps if graph else self.L.cf_profile_steps
+        self._check(fn(self.h, nsteps, mx, names, _dp(ms), cnt, C.byref(n)))
         out = {}
         for k in range(n.value):
             nm = names.raw[48 * k:48 * (k + 1)].split(b"\0", 1)[0].decode()

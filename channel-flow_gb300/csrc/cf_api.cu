@@ -1108,20 +1108,29 @@ extern "C" int cf_time_step_rk3(cf_ctx *ctx, int nsteps, int sync) {
         }
         if (!ctx->graphs[X]) {
             // first step from this buffer: count launches eagerly-captured
-            cudaGraph_t g;
+            cudaGraph_t g = nullptr;
             ctx->launches = 0;
             ctx->counting = true;
             CF_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
             int rc = step_eager(ctx);
             cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
             ctx->counting = false;
-            if (rc) return rc;
-            if (e != cudaSuccess) return cf_fail(ctx, CF_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
-            ctx->step_launches = ctx->launches;
-            ctx->next_buf[X] = ctx->cur;
+            // the captured launches did not run: the state is still buffer X
+            const int after = ctx->cur;
             ctx->cur = X;
-            CF_CUDA(cudaGraphInstantiate(&ctx->graphs[X], g, 0));
-            CF_CUDA(cudaGraphDestroy(g));
+            if (rc || e != cudaSuccess) {
+                if (g) cudaGraphDestroy(g);
+                if (rc) return rc;
+                return cf_fail(ctx, CF_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(e));
+            }
+            ctx->step_launches = ctx->launches;
+            ctx->next_buf[X] = after;
+            cudaError_t ei = cudaGraphInstantiate(&ctx->graphs[X], g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) {
+                ctx->graphs[X] = nullptr;
+                return cf_fail(ctx, CF_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ei));
+            }
         }
         CF_CUDA(cudaGraphLaunch(ctx->graphs[X], ctx->st));
         ctx->cur = ctx->next_buf[X];
@@ -1242,8 +1251,51 @@ extern "C" int cf_apply_mass_flow_correction(cf_ctx *ctx, int comp, double value
 // Per-kernel device time over nsteps eager (non-graph) steps, from one event
 // recorded after every launch on the context's stream.  names: max_names
 // rows of 48 chars.
-extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
-                                int *n_names) {
+// One step with an event after every launch: eagerly (graph = false) or
+// captured with the events as event-record nodes into a graph that is then
+// launched once (graph = true), so that the kernels run as in the replayed
+// step graph of cf_time_step_rk3.
+static int profiled_step(cf_ctx *ctx, cudaEvent_t start, bool graph) {
+    ctx->pn = 0;
+    if (!graph) {
+        CF_CUDA(cudaEventRecord(start, ctx->st));
+        ctx->profiling = true;
+        int rc = step_eager(ctx);
+        ctx->profiling = false;
+        if (rc) return rc;
+        CF_CUDA(cudaStreamSynchronize(ctx->st));
+        return 0;
+    }
+    const int X = ctx->cur;
+    cudaGraph_t g = nullptr;
+    CF_CUDA(cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal));
+    cudaEventRecordWithFlags(start, ctx->st, cudaEventRecordExternal);
+    ctx->profiling = ctx->profiling_in_graph = true;
+    int rc = step_eager(ctx);
+    ctx->profiling = ctx->profiling_in_graph = false;
+    cudaError_t e = cudaStreamEndCapture(ctx->st, &g);
+    const int after = ctx->cur;
+    ctx->cur = X;  // nothing ran yet
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        if (rc) return rc;
+        return cf_fail(ctx, CF_ERR_CUDA, std::string("profile capture: ") + cudaGetErrorString(e));
+    }
+    cudaGraphExec_t ge = nullptr;
+    cudaError_t ei = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return cf_fail(ctx, CF_ERR_CUDA, std::string("profile instantiate: ") + cudaGetErrorString(ei));
+    cudaError_t el = cudaGraphLaunch(ge, ctx->st);
+    if (el == cudaSuccess) el = cudaStreamSynchronize(ctx->st);
+    cudaGraphExecDestroy(ge);
+    if (el != cudaSuccess) return cf_fail(ctx, CF_ERR_CUDA, std::string("profile launch: ") + cudaGetErrorString(el));
+    ctx->cur = after;
+    ctx->old = after;
+    return 0;
+}
+
+static int profile_steps(cf_ctx *ctx, int nsteps, bool graph, int max_names, char *names, double *total_ms,
+                         int *counts, int *n_names) {
     if (!ctx || !names || !total_ms || !counts || !n_names) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
     CF_CUDA(cudaSetDevice(ctx->dev));
     cudaEvent_t start;
@@ -1253,14 +1305,8 @@ extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *na
     std::vector<int> cnt;
     for (int s = 0; s < nsteps; s++) {
         for (int attempt = 0; attempt < 2; attempt++) {
-            int save_cur = ctx->cur, save_old = ctx->old;
-            ctx->pn = 0;
-            CF_CUDA(cudaEventRecord(start, ctx->st));
-            ctx->profiling = true;
-            int rc = step_eager(ctx);
-            ctx->profiling = false;
+            int rc = profiled_step(ctx, start, graph);
             if (rc) { cudaEventDestroy(start); return rc; }
-            CF_CUDA(cudaStreamSynchronize(ctx->st));
             if (ctx->pn <= (int)ctx->pev.size()) break;
             // pool too small: the step ran without complete timing; grow and
             // time the next step instead
@@ -1268,7 +1314,6 @@ extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *na
             ctx->pev.resize(ctx->pn + 64);
             ctx->pname.resize(ctx->pn + 64);
             for (size_t q = old; q < ctx->pev.size(); q++) CF_CUDA(cudaEventCreate(&ctx->pev[q]));
-            (void)save_cur; (void)save_old;
         }
         cudaEvent_t prev = start;
         for (int q = 0; q < ctx->pn; q++) {
@@ -1293,6 +1338,16 @@ extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *na
     }
     *n_names = n;
     return CF_OK;
+}
+
+extern "C" int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
+                                int *n_names) {
+    return profile_steps(ctx, nsteps, false, max_names, names, total_ms, counts, n_names);
+}
+
+extern "C" int cf_profile_graph_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms,
+                                      int *counts, int *n_names) {
+    return profile_steps(ctx, nsteps, true, max_names, names, total_ms, counts, n_names);
 }
 
 // ---------------------------------------------------------------------------

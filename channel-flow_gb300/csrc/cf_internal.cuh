@@ -256,8 +256,10 @@ struct cf_ctx {
     int step_launches = 0;
     int launches = 0;
     bool counting = false;
-    // per-kernel timing pass
+    // per-kernel timing pass (in_graph: the events are captured into the
+    // step's graph as event-record nodes)
     bool profiling = false;
+    bool profiling_in_graph = false;
     std::vector<cudaEvent_t> pev;
     std::vector<const char *> pname;
     int pn = 0;
@@ -320,7 +322,8 @@ static inline void count_launch(cf_ctx *ctx, const char *name) {
     if (ctx->counting) ctx->launches++;
     if (ctx->profiling) {
         if (ctx->pn < (int)ctx->pev.size()) {
-            cudaEventRecord(ctx->pev[ctx->pn], ctx->st);
+            cudaEventRecordWithFlags(ctx->pev[ctx->pn], ctx->st,
+                                     ctx->profiling_in_graph ? cudaEventRecordExternal : cudaEventRecordDefault);
             ctx->pname[ctx->pn] = name;
         }
         ctx->pn++;

@@ -159,6 +159,12 @@ int cf_launches_per_step(cf_ctx *ctx);
  * device milliseconds and launch counts (names: max_names rows of 48 chars). */
 int cf_profile_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
                      int *n_names);
+/* The same per-kernel figures from the graph form of the step: each of the
+ * nsteps steps is captured with an event-record node after every kernel,
+ * launched as one graph (as cf_time_step_rk3 replays it) and timed from those
+ * events. */
+int cf_profile_graph_steps(cf_ctx *ctx, int nsteps, int max_names, char *names, double *total_ms, int *counts,
+                           int *n_names);
 
 /* Empirical tuning of the z-chunk counts of the marching kernels (fused
  * right-hand side, fused dynamic Smagorinsky pass or AMD pass) on the
@@ -310,7 +316,8 @@ int cf_ensemble_set_batched_tri(cf_ensemble *e, int on);
  *   U, V, W  device arrays, reference layout and extents (top of this file)
  *   x, y, z  face coordinates on the device (nx, ny, nz doubles)
  *   out      2 device doubles: max(0, max div) and max |div| over the interior
- *            cells i = 2..nx, j = 2..ny, k = 2..nz
+ *            cells i = 2..nx, j = 2..ny, k = 2..nz; both NaN when the
+ *            divergence of any of those cells is NaN
  *   stream   a cudaStream_t (NULL: the legacy default stream); the work is
  *            enqueued on it and not waited for.
  * Scratch: one static device array per device holding CF_NOALLOC_MAX_PLANES
