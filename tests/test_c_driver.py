@@ -2,8 +2,9 @@
 the reference's compute_time_step_RK3 (time_integration.f90:89-173) issued
 call by call through the mirror entry points, in the reference's order and
 with its mass-flow branches, against the graph-captured cf_time_step_rk3 on
-the same snapshot.  FP64: U, V, W and nu_t within 1e-13, P within 1e-11 (the
-pseudo-pressure phi/(dt 8/15) carries the cancellation of div u* = O(dt))."""
+the same snapshot.  FP64: U, V, W within 1e-13, nu_t within 1e-12, P within
+1e-11 (the pseudo-pressure phi/(dt 8/15) carries the cancellation of
+div u* = O(dt))."""
 import json
 import os
 import subprocess
@@ -63,8 +64,11 @@ def test_c_mirror_matches_fast_path(tmp_path, dims, kw, steps, xmass):
     assert r.returncode == 0, r.stdout + r.stderr
     res = json.loads(r.stdout.strip().splitlines()[-1])
     print(dims, kw, res)
-    for n in ("U", "V", "W", "nu_t"):
+    for n in ("U", "V", "W"):
         assert res[n] <= 1e-13, (n, res[n])
+    # nu_t: the fast path forms max(-C|S|/2, 0) inside the fused right-hand
+    # side, the mirror materialises it first (different contraction)
+    assert res["nu_t"] <= 1e-12, res["nu_t"]
     assert res["P"] <= 1e-11, res["P"]
     assert res["t"][0] == res["t"][1] and res["t"][0] > 0
     # dPdx = (Q0 - Q)/dt is a cancellation: compare the correction Q0 - Q
