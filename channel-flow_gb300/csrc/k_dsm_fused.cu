@@ -16,10 +16,21 @@
 // z-accumulators held in registers (weights 1/6, 2/3, 1/6 to planes p-1, p,
 // p+1), so L_ij and hat(|S| S_ij) of plane k are complete once Q(k+1) has
 // been filtered; M_ij then needs S_ij of Uf, Vf, Wf at k, i.e. F(k-1..k+1).
-// With raw plane r entering the ring, the block therefore emits plane r-2.
-// Three barriers per plane: after the raw column pass, after G/F/Q, after
-// the Q column pass (with the next raw plane committed and the strain of the
-// filtered velocities read before it).
+// The march is a two-phase software pipeline with two barriers per raw
+// plane r:
+//   phase A(r): the raw column tasks store R(r) -- loaded into registers one
+//     step earlier, one (field, column) per task -- into the ring and filter
+//     it in y from those registers, then issue the loads of R(r+1); the Q
+//     column pass filters Q(r-2) in y; the strain rate of Uf, Vf, Wf at the
+//     output plane r-3 (from F(r-4), F(r-3), F(r-2)) and |S| of Q(r-2) at the
+//     own point go to registers.
+//   phase B(r): G(r) (x filter of the y-filtered raw plane), F(r-1) and
+//     Q(r-1) at the own and halo points; the x filter of the y-filtered
+//     Q(r-2) is added to the z accumulators of planes r-3 (its last
+//     contribution), r-2 and r-1 (its first); plane r-3 is output.
+// Phase A reads only what phase B of the step before wrote (Q, F) and what it
+// writes itself, phase B only what phase A wrote, so one barrier after each
+// phase orders every shared-memory access.
 //
 // The halo is read through the periodic wrap, which reproduces the
 // reference's periodic copies whenever U, V, W are themselves periodic in x
@@ -69,11 +80,16 @@ struct DsmSmem {
 template <typename T> struct DsmMinB { static constexpr int v = 2; };
 
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_dsm_fused(Fld<T> U, Fld<T> V, Fld<T> W, RGeo rgv, int nx, int ny, int nyg,
-                                                      int nz, int nxp, int nzp, int kc_len, T *Sout, double *part,
-                                                      int nchunk) {
+__global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v)
+    k_dsm_fused(Fld<T> U, Fld<T> V, Fld<T> W, RGeo rgv, int nx, int ny, int nyg, int nz, int nxp, int nzp, int kc_len,
+               T *Sout, double *part, int nchunk) {
     typedef DsmSmem<T, TX, TY> SM;
     constexpr int RX = SM::RX, RY = SM::RY, QX = SM::QX, QY = SM::QY;
+    constexpr int NTH = TX * TY, NRT = 3 * RX;
+    // the Q column pass is one (pair, column) task per thread for the TX own
+    // columns and 16 tasks for the two halo columns, on threads without a
+    // raw column task
+    static_assert(TY == 8 && NTH == 8 * TX && NRT + 16 <= NTH, "tile shape of the pipelined DSM pass");
     extern __shared__ unsigned char sm_raw[];
     T *R = (T *)sm_raw;         // [slot 3][field 3][RY][RX]
     T *G = R + SM::NR;          // [slot 3][field 3][QY][QX]
@@ -97,8 +113,6 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
     auto QS = [&](int p, int sy, int sx) -> PT & { return Qs[(p * QY + sy) * QX + sx]; };
     auto CS = [&](int p, int oy, int sx) -> PT & { return Cs[(p * TY + oy) * QX + sx]; };
     auto YS = [&](int f, int sy, int rx) -> T & { return Ry[(f * QY + sy) * RX + rx]; };
-
-    // y filter weights of a row in [lo, hi] (one-sided at the ends)
     auto yw = [&](int j, int lo, int hi, T &wm, T &w0, T &wp) {
         if (j <= lo) { wm = T(0); w0 = f23; wp = f13; }
         else if (j >= hi) { wm = f13; w0 = f23; wp = T(0); }
@@ -106,45 +120,37 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
     };
     const T fw[3] = {f6, f23, f6};
 
-    // reciprocal spacings of the region columns and rows (z is per plane)
     __shared__ T gsx[3][QX], gsy[3][QY];
-    // z spacings of every plane the chunk touches (rs .. re), so that no
-    // plane starts with a global load
     __shared__ T gsz[3][DSM_ZMAX + 4];
     {
-        const int zs = 2 + blockIdx.z * kc_len - 2, ze = min(2 + blockIdx.z * kc_len + kc_len - 1, nz - 1) + 2;
-        for (int t = tid; t <= ze - zs; t += TX * TY) {
+        const int zs = kb - 2, ze = ke + 2;
+        for (int t = tid; t <= ze - zs; t += NTH) {
             const int kc = wrapc(zs + t, nzp);
             gsz[0][t] = rdz[kc];
             gsz[1][t] = rdzg[kc];
             gsz[2][t] = rdzg[kc + 1];
         }
     }
-    for (int t = tid; t < QX; t += TX * TY) {
+    for (int t = tid; t < QX; t += NTH) {
         int ic = wrapq(i0 + t - 1, nxp);
         gsx[0][t] = rdx[ic];
         gsx[1][t] = rdxg[ic];
         gsx[2][t] = rdxg[ic + 1];
     }
-    for (int t = tid; t < QY; t += TX * TY) {
+    for (int t = tid; t < QY; t += NTH) {
         int jj = min(max(j0 + t - 1, 2), nyg - 1);
         gsy[0][t] = rdy[jj];
         gsy[1][t] = rdyg[jj];
         gsy[2][t] = rdyg[jj + 1];
     }
-    // z-accumulators of the x-y filtered pairs (uc,vc) (wc,uu) (vv,ww) (uv,uw)
-    // (vw,|S|S11) (|S|S22,|S|S33) (|S|S12,|S|S13) (|S|S23,|S|) for the three
-    // planes in flight
     PT acc[3][8];
 #pragma unroll
     for (int s = 0; s < 3; s++)
 #pragma unroll
         for (int q = 0; q < 8; q++) acc[s][q] = psplat(T(0));
-    T Sprev = T(0);
-    T sl = T(0), smm = T(0);  // this thread's plane sums (widened per block)
+    T S_m2 = T(0), S_m3 = T(0);  // |S| of Q(r-2), Q(r-3) at the own point
+    T sl = T(0), smm = T(0);
 
-    // this thread's point of the halo ring of the QX x QY region (top row,
-    // bottom row, left column, right column), if any
     const bool hal = tid < 2 * QX + 2 * TY;
     int hsx = 0, hsy = 0;
     if (tid < QX) { hsx = tid; hsy = 0; }
@@ -152,105 +158,157 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
     else if (tid < 2 * QX + TY) { hsx = 0; hsy = tid - 2 * QX + 1; }
     else if (hal) { hsx = QX - 1; hsy = tid - 2 * QX - TY + 1; }
     const int rs = kb - 2, re = ke + 2;
-    // one march step for raw plane r; PH = (r - rs) % 3 is the ring phase
-    // raw-tile elements of this thread (same for every plane)
-    constexpr int NTH = TX * TY, NRP = RX * RY, NLR = (NRP + NTH - 1) / NTH;
-    int eia[NLR], eja[NLR], ers[NLR];
-#pragma unroll
-    for (int q = 0; q < NLR; q++) {
-        int rem = tid + q * NTH;
-        ers[q] = rem;
-        int sy = rem / RX, sx = rem - sy * RX;
-        eia[q] = wrapq(i0 + sx - 2, nxp);
-        eja[q] = j0 + sy - 2;
-    }
-    T pre[3][NLR];
-    auto fetch = [&](int r) {  // issue every load of raw plane r
+
+    // raw column task: field rf, region column rcx, on the last NRT threads
+    // (the halo points of phase B are on the first threads)
+    const int rtid = tid - (NTH - NRT);
+    const bool has_rt = rtid >= 0;
+    const int rf = has_rt ? rtid / RX : 0, rcx = has_rt ? rtid - rf * RX : 0;
+    const int ria = wrapq(i0 + rcx - 2, nxp), rjhi = rf == 1 ? ny : nyg;
+    const Fld<T> RF = rf == 0 ? U : (rf == 1 ? V : W);
+    T colv[RY];
+    auto fetch_col = [&](int r) {
         const int kc = wrapn(r, nzp);
 #pragma unroll
-        for (int q = 0; q < NLR; q++) {
-            const bool in = ers[q] < NRP;
-            const int ia = eia[q], ja = eja[q];
-            pre[0][q] = (in && ja >= 1 && ja <= nyg) ? U(ia, ja, kc) : T(0);
-            pre[1][q] = (in && ja >= 1 && ja <= ny) ? V(ia, ja, kc) : T(0);
-            pre[2][q] = (in && ja >= 1 && ja <= nyg) ? W(ia, ja, kc) : T(0);
+        for (int q = 0; q < RY; q++) {
+            const int j = j0 + q - 2;
+            colv[q] = (has_rt && j >= 1 && j <= rjhi) ? RF(ria, j, kc) : T(0);
         }
     };
-    auto commit = [&](int slot) {
+    // halo-column task of the Q column pass (the 16 threads below the raw
+    // column tasks)
+    const int htid = tid - (NTH - NRT - 16);
+    const bool has_hc = htid >= 0 && htid < 16;
+    const int hcq = has_hc ? htid >> 1 : 0, hcx = TX + (htid & 1);
+    // the raw plane's y filter has interior weights in every region row
+    const bool raw_inner = j0 - 1 > 1 && j0 + TY < rjhi;
+
+    auto colpass = [&](int q, int sx, bool inner) {
+        PT col[QY];
 #pragma unroll
-        for (int q = 0; q < NLR; q++)
-            if (ers[q] < NRP) {
+        for (int s = 0; s < QY; s++) col[s] = QS(q, s, sx);
+        if (inner) {
+            const PT pf6 = psplat(f6), pf23 = psplat(f23);
 #pragma unroll
-                for (int f = 0; f < 3; f++) R[(slot * 3 + f) * NRP + ers[q]] = pre[f][q];
+            for (int oy = 0; oy < TY; oy++) {
+                PT c = pmul(pf23, col[oy + 1]);
+                c = pfma(pf6, col[oy], c);
+                c = pfma(pf6, col[oy + 2], c);
+                CS(q, oy, sx) = c;
             }
+        } else {
+#pragma unroll
+            for (int oy = 0; oy < TY; oy++) {
+                const int j = j0 + oy;
+                T wm, w0, wp;
+                yw(j, 2, nyg - 1, wm, w0, wp);
+                const PT cm = j > 2 ? col[oy] : col[oy + 1], cp = j < nyg - 1 ? col[oy + 2] : col[oy + 1];
+                PT c = pmul(psplat(w0), col[oy + 1]);
+                c = pfma(psplat(wm), cm, c);
+                c = pfma(psplat(wp), cp, c);
+                CS(q, oy, sx) = c;
+            }
+        }
     };
-    // one march step for raw plane r; PH = (r - rs) % 3 is the ring phase.
-    // On entry R(r) is in slot PH; R(r+1) is fetched during the step.
+
     auto step = [&](int r, auto PHc) {
         constexpr int PH = decltype(PHc)::value;
         constexpr int P1 = (PH + 1) % 3, P2 = (PH + 2) % 3;
-        if (r + 1 <= re) fetch(r + 1);
-        // -- y filter of the raw plane R(r) (slot PH), one (field, raw
-        // column) per task: the column's RY values give the QY rows of the
-        // region (one-sided at rows 1 and jhi); G below is its x filter
-        for (int t = tid; t < 3 * RX; t += NTH) {
-            const int f = t / RX, rx = t - f * RX, jhi = f == 1 ? ny : nyg;
-            T col[RY];
+        // ================= phase A(r)
+        if (r <= re && has_rt) {
+            // R(r): into the ring slot of R(r-3) (last read by Q(r-2) in
+            // phase B of the step before), and filtered in y into Ry
 #pragma unroll
-            for (int q = 0; q < RY; q++) col[q] = RS(PH, f, q, rx);
+            for (int q = 0; q < RY; q++) RS(PH, rf, q, rcx) = colv[q];
+            if (raw_inner) {
 #pragma unroll
-            for (int sy = 0; sy < QY; sy++) {
-                const int j = j0 + sy - 1;
-                T wm, w0, wp;
-                yw(j, 1, jhi, wm, w0, wp);
-                const T cm = j > 1 ? col[sy] : col[sy + 1], cp = j < jhi ? col[sy + 2] : col[sy + 1];
-                YS(f, sy, rx) = wm * cm + w0 * col[sy + 1] + wp * cp;
+                for (int sy = 0; sy < QY; sy++) YS(rf, sy, rcx) = f6 * colv[sy] + f23 * colv[sy + 1] + f6 * colv[sy + 2];
+            } else {
+#pragma unroll
+                for (int sy = 0; sy < QY; sy++) {
+                    const int j = j0 + sy - 1;
+                    T wm, w0, wp;
+                    yw(j, 1, rjhi, wm, w0, wp);
+                    const T cm = j > 1 ? colv[sy] : colv[sy + 1], cp = j < rjhi ? colv[sy + 2] : colv[sy + 1];
+                    YS(rf, sy, rcx) = wm * cm + w0 * colv[sy + 1] + wp * cp;
+                }
+            }
+            if (r + 1 <= re) fetch_col(r + 1);
+        }
+        T sf[6], Sf = T(0);
+#pragma unroll
+        for (int q = 0; q < 6; q++) sf[q] = T(0);
+        if (r >= kb + 1) {  // Q(r-2) exists (planes kb-1 .. ke+1)
+            const bool inner = j0 > 2 && j0 + TY - 1 < nyg - 1;
+            colpass(tid / TX, tx, inner);
+            if (has_hc) colpass(hcq, hcx, inner);
+            S_m3 = S_m2;
+            S_m2 = own ? QS(7, ty + 1, tx + 1).y : T(0);
+            if (r >= kb + 3 && own) {
+                // S_ij of Uf, Vf, Wf at the output plane k = r-3: F(k-1) [P2],
+                // F(k) [PH], F(k+1) [P1]
+                const int sx = tx + 1, sy = ty + 1, k = r - 3;
+                auto uf = [&](int di, int dj, int dk) { return FS(dk < 0 ? P2 : (dk == 0 ? PH : P1), 0, sy + dj, sx + di); };
+                auto vf = [&](int di, int dj, int dk) { return FS(dk < 0 ? P2 : (dk == 0 ? PH : P1), 1, sy + dj, sx + di); };
+                auto wf = [&](int di, int dj, int dk) { return FS(dk < 0 ? P2 : (dk == 0 ? PH : P1), 2, sy + dj, sx + di); };
+                const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
+                const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
+                const T rz = gsz[0][k - rs], rzg0 = gsz[1][k - rs], rzg1 = gsz[2][k - rs];
+                T s0 = (uf(0, 0, 0) - uf(-1, 0, 0)) * rx0;
+                T s1 = (vf(0, 0, 0) - vf(0, -1, 0)) * ry0;
+                T s2 = (wf(0, 0, 0) - wf(0, 0, -1)) * rz;
+                T s3 = T(0), s4 = T(0), s5 = T(0);
+#pragma unroll
+                for (int a = 0; a < 2; a++)
+#pragma unroll
+                    for (int b = 0; b < 2; b++) {
+                        const T rxa = a ? rxg1 : rxg0, ryb = b ? ryg1 : ryg0, rzb = b ? rzg1 : rzg0, rya = a ? ryg1 : ryg0;
+                        s3 += h * ((uf(a - 1, b, 0) - uf(a - 1, b - 1, 0)) * ryb + (vf(a, b - 1, 0) - vf(a - 1, b - 1, 0)) * rxa);
+                        s4 += h * ((uf(a - 1, 0, b) - uf(a - 1, 0, b - 1)) * rzb + (wf(a, 0, b - 1) - wf(a - 1, 0, b - 1)) * rxa);
+                        s5 += h * ((vf(0, a - 1, b) - vf(0, a - 1, b - 1)) * rzb + (wf(0, a, b - 1) - wf(0, a - 1, b - 1)) * rya);
+                    }
+                s3 *= qq; s4 *= qq; s5 *= qq;
+                Sf = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
+                          T(4) * s5 * s5);
+                sf[0] = s0; sf[1] = s1; sf[2] = s2; sf[3] = s3; sf[4] = s4; sf[5] = s5;
             }
         }
         __syncthreads();
-        // G(r), F(r-1) and Q(r-1) at this thread's points of the tile + 1 halo
-        // (its own point, and one point of the halo ring for the first
-        // 2 QX + 2 TY threads): G and F at a point only need that point's G
-        // history, and Q only the raw planes already in the ring.
-        const int zq = max(r - 1 - rs, 0);  // plane r-1 (used from r = kb on)
-        const T rz = gsz[0][zq], rzg0 = gsz[1][zq], rzg1 = gsz[2][zq];
-        for (int pt = 0; pt < 2; pt++) {
-            if (pt == 1 && !hal) break;
-            const int sx = pt ? hsx : tx + 1, sy = pt ? hsy : ty + 1;
-            const int j = j0 + sy - 1;
-            // -- G(r): x-y filtered U, V, W
-            T gc[3];
+        // ================= phase B(r)
+        if (r <= re) {
+            const int zq = max(r - 1 - rs, 0);  // plane r-1 (used from r = kb on)
+            const T rz = gsz[0][zq], rzg0 = gsz[1][zq], rzg1 = gsz[2][zq];
+            for (int pt = 0; pt < 2; pt++) {
+                if (pt == 1 && !hal) break;
+                const int sx = pt ? hsx : tx + 1, sy = pt ? hsy : ty + 1;
+                const int j = j0 + sy - 1;
+                T gc[3];
 #pragma unroll
-            for (int f = 0; f < 3; f++) {
-                const int jhi = f == 1 ? ny : nyg;
-                T g = T(0);
-                if (j >= 1 && j <= jhi) {
+                for (int f = 0; f < 3; f++) {
+                    const int jhi = f == 1 ? ny : nyg;
+                    T g = T(0);
+                    if (j >= 1 && j <= jhi) {
 #pragma unroll
-                    for (int a = -1; a <= 1; a++) g += fw[a + 1] * YS(f, sy, sx + 1 + a);
+                        for (int a = -1; a <= 1; a++) g += fw[a + 1] * YS(f, sy, sx + 1 + a);
+                    }
+                    GS(PH, f, sy, sx) = g;
+                    gc[f] = g;
                 }
-                GS(PH, f, sy, sx) = g;
-                gc[f] = g;
-            }
-            if (r < kb) continue;
-            // -- F(r-1) = z filter of G(r-2), G(r-1), G(r)
+                if (r < kb) continue;
 #pragma unroll
-            for (int f = 0; f < 3; f++) FS(P2, f, sy, sx) = f6 * GS(P1, f, sy, sx) + f23 * GS(P2, f, sy, sx) + f6 * gc[f];
-            // -- Q(r-1) from R(r-2) [P1], R(r-1) [P2], R(r) [PH]
-            if (j < 2 || j > nyg - 1) {
+                for (int f = 0; f < 3; f++) FS(P2, f, sy, sx) = f6 * GS(P1, f, sy, sx) + f23 * GS(P2, f, sy, sx) + f6 * gc[f];
+                if (j < 2 || j > nyg - 1) {
 #pragma unroll
-                for (int q = 0; q < 8; q++) QS(q, sy, sx) = psplat(T(0));
-                continue;
-            }
-            {
-                const int rx = sx + 1, ry = sy + 1;  // raw slot of the centre
-                // raw accessors with offsets (di, dj, dk), dk in {-1, 0, 1}
+                    for (int q = 0; q < 8; q++) QS(q, sy, sx) = psplat(T(0));
+                    continue;
+                }
+                const int rx = sx + 1, ry = sy + 1;
                 auto u = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 0, ry + dj, rx + di); };
                 auto v = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 1, ry + dj, rx + di); };
                 auto w = [&](int di, int dj, int dk) { return RS(dk < 0 ? P1 : (dk == 0 ? P2 : PH), 2, ry + dj, rx + di); };
                 T uc = h * (u(-1, 0, 0) + u(0, 0, 0));
                 T vc = h * (v(0, -1, 0) + v(0, 0, 0));
                 T wc = h * (w(0, 0, -1) + w(0, 0, 0));
-                // compute_Sij (subgrid.f90:900-946)
                 const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
                 const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
                 T s0 = (u(0, 0, 0) - u(-1, 0, 0)) * rx0;
@@ -282,91 +340,8 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
                 QS(4, sy, sx) = q4; QS(5, sy, sx) = q5; QS(6, sy, sx) = q6; QS(7, sy, sx) = q7;
             }
         }
-        __syncthreads();
-        // R(r-2) (slot P1) was last read by Q(r-1): R(r+1) takes its place
-        // (visible after the next barrier)
-        if (r + 1 <= re) commit(P1);
-        // S_ij of Uf, Vf, Wf at the output plane k = r-2 (from F(r-3) [PH],
-        // F(r-2) [P1], F(r-1) [P2]) and |S| of Q(r-1) at the own point, read
-        // before the barrier: the next step overwrites F(r-3) and Q
-        T sf[6], Sf = T(0), Snew = T(0);
-#pragma unroll
-        for (int q = 0; q < 6; q++) sf[q] = T(0);
-        if (r >= kb) {
-            // -- y filter of Q(r-1), one (pair, column) of the region per
-            // task: the column's QY values are read once and give the TY
-            // filtered rows (one-sided at the wall rows j = 2 and nyg-1).
-            // Tasks 0 .. 8 TX - 1 take columns 0 .. TX - 1 of one pair per
-            // TX lanes; the last 16 take columns TX and TX + 1.
-            const bool inner = j0 > 2 && j0 + TY - 1 < nyg - 1;
-            for (int t = tid; t < 8 * QX; t += NTH) {
-                int q, sx;
-                if (t < 8 * TX) { q = t / TX; sx = t - q * TX; }
-                else { q = (t - 8 * TX) >> 1; sx = TX + ((t - 8 * TX) & 1); }
-                PT col[QY];
-#pragma unroll
-                for (int s = 0; s < QY; s++) col[s] = QS(q, s, sx);
-                if (inner) {
-                    const PT pf6 = psplat(f6), pf23 = psplat(f23);
-#pragma unroll
-                    for (int oy = 0; oy < TY; oy++) {
-                        PT c = pmul(pf23, col[oy + 1]);
-                        c = pfma(pf6, col[oy], c);
-                        c = pfma(pf6, col[oy + 2], c);
-                        CS(q, oy, sx) = c;
-                    }
-                } else {
-#pragma unroll
-                    for (int oy = 0; oy < TY; oy++) {
-                        const int j = j0 + oy;
-                        T wm, w0, wp;
-                        yw(j, 2, nyg - 1, wm, w0, wp);
-                        const PT cm = j > 2 ? col[oy] : col[oy + 1], cp = j < nyg - 1 ? col[oy + 2] : col[oy + 1];
-                        PT c = pmul(psplat(w0), col[oy + 1]);
-                        c = pfma(psplat(wm), cm, c);
-                        c = pfma(psplat(wp), cp, c);
-                        CS(q, oy, sx) = c;
-                    }
-                }
-            }
-            if (own) {
-                const int sx = tx + 1, sy = ty + 1;
-                Snew = QS(7, sy, sx).y;
-                if (r >= kb + 2) {
-                    const int k = r - 2;
-                    auto uf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 0, sy + dj, sx + di); };
-                    auto vf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 1, sy + dj, sx + di); };
-                    auto wf = [&](int di, int dj, int dk) { return FS(dk < 0 ? PH : (dk == 0 ? P1 : P2), 2, sy + dj, sx + di); };
-                    const T rx0 = gsx[0][sx], rxg0 = gsx[1][sx], rxg1 = gsx[2][sx];
-                    const T ry0 = gsy[0][sy], ryg0 = gsy[1][sy], ryg1 = gsy[2][sy];
-                    const T rz = gsz[0][k - rs], rzg0 = gsz[1][k - rs], rzg1 = gsz[2][k - rs];
-                    T s0 = (uf(0, 0, 0) - uf(-1, 0, 0)) * rx0;
-                    T s1 = (vf(0, 0, 0) - vf(0, -1, 0)) * ry0;
-                    T s2 = (wf(0, 0, 0) - wf(0, 0, -1)) * rz;
-                    T s3 = T(0), s4 = T(0), s5 = T(0);
-#pragma unroll
-                    for (int a = 0; a < 2; a++)
-#pragma unroll
-                        for (int b = 0; b < 2; b++) {
-                            const T rxa = a ? rxg1 : rxg0, ryb = b ? ryg1 : ryg0, rzb = b ? rzg1 : rzg0, rya = a ? ryg1 : ryg0;
-                            s3 += h * ((uf(a - 1, b, 0) - uf(a - 1, b - 1, 0)) * ryb + (vf(a, b - 1, 0) - vf(a - 1, b - 1, 0)) * rxa);
-                            s4 += h * ((uf(a - 1, 0, b) - uf(a - 1, 0, b - 1)) * rzb + (wf(a, 0, b - 1) - wf(a - 1, 0, b - 1)) * rxa);
-                            s5 += h * ((vf(0, a - 1, b) - vf(0, a - 1, b - 1)) * rzb + (wf(0, a, b - 1) - wf(0, a - 1, b - 1)) * rya);
-                        }
-                    s3 *= qq; s4 *= qq; s5 *= qq;
-                    Sf = sqrt(T(2) * s0 * s0 + T(2) * s1 * s1 + T(2) * s2 * s2 + T(4) * s3 * s3 + T(4) * s4 * s4 +
-                              T(4) * s5 * s5);
-                    sf[0] = s0; sf[1] = s1; sf[2] = s2; sf[3] = s3; sf[4] = s4; sf[5] = s5;
-                }
-            }
-        }
-        __syncthreads();
-        // No barrier closes the step: the next step's first writes (G(r+1)
-        // over G(r-2), F(r) over F(r-3), Q(r)) touch nothing read below, and
-        // the filtered columns are rewritten only after its first barrier.
-        if (r >= kb && own) {
-            // -- x filter of the y-filtered Q(r-1) at the own point, spread
-            // over planes r-2, r-1, r
+        if (r >= kb + 1 && own) {
+            // x filter of the y-filtered Q(r-2): planes r-3 (last), r-2, r-1 (first)
             const int sx = tx + 1;
             const PT pf6 = psplat(f6), pf23 = psplat(f23);
 #pragma unroll
@@ -374,22 +349,20 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
                 PT a = psplat(T(0));
 #pragma unroll
                 for (int d = -1; d <= 1; d++) a = pfma(psplat(fw[d + 1]), CS(q, ty, sx + d), a);
-                acc[P1][q] = pfma(pf6, a, acc[P1][q]);   // plane r-2 (last contribution)
-                acc[P2][q] = pfma(pf23, a, acc[P2][q]);  // plane r-1
-                acc[PH][q] = pmul(pf6, a);               // plane r (first contribution; the slot held plane r-3)
+                acc[PH][q] = pfma(pf6, a, acc[PH][q]);
+                acc[P1][q] = pfma(pf23, a, acc[P1][q]);
+                acc[P2][q] = pmul(pf6, a);
             }
-            if (r >= kb + 2) {
-                // -- output plane k = r-2
-                const int kcn = wrapn(r - 2, nzp);
+            if (r >= kb + 3) {
+                const int kcn = wrapn(r - 3, nzp);
                 const T fs2 = T(4);  // fil_size**2 (subgrid.f90:156, 463)
-                // filtered quantities of plane r-2 in the order uc vc wc uu vv ww uv uw vw |S|S11..|S|S23
                 T fq[15];
 #pragma unroll
                 for (int q = 0; q < 7; q++) {
-                    fq[2 * q] = acc[P1][q].x;
-                    fq[2 * q + 1] = acc[P1][q].y;
+                    fq[2 * q] = acc[PH][q].x;
+                    fq[2 * q + 1] = acc[PH][q].y;
                 }
-                fq[14] = acc[P1][7].x;
+                fq[14] = acc[PH][7].x;
                 const T fu = fq[0], fv = fq[1], fwv = fq[2];
                 const T pa[6] = {fu, fv, fwv, fu, fu, fv}, pb[6] = {fu, fv, fwv, fv, fwv, fwv};
                 T lm = T(0), mm = T(0);
@@ -404,27 +377,22 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
                 T wgt = (io == 2 ? T(2) : T(1)) * (kcn == 2 ? T(2) : T(1));
                 sl += wgt * lm;
                 smm += wgt * mm;
-                Sout[(long)(io - 2) + (long)nxp * ((jo - 2) + (long)(nyg - 2) * (kcn - 2))] = Sprev;
+                Sout[(long)(io - 2) + (long)nxp * ((jo - 2) + (long)(nyg - 2) * (kcn - 2))] = S_m3;
             }
-            Sprev = Snew;  // |S| at plane r-1 for the next output
         }
+        __syncthreads();
     };
-    fetch(rs);
-    commit(0);
+    fetch_col(rs);
     __syncthreads();
     std::integral_constant<int, 0> c0;
     std::integral_constant<int, 1> c1;
     std::integral_constant<int, 2> c2;
-    for (int r = rs; r <= re; r += 3) {
+    for (int r = rs; r <= re + 1; r += 3) {
         step(r, c0);
-        if (r + 1 <= re) step(r + 1, c1);
-        if (r + 2 <= re) step(r + 2, c2);
+        if (r + 1 <= re + 1) step(r + 1, c1);
+        if (r + 2 <= re + 1) step(r + 2, c2);
     }
-    // plane partials of this block for row jo: reduce over the TX threads of the row
     if constexpr (sizeof(T) == 4 && TX == 32) {
-        // one warp per row: a float-float shuffle tree (FP64 instructions are
-        // dozens of times the cost of FP32 ones on this part); lane 0 writes
-        // (L.M hi, lo, M.M hi, lo)
         float ah = own ? (float)sl : 0.f, al = 0.f, bh = own ? (float)smm : 0.f, bl = 0.f;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -439,8 +407,7 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_
         }
         return;
     }
-    __syncthreads();
-    double *red = (double *)sm_raw;  // 2 * TX * TY doubles fit in the R ring
+    double *red = (double *)sm_raw;
     red[2 * tid] = own ? (double)sl : 0.0;
     red[2 * tid + 1] = own ? (double)smm : 0.0;
     __syncthreads();
