@@ -246,14 +246,17 @@ _NET = {}
 
 def wall_net(wl, device):
     """The learned wall stress of a workload that uses it: trained once per
-    process on 2^20 eqwm-labelled samples with the project's own kernels."""
+    process on 2^20 eqwm-labelled samples, half of them drawn from the
+    solver's own wall-modelled runs across Re_tau 500-10000, with the
+    project's own kernels."""
     key = (wl["ncv"], device)
     if key not in _NET:
         import torch
         from channelflow import wallmlp
         dev = torch.device("cuda", device)
         t0 = time.perf_counter()
-        u, h, nu, tau = wallmlp.training_set(1 << 20, seed=5200, device=dev, ncv=wl["ncv"], stretch=1.10)
+        (u, h, nu, tau), n_solver = wallmlp.training_set_mixed(1 << 20, solver_fraction=0.5, seed=5200, device=dev,
+                                                                ncv=wl["ncv"], stretch=1.10)
         t1 = time.perf_counter()
         net = wallmlp.WallMLP(seed=3, ncv=wl["ncv"], stretch=1.10)
         net.fit_normalisation(u, h, nu, tau)
@@ -263,7 +266,8 @@ def wall_net(wl, device):
         ut, ht, nt, tt = wallmlp.training_set(1 << 16, seed=5201, device=dev, ncv=wl["ncv"], stretch=1.10,
                                               **wallmlp.OPERATING)
         err = (net.predict(ut, ht, nt) / tt - 1).abs()
-        _NET[key] = (net, {"samples": int(u.numel()), "label_seconds": t1 - t0, "train_seconds": t2 - t1,
+        _NET[key] = (net, {"samples": int(u.numel()), "solver_samples": n_solver,
+                           "harvest_and_label_seconds": t1 - t0, "train_seconds": t2 - t1,
                            "final_loss": float(loss[-1]), "heldout_max_rel_err": float(err.max()),
                            "heldout_mean_rel_err": float(err.mean())})
     return _NET[key]

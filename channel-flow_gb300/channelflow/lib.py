@@ -147,6 +147,7 @@ class Channel:
                 self.L.cf_destroy(h)
             raise CfError(msg)
         self.h = h
+        self.device = device
         self.shapes = grids.field_shapes(self.nx, self.ny, self.nz)
         # unique (periodic) cells: nxp x nym x nzp (initialization.f90:246-247)
         self.nxp, self.nym, self.nzp = self.nx - 2, self.ny - 1, self.nz - 2

@@ -36,6 +36,8 @@ def _bind():
     L.cf_set_wall_mlp.argtypes = [vp, vp, C.c_int]
     L.cf_get_wall_mlp_log.argtypes = [vp, dp]
     L.cf_mlp_wait_expired.argtypes = [vp, ip]
+    L.cf_wall_model_inputs.argtypes = [vp, vp, C.c_long, C.POINTER(C.c_long), dp, dp]
+    L.cf_mlp_set_train_tensor_cores.argtypes = [vp, C.c_int]
     L.cf_mlp_test_skip_mma.argtypes = [vp, C.c_int]
     L._wmlp_bound = True
     return L
@@ -104,6 +106,88 @@ def training_set(n: int, seed: int = 0, device=None, ncv: int = 30, stretch: flo
     return u[keep].contiguous(), h[keep].contiguous(), nu[keep].contiguous(), tau[keep].contiguous()
 
 
+def wall_model_inputs(channel):
+    """The inputs the equilibrium wall model of `channel` (iwall_model 3)
+    hands to its eqwm solve for the current fields: (u_les, h, nu) with u_les
+    a device float64 tensor of every wall point's matching-plane velocity
+    (wallmodel.f90:597-621) and h, nu the matching height and viscosity."""
+    import torch
+    L = _bind()
+    n, h, nu = C.c_long(), C.c_double(), C.c_double()
+    _check(L, L.cf_wall_model_inputs(channel.h, None, 0, C.byref(n), C.byref(h), C.byref(nu)), "cf_wall_model_inputs")
+    u = torch.empty(n.value, dtype=torch.float64, device=torch.device("cuda", channel.device))
+    _check(L, L.cf_wall_model_inputs(channel.h, _ptr(u), n.value, C.byref(n), C.byref(h), C.byref(nu)),
+           "cf_wall_model_inputs")
+    return u, h.value, nu.value
+
+
+# Wall-modelled channels that supply solver samples: the layout of the
+# Re_tau 2000 configuration (2 pi x 2 x pi, uniform wall-normal grid, dynamic
+# Smagorinsky, equilibrium wall model, plug initial field) on a 64 x 48 x 64
+# grid, at friction Reynolds numbers spanning the operating range, matched at
+# the 3rd, 4th and 5th cell centres (0.06, 0.10, 0.15 half-heights).
+HARVEST_RUNS = ((500.0, 4), (1000.0, 3), (2000.0, 5), (4000.0, 4), (7000.0, 3), (10000.0, 5))
+
+
+def harvest_inputs(n: int, device=None, runs=HARVEST_RUNS, faces=(66, 49, 66), warm=600, every=40, ncv: int = 30,
+                   stretch: float = 1.10, seed: int = 1):
+    """About n wall-model inputs (u_les, h, nu) drawn from the solver's own
+    wall-modelled runs: each run of `runs` (Re_tau, jref) is advanced `warm`
+    split-path steps from its seeded plug field, then its wall-model inputs
+    are collected every `every` steps until it has supplied its share.
+    Returns device float64 tensors (u, h, nu) and the steps run."""
+    import torch
+    from . import lib
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    x, y, z = grids.channel_grid(*faces, stretch=0.0)
+    share = -(-n // len(runs))
+    us, hs, nus, steps = [], [], [], 0
+    for q, (retau, jref) in enumerate(runs):
+        nu = grids.dean_nu(retau)
+        U, V, W = grids.seeded_fields(x, y, z, seed=seed + q, profile="plug")
+        ch = lib.Channel(x, y, z, device=dev.index or 0, precision=lib.PREC_SPLIT, nu=nu, CFL=0.5,
+                         dPdx=(retau * nu) ** 2, LES_model=2, iwall_model=3, x_mass_cte=1, jref_eqwm=jref,
+                         eqwm_ncv=ncv, eqwm_stretch=stretch)
+        ch.upload(U, V, W)
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        ch.time_step_rk3(warm)
+        steps += warm
+        got = 0
+        while got < share:
+            ch.time_step_rk3(every)
+            steps += every
+            u, h, nuv = wall_model_inputs(ch)
+            us.append(u)
+            hs.append(torch.full_like(u, h))
+            nus.append(torch.full_like(u, nuv))
+            got += u.numel()
+        ch.close()
+    return torch.cat(us)[:n].contiguous(), torch.cat(hs)[:n].contiguous(), torch.cat(nus)[:n].contiguous(), steps
+
+
+def training_set_mixed(n: int, solver_fraction: float = 0.5, seed: int = 0, device=None, ncv: int = 30,
+                       stretch: float = 1.10, **kw):
+    """n labelled samples: a solver_fraction share drawn from the solver's own
+    wall-modelled runs (harvest_inputs), the rest from training_inputs (which
+    covers the envelope around the operating range evenly), all labelled by
+    the batched eqwm solve; unconverged solves are dropped.  Returns (u, h, nu,
+    tau) and the number of solver samples kept."""
+    import torch
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    ns = int(n * solver_fraction)
+    hu, hh, hn, _ = harvest_inputs(ns, device=dev, ncv=ncv, stretch=stretch, seed=seed + 1)
+    su, sh, sn = training_inputs(n - ns, seed=seed, **kw)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    src = torch.cat([torch.ones(hu.numel(), dtype=torch.bool, device=dev),
+                     torch.zeros(n - ns, dtype=torch.bool, device=dev)])
+    u, h, nu = torch.cat([hu, T(su)]), torch.cat([hh, T(sh)]), torch.cat([hn, T(sn)])
+    tau, it = eqwm_solve_batch(u, h, nu, ncv=ncv, stretch=stretch, iters=True)
+    keep = (it < 100) & torch.isfinite(tau) & (tau > 0)
+    return ((u[keep].contiguous(), h[keep].contiguous(), nu[keep].contiguous(), tau[keep].contiguous()),
+            int((keep & src).sum().item()))
+
+
 class WallMLP:
     """A device-resident network (FP32 master weights, Adam state)."""
 
@@ -151,6 +235,11 @@ class WallMLP:
         _check(self.L, self.L.cf_mlp_predict(self.h, u.numel(), _ptr(u), _ptr(h), _ptr(nu), _ptr(tau), _ptr(ins),
                                               1 if tensor_cores else 0, _stream(u)), "cf_mlp_predict")
         return (tau, ins) if inside else tau
+
+    def train_tensor_cores(self, on: bool):
+        """Gradients with layer 2's products on the tensor cores (default) or,
+        on=False, on the FP32 pipes."""
+        _check(self.L, self.L.cf_mlp_set_train_tensor_cores(self.h, 1 if on else 0), "cf_mlp_set_train_tensor_cores")
 
     def wait_expired(self) -> bool:
         """True when a tensor-core inference since the last call gave up

@@ -884,6 +884,21 @@ extern "C" int cf_compute_wall_model(cf_ctx *ctx) {
     return CF_OK;
 }
 
+extern "C" int cf_wall_model_inputs(cf_ctx *ctx, double *u_les, long cap, long *npts, double *h_wm, double *nu) {
+    if (!ctx || !npts) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
+    if (ctx->prm.iwall_model != 3) return cf_fail(ctx, CF_ERR_INVALID, "the wall-model inputs need iwall_model 3");
+    const long n = (long)ctx->nx * 2 * ctx->nzg;
+    *npts = n;
+    if (h_wm) *h_wm = ctx->hyg[ctx->prm.jref_eqwm];
+    if (nu) *nu = ctx->prm.nu;
+    if (!u_les) return CF_OK;
+    if (cap < n) return cf_fail(ctx, CF_ERR_INVALID, "u_les holds fewer than nx * 2 * (nz+1) values");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    TRY(DISPATCH(launch_wm_inputs<double>(ctx, ctx->cur, u_les), launch_wm_inputs<float>(ctx, ctx->cur, u_les)));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    return CF_OK;
+}
+
 extern "C" int cf_get_eqwm_counters(cf_ctx *ctx, int *n_nan, int *n_iter) {
     if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
     if (n_nan) *n_nan = ctx->n_nan;

@@ -310,6 +310,7 @@ template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // 
 template <typename T> int launch_mass_apply(cf_ctx *ctx, int buf, int mode, bool ghosts = false); // add ds->lmax[2], dPdx = it/dt (ghosts: whole array, as the BCs would)
 template <typename T> int launch_dt(cf_ctx *ctx, int buf, bool advance_t = false);  // advance_t: t += dt (fast path)
 template <typename T> int launch_eqwm(cf_ctx *ctx, int buf);
+template <typename T> int launch_wm_inputs(cf_ctx *ctx, int buf, double *ules);  // matching-plane |u| per wall point
 int wall_mlp_infer(cf_ctx *ctx, int npts, double h_wm, double nu);  // network stress of every wall point
 template <typename T> int launch_copy_state(cf_ctx *ctx, int src, int dst);
 template <typename T> int launch_stats(cf_ctx *ctx, int buf, double *d_out);

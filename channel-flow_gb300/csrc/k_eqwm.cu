@@ -369,3 +369,29 @@ int launch_eqwm(cf_ctx *ctx, int b) {
 
 template int launch_eqwm<double>(cf_ctx *, int);
 template int launch_eqwm<float>(cf_ctx *, int);
+
+// The matching-plane velocity |u| of every wall point for state buffer b --
+// the input the wall model hands to the eqwm solve (wallmodel.f90:597-621) --
+// into ules (device, nx * 2 * nzg values, wall-point order (i, wall, k)).
+template <typename T>
+int launch_wm_inputs(cf_ctx *ctx, int b, double *ules) {
+    int nx = ctx->nx, nxg = ctx->nxg, nyg = ctx->nyg, nzg = ctx->nzg;
+    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    k_eq_zinterp_t<T><<<dim3(cdiv(nxg, 128), nzg, 2), 128, 0, ctx->st>>>(W, ctx->prm.jref_eqwm, nxg, nyg, nzg,
+                                                                         ctx->eq_zst, ctx->eq_zw, ctx->wtemp1);
+    EqParams ep = {};
+    ep.ncv = ctx->prm.eqwm_ncv;
+    ep.jref = ctx->prm.jref_eqwm;
+    ep.nx = nx; ep.nxg = nxg; ep.nyg = nyg; ep.nzg = nzg;
+    ep.nu = ctx->prm.nu;
+    ep.h_wm = ctx->hyg[ep.jref];
+    const long npts = (long)nx * nzg * 2;
+    Fld<double> Ud = make_fld<double>(ctx->U[b], nx, nyg);
+    k_wm_ules<<<cdiv(npts, 256), 256, 0, ctx->st>>>(Ud, (const float *)ctx->U[b], sizeof(T) == 4, nx, nx * nyg,
+                                                    ctx->wtemp1, ctx->eq_xst, ctx->eq_xw, ep, ules);
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+template int launch_wm_inputs<double>(cf_ctx *, int, double *);
+template int launch_wm_inputs<float>(cf_ctx *, int, double *);

@@ -6,9 +6,12 @@
 // Parameters (FP32 master copy, 4481 values): W1[64][3], b1[64],
 // W2[64][64] (row = output unit), b2[64], W3[64], b3.  The 64 x 64 layer --
 // the tensor-core layer -- takes BF16 weights and BF16 inputs and
-// accumulates in FP32; layers 1 and 3 run in FP32.  Training back-propagates
-// through the rounding unchanged (straight-through) and updates the FP32
-// master copy with Adam.  Inputs are normalised logs,
+// accumulates in FP32; layers 1 and 3 run in FP32.  Training runs the three
+// products of that layer (forward, input gradient, weight gradient) on the
+// tensor cores with BF16 operands (the layer's output gradient rounded to
+// BF16 where it feeds them), back-propagates through the rounding of the
+// weights and inputs unchanged (straight-through) and updates the FP32
+// master copy with Adam; an FP32-pipe gradient kernel is the cross-check.  Inputs are normalised logs,
 // x = (log(u, h, nu) - mean)/std; the output is the normalised log of the
 // stress over its laminar value, y = (log(tau h / (nu u)) - mean)/std, a
 // bounded smooth function of the matching Reynolds number u h / nu.
@@ -514,6 +517,237 @@ __global__ void __launch_bounds__(TC_M) k_mlp_infer_tc(const float *__restrict__
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_N));
 }
 
+// ---------------------------------------------------------------------------
+// Forward + backward of 128 samples per CTA with the three 64-wide products
+// of layer 2 on the tensor cores (tcgen05.mma kind::f16, BF16 operands, FP32
+// accumulators in tensor memory), the rest on the FP32 pipes:
+//   MMA1  z2  = H1b W2^T        A = H1b [s][k],    B = W2 [nn][k]      -> cols   0..63
+//   MMA2  dh1 = D2b W2          A = D2b [s][nn],   B = W2^T [k][nn]    -> cols  64..127
+//   MMA3  dW2 = D2b^T H1b       A = D2b^T [nn][s] (rows 64..127 zero),
+//                               B = H1b^T [k][s]   (K = 128 samples)   -> cols 128..191
+// H1b = the BF16 layer-1 outputs, D2b = dL/dz2 rounded to BF16 (the products
+// that feed a tensor-core MMA take BF16 operands; the bias and layer-1/3
+// gradients use the FP32 dL/dz2).  Every operand tile is K-major with the
+// 128-byte swizzle: rows of 64 BF16 (128 B), 8-row groups 1024 B apart, a
+// K of 128 as two such tiles.  Thread s owns sample s = tensor-memory lane s.
+// Waits are bounded as in the inference; on expiry the CTA records it and
+// writes no gradient.
+// ---------------------------------------------------------------------------
+struct GradTcSmem {
+    unsigned char a1[128 * 128];      // H1b [s][k]
+    unsigned char a2[128 * 128];      // D2b [s][nn]
+    unsigned char a3[2][128 * 128];   // D2b^T [nn][s], K halves s < 64, s >= 64
+    unsigned char tb3[2][64 * 128];   // H1b^T [k][s], K halves
+    unsigned char b2f[64 * 128];      // W2 [nn][k]
+    unsigned char b2b[64 * 128];      // W2^T [k][nn]
+    float h2[GT][GP];                 // h2 (for the W3 gradient)
+    float d2[GT][GP];                 // FP32 dL/dz2 (b2 gradient)
+    float d1[GT][GP];                 // dL/dz1
+    float x[GT][3];
+    float dy[GT];
+    float w1[MH * 3], b1[MH], b2[MH], w3[MH], b3;
+    double lw[GT / 32];
+    unsigned long long mbar;
+    unsigned int tmem;
+};
+
+// byte offset of element (row r, K index c) in a K-major 128B-swizzled tile
+// of 64-element rows
+__device__ __forceinline__ uint32_t sw128_elem(int r, int c) { return sw128_off(r, c >> 3) + 2u * (uint32_t)(c & 7); }
+
+__device__ __forceinline__ void put_bf16(unsigned char *tile, int r, int c, float v) {
+    *reinterpret_cast<__nv_bfloat16 *>(tile + sw128_elem(r, c)) = __float2bfloat16_rn(v);
+}
+
+// one K-major MMA group: nk slices of K = 16 from A (tiles of 128 rows,
+// 16 KB apart per 64 K) and B (tiles of 64 rows, 8 KB apart per 64 K)
+__device__ __forceinline__ void mma_k(uint32_t tmem_d, uint32_t a0, uint32_t b0, int nk) {
+    for (int kk = 0; kk < nk; kk++) {
+        const uint32_t ah = a0 + (uint32_t)(kk >> 2) * (128u * 128u) + 32u * (kk & 3);
+        const uint32_t bh = b0 + (uint32_t)(kk >> 2) * (64u * 128u) + 32u * (kk & 3);
+        const uint64_t ad = sw128_desc(ah), bd = sw128_desc(bh);
+        const uint32_t acc = kk > 0 ? 1u : 0u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "setp.ne.b32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+            "l"(ad), "l"(bd), "r"(TC_IDESC), "r"(acc));
+    }
+}
+
+__global__ void __launch_bounds__(GT) k_mlp_grad_tc(const float *__restrict__ wm, MlpNorm nm, int n, long base, long pa,
+                                                    long pb, const double *u, const double *h, const double *nu,
+                                                    const double *tau, float inv_batch, float *part, double *lpart,
+                                                    int *err) {
+    extern __shared__ unsigned char tc_raw[];
+    const uint32_t raw = smem_u32(tc_raw);
+    GradTcSmem &S = *reinterpret_cast<GradTcSmem *>(tc_raw + (((raw + 1023u) & ~1023u) - raw));
+    const int s = threadIdx.x, warp = s >> 5;
+    const uint32_t mbar = smem_u32(&S.mbar);
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&S.tmem)),
+                     "r"(256));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (s == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // W2 as B of MMA1 (K-major rows nn) and, transposed, of MMA2 (rows k)
+    for (int q = s; q < MH * 8; q += GT) {
+        const int r = q >> 3, c = q & 7;
+        *reinterpret_cast<uint4 *>(S.b2f + sw128_off(r, c)) = pack8_bf16(wm + O_W2 + MH * r + 8 * c);
+    }
+    for (int q = s; q < MH * MH; q += GT) {
+        const int nn = q / MH, k = q % MH;
+        put_bf16(S.b2b, k, nn, wm[O_W2 + q]);
+    }
+    // rows 64..127 of D2b^T stay zero
+    for (int q = s; q < 2 * 64 * 8; q += GT) {
+        const int hf = q / (64 * 8), r = 64 + (q / 8) % 64, c = q & 7;
+        *reinterpret_cast<uint4 *>(S.a3[hf] + sw128_off(r, c)) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    for (int q = s; q < MH * 3; q += GT) S.w1[q] = wm[O_W1 + q];
+    for (int q = s; q < MH; q += GT) {
+        S.b1[q] = wm[O_B1 + q];
+        S.b2[q] = wm[O_B2 + q];
+        S.w3[q] = wm[O_W3 + q];
+    }
+    if (s == 0) S.b3 = wm[O_B3];
+    // layer 1 of sample s
+    const long i = (long)blockIdx.x * GT + s + base;
+    const long idx = (long)((unsigned long long)(pa * i + pb) % (unsigned long long)n);
+    float x[3];
+    const float llam = mlp_features(nm, u[idx], h[idx], nu[idx], x, nullptr);
+    const float tgt = (logf((float)tau[idx]) - llam - nm.m[3]) * nm.r[3];
+    __syncthreads();  // parameters staged
+#pragma unroll
+    for (int c = 0; c < 8; c++) {
+        float v[8];
+#pragma unroll
+        for (int e = 0; e < 8; e++) {
+            const int k = 8 * c + e;
+            v[e] = tanhf(S.b1[k] + S.w1[3 * k] * x[0] + S.w1[3 * k + 1] * x[1] + S.w1[3 * k + 2] * x[2]);
+        }
+        *reinterpret_cast<uint4 *>(S.a1 + sw128_off(s, c)) = pack8_bf16(v);
+#pragma unroll
+        for (int e = 0; e < 8; e++) put_bf16(S.tb3[s >> 6], 8 * c + e, s & 63, v[e]);
+    }
+    S.x[s][0] = x[0];
+    S.x[s][1] = x[1];
+    S.x[s][2] = x[2];
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = S.tmem;
+    if (s == 0) {
+        mma_k(tmem, smem_u32(S.a1), smem_u32(S.b2f), 4);
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                     : "memory");
+    }
+    bool ok = mbar_wait(mbar, 0u);
+    if (__syncthreads_or(!ok)) {
+        if (s == 0) atomicExch(err, 1);
+        if (!ok) mbar_wait(mbar, 0u);
+    } else {
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+        float z[MH];
+#pragma unroll
+        for (int q = 0; q < MH / 16; q++) tmem_ld16(trow + 16u * q, z + 16 * q);
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        float y = 0.f;
+#pragma unroll
+        for (int nn = 0; nn < MH; nn++) {
+            z[nn] = tanhf(z[nn] + S.b2[nn]);  // h2
+            y = fmaf(S.w3[nn], z[nn], y);
+        }
+        y += S.b3;
+        const float e = y - tgt;
+        const float dy = 2.f * e * inv_batch;
+        S.dy[s] = dy;
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            float v[8];
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                const int nn = 8 * c + q;
+                S.h2[s][nn] = z[nn];
+                v[q] = dy * S.w3[nn] * (1.f - z[nn] * z[nn]);  // dL/dz2
+                S.d2[s][nn] = v[q];
+                put_bf16(S.a3[s >> 6], nn, s & 63, v[q]);
+            }
+            *reinterpret_cast<uint4 *>(S.a2 + sw128_off(s, c)) = pack8_bf16(v);
+        }
+        double l = (double)e * (double)e;
+        for (int o = 16; o > 0; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
+        if ((s & 31) == 0) S.lw[warp] = l;
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (s == 0) {
+            mma_k(tmem + 64u, smem_u32(S.a2), smem_u32(S.b2b), 4);
+            mma_k(tmem + 128u, smem_u32(S.a3[0]), smem_u32(S.tb3[0]), 8);
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                         : "memory");
+        }
+        ok = mbar_wait(mbar, 1u);
+        if (__syncthreads_or(!ok)) {
+            if (s == 0) atomicExch(err, 1);
+            if (!ok) mbar_wait(mbar, 1u);
+        } else {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            float g[MH];
+#pragma unroll
+            for (int q = 0; q < MH / 16; q++) tmem_ld16(trow + 64u + 16u * q, g + 16 * q);
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            // dL/dz1 = (dL/dz2 W2) (1 - h1^2), h1 recomputed in FP32
+#pragma unroll
+            for (int k = 0; k < MH; k++) {
+                const float t1 = tanhf(S.b1[k] + S.w1[3 * k] * x[0] + S.w1[3 * k + 1] * x[1] + S.w1[3 * k + 2] * x[2]);
+                S.d1[s][k] = g[k] * (1.f - t1 * t1);
+            }
+            float *out = part + (long)blockIdx.x * NP;
+            if (warp < 2) {  // lanes 0..63 hold dW2[nn][k], nn = lane
+#pragma unroll
+                for (int q = 0; q < MH / 16; q++) tmem_ld16(trow + 128u + 16u * q, g + 16 * q);
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                for (int k = 0; k < MH; k++) out[O_W2 + MH * s + k] = g[k];
+            }
+            __syncthreads();
+            if (s < MH) {
+                float b2 = 0.f, w3 = 0.f, b1 = 0.f, w10 = 0.f, w11 = 0.f, w12 = 0.f;
+                for (int r = 0; r < GT; r++) {
+                    b2 += S.d2[r][s];
+                    w3 = fmaf(S.dy[r], S.h2[r][s], w3);
+                    const float d = S.d1[r][s];
+                    b1 += d;
+                    w10 = fmaf(d, S.x[r][0], w10);
+                    w11 = fmaf(d, S.x[r][1], w11);
+                    w12 = fmaf(d, S.x[r][2], w12);
+                }
+                out[O_B2 + s] = b2;
+                out[O_W3 + s] = w3;
+                out[O_B1 + s] = b1;
+                out[O_W1 + 3 * s] = w10;
+                out[O_W1 + 3 * s + 1] = w11;
+                out[O_W1 + 3 * s + 2] = w12;
+            } else if (s == MH) {
+                float b3 = 0.f;
+                for (int r = 0; r < GT; r++) b3 += S.dy[r];
+                out[O_B3] = b3;
+                lpart[blockIdx.x] = S.lw[0] + S.lw[1] + S.lw[2] + S.lw[3];
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(256));
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -523,6 +757,7 @@ struct cf_mlp {
     int dev = 0, ncv = 0, sms = 152;
     int *derr = nullptr;  // set by a tensor-core wait that expired
     int test_skip_mma = 0;  // test hook: the inference issues no MMA, so its waits expire
+    int train_tc = 1;       // gradients with layer 2 on the tensor cores (0: FP32 pipes)
     double stretch = 0.0;
     float *w = nullptr, *m1 = nullptr, *m2 = nullptr, *part = nullptr;
     double *lpart = nullptr, *unit = nullptr;
@@ -626,6 +861,8 @@ extern "C" int cf_mlp_create(int seed, int ncv, double stretch, cf_mlp **out) {
     if (e == cudaSuccess) e = cudaMemset(m->m1, 0, NP * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(m->m2, 0, NP * sizeof(float));
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradSmem));
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_mlp_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GradTcSmem) + 1024);
     if (e == cudaSuccess) e = cudaMalloc(&m->derr, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(m->derr, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->dev);
@@ -694,6 +931,23 @@ static int ensure_part(cf_mlp *m, int nblk) {
 
 static long gcdl(long a, long b) { return b == 0 ? a : gcdl(b, a % b); }
 
+// per-block partial gradients of nblk tiles of 128 samples
+static void launch_grad(cf_mlp *m, int nblk, const MlpNorm &nm, int n, long base, long pa, long pb, const double *u,
+                        const double *h, const double *nu, const double *tau, float inv_batch, cudaStream_t st) {
+    if (m->train_tc)
+        k_mlp_grad_tc<<<nblk, GT, sizeof(GradTcSmem) + 1024, st>>>(m->w, nm, n, base, pa, pb, u, h, nu, tau, inv_batch,
+                                                                    m->part, m->lpart, m->derr);
+    else
+        k_mlp_grad<<<nblk, GT, sizeof(GradSmem), st>>>(m->w, nm, n, base, pa, pb, u, h, nu, tau, inv_batch, m->part,
+                                                         m->lpart);
+}
+
+extern "C" int cf_mlp_set_train_tensor_cores(cf_mlp *m, int on) {
+    if (!m) return mlp_fail(m, CF_ERR_INVALID, "cf_mlp_set_train_tensor_cores: null network");
+    m->train_tc = on ? 1 : 0;
+    return CF_OK;
+}
+
 extern "C" int cf_mlp_gradient(cf_mlp *m, int n, const double *u, const double *h, const double *nu,
                                const double *tau, double *grad, double *loss, void *stream) {
     if (!m || n < GT || n % GT || !u || !h || !nu || !tau || !grad)
@@ -701,8 +955,7 @@ extern "C" int cf_mlp_gradient(cf_mlp *m, int n, const double *u, const double *
     const int nblk = n / GT;
     if (int rc = ensure_part(m, nblk)) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    k_mlp_grad<<<nblk, GT, sizeof(GradSmem), st>>>(m->w, norm_of(m), n, 0, 1, 0, u, h, nu, tau, 1.f / n, m->part,
-                                                     m->lpart);
+    launch_grad(m, nblk, norm_of(m), n, 0, 1, 0, u, h, nu, tau, 1.f / n, st);
     k_mlp_adam<<<cdiv(NP, 256), 256, 0, st>>>(m->w, m->m1, m->m2, m->part, nblk, grad, 0.f, 0.f, 0.f, 0.f, 1.f, 1.f,
                                                nullptr, nullptr);
     MLP_CUDA(cudaGetLastError());
@@ -747,8 +1000,7 @@ extern "C" int cf_mlp_train(cf_mlp *m, int n, const double *u, const double *h, 
             const double lr_t = lr * (0.01 + 0.99 * 0.5 * (1.0 + std::cos(3.141592653589793 * (double)k / (double)total)));
             m->step++;
             const float bc1 = 1.f - std::pow(b1, (float)m->step), bc2 = 1.f - std::pow(b2, (float)m->step);
-            k_mlp_grad<<<nblk, GT, sizeof(GradSmem), st>>>(m->w, nm, n, (long)bt * batch, pa, pb, u, h, nu, tau,
-                                                             1.f / batch, m->part, m->lpart);
+            launch_grad(m, nblk, nm, n, (long)bt * batch, pa, pb, u, h, nu, tau, 1.f / batch, st);
             k_mlp_adam<<<cdiv(NP, 256), 256, 0, st>>>(m->w, m->m1, m->m2, m->part, nblk, nullptr, (float)lr_t, b1,
                                                         b2, eps, bc1, bc2, m->lpart, lacc);
         }

@@ -242,6 +242,15 @@ Module channel_gpu
        Real(c_double)     :: out(*)
      End Function cf_download_avg_nu_t
 
+     ! u_les: device array (Type(c_ptr)) of cap doubles, or c_null_ptr to query npts
+     Integer(c_int) Function cf_wall_model_inputs(ctx, u_les, cap, npts, h_wm, nu) Bind(C, name="cf_wall_model_inputs")
+       Import :: c_int, c_long, c_double, c_ptr
+       Type(c_ptr), Value     :: ctx, u_les
+       Integer(c_long), Value :: cap
+       Integer(c_long)        :: npts
+       Real(c_double)         :: h_wm, nu
+     End Function cf_wall_model_inputs
+
      Integer(c_int) Function cf_get_eqwm_counters(ctx, n_nan, n_iter) Bind(C, name="cf_get_eqwm_counters")
        Import :: c_int, c_ptr
        Type(c_ptr), Value :: ctx
@@ -418,6 +427,12 @@ Module channel_gpu
        Real(c_double)        :: loss
        Type(c_ptr), Value    :: stream
      End Function cf_mlp_gradient
+
+     Integer(c_int) Function cf_mlp_set_train_tensor_cores(m, on) Bind(C, name="cf_mlp_set_train_tensor_cores")
+       Import :: c_int, c_ptr
+       Type(c_ptr), Value    :: m
+       Integer(c_int), Value :: on
+     End Function cf_mlp_set_train_tensor_cores
 
      Integer(c_int) Function cf_mlp_predict(m, n, u, h, nu, tau, inside, use_tensor_cores, stream) &
           Bind(C, name="cf_mlp_predict")

@@ -139,6 +139,14 @@ int cf_download_rhs(cf_ctx *ctx, int comp, int slot, double *out);
 int cf_download_avg_nu_t(cf_ctx *ctx, double *out);
 /* eqwm counters of the last wall-model call (wallmodel.f90:623-653). */
 int cf_get_eqwm_counters(cf_ctx *ctx, int *n_nan, int *n_iter);
+/* The inputs the equilibrium wall model hands to its ODE solve for the
+ * current fields (wallmodel.f90:597-621): *npts = nx * 2 * (nz+1) wall
+ * points, u_les (device array of cap >= *npts doubles, wall-point order
+ * (i, wall, k); may be NULL to query *npts) the matching-plane velocity
+ * magnitude of each, *h_wm the matching height yg(jref_eqwm), *nu the
+ * viscosity (either may be NULL).  iwall_model 3 only.  Used to draw the
+ * learned wall stress's training samples from the solver's own runs. */
+int cf_wall_model_inputs(cf_ctx *ctx, double *u_les, long cap, long *npts, double *h_wm, double *nu);
 
 /* ---- fast path ------------------------------------------------------- */
 /* compute_dt followed by compute_time_step_RK3 (time_integration.f90:89-173,
@@ -249,6 +257,12 @@ int cf_mlp_train(cf_mlp *m, int n, const double *u, const double *h, const doubl
  * the current parameters, into grad (CF_MLP_NPARAM doubles, device). */
 int cf_mlp_gradient(cf_mlp *m, int n, const double *u, const double *h, const double *nu, const double *tau,
                     double *grad, double *loss, void *stream);
+/* on = 1 (default): cf_mlp_train and cf_mlp_gradient run layer 2's three
+ * products (forward, input gradient, weight gradient) on the tensor cores,
+ * BF16 operands with FP32 accumulation (the output gradient of layer 2
+ * rounded to BF16 where it feeds them); 0: the FP32-pipe gradient kernel
+ * (layer-2 output gradient in FP32). */
+int cf_mlp_set_train_tensor_cores(cf_mlp *m, int on);
 /* tau = network(u, h, nu); use_tensor_cores 0 runs the same arithmetic on
  * the FP32 pipes (the cross-check).  inside (may be NULL): 1 where all three
  * inputs lie within the training envelope. */

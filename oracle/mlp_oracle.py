@@ -64,19 +64,23 @@ def forward(p, x):
     return dict(x=x, h1=h1, h1b=h1b, h2=h2, y=y, W2b=W2b, W3b=W3b)
 
 
-def gradient(p, x, t):
+def gradient(p, x, t, delta_bf16=False):
     """Gradient of mean((y - t)^2) over the batch with respect to the FP32
-    parameters (the rounding to BF16 passes gradients straight through)."""
+    parameters (the rounding to BF16 passes gradients straight through).
+    delta_bf16: layer 2's output gradient enters the input- and
+    weight-gradient products rounded to BF16 (their operands on the tensor
+    cores); its bias gradient keeps the FP32 values."""
     f = forward(p, x)
     B = x.shape[0]
     dy = (2.0 * (f["y"] - t) / B).astype(np.float32)
     g = np.zeros(NPARAM, dtype=np.float64)
     g[O_W3:O_B3] = dy @ f["h2"]
     g[O_B3] = dy.sum()
-    dz2 = dy[:, None] * f["W3b"][None, :] * (1.0 - f["h2"] ** 2)
-    g[O_W2:O_B2] = (dz2.T @ f["h1b"]).ravel()
+    dz2 = (dy[:, None] * f["W3b"][None, :] * (1.0 - f["h2"] ** 2)).astype(np.float32)
+    dz2m = bf16(dz2) if delta_bf16 else dz2
+    g[O_W2:O_B2] = (dz2m.astype(np.float64).T @ f["h1b"].astype(np.float64)).ravel()
     g[O_B2:O_W3] = dz2.sum(axis=0)
-    dh1 = dz2 @ f["W2b"]
+    dh1 = dz2m @ f["W2b"]
     dz1 = dh1 * (1.0 - f["h1"] ** 2)
     g[O_W1:O_B1] = (dz1.T @ x).ravel()
     g[O_B1:O_W2] = dz1.sum(axis=0)

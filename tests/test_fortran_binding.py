@@ -66,8 +66,8 @@ def c_prototypes():
     return out
 
 
-F_KIND = {"integer(c_int)": "int", "real(c_double)": "double", "real(c_float)": "float", "type(c_ptr)": "ptr",
-          "character(kind=c_char)": "char", "type(cf_params)": "cf_params"}
+F_KIND = {"integer(c_int)": "int", "integer(c_long)": "long", "real(c_double)": "double", "real(c_float)": "float",
+          "type(c_ptr)": "ptr", "character(kind=c_char)": "char", "type(cf_params)": "cf_params"}
 
 
 def fortran_interfaces():

@@ -89,14 +89,23 @@ def test_forward_and_gradient_match_oracle():
     d = np.abs(got / want - 1)
     # an ulp of difference before a BF16 rounding can flip one activation
     assert np.median(d) < 1e-6 and np.mean(d > 1e-5) < 0.02 and d.max() < 2e-3, (np.median(d), d.max())
-    # gradient over the batch
-    g, loss = net.gradient(u, h, nu, tau)
+    # gradient over the batch: layer 2 on the tensor cores (BF16 output
+    # gradient in its products), and on the FP32 pipes
     x = mo.features(un, hn, nn_, norm)
     t = mo.target(un, hn, nn_, tn, norm)
-    go, lo = mo.gradient(p, x, t)
-    g = g.cpu().numpy()
-    assert abs(loss - lo) <= 1e-4 * lo
-    assert np.max(np.abs(g - go)) <= 1e-4 * np.max(np.abs(go)), np.max(np.abs(g - go)) / np.max(np.abs(go))
+    for tc in (True, False):
+        net.train_tensor_cores(tc)
+        g, loss = net.gradient(u, h, nu, tau)
+        go, lo = mo.gradient(p, x, t, delta_bf16=tc)
+        g = g.cpu().numpy()
+        assert abs(loss - lo) <= 1e-4 * lo, (tc, loss, lo)
+        err = np.max(np.abs(g - go)) / np.max(np.abs(go))
+        print("tensor cores" if tc else "FP32 pipes", "gradient error", err)
+        assert err <= 1e-4, (tc, err)
+        # layer 2's weight gradient on its own (the tensor-core product)
+        gw, gwo = g[mo.O_W2:mo.O_B2], go[mo.O_W2:mo.O_B2]
+        assert np.max(np.abs(gw - gwo)) <= 1e-4 * np.max(np.abs(gwo)), tc
+    net.train_tensor_cores(True)
 
 
 @pytest.mark.gpu
@@ -271,3 +280,76 @@ def test_expired_tensor_core_wait_falls_back_to_eqwm():
     assert log["calls"] == 1 and log["served"] == 0 and log["fallback"] == 18 * 19 * 2
     for n in ("U", "V", "W", "P", "nu_t"):
         assert np.array_equal(out[True][n], out[False][n]), n
+
+
+@pytest.mark.gpu
+def test_wall_model_inputs_are_the_solver_inputs():
+    """cf_wall_model_inputs returns what the equilibrium wall model feeds to
+    its eqwm solve: solving eqwm on those inputs (batched, cold start)
+    reproduces the stress the wall-model call stored for every wall point."""
+    import torch
+    import channelflow as cf
+    from channelflow import wallmlp
+    from conftest import channel_case
+    case = channel_case(34, 33, 34, stretch=0.0, wall=3, retau=2000.0, profile="plug", jref=3, ncv=30)
+    ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_FP64, **case["prm"])
+    ch.upload(case["U"], case["V"], case["W"])
+    ch.apply_boundary_conditions()
+    ch.compute_eddy_viscosity()
+    ch.compute_wall_model()
+    tau_wm = ch.download_wall()["tau_eqwm_initial"]
+    u, h, nu = wallmlp.wall_model_inputs(ch)
+    assert u.numel() == 34 * 2 * 35 and h == pytest.approx(case["y"][2] * 0.5 + case["y"][1] * 0.5, rel=1e-12)
+    T = lambda v: torch.full_like(u, v)
+    tau = wallmlp.eqwm_solve_batch(u, T(h), T(nu), ncv=30, stretch=1.10, tau_init=1e-3).cpu().numpy()
+    want = np.ravel(tau_wm, order="F")
+    assert np.abs(tau / want - 1).max() < 1e-5, np.abs(tau / want - 1).max()
+    ch.close()
+
+
+@pytest.mark.gpu
+def test_harvested_solver_samples():
+    """Samples drawn from the solver's own wall-modelled runs across the
+    operating range: finite, positive, labelled by eqwm, and mixed into a
+    training set in the requested share."""
+    import torch
+    from channelflow import wallmlp
+    dev = torch.device("cuda:0")
+    runs = ((500.0, 4), (10000.0, 5))
+    u, h, nu, steps = wallmlp.harvest_inputs(20000, device=dev, runs=runs, warm=50, every=10)
+    assert u.numel() == 20000 and steps >= 2 * 60
+    assert torch.isfinite(u).all() and (u > 0).all()
+    assert len(torch.unique(h)) == 2 and len(torch.unique(nu)) == 2
+    (tu, th, tn, tt), kept = wallmlp.training_set_mixed(1 << 14, solver_fraction=0.5, device=dev, seed=3)
+    assert kept > 0.45 * (1 << 14) and tu.numel() > 0.9 * (1 << 14)
+    assert torch.isfinite(tt).all() and (tt > 0).all()
+
+
+@pytest.mark.gpu
+def test_tensor_core_training_against_fp32_pipes():
+    """The same two epochs trained with layer 2 on the tensor cores and on the
+    FP32 pipes from the same start: both reduce the loss alike; the time per
+    epoch of each is printed (CUDA events)."""
+    import torch
+    from channelflow import wallmlp
+    dev = torch.device("cuda:0")
+    u, h, nu, tau = _data(1 << 17, 51, dev)
+    out = {}
+    for tc in (True, False):
+        net = wallmlp.WallMLP(seed=9)
+        net.fit_normalisation(u, h, nu, tau)
+        net.train_tensor_cores(tc)
+        net.train(u, h, nu, tau, epochs=1, batch=4096, lr=3e-3, seed=0)  # warm-up
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        loss = net.train(u, h, nu, tau, epochs=2, batch=4096, lr=3e-3, seed=1)
+        e1.record()
+        e1.synchronize()
+        out[tc] = (loss, e0.elapsed_time(e1) / 2)
+        net.close()
+    print("ms per epoch of 2^17 samples, batch 4096: tensor cores %.3f, FP32 pipes %.3f" % (out[True][1], out[False][1]),
+          "losses", out[True][0], out[False][0])
+    for tc in (True, False):
+        assert out[tc][0][-1] < out[tc][0][0]
+    assert abs(out[True][0][-1] / out[False][0][-1] - 1) < 0.2
