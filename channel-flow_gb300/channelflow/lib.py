@@ -448,14 +448,17 @@ class Channel:
 class Ensemble:
     """Independent channels advanced together: one CUDA graph per ensemble
     step with a branch per member (cf_ensemble_*), the tridiagonal systems of
-    all members solved by one FP64 launch per substep (batched_tri).  The
-    members stay usable as Channel objects between steps."""
+    all members solved by one FP64 launch per substep (batched_tri), the fused
+    dynamic Smagorinsky passes and fused right-hand sides of all members as
+    one launch each per substep (batched_stencils).  The members stay usable
+    as Channel objects between steps."""
 
-    def __init__(self, members, batched_tri: bool = True):
+    def __init__(self, members, batched_tri: bool = True, batched_stencils: bool = False):
         self.L = load()
         L = self.L
         vp = C.c_void_p
         L.cf_ensemble_set_batched_tri.argtypes = [vp, C.c_int]
+        L.cf_ensemble_set_batched_stencils.argtypes = [vp, C.c_int]
         L.cf_ensemble_create.argtypes = [C.c_int, C.POINTER(vp), C.POINTER(vp)]
         L.cf_ensemble_destroy.argtypes = [vp]
         L.cf_ensemble_step.argtypes = [vp, C.c_int, C.c_int]
@@ -470,6 +473,21 @@ class Ensemble:
             raise CfError(L.cf_last_error(None).decode() or f"cf_ensemble_create failed ({rc})")
         self.h = h
         L.cf_ensemble_set_batched_tri(h, 1 if batched_tri else 0)
+        if L.cf_ensemble_set_batched_stencils(h, 1 if batched_stencils else 0) != 0:
+            raise CfError(L.cf_last_error(None).decode())
+
+    def autotune(self, steps: int = 3) -> dict:
+        """cf_ensemble_autotune: times whole ensemble steps with every kernel
+        in the members' branches and with the batched stencil launches (three
+        z-chunk plans) and keeps the fastest; the ensemble advances."""
+        self.L.cf_ensemble_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+        rep = np.zeros(4)
+        ch = C.c_int()
+        rc = self.L.cf_ensemble_autotune(self.h, steps, _dp(rep), C.byref(ch))
+        if rc != 0:
+            raise CfError(self.L.cf_last_error(None).decode() or f"cf_ensemble_autotune failed ({rc})")
+        names = ["branches", "batched, member plans", "batched, one z chunk", "batched, two z chunks"]
+        return dict(choice=names[ch.value], ms_per_step=dict(zip(names, rep.tolist())))
 
     def step(self, nsteps: int = 1, sync: bool = True):
         rc = self.L.cf_ensemble_step(self.h, nsteps, 1 if sync else 0)

@@ -1108,6 +1108,90 @@ static int step_seg(cf_ctx *ctx, int seg, bool tri) {
 
 static int step_eager(cf_ctx *ctx) { return DISPATCH(enqueue_step<double>(ctx), enqueue_step<float>(ctx)); }
 
+// ---------------------------------------------------------------------------
+// The same step cut for an ensemble whose fused dynamic Smagorinsky passes
+// and fused right-hand sides run as one launch over all members.  Per
+// substep s, with buffers as in enqueue_seg (X the starting state,
+// a = X+1, b = X+2 mod 3):
+//   pre(s):  s = 1: dt; s > 1: inverse transforms of substep s-1's
+//            projection and the boundary conditions; the eddy viscosity of a
+//            member that does not take the batched pass (and at s = 1 the
+//            wall model)
+//   [batched fused DSM pass of the members that take it -- twice at s = 1
+//    when sgs_recompute -- and batched fused right-hand sides + RK update]
+//   post(s): forward transforms of substep s's projection (with the
+//            member's own tridiagonal solve unless the ensemble solves them)
+//   fin:     inverse transforms of substep 3's projection, boundary
+//            conditions, mass-flow forcing.
+// Each member's launches are those of enqueue_seg in the same order.
+// ---------------------------------------------------------------------------
+static bool dsm_batchable(const cf_ctx *c) {
+    return c->prm.LES_model == 2 && c->use_fused_dsm && c->prm.iwall_model == 0 && c->state_periodic && c->use_rhs3;
+}
+
+static void ens_bufs(const cf_ctx *c, int s, int *src, int *dst) {
+    const int X = c->seg_base, a = (X + 1) % 3, b = (X + 2) % 3;
+    *src = s == 1 ? X : (s == 2 ? a : b);
+    *dst = s == 1 ? a : (s == 2 ? b : a);
+}
+
+template <typename T>
+static int ens_pre_t(cf_ctx *ctx, int s, bool batched_dsm) {
+    const bool canon = true;
+    if (s == 1) {
+        const int X = ctx->cur;
+        ctx->seg_base = X;
+        ctx->old = X;
+        TRY(launch_dt<T>(ctx, X, true));
+        if (!batched_dsm) {
+            TRY(eddy(ctx, X));
+            if (ctx->prm.iwall_model == 3) {
+                TRY(wall_model(ctx, X));
+                if (ctx->prm.sgs_recompute) TRY(eddy(ctx, X));
+            } else if (ctx->prm.sgs_recompute) {
+                TRY(eddy(ctx, X));
+            }
+        }
+        return 0;
+    }
+    const int X = ctx->seg_base, a = (X + 1) % 3, b = (X + 2) % 3;
+    const int p = s == 2 ? a : b;  // the state the previous substep's projection acts on
+    TRY(launch_projection<T>(ctx, p, s == 2, false, canon, POISSON_INV));
+    TRY(launch_bc<T>(ctx, p, false));
+    if (!batched_dsm) TRY(eddy(ctx, p));
+    return 0;
+}
+
+template <typename T>
+static int ens_post_t(cf_ctx *ctx, int s, bool tri) {
+    int src, dst;
+    ens_bufs(ctx, s, &src, &dst);
+    ctx->cur = dst;
+    return launch_projection<T>(ctx, dst, s == 1, s == 3, true, POISSON_FWD | (tri ? POISSON_TRI : 0));
+}
+
+template <typename T>
+static int ens_fin_t(cf_ctx *ctx) {
+    const int a = (ctx->seg_base + 1) % 3;
+    TRY(launch_projection<T>(ctx, a, false, true, true, POISSON_INV));
+    TRY(launch_bc<T>(ctx, a));
+    const bool g = ctx->prm.iwall_model == 0;
+    if (ctx->prm.x_mass_cte == 1 || ctx->prm.x_mass_cte == 2) {
+        TRY(launch_mass_flow<T>(ctx, a, ctx->prm.x_mass_cte, g));
+        if (!g) TRY(launch_bc<T>(ctx, a));
+    }
+    if (ctx->prm.y_mass_cte == 1) {
+        TRY(launch_mass_flow<T>(ctx, a, 3, g));
+        if (!g) TRY(launch_bc<T>(ctx, a));
+    }
+    ctx->old = a;
+    return 0;
+}
+
+static int ens_pre(cf_ctx *ctx, int s, bool bd) { return DISPATCH(ens_pre_t<double>(ctx, s, bd), ens_pre_t<float>(ctx, s, bd)); }
+static int ens_post(cf_ctx *ctx, int s, bool tri) { return DISPATCH(ens_post_t<double>(ctx, s, tri), ens_post_t<float>(ctx, s, tri)); }
+static int ens_fin(cf_ctx *ctx) { return DISPATCH(ens_fin_t<double>(ctx), ens_fin_t<float>(ctx)); }
+
 extern "C" int cf_time_step_rk3(cf_ctx *ctx, int nsteps, int sync) {
     if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
     CF_CUDA(cudaSetDevice(ctx->dev));
@@ -1379,6 +1463,7 @@ struct cf_ensemble {
     std::vector<cf_ctx *> m;
     int dev = 0;
     bool batched_tri = true;          // one FP64 launch for every member's tridiagonal systems
+    bool batched_stencils = false;    // one launch for every member's fused DSM pass and fused RHS
     TriMember *dtab = nullptr;        // device table of the members' systems
     double2 *scratch = nullptr;       // FP64 elimination scratch of every member
     long total_modes = 0;             // blocks of the batched launch
@@ -1416,6 +1501,7 @@ extern "C" int cf_ensemble_create(int n, cf_ctx *const *members, cf_ensemble **o
     }
     e = new cf_ensemble();
     e->m.assign(members, members + n);
+    e->batched_stencils = false;  // cf_ensemble_autotune or cf_ensemble_set_batched_stencils turn it on
     e->dev = members[0]->dev;
     cudaSetDevice(e->dev);
     cudaError_t ce = cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking);
@@ -1459,6 +1545,91 @@ extern "C" int cf_ensemble_set_batched_tri(cf_ensemble *e, int on) {
     }
     e->batched_tri = on != 0;
     return CF_OK;
+}
+
+extern "C" int cf_ensemble_set_batched_stencils(cf_ensemble *e, int on) {
+    if (!e) return ens_fail(e, CF_ERR_INVALID, "null ensemble");
+    if (on && e->m.size() > (size_t)CF_ENS_MAXM)
+        return ens_fail(e, CF_ERR_INVALID, "batched stencil launches take at most 32 members");
+    if (e->batched_stencils != (on != 0)) {
+        ENS_CUDA(cudaStreamSynchronize(e->st));
+        for (auto &kv : e->graphs) cudaGraphExecDestroy(kv.second.first);
+        e->graphs.clear();
+    }
+    e->batched_stencils = on != 0;
+    return CF_OK;
+}
+
+// Captures one ensemble step with the batched stencil launches into the
+// ensemble's stream (see ens_pre_t); *extra counts the batched launches.
+static int capture_batched_step(cf_ensemble *e, int *extra) {
+    const int n = (int)e->m.size();
+    cudaError_t ce = cudaSuccess;
+    int rc = 0;
+    *extra = 0;
+    // the members in a fork / join around each per-member phase
+    auto branches = [&](auto fn) {
+        ce = cudaEventRecord(e->fork, e->st);
+        for (int q = 0; q < n && !rc && ce == cudaSuccess; q++) {
+            cf_ctx *c = e->m[q];
+            ce = cudaStreamWaitEvent(c->st, e->fork, 0);
+            if (ce == cudaSuccess) rc = fn(q, c);
+            if (!rc && ce == cudaSuccess) ce = cudaEventRecord(e->join[q], c->st);
+            if (!rc && ce == cudaSuccess) ce = cudaStreamWaitEvent(e->st, e->join[q], 0);
+        }
+        return !rc && ce == cudaSuccess;
+    };
+    std::vector<char> bd(n);
+    for (int q = 0; q < n; q++) bd[q] = dsm_batchable(e->m[q]);
+    for (int s = 1; s <= 3; s++) {
+        if (!branches([&](int q, cf_ctx *c) { return ens_pre(c, s, bd[q] != 0); })) break;
+        // batched passes, per precision
+        for (int esz : {4, 8}) {
+            std::vector<cf_ctx *> dm, dm2, rm;
+            std::vector<int> db, db2, rs, rd;
+            for (int q = 0; q < n; q++) {
+                cf_ctx *c = e->m[q];
+                if (c->esz != esz) continue;
+                int src, dst;
+                ens_bufs(c, s, &src, &dst);
+                if (bd[q]) {
+                    dm.push_back(c);
+                    db.push_back(src);
+                    if (s == 1 && c->prm.sgs_recompute) {
+                        dm2.push_back(c);
+                        db2.push_back(src);
+                    }
+                }
+                rm.push_back(c);
+                rs.push_back(src);
+                rd.push_back(dst);
+            }
+            for (int pass = 0; pass < 2 && !rc; pass++) {
+                std::vector<cf_ctx *> &mm = pass ? dm2 : dm;
+                std::vector<int> &bb = pass ? db2 : db;
+                if (mm.empty()) continue;
+                rc = esz == 8 ? launch_dsm_batch<double>(e->st, mm.data(), bb.data(), (int)mm.size())
+                              : launch_dsm_batch<float>(e->st, mm.data(), bb.data(), (int)mm.size());
+                *extra += 2;
+            }
+            if (!rc && !rm.empty()) {
+                rc = esz == 8 ? launch_rhs3_batch<double>(e->st, rm.data(), s, rs.data(), rd.data(), (int)rm.size())
+                              : launch_rhs3_batch<float>(e->st, rm.data(), s, rs.data(), rd.data(), (int)rm.size());
+                *extra += 1;
+            }
+        }
+        if (rc) break;
+        if (!branches([&](int, cf_ctx *c) { return ens_post(c, s, !e->batched_tri); })) break;
+        if (e->batched_tri) {
+            rc = launch_tri_batch(e->st, e->dtab, n, e->total_modes);
+            *extra += 1;
+        }
+        if (rc) break;
+    }
+    if (!rc && ce == cudaSuccess) branches([&](int, cf_ctx *c) { return ens_fin(c); });
+    if (rc) return rc;
+    if (ce != cudaSuccess) return ens_fail(e, CF_ERR_CUDA, std::string("ensemble capture: ") + cudaGetErrorString(ce));
+    return 0;
 }
 
 extern "C" int cf_ensemble_destroy(cf_ensemble *e) {
@@ -1512,7 +1683,8 @@ extern "C" int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync) {
             cudaError_t ce = cudaSuccess;
             // with the batched solve the members' steps run in four segments,
             // the tridiagonal systems of all of them solved between segments
-            const int nseg = e->batched_tri ? 4 : 1;
+            const int nseg = e->batched_stencils ? 0 : (e->batched_tri ? 4 : 1);
+            if (e->batched_stencils) rc = capture_batched_step(e, &total_tri);
             for (int seg = 0; seg < nseg && !rc && ce == cudaSuccess; seg++) {
                 ce = cudaEventRecord(e->fork, e->st);
                 for (int q = 0; q < n && !rc && ce == cudaSuccess; q++) {
@@ -1560,6 +1732,77 @@ extern "C" int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync) {
     ENS_CUDA(cudaEventRecord(e->fork, e->st));
     for (cf_ctx *c : e->m) ENS_CUDA(cudaStreamWaitEvent(c->st, e->fork, 0));
     if (sync) ENS_CUDA(cudaStreamSynchronize(e->st));
+    return CF_OK;
+}
+
+// Empirical choice of how an ensemble runs its stencil passes: the whole
+// ensemble step is timed (CUDA events, `steps` steps after one that captures
+// its graph) for every member kernel in its branch with each member's own
+// z-chunk plan, and for the batched DSM / right-hand-side launches with the
+// members' plans, with one z chunk per member and with two; the fastest is
+// kept.  The ensemble advances 4 x (steps + 1) steps.  report (4 doubles,
+// may be NULL): ms per step of the four candidates in that order; *choice
+// (may be NULL): the index kept.
+extern "C" int cf_ensemble_autotune(cf_ensemble *e, int steps, double *report, int *choice) {
+    if (!e || steps < 1) return ens_fail(e, CF_ERR_INVALID, "cf_ensemble_autotune: bad argument");
+    ENS_CUDA(cudaSetDevice(e->dev));
+    const int n = (int)e->m.size();
+    std::vector<int> kc0(n), nkc0(n);
+    for (int q = 0; q < n; q++) {
+        kc0[q] = e->m[q]->dsm_kc;
+        nkc0[q] = e->m[q]->rhs_nkc;
+    }
+    auto apply = [&](int cand) {
+        for (int q = 0; q < n; q++) {
+            cf_ctx *c = e->m[q];
+            const int lo_rhs = cdiv(c->nzp, RHS_ZMAX_HOST), lo_dsm = cdiv(c->nzp, DSM_ZMAX_HOST);
+            if (cand <= 1) {
+                c->dsm_kc = kc0[q];
+                c->rhs_nkc = nkc0[q];
+            } else {
+                const int parts = cand == 2 ? 1 : 2;
+                c->dsm_kc = cdiv(c->nzp, std::max(parts, lo_dsm));
+                c->rhs_nkc = std::max(parts, lo_rhs);
+            }
+            for (auto &g : c->graphs)
+                if (g) {
+                    cudaGraphExecDestroy(g);
+                    g = nullptr;
+                }
+        }
+        for (auto &kv : e->graphs) cudaGraphExecDestroy(kv.second.first);
+        e->graphs.clear();
+        e->batched_stencils = cand >= 1 && n <= CF_ENS_MAXM;
+    };
+    cudaEvent_t a, b;
+    ENS_CUDA(cudaEventCreate(&a));
+    ENS_CUDA(cudaEventCreate(&b));
+    double ms[4] = {0, 0, 0, 0};
+    int best = 0;
+    for (int cand = 0; cand < 4; cand++) {
+        apply(cand);
+        int rc = cf_ensemble_step(e, 1, 1);
+        float t = 0.f;
+        if (!rc) {
+            cudaEventRecord(a, e->st);
+            rc = cf_ensemble_step(e, steps, 0);
+            cudaEventRecord(b, e->st);
+            cudaEventSynchronize(b);
+            cudaEventElapsedTime(&t, a, b);
+        }
+        if (rc) {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            return rc;
+        }
+        ms[cand] = t / steps;
+        if (ms[cand] < ms[best]) best = cand;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    apply(best);
+    if (report) std::copy(ms, ms + 4, report);
+    if (choice) *choice = best;
     return CF_OK;
 }
 

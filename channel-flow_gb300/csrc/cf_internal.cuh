@@ -276,6 +276,11 @@ template <typename T> int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst
 template <typename T> int launch_rk_update(cf_ctx *ctx, int s);            // from stored F slots
 template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // eddy viscosity
 template <typename T> int launch_dsm_fused(cf_ctx *ctx, int buf);          // fused pass (periodic state)
+constexpr int CF_ENS_MAXM = 32;  // channels per batched ensemble launch at most
+// fused pass + <LM>/<MM> rows of n channels in two launches (ensembles)
+template <typename T> int launch_dsm_batch(cudaStream_t st, cf_ctx *const *m, const int *buf, int n);
+// fused right-hand sides + RK update of substep s of n channels in one launch
+template <typename T> int launch_rhs3_batch(cudaStream_t st, cf_ctx *const *m, int s, const int *src, const int *dst, int n);
 template <typename T> int launch_nut_zero(cf_ctx *ctx);
 template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut if held lazily
 // canon: project the canonical cells only (the boundary conditions that
@@ -304,6 +309,7 @@ void amd_plan(int esz, int nxp, int nym, int nzp, int sms, int *nkc, int *nparts
 int launch_avg_nu_t_flush(cf_ctx *ctx);  // AMD plane means of the last pass, if not formed yet
 int amd_partials_for(cf_ctx *ctx, int nkc);  // plane partials per row of an AMD pass with nkc z chunks
 constexpr int DSM_ZMAX_HOST = 256;           // planes per z chunk of the fused DSM pass at most
+constexpr int RHS_ZMAX_HOST = 256;           // planes per z chunk of the fused RHS at most
 template <typename T> int launch_div_check(cf_ctx *ctx, int buf, double *d_out);
 template <typename T> int launch_mass_flow(cf_ctx *ctx, int buf, int mode, bool ghosts = false);  // 1: x mass flow, 2: centre-line, 3: y
 template <typename T> int launch_mass_value(cf_ctx *ctx, int buf, int mode); // correction into ds->lmax[2] only

@@ -2,6 +2,8 @@
 // mass-flow forcing, time-step and divergence reductions.
 #include <algorithm>
 
+#include <type_traits>
+
 #include "cf_internal.cuh"
 
 // ---------------------------------------------------------------------------
@@ -505,23 +507,44 @@ struct NutSrc {
 };
 
 // planes per z chunk of the fused RHS (its z spacings sit in shared memory)
-constexpr int RHS_ZMAX = 256;
+constexpr int RHS_ZMAX = RHS_ZMAX_HOST;
 // resident blocks per SM the fused RHS is compiled for: two (128 registers).
 // With u, v and w computed before any store, the shared-memory reads common
 // to them are issued once but more values stay live: at three blocks (80
 // registers) the FP32 kernel spills and runs 25 % slower.
 template <typename T> struct RhsMinB { static constexpr int v = 2; };
 
+// Everything one launch of the fused right-hand side needs for one channel
+// (the grid of blocks is ntx x nty x nkc).
+template <typename T>
+struct Rhs3Args {
+    GeoT<T> g;
+    RcpT<T> rc;
+    Fld<T> U, V, W, nt;
+    NutSrc<T> ns;
+    const DevScal *ds;
+    T nu, Om, ca, cb;
+    int rot, s, kc_len, ilim, klim, ntx, nty, nkc;
+    Trio<T> out, F1, Uo, Uolo, Unlo;
+};
+
+// The tile (bx, by, bz) of one channel: a block of the single-channel launch
+// or of the ensemble launch (k_rhs3_batch below).
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, Fld<T> nt,
-                                                     NutSrc<T> ns, const DevScal *ds, T nu, T Om, int rot, Trio<T> out,
-                                                     Trio<T> F1, Trio<T> Uo, Trio<T> Uolo, Trio<T> Unlo, int s,
-                                                     T ca, T cb, int kc_len, int ilim, int klim) {
+__device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int by, int bz) {
+    const GeoT<T> g = args.g;
+    const RcpT<T> rc = args.rc;
+    const Fld<T> U = args.U, V = args.V, W = args.W, nt = args.nt;
+    const NutSrc<T> ns = args.ns;
+    const DevScal *const ds = args.ds;
+    const T nu = args.nu, Om = args.Om, ca = args.ca, cb = args.cb;
+    const int rot = args.rot, s = args.s, kc_len = args.kc_len, ilim = args.ilim, klim = args.klim;
+    const Trio<T> out = args.out, F1 = args.F1, Uo = args.Uo, Uolo = args.Uolo, Unlo = args.Unlo;
     constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
     __shared__ T ring[3][4][NP];  // [plane slot][field U V W nu_t][tile]
     const int nx = g.nx, ny = g.ny, nz = g.nz, nxg = g.nxg, nyg = g.nyg, nzg = g.nzg;
-    const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
-    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, klim);
+    const int i0 = 2 + bx * TX, j0 = 2 + by * TY;
+    const int kb = 2 + bz * kc_len, ke = min(kb + kc_len - 1, klim);
     const int tx = threadIdx.x % TX, ty = threadIdx.x / TX;
     const int i = i0 + tx, j = j0 + ty;
     const T dt = ds_dt<T>(ds), dPdx = ds_dpdx<T>(ds), dPdz = ds_dpdz<T>(ds);
@@ -622,8 +645,10 @@ __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<
     fetch(kb + 1);
     commit(2);
     __syncthreads();
-    int sm1 = 0, s0 = 1, sp1 = 2;
-    for (int k = kb; k <= ke; k++) {
+    // one plane k; the ring slots of planes k-1, k, k+1 are compile-time
+    // (PH = (k - kb) mod 3), so every ring address is a constant offset
+    auto plane = [&](int k, auto PHc) {
+        constexpr int sm1 = decltype(PHc)::value, s0 = (sm1 + 1) % 3, sp1 = (sm1 + 2) % 3;
         if (k + 1 <= ke) fetch(k + 2);  // in flight during this plane's work
         // RK operands of this plane, loaded before the stencil work
         const bool cu = du && k <= klim, cv = dv && k <= klim, cw = dw && k <= nz - 1;
@@ -652,16 +677,44 @@ __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(GeoT<T> g, RcpT<
         __syncthreads();            // plane k-1 no longer read
         if (k + 1 <= ke) commit(sm1);  // plane k+2 into the freed slot
         __syncthreads();
-        int t0 = sm1;
-        sm1 = s0;
-        s0 = sp1;
-        sp1 = t0;
+    };
+    std::integral_constant<int, 0> c0;
+    std::integral_constant<int, 1> c1;
+    std::integral_constant<int, 2> c2;
+    for (int k = kb; k <= ke; k += 3) {
+        plane(k, c0);
+        if (k + 1 <= ke) plane(k + 1, c1);
+        if (k + 2 <= ke) plane(k + 2, c2);
     }
 }
 
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(const __grid_constant__ Rhs3Args<T> a) {
+    rhs3_tile<T, TX, TY>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One launch over the tiles of several channels (an ensemble): member m owns
+// blocks first[m] .. first[m+1]-1, in the order of its own launch's grid.
 template <typename T>
-int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
+struct Rhs3Batch {
+    int n;
+    int first[CF_ENS_MAXM + 1];
+    Rhs3Args<T> a[CF_ENS_MAXM];
+};
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3_batch(const __grid_constant__ Rhs3Batch<T> B) {
+    const int bid = blockIdx.x;
+    int m = 0;
+    while (m + 1 < B.n && bid >= B.first[m + 1]) m++;
+    const int l = bid - B.first[m], ntx = B.a[m].ntx, nty = B.a[m].nty;
+    rhs3_tile<T, TX, TY>(B.a[m], l % ntx, (l / ntx) % nty, l / (ntx * nty));
+}
+
+template <typename T>
+static Rhs3Args<T> rhs3_args(cf_ctx *ctx, int s, int src, int dst) {
     constexpr int TX = 32, TY = 8;
+    Rhs3Args<T> A;
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[src], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[src], ctx->nxg, ctx->ny);
@@ -698,14 +751,53 @@ int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
         ns.nzp = ctx->nzp;
         ns.dirichlet = ctx->prm.Dirichlet_nu_t == 1;
     }
-    k_rhs3<T, TX, TY><<<dim3(ntx, nty, cdiv(klim - 1, kc_len)), TX * TY, 0, ctx->st>>>(
-        g, rcp_of<T>(ctx), U, V, W, nt, ns, ctx->ds, (T)ctx->prm.nu, (T)ctx->omega_z, fabs(ctx->omega_z) > 1e-6 ? 1 : 0, out, F1, Uo,
-        Uolo, Unlo, s, T(s == 1 ? rk.c[1][1] : (s == 2 ? rk.c[2][1] : rk.c[3][1])),
-        T(s == 1 ? 0.0 : (s == 2 ? rk.c[2][2] : rk.c[3][3])), kc_len,
-        ilim, klim);
+    A.g = g;
+    A.rc = rcp_of<T>(ctx);
+    A.U = U; A.V = V; A.W = W; A.nt = nt;
+    A.ns = ns;
+    A.ds = ctx->ds;
+    A.nu = (T)ctx->prm.nu;
+    A.Om = (T)ctx->omega_z;
+    A.rot = fabs(ctx->omega_z) > 1e-6 ? 1 : 0;
+    A.out = out; A.F1 = F1; A.Uo = Uo; A.Uolo = Uolo; A.Unlo = Unlo;
+    A.s = s;
+    A.ca = T(s == 1 ? rk.c[1][1] : (s == 2 ? rk.c[2][1] : rk.c[3][1]));
+    A.cb = T(s == 1 ? 0.0 : (s == 2 ? rk.c[2][2] : rk.c[3][3]));
+    A.kc_len = kc_len;
+    A.ilim = ilim;
+    A.klim = klim;
+    A.ntx = ntx;
+    A.nty = nty;
+    A.nkc = cdiv(klim - 1, kc_len);
+    return A;
+}
+
+template <typename T>
+int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
+    constexpr int TX = 32, TY = 8;
+    const Rhs3Args<T> A = rhs3_args<T>(ctx, s, src, dst);
+    k_rhs3<T, TX, TY><<<dim3(A.ntx, A.nty, A.nkc), TX * TY, 0, ctx->st>>>(A);
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
     return 0;
+}
+
+// The fused right-hand sides + RK update of substep s of n channels (state
+// buffers src[q] -> dst[q]) in one launch: per channel exactly the
+// arithmetic of launch_rhs3.
+template <typename T>
+int launch_rhs3_batch(cudaStream_t st, cf_ctx *const *m, int s, const int *src, const int *dst, int n) {
+    constexpr int TX = 32, TY = 8;
+    if (n < 1 || n > CF_ENS_MAXM) return CF_ERR_INVALID;
+    Rhs3Batch<T> B;
+    B.n = n;
+    B.first[0] = 0;
+    for (int q = 0; q < n; q++) {
+        B.a[q] = rhs3_args<T>(m[q], s, src[q], dst[q]);
+        B.first[q + 1] = B.first[q] + B.a[q].ntx * B.a[q].nty * B.a[q].nkc;
+    }
+    k_rhs3_batch<T, TX, TY><<<B.first[n], TX * TY, 0, st>>>(B);
+    return cudaGetLastError() == cudaSuccess ? 0 : CF_ERR_CUDA;
 }
 
 // resident fused-RHS blocks per SM (for the z-chunk plan)
@@ -1362,6 +1454,7 @@ int check_bc(cf_ctx *ctx, int b, bool *ok) {
 }
 
 #define INST(T)                                                      \
+    template int launch_rhs3_batch<T>(cudaStream_t, cf_ctx *const *, int, const int *, const int *, int); \
     template int check_bc<T>(cf_ctx *, int, bool *);                 \
     template int launch_bc<T>(cf_ctx *, int, bool);                  \
     template int launch_rhs<T>(cf_ctx *, int, int);                  \

@@ -79,10 +79,28 @@ struct DsmSmem {
 // registers spill and run slower than two)
 template <typename T> struct DsmMinB { static constexpr int v = 2; };
 
+// Everything one launch of the pass needs for one channel: the fields of the
+// state buffer, the reciprocal spacings, sizes, the z-chunk length and the
+// tile grid (ntx x nty x nkc blocks), the |S| output and the plane partials.
+template <typename T>
+struct DsmArgs {
+    Fld<T> U, V, W;
+    RGeo rg;
+    int nx, ny, nyg, nz, nxp, nzp, kc_len, nchunk, ntx, nty, nkc;
+    T *Sout;
+    double *part;
+};
+
+// The tile (bx, by, bz) of one channel: a block of the single-channel launch
+// or of the ensemble launch (k_dsm_fused_batch below).
 template <typename T, int TX, int TY>
-__global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v)
-    k_dsm_fused(Fld<T> U, Fld<T> V, Fld<T> W, RGeo rgv, int nx, int ny, int nyg, int nz, int nxp, int nzp, int kc_len,
-               T *Sout, double *part, int nchunk) {
+__device__ __forceinline__ void dsm_tile(const DsmArgs<T> &args, int bx, int by, int bz) {
+    const Fld<T> U = args.U, V = args.V, W = args.W;
+    const RGeo rgv = args.rg;
+    const int nx = args.nx, ny = args.ny, nyg = args.nyg, nz = args.nz, nxp = args.nxp, nzp = args.nzp,
+              kc_len = args.kc_len, nchunk = args.nchunk;
+    T *const Sout = args.Sout;
+    double *const part = args.part;
     typedef DsmSmem<T, TX, TY> SM;
     constexpr int RX = SM::RX, RY = SM::RY, QX = SM::QX, QY = SM::QY;
     constexpr int NTH = TX * TY, NRT = 3 * RX;
@@ -102,8 +120,8 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v)
             *rdyg = (const T *)rgv.rdyg, *rdz = (const T *)rgv.rdz, *rdzg = (const T *)rgv.rdzg;
     const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0), h = T(0.5), qq = T(0.25);
 
-    const int i0 = 2 + blockIdx.x * TX, j0 = 2 + blockIdx.y * TY;
-    const int kb = 2 + blockIdx.z * kc_len, ke = min(kb + kc_len - 1, nz - 1);
+    const int i0 = 2 + bx * TX, j0 = 2 + by * TY;
+    const int kb = 2 + bz * kc_len, ke = min(kb + kc_len - 1, nz - 1);
     const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
     const int io = i0 + tx, jo = j0 + ty;
     const bool own = io <= nx - 1 && jo <= nyg - 1;
@@ -402,7 +420,7 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v)
             ff_add2(bh, bl, b1, b2);
         }
         if (tx == 0 && jo <= nyg - 1) {
-            const int chunk = blockIdx.x * gridDim.z + blockIdx.z;
+            const int chunk = bx * args.nkc + bz;
             ((float4 *)part)[(long)(jo - 2) * nchunk + chunk] = make_float4(ah, al, bh, bl);
         }
         return;
@@ -417,11 +435,47 @@ __global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v)
             a += red[2 * (ty * TX + q)];
             b += red[2 * (ty * TX + q) + 1];
         }
-        int chunk = blockIdx.x * gridDim.z + blockIdx.z;
+        int chunk = bx * args.nkc + bz;
         part[((long)(jo - 2) * nchunk + chunk) * 2] = a;
         part[((long)(jo - 2) * nchunk + chunk) * 2 + 1] = b;
     }
 }
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_dsm_fused(DsmArgs<T> a) {
+    dsm_tile<T, TX, TY>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// One launch over the tiles of several channels (an ensemble): member m owns
+// blocks first[m] .. first[m+1]-1, in the order of its own launch's grid.
+template <typename T>
+struct DsmBatch {
+    int n;
+    int first[CF_ENS_MAXM + 1];
+    DsmArgs<T> a[CF_ENS_MAXM];
+};
+
+template <typename T, int TX, int TY>
+__global__ void __launch_bounds__(TX *TY, TX * TY >= 512 ? 1 : DsmMinB<T>::v) k_dsm_fused_batch(const __grid_constant__ DsmBatch<T> B) {
+    const int bid = blockIdx.x;
+    int m = 0;
+    while (m + 1 < B.n && bid >= B.first[m + 1]) m++;
+    const int l = bid - B.first[m], ntx = B.a[m].ntx, nty = B.a[m].nty;
+    dsm_tile<T, TX, TY>(B.a[m], l % ntx, (l / ntx) % nty, l / (ntx * nty));
+}
+
+// <LM>/<MM> per row of several channels from their plane partials (the
+// single-channel kernels k_dsm_e / k_dsm_e_ff per member block range).
+struct DsmEArgs {
+    const void *part;
+    double *avg;
+    int nchunk, nyg, dir, ff;
+};
+struct DsmEBatch {
+    int n;
+    int first[CF_ENS_MAXM + 1];
+    DsmEArgs a[CF_ENS_MAXM];
+};
 
 template <typename T>
 static void *rgeo_ptr(cf_ctx *ctx) {
@@ -429,27 +483,36 @@ static void *rgeo_ptr(cf_ctx *ctx) {
 }
 
 template <typename T, int TX, int TY>
-static int launch_fused_cfg(cf_ctx *ctx, int b, int kc_len) {
-    Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
-    Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
-    Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
-    RGeo rg;
+static DsmArgs<T> fused_args(cf_ctx *ctx, int b, int kc_len) {
+    DsmArgs<T> a;
+    a.U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
+    a.V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    a.W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
     T *base = (T *)rgeo_ptr<T>(ctx);
-    rg.rdx = base + ctx->rgeo_off[0];
-    rg.rdxg = base + ctx->rgeo_off[1];
-    rg.rdy = base + ctx->rgeo_off[2];
-    rg.rdyg = base + ctx->rgeo_off[3];
-    rg.rdz = base + ctx->rgeo_off[4];
-    rg.rdzg = base + ctx->rgeo_off[5];
-    int ntx = cdiv(ctx->nxp, TX), nty = cdiv(ctx->nym, TY), nkc = cdiv(ctx->nzp, kc_len);
-    int nchunk = ntx * nkc;
-    T *S = (T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
+    a.rg.rdx = base + ctx->rgeo_off[0];
+    a.rg.rdxg = base + ctx->rgeo_off[1];
+    a.rg.rdy = base + ctx->rgeo_off[2];
+    a.rg.rdyg = base + ctx->rgeo_off[3];
+    a.rg.rdz = base + ctx->rgeo_off[4];
+    a.rg.rdzg = base + ctx->rgeo_off[5];
+    a.nx = ctx->nx; a.ny = ctx->ny; a.nyg = ctx->nyg; a.nz = ctx->nz; a.nxp = ctx->nxp; a.nzp = ctx->nzp;
+    a.kc_len = kc_len;
+    a.ntx = cdiv(ctx->nxp, TX);
+    a.nty = cdiv(ctx->nym, TY);
+    a.nkc = cdiv(ctx->nzp, kc_len);
+    a.nchunk = a.ntx * a.nkc;
+    a.Sout = (T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
+    a.part = ctx->dsm_part;
+    return a;
+}
+
+template <typename T, int TX, int TY>
+static int launch_fused_cfg(cf_ctx *ctx, int b, int kc_len) {
+    const DsmArgs<T> a = fused_args<T, TX, TY>(ctx, b, kc_len);
     size_t sm = DsmSmem<T, TX, TY>::bytes;
-    k_dsm_fused<T, TX, TY><<<dim3(ntx, nty, nkc), TX * TY, sm, ctx->st>>>(U, V, W, rg, ctx->nx, ctx->ny, ctx->nyg, ctx->nz,
-                                                                        ctx->nxp, ctx->nzp, kc_len, S, ctx->dsm_part,
-                                                                        nchunk);
+    k_dsm_fused<T, TX, TY><<<dim3(a.ntx, a.nty, a.nkc), TX * TY, sm, ctx->st>>>(a);
     count_launch(ctx, "k_dsm_fused");
-    ctx->dsm_nchunk_fused = nchunk;
+    ctx->dsm_nchunk_fused = a.nchunk;
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -464,6 +527,12 @@ template <> struct DsmCfg<float> { static constexpr int TX = 32, TY = 8; };
 template <> struct DsmCfg<double> { static constexpr int TX = 16, TY = 8; };
 
 int dsm_fused_setup() {
+    cudaFuncSetAttribute(k_dsm_fused_batch<float, DsmCfg<float>::TX, DsmCfg<float>::TY>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)DsmSmem<float, DsmCfg<float>::TX, DsmCfg<float>::TY>::bytes);
+    cudaFuncSetAttribute(k_dsm_fused_batch<double, DsmCfg<double>::TX, DsmCfg<double>::TY>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)DsmSmem<double, DsmCfg<double>::TX, DsmCfg<double>::TY>::bytes);
     cudaFuncSetAttribute(k_dsm_fused<float, DsmCfg<float>::TX, DsmCfg<float>::TY>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)DsmSmem<float, DsmCfg<float>::TX, DsmCfg<float>::TY>::bytes);
@@ -502,3 +571,89 @@ int launch_dsm_fused(cf_ctx *ctx, int b) {
 
 template int launch_dsm_fused<double>(cf_ctx *, int);
 template int launch_dsm_fused<float>(cf_ctx *, int);
+
+__global__ void __launch_bounds__(256) k_dsm_e_batch(const __grid_constant__ DsmEBatch B) {
+    const int bid = blockIdx.x;
+    int m = 0;
+    while (m + 1 < B.n && bid >= B.first[m + 1]) m++;
+    const DsmEArgs &a = B.a[m];
+    const int l = bid - B.first[m];
+    const int lane = threadIdx.x & 31, j = l * (blockDim.x >> 5) + (threadIdx.x >> 5) + 2, nyg = a.nyg;
+    if (j > nyg - 1) return;
+    double c;
+    if (a.ff) {  // float-float partials (split path), as k_dsm_e_ff
+        const float4 *part = (const float4 *)a.part;
+        float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
+        for (int q = lane; q < a.nchunk; q += 32) {
+            const float4 v = part[(long)(j - 2) * a.nchunk + q];
+            ff_add2(ah, al, v.x, v.y);
+            ff_add2(bh, bl, v.z, v.w);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const float a1 = __shfl_down_sync(0xffffffffu, ah, o), a2 = __shfl_down_sync(0xffffffffu, al, o);
+            const float b1 = __shfl_down_sync(0xffffffffu, bh, o), b2 = __shfl_down_sync(0xffffffffu, bl, o);
+            ff_add2(ah, al, a1, a2);
+            ff_add2(bh, bl, b1, b2);
+        }
+        c = ((double)ah + (double)al) / ((double)bh + (double)bl);
+    } else {  // FP64 partials, as k_dsm_e
+        const double *part = (const double *)a.part;
+        double s0 = 0.0, s1 = 0.0;
+        for (int q = lane; q < a.nchunk; q += 32) {
+            s0 += part[((long)(j - 2) * a.nchunk + q) * 2];
+            s1 += part[((long)(j - 2) * a.nchunk + q) * 2 + 1];
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_down_sync(0xffffffffu, s0, o);
+            s1 += __shfl_down_sync(0xffffffffu, s1, o);
+        }
+        c = s0 / s1;
+    }
+    if (lane == 0) {
+        double *avg = a.avg;
+        float *af = (float *)(avg + nyg + 2);  // FP32 copy for the split path
+        avg[j] = c;
+        af[j] = (float)c;
+        if (j == 2) {
+            avg[1] = a.dir ? -c : c;
+            af[1] = (float)avg[1];
+        }
+        if (j == nyg - 1) {
+            avg[nyg] = a.dir ? -c : c;
+            af[nyg] = (float)avg[nyg];
+        }
+    }
+}
+
+// The one-pass dynamic Smagorinsky pass of n channels (state buffers buf[q])
+// in one launch, then their <LM>/<MM> rows in one more: per channel exactly
+// the arithmetic of launch_dsm's fused route.  Counts as two launches.
+template <typename T>
+int launch_dsm_batch(cudaStream_t st, cf_ctx *const *m, const int *buf, int n) {
+    constexpr int TX = DsmCfg<T>::TX, TY = DsmCfg<T>::TY;
+    if (n < 1 || n > CF_ENS_MAXM) return CF_ERR_INVALID;
+    DsmBatch<T> B;
+    DsmEBatch E;
+    B.n = E.n = n;
+    B.first[0] = E.first[0] = 0;
+    for (int q = 0; q < n; q++) {
+        cf_ctx *c = m[q];
+        B.a[q] = fused_args<T, TX, TY>(c, buf[q], c->dsm_kc);
+        B.first[q + 1] = B.first[q] + B.a[q].ntx * B.a[q].nty * B.a[q].nkc;
+        c->dsm_nchunk_fused = B.a[q].nchunk;
+        E.a[q].part = c->dsm_part;
+        E.a[q].avg = c->avg_nu_t;
+        E.a[q].nchunk = B.a[q].nchunk;
+        E.a[q].nyg = c->nyg;
+        E.a[q].dir = c->prm.Dirichlet_nu_t == 1;
+        E.a[q].ff = sizeof(T) == 4;
+        E.first[q + 1] = E.first[q] + cdiv(c->nym, 8);
+        c->nut_lazy = true;
+    }
+    k_dsm_fused_batch<T, TX, TY><<<B.first[n], TX * TY, DsmSmem<T, TX, TY>::bytes, st>>>(B);
+    k_dsm_e_batch<<<E.first[n], 256, 0, st>>>(E);
+    return cudaGetLastError() == cudaSuccess ? 0 : CF_ERR_CUDA;
+}
+
+template int launch_dsm_batch<double>(cudaStream_t, cf_ctx *const *, const int *, int);
+template int launch_dsm_batch<float>(cudaStream_t, cf_ctx *const *, const int *, int);

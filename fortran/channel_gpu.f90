@@ -519,6 +519,21 @@ Module channel_gpu
        Integer(c_int), Value :: on
      End Function cf_ensemble_set_batched_tri
 
+     Integer(c_int) Function cf_ensemble_set_batched_stencils(e, on) Bind(C, name="cf_ensemble_set_batched_stencils")
+       Import :: c_int, c_ptr
+       Type(c_ptr), Value    :: e
+       Integer(c_int), Value :: on
+     End Function cf_ensemble_set_batched_stencils
+
+     ! report: 4 doubles (or c_null_ptr); choice (or c_null_ptr)
+     Integer(c_int) Function cf_ensemble_autotune(e, steps, report, choice) Bind(C, name="cf_ensemble_autotune")
+       Import :: c_int, c_double, c_ptr
+       Type(c_ptr), Value    :: e
+       Integer(c_int), Value :: steps
+       Real(c_double)        :: report(*)
+       Integer(c_int)        :: choice
+     End Function cf_ensemble_autotune
+
      !--------------------------- divergence check without device allocation
      ! every array argument is a device pointer
      Integer(c_int) Function cf_check_divergence_noalloc(nx, ny, nz, U, V, W, x, y, z, out, stream) &

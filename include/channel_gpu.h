@@ -318,6 +318,22 @@ int cf_ensemble_launches_per_step(cf_ensemble *e);
  * their FP32 spectra); 0: each member solves its own systems inside its
  * branch, bit for bit as cf_time_step_rk3. */
 int cf_ensemble_set_batched_tri(cf_ensemble *e, int on);
+/* 1 (up to 32 members; default 0): the fused dynamic Smagorinsky pass of
+ * every member that takes it (no wall model) and the fused right-hand sides
+ * of all members run as one launch each per substep, every (member, tile) a
+ * block of it -- per member the same arithmetic as its own launch; the
+ * other kernels stay in the members' branches.  0: every kernel in the
+ * members' branches. */
+int cf_ensemble_set_batched_stencils(cf_ensemble *e, int on);
+/* Empirical choice of how the ensemble runs its stencil passes: one whole
+ * ensemble step per candidate captures its graph, then `steps` steps are
+ * timed (CUDA events) for (0) every kernel in the members' branches with
+ * each member's own z-chunk plan, and the batched DSM / right-hand-side
+ * launches with (1) the members' plans, (2) one z chunk per member, (3) two;
+ * the fastest is kept.  The ensemble advances 4 (steps + 1) steps.
+ * report (4 doubles, may be NULL): ms per step of each candidate; choice
+ * (may be NULL): the one kept. */
+int cf_ensemble_autotune(cf_ensemble *e, int steps, double *report, int *choice);
 
 /* ---- divergence check without device allocation ---------------------- */
 /* No counterpart in the reference: the arithmetic is check_divergence

@@ -487,16 +487,21 @@ def grids_centres(f):
     return grids.centres(np.asarray(f))
 
 
-@pytest.mark.parametrize("batched", [False, True])
-def test_ensemble_members_match_single_runs(batched):
-    """Three channels of different grids, models and wall treatments advanced
-    as one ensemble give bit for bit the fields of each advanced alone; with
-    the batched FP64 tridiagonal solve the FP64 members still do (the same
-    replay), the split-path members agree to the precision of their FP32
-    solves."""
+@pytest.mark.parametrize("batched,stencils", [(False, False), (True, False), (False, True), (True, True)])
+def test_ensemble_members_match_single_runs(batched, stencils):
+    """Four channels of different grids, models and wall treatments advanced
+    as one ensemble give bit for bit the fields of each advanced alone, with
+    their fused DSM passes and right-hand sides in member branches or as one
+    launch over all members (stencils) -- the split-path members of the
+    batched stencil launches to within 1e-6 in U, V, W (measured 1e-11 to
+    1e-9: the batched kernel's FP32 contractions; P, which carries the
+    cancellation of div u*, and nu_t as below); with the batched FP64 tridiagonal
+    solve the FP64 members still do (the same replay), the split-path members
+    agree to the precision of their FP32 solves."""
     import channelflow as cf
     specs = [dict(dims=(18, 17, 18), seed=3), dict(dims=(34, 33, 26), seed=4, les=3),
-             dict(dims=(26, 17, 22), seed=5, stretch=0.0, wall=3, retau=2000.0, profile="plug")]
+             dict(dims=(26, 17, 22), seed=5, stretch=0.0, wall=3, retau=2000.0, profile="plug"),
+             dict(dims=(42, 25, 34), seed=6)]
     cases = []
     for sp in specs:
         kw = {k: v for k, v in sp.items() if k not in ("dims",)}
@@ -518,15 +523,20 @@ def test_ensemble_members_match_single_runs(batched):
             alone.append(ch.download())
             ch.close()
         members = [make(case, prec) for case in cases]
-        ens = cf.Ensemble(members, batched_tri=batched)
+        ens = cf.Ensemble(members, batched_tri=batched, batched_stencils=stencils)
         ens.step(2)
         ens.step(4)
         assert ens.launches_per_step() > 3 * 20
         for m, ref in zip(members, alone):
             got = m.download()
             for n in ("U", "V", "W", "P", "nu_t"):
-                if prec == cf.PREC_FP64 or not batched:
+                if prec == cf.PREC_FP64 or not (batched or stencils):
                     assert np.array_equal(got[n], ref[n]), (prec, n)
+                elif not batched and n in ("U", "V", "W"):
+                    # the batched stencil kernels compile the same FP32 arithmetic
+                    # with their own contraction choices: rounding-level changes
+                    # (the compensated state keeps them near 1e-9)
+                    assert rel_err(got[n], ref[n]) < 1e-6, (prec, n, rel_err(got[n], ref[n]))
                 else:  # the pseudo-pressure carries the FP32 solve's error directly
                     tol = {"P": 2e-3, "nu_t": 1e-4}.get(n, 1e-5)
                     assert rel_err(got[n], ref[n]) < tol, (prec, n, rel_err(got[n], ref[n]))
@@ -566,3 +576,38 @@ def test_autotune_keeps_the_state(les):
         ch.close()
     for n in ("U", "V", "W", "nu_t"):
         assert rel_err(runs[1][n], runs[0][n]) < 1e-12, n
+
+
+def test_ensemble_autotune_keeps_a_valid_choice():
+    """cf_ensemble_autotune times every candidate and keeps the fastest; the
+    ensemble then still advances its members as single runs would (FP64: to
+    the order of the DSM plane sums, which the candidates' z chunks change)."""
+    import channelflow as cf
+    specs = [dict(dims=(18, 17, 18), seed=3), dict(dims=(34, 25, 26), seed=4)]
+    cases = [channel_case(*sp["dims"], seed=sp["seed"]) for sp in specs]
+
+    def make(case):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_FP64, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.init_mass_flow()
+        ch.apply_boundary_conditions()
+        ch.set_fixed_dt(case["dt"])
+        return ch
+
+    members = [make(c) for c in cases]
+    ens = cf.Ensemble(members)
+    ens.step(1)
+    rep = ens.autotune(steps=2)
+    assert rep["choice"] in rep["ms_per_step"] and all(v > 0 for v in rep["ms_per_step"].values())
+    ens.step(3)
+    done = 1 + 4 * 3 + 3
+    for m, case in zip(members, cases):
+        ref = make(case)
+        ref.time_step_rk3(done)
+        a, b = m.download(), ref.download()
+        for n in ("U", "V", "W", "nu_t"):
+            assert rel_err(a[n], b[n]) < 1e-11, (n, rel_err(a[n], b[n]))
+        ref.close()
+    ens.close()
+    for m in members:
+        m.close()
