@@ -1062,8 +1062,7 @@ static int enqueue_seg(cf_ctx *ctx, int seg, bool tri) {
     }
     const int X = ctx->seg_base, a = (X + 1) % 3, b = (X + 2) % 3;
     if (seg == 1) {
-        TRY(launch_projection<T>(ctx, a, true, false, canon, POISSON_INV));
-        TRY(launch_bc<T>(ctx, a, false));
+        TRY(launch_projection<T>(ctx, a, true, false, canon, POISSON_INV, true));
         // substep 2 (:118-131)
         TRY(eddy(ctx, a));
         TRY(launch_rhs_update<T>(ctx, 2, a, b));
@@ -1071,16 +1070,14 @@ static int enqueue_seg(cf_ctx *ctx, int seg, bool tri) {
         return launch_projection<T>(ctx, b, false, false, canon, fwd);
     }
     if (seg == 2) {
-        TRY(launch_projection<T>(ctx, b, false, false, canon, POISSON_INV));
-        TRY(launch_bc<T>(ctx, b, false));
+        TRY(launch_projection<T>(ctx, b, false, false, canon, POISSON_INV, true));
         // substep 3 (:134-150)
         TRY(eddy(ctx, b));
         TRY(launch_rhs_update<T>(ctx, 3, b, a));
         ctx->cur = a;
         return launch_projection<T>(ctx, a, false, true, canon, fwd);
     }
-    TRY(launch_projection<T>(ctx, a, false, true, canon, POISSON_INV));
-    TRY(launch_bc<T>(ctx, a));
+    TRY(launch_projection<T>(ctx, a, false, true, canon, POISSON_INV, true));
     // mass-flow forcing (:153-171); with no-slip walls the correction is
     // added to the ghosts as apply_boundary_conditions would propagate it
     const bool g = ctx->prm.iwall_model == 0;
@@ -1156,8 +1153,7 @@ static int ens_pre_t(cf_ctx *ctx, int s, bool batched_dsm) {
     }
     const int X = ctx->seg_base, a = (X + 1) % 3, b = (X + 2) % 3;
     const int p = s == 2 ? a : b;  // the state the previous substep's projection acts on
-    TRY(launch_projection<T>(ctx, p, s == 2, false, canon, POISSON_INV));
-    TRY(launch_bc<T>(ctx, p, false));
+    TRY(launch_projection<T>(ctx, p, s == 2, false, canon, POISSON_INV, true));
     if (!batched_dsm) TRY(eddy(ctx, p));
     return 0;
 }
@@ -1173,8 +1169,7 @@ static int ens_post_t(cf_ctx *ctx, int s, bool tri) {
 template <typename T>
 static int ens_fin_t(cf_ctx *ctx) {
     const int a = (ctx->seg_base + 1) % 3;
-    TRY(launch_projection<T>(ctx, a, false, true, true, POISSON_INV));
-    TRY(launch_bc<T>(ctx, a));
+    TRY(launch_projection<T>(ctx, a, false, true, true, POISSON_INV, true));
     const bool g = ctx->prm.iwall_model == 0;
     if (ctx->prm.x_mass_cte == 1 || ctx->prm.x_mass_cte == 2) {
         TRY(launch_mass_flow<T>(ctx, a, ctx->prm.x_mass_cte, g));

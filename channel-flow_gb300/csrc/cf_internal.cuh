@@ -301,8 +301,11 @@ int launch_tri_batch(cudaStream_t st, const TriMember *dtab, int nmem, long tota
 // Poisson phases (forward transforms, tridiagonal solves, inverse transforms
 // and the projection)
 enum { POISSON_FWD = 1, POISSON_TRI = 2, POISSON_INV = 4, POISSON_ALL = 7 };
+// bc: apply_boundary_conditions after the projection (written by the
+// projection kernel itself where it projects canonical cells with no-slip
+// walls; launch_bc otherwise)
 template <typename T> int launch_projection(cf_ctx *ctx, int buf, bool store_p, bool lo = true, bool canon = false,
-                                            int phases = POISSON_ALL);
+                                            int phases = POISSON_ALL, bool bc = false);
 template <typename T> int launch_pressure(cf_ctx *ctx, int buf);  // actual pressure into P (pressure.f90:21)
 template <typename T> int launch_amd(cf_ctx *ctx, int buf);  // AMD eddy viscosity (subgrid.f90:639)
 void amd_plan(int esz, int nxp, int nym, int nzp, int sms, int *nkc, int *nparts);  // z chunks of the AMD pass

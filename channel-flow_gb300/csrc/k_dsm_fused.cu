@@ -67,11 +67,18 @@ struct RGeo {  // reciprocal spacings, 1-based like the coordinates
 // planes per z chunk at most (their z spacings sit in static shared memory)
 constexpr int DSM_ZMAX = DSM_ZMAX_HOST;
 
+// smallest m >= n with m = 4 (mod 32): the stride of the per-field blocks
+// that the raw column tasks store to, so that a warp whose tasks span two
+// fields writes disjoint banks (the columns of the second field start 4
+// banks after the first field's, past the first field's wrapped columns)
+constexpr int bank_pad4(int n) { return n + ((36 - n % 32) % 32); }
+
 template <typename T, int TX, int TY>
 struct DsmSmem {
     static constexpr int RX = TX + 4, RY = TY + 4, QX = TX + 2, QY = TY + 2;
-    static constexpr int NR = 9 * RX * RY, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY, NC = 16 * QX * TY,
-                         NY = 3 * QY * RX;
+    static constexpr int RFS = bank_pad4(RY * RX), YFS = bank_pad4(QY * RX);  // field strides of R and Ry
+    static constexpr int NR = 9 * RFS, NG = 9 * QX * QY, NF = 9 * QX * QY, NQ = 16 * QX * QY, NC = 16 * QX * TY,
+                         NY = 3 * YFS;
     static constexpr size_t bytes = (size_t)(NR + NG + NF + NQ + NC + NY) * sizeof(T);
 };
 
@@ -125,12 +132,13 @@ __device__ __forceinline__ void dsm_tile(const DsmArgs<T> &args, int bx, int by,
     const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
     const int io = i0 + tx, jo = j0 + ty;
     const bool own = io <= nx - 1 && jo <= nyg - 1;
-    auto RS = [&](int slot, int f, int sy, int sx) -> T & { return R[((slot * 3 + f) * RY + sy) * RX + sx]; };
+    constexpr int RFS = SM::RFS, YFS = SM::YFS;
+    auto RS = [&](int slot, int f, int sy, int sx) -> T & { return R[(slot * 3 + f) * RFS + sy * RX + sx]; };
     auto GS = [&](int slot, int f, int sy, int sx) -> T & { return G[((slot * 3 + f) * QY + sy) * QX + sx]; };
     auto FS = [&](int slot, int f, int sy, int sx) -> T & { return F[((slot * 3 + f) * QY + sy) * QX + sx]; };
     auto QS = [&](int p, int sy, int sx) -> PT & { return Qs[(p * QY + sy) * QX + sx]; };
     auto CS = [&](int p, int oy, int sx) -> PT & { return Cs[(p * TY + oy) * QX + sx]; };
-    auto YS = [&](int f, int sy, int rx) -> T & { return Ry[(f * QY + sy) * RX + rx]; };
+    auto YS = [&](int f, int sy, int rx) -> T & { return Ry[f * YFS + sy * RX + rx]; };
     auto yw = [&](int j, int lo, int hi, T &wm, T &w0, T &wp) {
         if (j <= lo) { wm = T(0); w0 = f23; wp = f13; }
         else if (j >= hi) { wm = f13; w0 = f23; wp = T(0); }
@@ -169,10 +177,15 @@ __device__ __forceinline__ void dsm_tile(const DsmArgs<T> &args, int bx, int by,
     T S_m2 = T(0), S_m3 = T(0);  // |S| of Q(r-2), Q(r-3) at the own point
     T sl = T(0), smm = T(0);
 
+    // halo points of phase B: the first TX points of the rows below and
+    // above the tile on one warp each, then the four points past them and
+    // the two halo columns (for TX = 32 the accesses of every warp fall in
+    // distinct banks)
     const bool hal = tid < 2 * QX + 2 * TY;
     int hsx = 0, hsy = 0;
-    if (tid < QX) { hsx = tid; hsy = 0; }
-    else if (tid < 2 * QX) { hsx = tid - QX; hsy = QY - 1; }
+    if (tid < TX) { hsx = tid; hsy = 0; }
+    else if (tid < 2 * TX) { hsx = tid - TX; hsy = QY - 1; }
+    else if (tid < 2 * TX + 4) { hsx = TX + (tid & 1); hsy = ((tid - 2 * TX) >> 1) ? QY - 1 : 0; }
     else if (tid < 2 * QX + TY) { hsx = 0; hsy = tid - 2 * QX + 1; }
     else if (hal) { hsx = QX - 1; hsy = tid - 2 * QX - TY + 1; }
     const int rs = kb - 2, re = ke + 2;

@@ -917,27 +917,59 @@ struct RSpG {
     const float *rxg, *ryg, *rzg;  // 1/(xg(i)-xg(i-1)) etc., 1-based
 };
 
-template <typename T>
-__device__ __forceinline__ void proj_update(const Fld<T> &F, const Fld<T> &Flo, int i, int j, int k, T grad) {
-    if constexpr (sizeof(T) == 4) {
-        if (Flo.p) {
-            float hi = F(i, j, k), lo = Flo(i, j, k);
-            ff_add(hi, lo, -grad);
-            F(i, j, k) = hi;
-            Flo(i, j, k) = lo;
-            return;
-        }
-    }
-    F(i, j, k) = F(i, j, k) - grad;
-}
-
 // KP consecutive planes per thread: every load of the thread is issued
 // before the first store (the fields may alias as far as the compiler knows).
 constexpr int PROJ_KP = 2;
 
-// ilim, klim: last x and z index projected (nxg-1 and nzg-1 for the full
-// interior; nxp+1 and nzp+1 for the canonical cells only)
+// The ghost copies apply_boundary_conditions (boundary_conditions.f90:20-75)
+// makes of a canonical cell with no-slip walls: its periodic images in x and
+// z (update of the duplicate columns and planes, :87-244) and, on the rows
+// next to a wall, the wall ghost of the cell and of each image (:257-272):
+// -value at y centres, 0 at y faces.  xc/zc: the field sits at x/z centres
+// (extent np + 3, images of 2, 3 and np + 1) rather than faces (extent
+// np + 2, images of 2 and np + 1); yf: the field sits at y faces.
+struct ImgAxes {
+    int n1, n2, n3;
+    bool xc, zc, yf;
+};
+
+// the periodic image of canonical index i on an axis of extent n (0: none);
+// at most one per cell when np >= 4 (checked on the host)
+__device__ __forceinline__ int img_of(int i, int n, bool centre) {
+    if (centre) return i == 2 ? n - 1 : (i == 3 ? n : (i == n - 2 ? 1 : 0));
+    return i == 2 ? n : (i == n - 1 ? 1 : 0);
+}
+
 template <typename T>
+__device__ __forceinline__ void put_images(const Fld<T> &F, const Fld<T> &Flo, bool lo, const ImgAxes &a, int i, int j,
+                                           int k, T v, T vl) {
+    const int xi = img_of(i, a.n1, a.xc), zi = img_of(k, a.n3, a.zc);
+    const bool yw = j == 2 || j == a.n2 - 1;
+    if (!(xi | zi) && !yw) return;
+    auto put = [&](int ii, int jj, int kk, T x, T xl) {
+        F(ii, jj, kk) = x;
+        if (lo) Flo(ii, jj, kk) = xl;
+    };
+    if (xi) put(xi, j, k, v, vl);
+    if (zi) put(i, j, zi, v, vl);
+    if (xi && zi) put(xi, j, zi, v, vl);
+    if (yw) {
+        const int jg = j == 2 ? 1 : a.n2;
+        const T gv = a.yf ? T(0) : -v, gl = a.yf ? T(0) : -vl;
+        put(i, jg, k, gv, gl);
+        if (xi) put(xi, jg, k, gv, gl);
+        if (zi) put(i, jg, zi, gv, gl);
+        if (xi && zi) put(xi, jg, zi, gv, gl);
+    }
+}
+
+// ilim, klim: last x and z index projected (nxg-1 and nzg-1 for the full
+// interior; nxp+1 and nzp+1 for the canonical cells only).  IMG (canonical
+// cells, no-slip walls): every ghost copy of the new values is written as
+// well, which is what apply_boundary_conditions after the projection would
+// do.  Index arithmetic: the (i, j) offsets of the thread are formed once,
+// planes follow by adding the plane strides.
+template <typename T, bool IMG>
 __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ulo, Fld<T> V, Fld<T> Vlo, Fld<T> W,
                                                   Fld<T> Wlo, const T *__restrict__ phi, PhiView pv, RSpG rs, int ilim,
                                                   int klim) {
@@ -948,26 +980,31 @@ __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ul
     if (i > ilim || j > g.nyg - 1) return;
     const bool du = i <= g.nx - 1, dv = j <= g.ny - 1;
     const bool lo = Ulo.p != nullptr;
+    // phi offsets: canonical x of i and i+1, rows j and j+1, planes
+    const int nxp = pv.nxp, pls = nxp * pv.nym;
+    const int ic0 = wrapf(i, nxp) - 2, ic1 = wrapf(i + 1, nxp) - 2;
+    const int r0 = nxp * (j - 2), r1 = r0 + nxp;
+    int kof[KP + 1];
+#pragma unroll
+    for (int q = 0; q <= KP; q++) kof[q] = pls * (wrapf(k0 + q, pv.nzp) - 2);
+    const int iu = U.idx(i, j, k0), iv = V.idx(i, j, k0), iw = W.idx(i, j, k0);
     T p0[KP + 1], px[KP], py[KP];
     T u[KP], v[KP], w[KP], ul[KP], vl[KP], wl[KP];
 #pragma unroll
-    for (int q = 0; q <= KP; q++) {
-        const int k = k0 + q;
-        p0[q] = k <= g.nzg - 1 ? phi[pv(i, j, k)] : T(0);  // plane k0+KP: the z neighbour of the last plane
-    }
+    for (int q = 0; q <= KP; q++) p0[q] = k0 + q <= g.nzg - 1 ? phi[ic0 + r0 + kof[q]] : T(0);
 #pragma unroll
     for (int q = 0; q < KP; q++) {
         const int k = k0 + q;
         const bool kin = k <= klim, dw = k <= g.nz - 1;
-        px[q] = du && kin ? phi[pv(i + 1, j, k)] : T(0);
-        py[q] = dv && kin ? phi[pv(i, j + 1, k)] : T(0);
-        u[q] = du && kin ? U(i, j, k) : T(0);
-        v[q] = dv && kin ? V(i, j, k) : T(0);
-        w[q] = dw ? W(i, j, k) : T(0);
+        px[q] = du && kin ? phi[ic1 + r0 + kof[q]] : T(0);
+        py[q] = dv && kin ? phi[ic0 + r1 + kof[q]] : T(0);
+        u[q] = du && kin ? U.p[iu + q * U.sz] : T(0);
+        v[q] = dv && kin ? V.p[iv + q * V.sz] : T(0);
+        w[q] = dw ? W.p[iw + q * W.sz] : T(0);
         if (lo) {
-            ul[q] = du && kin ? Ulo(i, j, k) : T(0);
-            vl[q] = dv && kin ? Vlo(i, j, k) : T(0);
-            wl[q] = dw ? Wlo(i, j, k) : T(0);
+            ul[q] = du && kin ? Ulo.p[iu + q * U.sz] : T(0);
+            vl[q] = dv && kin ? Vlo.p[iv + q * V.sz] : T(0);
+            wl[q] = dw ? Wlo.p[iw + q * W.sz] : T(0);
         }
     }
     T rx, ry;
@@ -995,21 +1032,39 @@ __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ul
         }
         (void)rx;
         (void)ry;
-        auto upd = [&](const Fld<T> &F, const Fld<T> &Flo, T f, T fl, T gr) {
+        auto upd = [&](const Fld<T> &F, const Fld<T> &Flo, int o, T f, T fl, T gr) {
+            T hi = f - gr;
             if constexpr (sizeof(T) == 4) {
                 if (lo) {
-                    float hi = f, l = fl;
+                    float l = fl;
+                    hi = f;
                     ff_add(hi, l, -gr);
-                    F(i, j, k) = hi;
-                    Flo(i, j, k) = l;
-                    return;
+                    Flo.p[o] = l;
                 }
             }
-            F(i, j, k) = f - gr;
+            F.p[o] = hi;
         };
-        if (du) upd(U, Ulo, u[q], ul[q], gx);
-        if (dv) upd(V, Vlo, v[q], vl[q], gy);
-        if (k <= g.nz - 1) upd(W, Wlo, w[q], wl[q], gz);
+        if (du) upd(U, Ulo, iu + q * U.sz, u[q], ul[q], gx);
+        if (dv) upd(V, Vlo, iv + q * V.sz, v[q], vl[q], gy);
+        if (k <= g.nz - 1) upd(W, Wlo, iw + q * W.sz, w[q], wl[q], gz);
+    }
+    if constexpr (IMG) {
+        // the ghost copies, from the values just stored (read back by the
+        // thread that stored them), on the few threads whose cells have any
+        const bool ex = i <= 3 || i >= g.nxg - 2, ey = j == 2 || j >= g.ny - 1, ez = k0 <= 3 || k0 + KP - 1 >= g.nzg - 2;
+        if (ex || ey || ez) {
+            const ImgAxes au = {g.nx, g.nyg, g.nzg, false, true, false}, av = {g.nxg, g.ny, g.nzg, true, true, true},
+                          aw = {g.nxg, g.nyg, g.nz, true, false, false};
+#pragma unroll 1
+            for (int q = 0; q < KP; q++) {
+                const int k = k0 + q;
+                if (k > klim) break;
+                if (du) put_images<T>(U, Ulo, lo, au, i, j, k, U.p[iu + q * U.sz], lo ? Ulo.p[iu + q * U.sz] : T(0));
+                if (dv) put_images<T>(V, Vlo, lo, av, i, j, k, V.p[iv + q * V.sz], lo ? Vlo.p[iv + q * V.sz] : T(0));
+                if (k <= g.nz - 1)
+                    put_images<T>(W, Wlo, lo, aw, i, j, k, W.p[iw + q * W.sz], lo ? Wlo.p[iw + q * W.sz] : T(0));
+            }
+        }
     }
 }
 
@@ -1157,7 +1212,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
 }
 
 template <typename T>
-int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon, int phases) {
+int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon, int phases, bool bc) {
     GeoT<T> g = geo_of<T>(ctx);
     Fld<T> U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
     Fld<T> V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
@@ -1176,11 +1231,20 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon, int
         rg.ryg = ctx->d_rgeo_f + ctx->rgeo_off[3];
         rg.rzg = ctx->d_rgeo_f + ctx->rgeo_off[5];
         const int ilim = canon ? ctx->nxp + 1 : ctx->nxg - 1, klim = canon ? ctx->nzp + 1 : ctx->nzg - 1;
-        k_project3<T><<<dim3(cdiv(ilim - 1, 32), cdiv(ctx->nyg - 2, 4), cdiv(klim - 1, PROJ_KP)), blk, 0, ctx->st>>>(
-            g, U, make_fld<T>(lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg), V,
-            make_fld<T>(lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny), W,
-            make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg), phi, pv, rg, ilim, klim);
+        // the boundary conditions as ghost copies written by the projection
+        // itself: canonical cells, no-slip walls
+        const bool img = bc && canon && ctx->prm.iwall_model == 0 && ctx->nxp >= 4 && ctx->nzp >= 4;
+        const dim3 grd(cdiv(ilim - 1, 32), cdiv(ctx->nyg - 2, 4), cdiv(klim - 1, PROJ_KP));
+        const Fld<T> Ul = make_fld<T>(lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg),
+                     Vl = make_fld<T>(lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny),
+                     Wl = make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg);
+        if (img) k_project3<T, true><<<grd, blk, 0, ctx->st>>>(g, U, Ul, V, Vl, W, Wl, phi, pv, rg, ilim, klim);
+        else k_project3<T, false><<<grd, blk, 0, ctx->st>>>(g, U, Ul, V, Vl, W, Wl, phi, pv, rg, ilim, klim);
         count_launch(ctx, "k_project3");
+        if (img) ctx->state_periodic = true;  // as launch_bc: holds for every later launch on the stream
+        else if (bc) {
+            if (int rc = launch_bc<T>(ctx, b, lo)) return rc;
+        }
     }
     if (store_p) {
         Fld<T> P = make_fld<T>(ctx->P, ctx->nxg, ctx->nyg);
@@ -1317,7 +1381,7 @@ int fft_setup_attrs() {
     return 0;
 }
 
-template int launch_projection<double>(cf_ctx *, int, bool, bool, bool, int);
-template int launch_projection<float>(cf_ctx *, int, bool, bool, bool, int);
+template int launch_projection<double>(cf_ctx *, int, bool, bool, bool, int, bool);
+template int launch_projection<float>(cf_ctx *, int, bool, bool, bool, int, bool);
 template int launch_pressure<double>(cf_ctx *, int);
 template int launch_pressure<float>(cf_ctx *, int);

@@ -80,6 +80,30 @@ def test_boundary_conditions_exact(which):
         assert np.array_equal(g[n], f[n]), n
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("dims", [(34, 33, 34), (18, 17, 22), (66, 65, 66)])
+def test_step_ghosts_are_the_boundary_conditions(precision, dims):
+    """After graph-captured steps (no-slip walls: the projection writes every
+    ghost copy of its canonical cells instead of a separate
+    apply_boundary_conditions), the ghosts hold exactly what
+    apply_boundary_conditions would put there: the fields do not change
+    when it is applied once more (low words included in the split path)."""
+    import channelflow as cf
+    case = channel_case(*dims, seed=11)
+    ch = cf.Channel(case["x"], case["y"], case["z"], precision=precision, **case["prm"])
+    ch.upload(case["U"], case["V"], case["W"])
+    ch.init_mass_flow()
+    ch.apply_boundary_conditions()
+    ch.set_fixed_dt(case["dt"])
+    ch.time_step_rk3(3)
+    a = ch.download()
+    ch.apply_boundary_conditions()
+    b = ch.download()
+    for n in ("U", "V", "W"):
+        assert np.array_equal(a[n], b[n]), n
+    ch.close()
+
+
 @pytest.mark.parametrize("which", ["small", "config1"])
 def test_eddy_viscosity_and_rhs(which):
     case = channel_case(*CASES[which])
