@@ -379,6 +379,138 @@ __global__ void k_fft_z(typename C2<T>::t *spec, FftPlan pl, const typename C2<T
 }
 
 // ---------------------------------------------------------------------------
+// z transforms of the compile-time lengths up to 256 as at most two Stockham
+// stages of composite radix (16 = 4x4, 12 = 4x3, 8 = 4x2), each radix-R
+// butterfly a register DFT: the first stage reads its R elements straight
+// from the spectrum and stores to shared memory, the second reads them back
+// and stores its results straight to the spectrum -- one shared-memory round
+// trip per element instead of one per radix-2..5 stage plus the copies in
+// and out.  Same Stockham ordering as fft_fixed (natural order in and out).
+// ---------------------------------------------------------------------------
+constexpr int zr_r0(int n) {
+    return n == 16 ? 16 : n == 32 ? 8 : n == 64 ? 8 : n == 96 ? 8 : n == 128 ? 16 : n == 192 ? 16 : n == 256 ? 16 : 0;
+}
+constexpr int zr_r1(int n) {
+    return n == 16 ? 1 : n == 32 ? 4 : n == 64 ? 8 : n == 96 ? 12 : n == 128 ? 8 : n == 192 ? 12 : n == 256 ? 16 : 0;
+}
+// threads per line: the butterflies of both stages spread evenly where the
+// counts allow it
+constexpr int zr_threads(int n) {
+    return n == 16 ? 1 : n == 32 ? 4 : n == 64 ? 8 : n == 96 ? 4 : n == 128 ? 8 : n == 192 ? 16 : n == 256 ? 16 : 0;
+}
+constexpr int ZR_T = 256;  // threads per block
+
+// DFT of R values in registers (natural order in and out): R = Ra Rb split
+// as X[qa + Ra qb] = sum_rb W_Rb^(rb qb) W_R^(rb qa) sum_ra v[Rb ra + rb] W_Ra^(ra qa),
+// roots W_R^m = tw[(N/R) m] from the length-N table.
+template <int R> constexpr int reg_ra() { return R % 4 == 0 ? 4 : (R % 2 == 0 ? 2 : (R % 3 == 0 ? 3 : 5)); }
+
+template <int R, int N, typename C>
+__device__ __forceinline__ void reg_dft(C *v, const C *tw) {
+    if constexpr (R == 2 || R == 3 || R == 4 || R == 5) {
+        butterfly<R, N>(v, tw);
+    } else if constexpr (R > 5) {
+        constexpr int Ra = reg_ra<R>(), Rb = R / Ra;
+        C u[R];
+#pragma unroll
+        for (int rb = 0; rb < Rb; rb++) {
+            C s[Ra];
+#pragma unroll
+            for (int ra = 0; ra < Ra; ra++) s[ra] = v[Rb * ra + rb];
+            reg_dft<Ra, N>(s, tw);
+#pragma unroll
+            for (int qa = 0; qa < Ra; qa++) u[rb * Ra + qa] = (rb * qa) ? cmul(s[qa], tw[(N / R) * rb * qa]) : s[qa];
+        }
+#pragma unroll
+        for (int qa = 0; qa < Ra; qa++) {
+            C s[Rb];
+#pragma unroll
+            for (int rb = 0; rb < Rb; rb++) s[rb] = u[rb * Ra + qa];
+            reg_dft<Rb, N>(s, tw);
+#pragma unroll
+            for (int qb = 0; qb < Rb; qb++) v[qa + Ra * qb] = s[qb];
+        }
+    }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ZR_T) k_fft_zr(typename C2<T>::t *__restrict__ spec,
+                                                 const typename C2<T>::t *__restrict__ tw_g, int nlines, int nh) {
+    typedef typename C2<T>::t C;
+    constexpr int R0 = zr_r0(N), R1 = zr_r1(N), G = zr_threads(N), LB = ZR_T / G, NB0 = N / R0, NB1 = N / R1;
+    constexpr int I0 = (NB0 + G - 1) / G, I1 = (NB1 + G - 1) / G, LS = N + 1;
+    static_assert(R0 * R1 == N && LB * G == ZR_T, "z transform plan");
+    __shared__ C stw[N];
+    extern __shared__ unsigned char smraw[];
+    C *buf = (C *)smraw;  // [LB][LS]: the line between the stages
+    // lines fastest across the threads: a half-warp reads 16 adjacent kx
+    const int l = threadIdx.x % LB, t = threadIdx.x / LB;
+    const long L = (long)blockIdx.x * LB + l;
+    const bool act = L < nlines;
+    long gb = 0;
+    if (act) {
+        const long j = L / nh, kx = L - j * nh;
+        gb = j * N * nh + kx;
+    }
+    // first stage: every load issued before the twiddle table is staged
+    C v[I0][R0];
+#pragma unroll
+    for (int it = 0; it < I0; it++) {
+        const int j = t + it * G;
+#pragma unroll
+        for (int r = 0; r < R0; r++) v[it][r] = (act && j < NB0) ? spec[gb + (long)(j + r * NB0) * nh] : cmk<C>(0.0, 0.0);
+    }
+    for (int e = threadIdx.x; e < N; e += ZR_T) stw[e] = tw_g[e];
+    __syncthreads();
+    if constexpr (R1 == 1) {
+        // one stage (N = R0): the DFT of the line, stored in natural order
+#pragma unroll
+        for (int it = 0; it < I0; it++) {
+            reg_dft<R0, N>(v[it], stw);
+            if (act && t + it * G < NB0) {
+#pragma unroll
+                for (int r = 0; r < R0; r++) spec[gb + (long)r * nh] = v[it][r];
+            }
+        }
+    } else {
+        C *bl = buf + l * LS;
+#pragma unroll
+        for (int it = 0; it < I0; it++) {
+            const int j = t + it * G;
+            if (j < NB0) {
+                reg_dft<R0, N>(v[it], stw);
+#pragma unroll
+                for (int r = 0; r < R0; r++) bl[j * R0 + r] = v[it][r];
+            }
+        }
+        __syncthreads();
+        // second stage (Ns = R0 = NB1, so k = j, the twiddle step is 1 and
+        // output r of butterfly j goes to j + r R0)
+#pragma unroll
+        for (int it = 0; it < I1; it++) {
+            const int j = t + it * G;
+            if (j < NB1) {
+                C w[R1];
+#pragma unroll
+                for (int r = 0; r < R1; r++) w[r] = bl[j + r * NB1];
+#pragma unroll
+                for (int r = 1; r < R1; r++) w[r] = cmul(w[r], stw[r * j]);
+                reg_dft<R1, N>(w, stw);
+                if (act) {
+#pragma unroll
+                    for (int r = 0; r < R1; r++) spec[gb + (long)(j + r * R0) * nh] = w[r];
+                }
+            }
+        }
+    }
+}
+
+template <typename T, int N>
+static size_t zr_smem() {
+    return zr_r1(N) > 1 ? (size_t)(ZR_T / zr_threads(N)) * (N + 1) * sizeof(typename C2<T>::t) : 0;
+}
+
+// ---------------------------------------------------------------------------
 // Tridiagonal solve per mode m = kz*nh + kx along j (projection.f90:90-113).
 // The matrices D(j) = Dyy(j,j) + kxx + kzz (with D(2)*1.5 for the (0,0)
 // mode) never change, so zgtsv's elimination -- pivot choices, multipliers
@@ -1134,7 +1266,10 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
     rs.rz = ctx->d_rgeo_f + ctx->rgeo_off[4];
 #define CF_FFT_SIZES(X) X(16) X(32) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
 #define CF_FWDX(N) case N: k_fwd_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP, rs); break;
-#define CF_FFTZ(N, TW) case N: k_fft_z<T, N><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, TW, (int)nlines, nh, LB); break;
+#define CF_FFTZ(N, TW) case N: \
+    if constexpr (zr_r0(N) > 0) k_fft_zr<T, N><<<cdiv(nlines, ZR_T / zr_threads(N)), ZR_T, zr_smem<T, N>(), ctx->st>>>(spec, TW, (int)nlines, nh); \
+    else k_fft_z<T, N><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, TW, (int)nlines, nh, LB); \
+    break;
 #define CF_FFTZF(N) CF_FFTZ(N, twzf)
 #define CF_FFTZB(N) CF_FFTZ(N, twzb)
 #define CF_INVX(N) case N: k_inv_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale); break;
@@ -1370,6 +1505,7 @@ static void fft_attrs_one() {
     cudaFuncSetAttribute(k_fwd_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_inv_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_fft_z<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if constexpr (zr_r0(N) > 0) cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
 }
 
 // smem opt-in for the FFT and tridiagonal kernels (called once at context creation)
