@@ -511,6 +511,240 @@ static size_t zr_smem() {
 }
 
 // ---------------------------------------------------------------------------
+// x transforms of the compile-time lengths up to 256 with the same two-stage
+// plan (the forward one with the divergence fused, projection.f90:40-87; the
+// inverse one into phi, :116-120).  The first stage of the forward transform
+// forms its R0 divergences straight from U, V, W, the second stage of the
+// inverse one stores phi directly.  A line sits in shared memory with one
+// padding element after every R0 (position x at x + x / R0): the first
+// stage's butterflies store R0 adjacent elements each, and with the padding
+// both stages' accesses fall in distinct banks.
+// ---------------------------------------------------------------------------
+template <int N> __device__ __forceinline__ int xr_pos(int x) { return x + x / zr_r0(N); }
+template <int N> constexpr int xr_ls() { return N + N / zr_r0(N); }
+
+// Forward: the divergence of the packed line pair is formed by 32 threads
+// per pair (x positions t + 32 e, every load of a thread issued before the
+// arithmetic) into the padded line, then the two register stages (the first
+// stage reads all its butterflies' inputs before any of them is stored back)
+// and the split into the two half spectra.
+constexpr int XR_FT = 32;  // threads per line pair of the forward x transform
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ZR_T) k_fwd_xr(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>::t *spec,
+                                                 const typename C2<T>::t *__restrict__ tw_g, RSp rs) {
+    typedef typename C2<T>::t C;
+    constexpr int R0 = zr_r0(N), R1 = zr_r1(N), G = XR_FT, LP = ZR_T / G, NB0 = N / R0, NB1 = N / R1;
+    constexpr int I0 = (NB0 + G - 1) / G, I1 = (NB1 + G - 1) / G, LS = xr_ls<N>(), NH = N / 2 + 1;
+    constexpr int NPT = (N + G - 1) / G, XB = NPT < 3 ? NPT : 3;
+    __shared__ C stw[N];
+    extern __shared__ unsigned char smraw[];
+    const int lp = threadIdx.x / G, t = threadIdx.x % G;
+    const int nym = g.nym, nzp = g.nzp;
+    const long pair = (long)blockIdx.x * LP + lp;
+    const bool act = pair < (long)nym * (nzp / 2);
+    int j = 2, k = 2;
+    if (act) {
+        j = (int)(pair % nym) + 2;
+        k = (int)(pair / nym) * 2 + 2;
+    }
+    C *bl = (C *)smraw + lp * LS;
+    // divergences of lines k (real part) and k+1 (imaginary part); the x and
+    // z neighbours below the first interior index through the periodic wrap
+    // (U(1) = U(nxp+1), W(k=1) = W(nzp+1))
+    const int km = k == 2 ? nzp + 1 : k - 1, k1 = k + 1;
+    if (act) {
+        T ry = T(0), rz0 = T(0), rz1 = T(0);
+        if constexpr (sizeof(T) == 4) {
+            ry = rs.ry[j];
+            rz0 = rs.rz[k];
+            rz1 = rs.rz[k + 1];
+        }
+#pragma unroll
+        for (int e0 = 0; e0 < NPT; e0 += XB) {
+            T ua[XB], uam[XB], ub[XB], ubm[XB], va[XB], vam[XB], vb[XB], vbm[XB], wa[XB], wb[XB], wm[XB];
+#pragma unroll
+            for (int b = 0; b < XB; b++) {
+                const int x = t + (e0 + b) * G, i = x + 2, im = i == 2 ? N + 1 : i - 1;
+                if (e0 + b < NPT && x < N) {
+                    ua[b] = U(i, j, k); uam[b] = U(im, j, k); ub[b] = U(i, j, k1); ubm[b] = U(im, j, k1);
+                    va[b] = V(i, j, k); vam[b] = V(i, j - 1, k); vb[b] = V(i, j, k1); vbm[b] = V(i, j - 1, k1);
+                    wa[b] = W(i, j, k); wb[b] = W(i, j, k1); wm[b] = W(i, j, km);
+                }
+            }
+#pragma unroll
+            for (int b = 0; b < XB; b++) {
+                const int x = t + (e0 + b) * G, i = x + 2;
+                if (e0 + b < NPT && x < N) {
+                    C z;
+                    if constexpr (sizeof(T) == 4) {
+                        const T rx = rs.rx[i];
+                        z.x = (ua[b] - uam[b]) * rx + (va[b] - vam[b]) * ry + (wa[b] - wm[b]) * rz0;
+                        z.y = (ub[b] - ubm[b]) * rx + (vb[b] - vbm[b]) * ry + (wb[b] - wa[b]) * rz1;
+                    } else {
+                        z.x = (ua[b] - uam[b]) / (g.x[i] - g.x[i - 1]) + (va[b] - vam[b]) / (g.y[j] - g.y[j - 1]) +
+                              (wa[b] - wm[b]) / (g.z[k] - g.z[k - 1]);
+                        z.y = (ub[b] - ubm[b]) / (g.x[i] - g.x[i - 1]) + (vb[b] - vbm[b]) / (g.y[j] - g.y[j - 1]) +
+                              (wb[b] - wa[b]) / (g.z[k1] - g.z[k1 - 1]);
+                    }
+                    bl[xr_pos<N>(x)] = z;
+                }
+            }
+        }
+    }
+    for (int e = threadIdx.x; e < N; e += ZR_T) stw[e] = tw_g[e];
+    __syncthreads();
+    // first stage: inputs jb + NB0 r, outputs jb R0 + r (read all, then store)
+    C v[I0][R0];
+#pragma unroll
+    for (int it = 0; it < I0; it++) {
+        const int jb = t + it * G;
+        if (jb < NB0) {
+#pragma unroll
+            for (int r = 0; r < R0; r++) v[it][r] = bl[xr_pos<N>(jb + NB0 * r)];
+            reg_dft<R0, N>(v[it], stw);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < I0; it++) {
+        const int jb = t + it * G;
+        if (jb < NB0) {
+#pragma unroll
+            for (int r = 0; r < R0; r++) bl[xr_pos<N>(jb * R0 + r)] = v[it][r];
+        }
+    }
+    if constexpr (R1 > 1) {
+        __syncthreads();
+        // second stage in place: butterfly jb reads and writes jb + r R0
+#pragma unroll
+        for (int it = 0; it < I1; it++) {
+            const int jb = t + it * G;
+            if (jb < NB1) {
+                C w[R1];
+#pragma unroll
+                for (int r = 0; r < R1; r++) w[r] = bl[xr_pos<N>(jb + r * R0)];
+#pragma unroll
+                for (int r = 1; r < R1; r++) w[r] = cmul(w[r], stw[r * jb]);
+                reg_dft<R1, N>(w, stw);
+#pragma unroll
+                for (int r = 0; r < R1; r++) bl[xr_pos<N>(jb + r * R0)] = w[r];
+            }
+        }
+    }
+    __syncthreads();
+    if (!act) return;
+    // the two half spectra of the packed lines: Z(q) = A(q) + i B(q)
+    C *o0 = spec + ((long)(j - 2) * nzp + (k - 2)) * NH, *o1 = spec + ((long)(j - 2) * nzp + (k - 1)) * NH;
+    for (int q = t; q < NH; q += G) {
+        const C Zk = bl[xr_pos<N>(q)], Zc = cconj(bl[xr_pos<N>((N - q) % N)]);
+        C A, B;
+        A.x = T(0.5) * (Zk.x + Zc.x);
+        A.y = T(0.5) * (Zk.y + Zc.y);
+        B.x = T(0.5) * (Zk.y - Zc.y);  // (Zk - Zc)/(2i)
+        B.y = -T(0.5) * (Zk.x - Zc.x);
+        o0[q] = A;
+        o1[q] = B;
+    }
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ZR_T) k_inv_xr(const typename C2<T>::t *__restrict__ spec, T *__restrict__ phi,
+                                                 const typename C2<T>::t *__restrict__ tw_g, int nym, int nzp, T scale) {
+    typedef typename C2<T>::t C;
+    constexpr int R0 = zr_r0(N), R1 = zr_r1(N), G = zr_threads(N), LP = ZR_T / G, NB0 = N / R0, NB1 = N / R1;
+    constexpr int I0 = (NB0 + G - 1) / G, I1 = (NB1 + G - 1) / G, LS = xr_ls<N>(), NH = N / 2 + 1;
+    __shared__ C stw[N];
+    extern __shared__ unsigned char smraw[];
+    const int lp = threadIdx.x / G, t = threadIdx.x % G;
+    const long pair = (long)blockIdx.x * LP + lp;
+    const bool act = pair < (long)nym * (nzp / 2);
+    int jj = 0, kk = 0;
+    if (act) {
+        jj = (int)(pair % nym);
+        kk = (int)(pair / nym) * 2;
+    }
+    const C *s0 = spec + ((long)jj * nzp + kk) * NH, *s1 = spec + ((long)jj * nzp + kk + 1) * NH;
+    // first stage: z(q) = A(q) + i B(q) from the two half spectra
+    // (conjugate symmetric above NH, real at q = 0 and N/2)
+    C v[I0][R0];
+#pragma unroll
+    for (int it = 0; it < I0; it++) {
+        const int jb = t + it * G;
+#pragma unroll
+        for (int r = 0; r < R0; r++) {
+            C z = cmk<C>(0.0, 0.0);
+            if (act && jb < NB0) {
+                const int q = jb + NB0 * r, src = q < NH ? q : N - q;
+                C a0 = s0[src], b0 = s1[src];
+                if (q < NH) {
+                    if (q == 0 || 2 * q == N) { a0.y = 0; b0.y = 0; }
+                } else {
+                    a0 = cconj(a0);
+                    b0 = cconj(b0);
+                }
+                z.x = a0.x - b0.y;
+                z.y = a0.y + b0.x;
+            }
+            v[it][r] = z;
+        }
+    }
+    for (int e = threadIdx.x; e < N; e += ZR_T) stw[e] = tw_g[e];
+    __syncthreads();
+    T *p0 = phi + (long)N * (jj + (long)nym * kk), *p1 = phi + (long)N * (jj + (long)nym * (kk + 1));
+    if constexpr (R1 == 1) {
+        reg_dft<R0, N>(v[0], stw);
+        if (act) {
+#pragma unroll
+            for (int r = 0; r < R0; r++) {
+                p0[r] = v[0][r].x * scale;
+                p1[r] = v[0][r].y * scale;
+            }
+        }
+    } else {
+        C *bl = (C *)smraw + lp * LS;
+#pragma unroll
+        for (int it = 0; it < I0; it++) {
+            const int jb = t + it * G;
+            if (jb < NB0) {
+                reg_dft<R0, N>(v[it], stw);
+#pragma unroll
+                for (int r = 0; r < R0; r++) bl[xr_pos<N>(jb * R0 + r)] = v[it][r];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < I1; it++) {
+            const int jb = t + it * G;
+            if (jb < NB1) {
+                C w[R1];
+#pragma unroll
+                for (int r = 0; r < R1; r++) w[r] = bl[xr_pos<N>(jb + r * R0)];
+#pragma unroll
+                for (int r = 1; r < R1; r++) w[r] = cmul(w[r], stw[r * jb]);
+                reg_dft<R1, N>(w, stw);
+                if (act) {
+#pragma unroll
+                    for (int r = 0; r < R1; r++) {
+                        p0[jb + r * R0] = w[r].x * scale;
+                        p1[jb + r * R0] = w[r].y * scale;
+                    }
+                }
+            }
+        }
+    }
+}
+
+template <typename T, int N>
+static size_t xr_smem() {
+    return zr_r1(N) > 1 ? (size_t)(ZR_T / zr_threads(N)) * xr_ls<N>() * sizeof(typename C2<T>::t) : 0;
+}
+template <typename T, int N>
+static size_t xr_fwd_smem() {
+    return (size_t)(ZR_T / XR_FT) * xr_ls<N>() * sizeof(typename C2<T>::t);
+}
+
+// ---------------------------------------------------------------------------
 // Tridiagonal solve per mode m = kz*nh + kx along j (projection.f90:90-113).
 // The matrices D(j) = Dyy(j,j) + kxx + kzz (with D(2)*1.5 for the (0,0)
 // mode) never change, so zgtsv's elimination -- pivot choices, multipliers
@@ -1265,14 +1499,20 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
     rs.ry = ctx->d_rgeo_f + ctx->rgeo_off[2];
     rs.rz = ctx->d_rgeo_f + ctx->rgeo_off[4];
 #define CF_FFT_SIZES(X) X(16) X(32) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
-#define CF_FWDX(N) case N: k_fwd_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP, rs); break;
+#define CF_FWDX(N) case N: \
+    if constexpr (zr_r0(N) > 0) k_fwd_xr<T, N><<<cdiv(npairs, ZR_T / XR_FT), ZR_T, xr_fwd_smem<T, N>(), ctx->st>>>(g, U, V, W, spec, twxf, rs); \
+    else k_fwd_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP, rs); \
+    break;
 #define CF_FFTZ(N, TW) case N: \
     if constexpr (zr_r0(N) > 0) k_fft_zr<T, N><<<cdiv(nlines, ZR_T / zr_threads(N)), ZR_T, zr_smem<T, N>(), ctx->st>>>(spec, TW, (int)nlines, nh); \
     else k_fft_z<T, N><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, TW, (int)nlines, nh, LB); \
     break;
 #define CF_FFTZF(N) CF_FFTZ(N, twzf)
 #define CF_FFTZB(N) CF_FFTZ(N, twzb)
-#define CF_INVX(N) case N: k_inv_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale); break;
+#define CF_INVX(N) case N: \
+    if constexpr (zr_r0(N) > 0) k_inv_xr<T, N><<<cdiv(npairs, ZR_T / zr_threads(N)), ZR_T, xr_smem<T, N>(), ctx->st>>>(spec, phi, twxb, nym, nzp, scale); \
+    else k_inv_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale); \
+    break;
     if (phases & POISSON_FWD) {
     // forward x (divergence fused)
     switch (nxp) {
@@ -1505,7 +1745,11 @@ static void fft_attrs_one() {
     cudaFuncSetAttribute(k_fwd_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_inv_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_fft_z<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    if constexpr (zr_r0(N) > 0) cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if constexpr (zr_r0(N) > 0) {
+        cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_fwd_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        cudaFuncSetAttribute(k_inv_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    }
 }
 
 // smem opt-in for the FFT and tridiagonal kernels (called once at context creation)
