@@ -938,93 +938,144 @@ struct TriSplit {
     int nh;
 };
 
-__device__ void tri_refined_mode(float2 *__restrict__ spec, const TriFac &f, const TriSplit &ts, int nym, long NM,
-                                 long mo, unsigned char *smraw) {
+// col(q): the mode's right-hand side / solution at row q; one warp, lane =
+// its lane; the scratch smraw holds tri_refined_smem(nym) bytes.
+// col(q): the mode's right-hand side / solution at row q; one warp, lane =
+// its lane; the scratch smraw holds tri_refined_smem(nym) bytes.
+//
+// Each FP32 replay runs across the warp as a segmented scan (lane L takes a
+// contiguous block of steps).  Forward, step k with carry c (the current
+// value of row k): no interchange keeps c in row k and carries
+// w_{k+1} - m_k c; an interchange puts w_{k+1} in row k and carries
+// c - m_k w_{k+1} -- in both cases c' = alpha c + beta, an affine map
+// (|alpha| <= 1 by the pivoting), composed per lane, scanned over the lanes
+// and replayed with the true carry.  Backward, x_q = rd_q o_q -
+// (rd du)_q x_{q+1} - (rd dl)_q x_{q+2}: the affine map of the state
+// (x_{q+1}, x_{q+2}) -> (x_q, x_{q+1}) with a 2x2 matrix, scanned the same way
+// from the last row (state 0 beyond it).
+template <typename Col>
+__device__ void tri_refined_col(Col col, const TriFac &f, const TriSplit &ts, int nym, long NM, long mo,
+                                unsigned char *smraw, int lane) {
     double *b_re = (double *)smraw, *b_im = b_re + nym, *x_re = b_im + nym, *x_im = x_re + nym;
-    float *w_re = (float *)(x_im + nym), *w_im = w_re + nym, *fm = w_im + nym, *frd = fm + nym, *fdu = frd + nym,
-          *fdl = fdu + nym;
+    float *w_re = (float *)(x_im + nym), *w_im = w_re + nym, *o_re = w_im + nym, *o_im = o_re + nym,
+          *fm = o_im + nym, *frd = fm + nym, *fdu = frd + nym, *fdl = fdu + nym;
     unsigned char *fp = (unsigned char *)(fdl + nym);
-    const int lane = threadIdx.x, nt = 32;
+    const int nt = 32;
+    const unsigned FULL = 0xffffffffu;
     const int kx = (int)(mo % ts.nh), kz = (int)(mo / ts.nh);
     const double k2 = ts.kxx[kx] + ts.kzz[kz];
     for (int q = lane; q < nym; q += nt) {
         const long o = (long)q * NM + mo;
-        const float2 v = spec[o];
+        const float2 v = col(q);
         b_re[q] = v.x;
         b_im[q] = v.y;
         x_re[q] = 0.0;
         x_im[q] = 0.0;
         w_re[q] = v.x;
         w_im[q] = v.y;
+        // back substitution coefficients scaled by 1/d; zero beyond the band
         fm[q] = (float)f.m[o];
         frd[q] = (float)f.rd[o];
-        fdu[q] = (float)f.du[o];
-        fdl[q] = (float)f.dl[o];
+        fdu[q] = q < nym - 1 ? (float)(f.rd[o] * f.du[o]) : 0.f;
+        fdl[q] = q < nym - 2 ? (float)(f.rd[o] * f.dl[o]) : 0.f;
         fp[q] = f.piv[o];
     }
     __syncwarp();
+    const int nf = nym - 1, SF = (nf + nt - 1) / nt, SB = (nym + nt - 1) / nt;
+    const int k0 = min(lane * SF, nf), k1 = min(k0 + SF, nf);
+    const int t0 = min(lane * SB, nym), t1 = min(t0 + SB, nym);
     for (int it = 0; it < 2; it++) {
-        if (lane == 0) {
-            // loads of a group of 8 rows are issued together ahead of the
-            // dependent arithmetic
-            float r0 = w_re[0], i0 = w_im[0];
-            for (int q0 = 0; q0 < nym - 1; q0 += 8) {
-                float gr[8], gi[8], gm[8];
-                unsigned char gp[8];
-#pragma unroll
-                for (int r = 0; r < 8; r++)
-                    if (q0 + r < nym - 1) {
-                        gr[r] = w_re[q0 + r + 1];
-                        gi[r] = w_im[q0 + r + 1];
-                        gm[r] = fm[q0 + r];
-                        gp[r] = fp[q0 + r];
-                    }
-#pragma unroll
-                for (int r = 0; r < 8; r++)
-                    if (q0 + r < nym - 1) {
-                        const float m = gm[r];
-                        float nre = gr[r], nim = gi[r];
-                        if (gp[r]) {
-                            w_re[q0 + r] = nre;
-                            w_im[q0 + r] = nim;
-                            nre = r0 - m * nre;
-                            nim = i0 - m * nim;
-                        } else {
-                            w_re[q0 + r] = r0;
-                            w_im[q0 + r] = i0;
-                            nre = nre - m * r0;
-                            nim = nim - m * i0;
-                        }
-                        r0 = nre;
-                        i0 = nim;
-                    }
+        // ---- forward: steps k = 0 .. nym-2, carry c_0 = w_0
+        {
+            float A = 1.f, Br = 0.f, Bi = 0.f;
+            for (int k = k0; k < k1; k++) {
+                const float m = fm[k], wr = w_re[k + 1], wi = w_im[k + 1];
+                const bool pv = fp[k] != 0;
+                const float al = pv ? 1.f : -m;
+                Br = al * Br + (pv ? -m * wr : wr);
+                Bi = al * Bi + (pv ? -m * wi : wi);
+                A = al * A;
             }
-            float x1r = r0 * frd[nym - 1], x1i = i0 * frd[nym - 1], x2r = 0.0f, x2i = 0.0f;
-            w_re[nym - 1] = x1r;
-            w_im[nym - 1] = x1i;
-            for (int q1 = nym - 2; q1 >= 0; q1 -= 8) {
-                float gr[8], gi[8], gu[8], gl[8], gd[8];
 #pragma unroll
-                for (int r = 0; r < 8; r++)
-                    if (q1 - r >= 0) {
-                        gr[r] = w_re[q1 - r];
-                        gi[r] = w_im[q1 - r];
-                        gu[r] = fdu[q1 - r];
-                        gl[r] = fdl[q1 - r];
-                        gd[r] = frd[q1 - r];
-                    }
+            for (int d = 1; d < 32; d <<= 1) {
+                const float Ap = __shfl_up_sync(FULL, A, d), Brp = __shfl_up_sync(FULL, Br, d),
+                            Bip = __shfl_up_sync(FULL, Bi, d);
+                if (lane >= d) {
+                    Br = A * Brp + Br;
+                    Bi = A * Bip + Bi;
+                    A = A * Ap;
+                }
+            }
+            const float pA = __shfl_up_sync(FULL, A, 1), pBr = __shfl_up_sync(FULL, Br, 1),
+                        pBi = __shfl_up_sync(FULL, Bi, 1);
+            const float c0r = w_re[0], c0i = w_im[0];
+            float cr = lane ? pA * c0r + pBr : c0r, ci = lane ? pA * c0i + pBi : c0i;
+            for (int k = k0; k < k1; k++) {
+                const float m = fm[k], wr = w_re[k + 1], wi = w_im[k + 1];
+                const bool pv = fp[k] != 0;
+                const float orr = pv ? wr : cr, oi = pv ? wi : ci;
+                o_re[k] = orr;
+                o_im[k] = oi;
+                cr = (pv ? cr : wr) - m * orr;
+                ci = (pv ? ci : wi) - m * oi;
+            }
+            if (k1 == nf && k0 < k1) {  // the lane with the last step
+                o_re[nf] = cr;
+                o_im[nf] = ci;
+            }
+            if (nf == 0 && lane == 0) {
+                o_re[0] = c0r;
+                o_im[0] = c0i;
+            }
+        }
+        __syncwarp();
+        // ---- backward: steps t = 0 .. nym-1 on rows q = nym-1-t
+        {
+            float m00 = 1.f, m01 = 0.f, m10 = 0.f, m11 = 1.f, v0r = 0.f, v0i = 0.f, v1r = 0.f, v1i = 0.f;
+            for (int t = t0; t < t1; t++) {
+                const int q = nym - 1 - t;
+                const float a = fdu[q], bq = fdl[q], r = frd[q];
+                const float n00 = -a * m00 - bq * m10, n01 = -a * m01 - bq * m11;
+                m10 = m00;
+                m11 = m01;
+                m00 = n00;
+                m01 = n01;
+                const float u0r = -a * v0r - bq * v1r + r * o_re[q], u0i = -a * v0i - bq * v1i + r * o_im[q];
+                v1r = v0r;
+                v1i = v0i;
+                v0r = u0r;
+                v0i = u0i;
+            }
 #pragma unroll
-                for (int r = 0; r < 8; r++)
-                    if (q1 - r >= 0) {
-                        const float yr = (gr[r] - gu[r] * x1r - gl[r] * x2r) * gd[r];
-                        const float yi = (gi[r] - gu[r] * x1i - gl[r] * x2i) * gd[r];
-                        w_re[q1 - r] = yr;
-                        w_im[q1 - r] = yi;
-                        x2r = x1r;
-                        x2i = x1i;
-                        x1r = yr;
-                        x1i = yi;
-                    }
+            for (int d = 1; d < 32; d <<= 1) {
+                const float p00 = __shfl_up_sync(FULL, m00, d), p01 = __shfl_up_sync(FULL, m01, d),
+                            p10 = __shfl_up_sync(FULL, m10, d), p11 = __shfl_up_sync(FULL, m11, d);
+                const float q0r = __shfl_up_sync(FULL, v0r, d), q0i = __shfl_up_sync(FULL, v0i, d),
+                            q1r = __shfl_up_sync(FULL, v1r, d), q1i = __shfl_up_sync(FULL, v1i, d);
+                if (lane >= d) {
+                    // (M, v) after (P, p): (M P, M p + v)
+                    const float n0r = m00 * q0r + m01 * q1r + v0r, n0i = m00 * q0i + m01 * q1i + v0i;
+                    const float n1r = m10 * q0r + m11 * q1r + v1r, n1i = m10 * q0i + m11 * q1i + v1i;
+                    const float a00 = m00 * p00 + m01 * p10, a01 = m00 * p01 + m01 * p11;
+                    const float a10 = m10 * p00 + m11 * p10, a11 = m10 * p01 + m11 * p11;
+                    m00 = a00; m01 = a01; m10 = a10; m11 = a11;
+                    v0r = n0r; v0i = n0i; v1r = n1r; v1i = n1i;
+                }
+            }
+            // carry in: the state after the lanes before (from state 0)
+            const float s0r = __shfl_up_sync(FULL, v0r, 1), s0i = __shfl_up_sync(FULL, v0i, 1),
+                        s1r = __shfl_up_sync(FULL, v1r, 1), s1i = __shfl_up_sync(FULL, v1i, 1);
+            float x1r = lane ? s0r : 0.f, x1i = lane ? s0i : 0.f, x2r = lane ? s1r : 0.f, x2i = lane ? s1i : 0.f;
+            for (int t = t0; t < t1; t++) {
+                const int q = nym - 1 - t;
+                const float a = fdu[q], bq = fdl[q], r = frd[q];
+                const float yr = (r * o_re[q] - bq * x2r) - a * x1r, yi = (r * o_im[q] - bq * x2i) - a * x1i;
+                w_re[q] = yr;
+                w_im[q] = yi;
+                x2r = x1r;
+                x2i = x1i;
+                x1r = yr;
+                x1i = yi;
             }
         }
         __syncwarp();
@@ -1052,10 +1103,12 @@ __device__ void tri_refined_mode(float2 *__restrict__ spec, const TriFac &f, con
         }
         __syncwarp();
     }
-    for (int q = lane; q < nym; q += nt) spec[(long)q * NM + mo] = make_float2((float)x_re[q], (float)x_im[q]);
+    for (int q = lane; q < nym; q += nt) col(q) = make_float2((float)x_re[q], (float)x_im[q]);
 }
 
-static size_t tri_refined_smem(int nym) { return (size_t)nym * (4 * sizeof(double) + 6 * sizeof(float) + 1); }
+__host__ __device__ static inline size_t tri_refined_smem(int nym) {
+    return (size_t)nym * (4 * sizeof(double) + 8 * sizeof(float) + 1);
+}
 
 // Bulk modes: the no-pivot replay y_j = b_j - m_{j-1} y_{j-1},
 // x_j = (y_j - du_j x_{j+1}) rd_j split over P = blockDim.y segments of
@@ -1164,24 +1217,31 @@ __device__ void tri_bulk_segmented(float2 *__restrict__ spec, const TriSplit &ts
     }
 }
 
-// Blocks 0..nlist-1: one pivoting mode each (the threadIdx.y == 0 warp);
-// blocks nlist..: 32 bulk modes x P segments of RS rows.
+// The split-path solve as two launches: the pivoting modes on the side
+// stream, up to TRI_PW warps (modes) per block -- one per SM sub-partition,
+// so that their FP64 residuals use different FP64 pipes -- beside the bulk
+// modes on the main stream.
+constexpr int TRI_PW = 4;
+constexpr size_t TRI_PIVOT_SMEM = 96 * 1024;  // shared memory of a pivoting block at most
+__global__ void __launch_bounds__(32 * TRI_PW) k_tri_pivot(float2 *__restrict__ spec, TriFac f, TriSplit ts, int nym,
+                                                           long NM) {
+    extern __shared__ unsigned char tpv[];
+    const int w = threadIdx.y, e = blockIdx.x * blockDim.y + w;
+    if (e >= ts.nlist) return;
+    const long mo = ts.list[e];
+    auto col = [&](int q) -> float2 & { return spec[(long)q * NM + mo]; };
+    tri_refined_col(col, f, ts, nym, NM, mo, tpv + (size_t)w * ((tri_refined_smem(nym) + 15) & ~(size_t)15),
+                    (int)threadIdx.x);
+}
+
 template <int RS>
-__global__ void __launch_bounds__(512) k_tri_split(float2 *__restrict__ spec, TriFac f, TriSplit ts, int nym, long NM) {
+__global__ void __launch_bounds__(512) k_tri_bulk(float2 *__restrict__ spec, TriSplit ts, int nym, long NM) {
     extern __shared__ float2 t32[];
-    if ((int)blockIdx.x < ts.nlist) {
-        if (threadIdx.y == 0) tri_refined_mode(spec, f, ts, nym, NM, ts.list[blockIdx.x], (unsigned char *)t32);
-        return;
-    }
-    tri_bulk_segmented<RS>(spec, ts, nym, NM, blockIdx.x - ts.nlist, (unsigned char *)t32);
+    tri_bulk_segmented<RS>(spec, ts, nym, NM, blockIdx.x, (unsigned char *)t32);
 }
 
 // rows per segment: 16 up to 256 rows (at most 16 segments), else 32
 static int tri_split_rs(int nym) { return nym <= 256 ? 16 : 32; }
-static size_t tri_split_smem(int nym) {
-    const int P = (nym + tri_split_rs(nym) - 1) / tri_split_rs(nym);
-    return std::max((size_t)P * 32 * 12, tri_refined_smem(nym));
-}
 
 // ---------------------------------------------------------------------------
 // Inverse x: two half spectra -> one complex sequence -> FFT (+) -> real
@@ -1553,10 +1613,26 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
         ts.nh = nh;
         const int rs = tri_split_rs(nym);
         const dim3 tb(32, (nym + rs - 1) / rs);
-        const unsigned nb = (unsigned)(ts.nlist + cdiv(NM, 32));
-        if (rs == 16) k_tri_split<16><<<nb, tb, tri_split_smem(nym), ctx->st>>>((float2 *)spec, tf, ts, nym, NM);
-        else k_tri_split<32><<<nb, tb, tri_split_smem(nym), ctx->st>>>((float2 *)spec, tf, ts, nym, NM);
-        count_launch(ctx, "k_tri_split");
+        // the pivoting modes on the side stream, forked from the main one
+        // and joined back after the bulk launch (they write other modes)
+        const bool side = ts.nlist > 0;
+        if (side) {
+            CF_CUDA(cudaEventRecord(ctx->ev_fork, ctx->st));
+            CF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+            const size_t per = (tri_refined_smem(nym) + 15) & ~(size_t)15;
+            const int pw = (int)std::max<size_t>(1, std::min<size_t>(TRI_PW, TRI_PIVOT_SMEM / per));
+            k_tri_pivot<<<cdiv(ts.nlist, pw), dim3(32, pw), pw * per, ctx->side>>>((float2 *)spec, tf, ts, nym, NM);
+            CF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
+        }
+        const unsigned nb = (unsigned)cdiv(NM, 32);
+        const size_t sb = (size_t)tb.y * 32 * 12;
+        if (rs == 16) k_tri_bulk<16><<<nb, tb, sb, ctx->st>>>((float2 *)spec, ts, nym, NM);
+        else k_tri_bulk<32><<<nb, tb, sb, ctx->st>>>((float2 *)spec, ts, nym, NM);
+        count_launch(ctx, "k_tri_bulk");
+        if (side) {
+            CF_CUDA(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
+            count_launch(ctx, "k_tri_pivot");  // its event: the wait beyond the bulk launch
+        }
     } else {
         k_tri_mode<T><<<(unsigned)NM, 32, tri_mode_smem(nym), ctx->st>>>(spec, tf, nym, NM, nullptr);
         count_launch(ctx, "k_tri_mode");
@@ -1746,14 +1822,16 @@ static void fft_attrs_one() {
     cudaFuncSetAttribute(k_inv_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_fft_z<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     if constexpr (zr_r0(N) > 0) {
-        cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_fwd_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-        cudaFuncSetAttribute(k_inv_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        // exactly what the launches request (up to 110 KB: FP64, length 96)
+        cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zr_smem<T, N>());
+        cudaFuncSetAttribute(k_fwd_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xr_fwd_smem<T, N>());
+        cudaFuncSetAttribute(k_inv_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xr_smem<T, N>());
     }
 }
 
 // smem opt-in for the FFT and tridiagonal kernels (called once at context creation)
 int fft_setup_attrs() {
+    cudaFuncSetAttribute(k_tri_pivot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_PIVOT_SMEM);
 #define CF_ATTRS(N) fft_attrs_one<double, N>(); fft_attrs_one<float, N>();
     CF_FFT_SIZES(CF_ATTRS)
     CF_ATTRS(0)
