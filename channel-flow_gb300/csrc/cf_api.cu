@@ -403,9 +403,6 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
     *out = ctx;
     CF_CUDA(cudaSetDevice(device));
     CF_CUDA(cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking));
-    CF_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
-    CF_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-    CF_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
 
     // host geometry, 1-based
     ctx->hx.assign(nx + 2, 0.0); ctx->hy.assign(ny + 2, 0.0); ctx->hz.assign(nz + 2, 0.0);
@@ -588,9 +585,6 @@ extern "C" int cf_destroy(cf_ctx *ctx) {
             if (ctx->F[b][c]) cudaFree(ctx->F[b][c]);
     }
     if (ctx->st) cudaStreamDestroy(ctx->st);
-    if (ctx->side) cudaStreamDestroy(ctx->side);
-    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
-    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     delete ctx;
     return CF_OK;
 }

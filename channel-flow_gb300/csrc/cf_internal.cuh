@@ -167,10 +167,6 @@ struct cf_ctx {
     int nx, ny, nz, nxg, nyg, nzg, nxp, nym, nzp, nxh;
     size_t nU, nV, nW, nC, nCan, nSpec;
     cudaStream_t st = nullptr;
-    // a second stream forked from st (and joined back) for work that runs
-    // beside a kernel of st: the pivoting modes' tridiagonal solves
-    cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
 
     // host geometry (1-based vectors)

@@ -1217,27 +1217,26 @@ __device__ void tri_bulk_segmented(float2 *__restrict__ spec, const TriSplit &ts
     }
 }
 
-// The split-path solve as two launches: the pivoting modes on the side
-// stream, up to TRI_PW warps (modes) per block -- one per SM sub-partition,
-// so that their FP64 residuals use different FP64 pipes -- beside the bulk
-// modes on the main stream.
-constexpr int TRI_PW = 4;
-constexpr size_t TRI_PIVOT_SMEM = 96 * 1024;  // shared memory of a pivoting block at most
-__global__ void __launch_bounds__(32 * TRI_PW) k_tri_pivot(float2 *__restrict__ spec, TriFac f, TriSplit ts, int nym,
-                                                           long NM) {
-    extern __shared__ unsigned char tpv[];
-    const int w = threadIdx.y, e = blockIdx.x * blockDim.y + w;
-    if (e >= ts.nlist) return;
-    const long mo = ts.list[e];
-    auto col = [&](int q) -> float2 & { return spec[(long)q * NM + mo]; };
-    tri_refined_col(col, f, ts, nym, NM, mo, tpv + (size_t)w * ((tri_refined_smem(nym) + 15) & ~(size_t)15),
-                    (int)threadIdx.x);
-}
-
+// The split-path solve in one launch: blocks 0 .. npb-1 solve the pivoting
+// modes, one per warp (pw warps per block), their replays warp-wide so that
+// they finish within the first wave of the bulk blocks; the remaining blocks
+// take 32 bulk modes x P segments of RS rows each.
+constexpr size_t TRI_SPLIT_SMEM = 96 * 1024;  // shared memory of a block at most
 template <int RS>
-__global__ void __launch_bounds__(512) k_tri_bulk(float2 *__restrict__ spec, TriSplit ts, int nym, long NM) {
+__global__ void __launch_bounds__(512) k_tri_split(float2 *__restrict__ spec, TriFac f, TriSplit ts, int nym, long NM,
+                                                   int npb, int pw) {
     extern __shared__ float2 t32[];
-    tri_bulk_segmented<RS>(spec, ts, nym, NM, blockIdx.x, (unsigned char *)t32);
+    if ((int)blockIdx.x < npb) {
+        const int w = threadIdx.y, e = blockIdx.x * pw + w;
+        if (w >= pw || e >= ts.nlist) return;
+        const long mo = ts.list[e];
+        auto col = [&](int q) -> float2 & { return spec[(long)q * NM + mo]; };
+        tri_refined_col(col, f, ts, nym, NM, mo,
+                        (unsigned char *)t32 + (size_t)w * ((tri_refined_smem(nym) + 15) & ~(size_t)15),
+                        (int)threadIdx.x);
+        return;
+    }
+    tri_bulk_segmented<RS>(spec, ts, nym, NM, blockIdx.x - npb, (unsigned char *)t32);
 }
 
 // rows per segment: 16 up to 256 rows (at most 16 segments), else 32
@@ -1613,26 +1612,15 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
         ts.nh = nh;
         const int rs = tri_split_rs(nym);
         const dim3 tb(32, (nym + rs - 1) / rs);
-        // the pivoting modes on the side stream, forked from the main one
-        // and joined back after the bulk launch (they write other modes)
-        const bool side = ts.nlist > 0;
-        if (side) {
-            CF_CUDA(cudaEventRecord(ctx->ev_fork, ctx->st));
-            CF_CUDA(cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
-            const size_t per = (tri_refined_smem(nym) + 15) & ~(size_t)15;
-            const int pw = (int)std::max<size_t>(1, std::min<size_t>(TRI_PW, TRI_PIVOT_SMEM / per));
-            k_tri_pivot<<<cdiv(ts.nlist, pw), dim3(32, pw), pw * per, ctx->side>>>((float2 *)spec, tf, ts, nym, NM);
-            CF_CUDA(cudaEventRecord(ctx->ev_join, ctx->side));
-        }
-        const unsigned nb = (unsigned)cdiv(NM, 32);
-        const size_t sb = (size_t)tb.y * 32 * 12;
-        if (rs == 16) k_tri_bulk<16><<<nb, tb, sb, ctx->st>>>((float2 *)spec, ts, nym, NM);
-        else k_tri_bulk<32><<<nb, tb, sb, ctx->st>>>((float2 *)spec, ts, nym, NM);
-        count_launch(ctx, "k_tri_bulk");
-        if (side) {
-            CF_CUDA(cudaStreamWaitEvent(ctx->st, ctx->ev_join, 0));
-            count_launch(ctx, "k_tri_pivot");  // its event: the wait beyond the bulk launch
-        }
+        const int P = (int)tb.y;
+        const size_t per = (tri_refined_smem(nym) + 15) & ~(size_t)15, sb = (size_t)P * 32 * 12;
+        const int pw = (int)std::max<size_t>(1, std::min<size_t>(P, TRI_SPLIT_SMEM / per));
+        const int npb = cdiv(ts.nlist, pw);
+        const size_t sm = std::max(sb, ts.nlist > 0 ? pw * per : 0);
+        const unsigned nb = (unsigned)(npb + cdiv(NM, 32));
+        if (rs == 16) k_tri_split<16><<<nb, tb, sm, ctx->st>>>((float2 *)spec, tf, ts, nym, NM, npb, pw);
+        else k_tri_split<32><<<nb, tb, sm, ctx->st>>>((float2 *)spec, tf, ts, nym, NM, npb, pw);
+        count_launch(ctx, "k_tri_split");
     } else {
         k_tri_mode<T><<<(unsigned)NM, 32, tri_mode_smem(nym), ctx->st>>>(spec, tf, nym, NM, nullptr);
         count_launch(ctx, "k_tri_mode");
@@ -1831,7 +1819,8 @@ static void fft_attrs_one() {
 
 // smem opt-in for the FFT and tridiagonal kernels (called once at context creation)
 int fft_setup_attrs() {
-    cudaFuncSetAttribute(k_tri_pivot, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_PIVOT_SMEM);
+    cudaFuncSetAttribute(k_tri_split<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_SPLIT_SMEM);
+    cudaFuncSetAttribute(k_tri_split<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TRI_SPLIT_SMEM);
 #define CF_ATTRS(N) fft_attrs_one<double, N>(); fft_attrs_one<float, N>();
     CF_FFT_SIZES(CF_ATTRS)
     CF_ATTRS(0)
