@@ -531,7 +531,7 @@ def run_ensemble(args, rank, world, local):
     value = world * nc * args.steps / (ms / 1e3)
     # the same ensemble with every kernel in the members' branches (no
     # batched stencil launches), for comparison
-    ens_b = cf.Ensemble(chans, batched_tri=True, batched_stencils=False)
+    ens_b = cf.Ensemble(chans, batched_tri=False, batched_stencils=False)
     ens_b.step(args.warmup)
     strm_b = torch.cuda.ExternalStream(ens_b.stream(), device=torch.device("cuda", dev))
     torch.cuda.synchronize()
@@ -593,10 +593,12 @@ def run_ensemble(args, rank, world, local):
             "vs_baseline": None, "dtype": "f32+f64 (split)", "data": "synthetic (16 seeded perturbed laminar fields)",
             "config": {"workload": ENSEMBLE["name"], "members": len(chans), "grid_points": nc,
                        "retau": [m[1] for m in mem], "precision": "split",
-                       "graph": ("one CUDA graph per ensemble step: the tridiagonal systems of all members in "
-                                 "one FP64 launch per substep; " +
+                       "graph": ("one CUDA graph per ensemble step: " +
+                                 ("the tridiagonal systems of all members in one FP64 launch per substep; "
+                                  if ens_tuned and "batched FP64" in ens_tuned["choice"] else
+                                  "each member's tridiagonal solves in its branch; ") +
                                  ("every other kernel in a branch per member"
-                                  if ens_tuned and ens_tuned["choice"] == "branches" else
+                                  if ens_tuned and ens_tuned["choice"].startswith("branches") else
                                   "the fused DSM passes and fused right-hand sides of all members as one launch "
                                   "each per substep, the other kernels in a branch per member") +
                                  " (chosen by cf_ensemble_autotune)"),
@@ -605,7 +607,8 @@ def run_ensemble(args, rank, world, local):
                        "l2": "members' working set (~2.5 GB) larger than L2; no flush needed"},
             "ensemble_autotune": ens_tuned,
             "branches_only": {"value": world * nc * args.steps / (ms_b / 1e3), "ms_per_step": ms_b / args.steps,
-                              "how": "the same ensemble graph with every kernel in the members' branches"},
+                              "how": "the same ensemble graph with every kernel (tridiagonal solves included) "
+                                     "in the members' branches"},
             "sequential_members": {"value": world * nc * args.steps / seq, "ms_per_step": 1e3 * seq / args.steps,
                                    "how": "each member's own graph, one member after another"},
             "ensemble_over_sequential": (world * nc * args.steps / seq and value / (world * nc * args.steps / seq)),

@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(PKG, "libchannel_gpu.so")
 HEADER = os.path.join(ROOT, "include", "channel_gpu.h")
 
 PREC_FP64, PREC_SPLIT = 0, 1
+ENS_TUNE_CANDIDATES = 8  # CF_ENS_TUNE_CANDIDATES
 
 
 class CfParams(C.Structure):
@@ -479,14 +480,17 @@ class Ensemble:
     def autotune(self, steps: int = 3) -> dict:
         """cf_ensemble_autotune: times whole ensemble steps with every kernel
         in the members' branches and with the batched stencil launches (three
-        z-chunk plans) and keeps the fastest; the ensemble advances."""
+        z-chunk plans), each with the members' own tridiagonal solves and with
+        one FP64 launch for all of them, and keeps the fastest; the ensemble
+        advances ENS_TUNE_CANDIDATES * (steps + 1) steps."""
         self.L.cf_ensemble_autotune.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]
-        rep = np.zeros(4)
+        rep = np.zeros(ENS_TUNE_CANDIDATES)
         ch = C.c_int()
         rc = self.L.cf_ensemble_autotune(self.h, steps, _dp(rep), C.byref(ch))
         if rc != 0:
             raise CfError(self.L.cf_last_error(None).decode() or f"cf_ensemble_autotune failed ({rc})")
-        names = ["branches", "batched, member plans", "batched, one z chunk", "batched, two z chunks"]
+        modes = ["branches", "batched, member plans", "batched, one z chunk", "batched, two z chunks"]
+        names = [f"{m}; {t}" for t in ("own tridiagonal solves", "batched FP64 tridiagonal") for m in modes]
         return dict(choice=names[ch.value], ms_per_step=dict(zip(names, rep.tolist())))
 
     def step(self, nsteps: int = 1, sync: bool = True):

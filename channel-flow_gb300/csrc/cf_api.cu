@@ -1751,11 +1751,11 @@ extern "C" int cf_ensemble_autotune(cf_ensemble *e, int steps, double *report, i
         for (int q = 0; q < n; q++) {
             cf_ctx *c = e->m[q];
             const int lo_rhs = cdiv(c->nzp, RHS_ZMAX_HOST), lo_dsm = cdiv(c->nzp, DSM_ZMAX_HOST);
-            if (cand <= 1) {
+            if ((cand & 3) <= 1) {
                 c->dsm_kc = kc0[q];
                 c->rhs_nkc = nkc0[q];
             } else {
-                const int parts = cand == 2 ? 1 : 2;
+                const int parts = (cand & 3) == 2 ? 1 : 2;
                 c->dsm_kc = cdiv(c->nzp, std::max(parts, lo_dsm));
                 c->rhs_nkc = std::max(parts, lo_rhs);
             }
@@ -1767,14 +1767,15 @@ extern "C" int cf_ensemble_autotune(cf_ensemble *e, int steps, double *report, i
         }
         for (auto &kv : e->graphs) cudaGraphExecDestroy(kv.second.first);
         e->graphs.clear();
-        e->batched_stencils = cand >= 1 && n <= CF_ENS_MAXM;
+        e->batched_stencils = (cand & 3) >= 1 && n <= CF_ENS_MAXM;
+        e->batched_tri = cand >= 4;
     };
     cudaEvent_t a, b;
     ENS_CUDA(cudaEventCreate(&a));
     ENS_CUDA(cudaEventCreate(&b));
-    double ms[4] = {0, 0, 0, 0};
+    double ms[CF_ENS_TUNE_CANDIDATES] = {};
     int best = 0;
-    for (int cand = 0; cand < 4; cand++) {
+    for (int cand = 0; cand < CF_ENS_TUNE_CANDIDATES; cand++) {
         apply(cand);
         int rc = cf_ensemble_step(e, 1, 1);
         float t = 0.f;
@@ -1796,7 +1797,7 @@ extern "C" int cf_ensemble_autotune(cf_ensemble *e, int steps, double *report, i
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     apply(best);
-    if (report) std::copy(ms, ms + 4, report);
+    if (report) std::copy(ms, ms + CF_ENS_TUNE_CANDIDATES, report);
     if (choice) *choice = best;
     return CF_OK;
 }

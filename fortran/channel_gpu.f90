@@ -33,6 +33,7 @@ Module channel_gpu
   Integer(c_int), Parameter :: CF_PREC_FP64 = 0, CF_PREC_SPLIT = 1
   Integer(c_int), Parameter :: CF_MLP_NPARAM = 4481
   Integer(c_int), Parameter :: CF_NOALLOC_MAX_PLANES = 4096
+  Integer(c_int), Parameter :: CF_ENS_TUNE_CANDIDATES = 8
 
   ! the scalars of read_input_parameters (input_output.f90:21-133) plus the
   ! library's options; field order and kinds are those of the C struct

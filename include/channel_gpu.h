@@ -325,14 +325,18 @@ int cf_ensemble_set_batched_tri(cf_ensemble *e, int on);
  * other kernels stay in the members' branches.  0: every kernel in the
  * members' branches. */
 int cf_ensemble_set_batched_stencils(cf_ensemble *e, int on);
-/* Empirical choice of how the ensemble runs its stencil passes: one whole
- * ensemble step per candidate captures its graph, then `steps` steps are
- * timed (CUDA events) for (0) every kernel in the members' branches with
- * each member's own z-chunk plan, and the batched DSM / right-hand-side
- * launches with (1) the members' plans, (2) one z chunk per member, (3) two;
- * the fastest is kept.  The ensemble advances 4 (steps + 1) steps.
- * report (4 doubles, may be NULL): ms per step of each candidate; choice
- * (may be NULL): the one kept. */
+/* Empirical choice of how the ensemble runs its stencil passes and its
+ * tridiagonal solves: one whole ensemble step per candidate captures its
+ * graph, then `steps` steps are timed (CUDA events).  Candidates 0-3: each
+ * member solves its own tridiagonal systems (as cf_time_step_rk3); 4-7: one
+ * FP64 launch for all members' systems.  Within each group: (+0) every
+ * kernel in the members' branches with each member's own z-chunk plan, and
+ * the batched DSM / right-hand-side launches with (+1) the members' plans,
+ * (+2) one z chunk per member, (+3) two.  The fastest is kept.  The ensemble
+ * advances CF_ENS_TUNE_CANDIDATES (steps + 1) steps.  report
+ * (CF_ENS_TUNE_CANDIDATES doubles, may be NULL): ms per step of each
+ * candidate; choice (may be NULL): the one kept. */
+enum { CF_ENS_TUNE_CANDIDATES = 8 };
 int cf_ensemble_autotune(cf_ensemble *e, int steps, double *report, int *choice);
 
 /* ---- divergence check without device allocation ---------------------- */

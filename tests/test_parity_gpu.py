@@ -651,7 +651,7 @@ def test_ensemble_autotune_keeps_a_valid_choice():
     rep = ens.autotune(steps=2)
     assert rep["choice"] in rep["ms_per_step"] and all(v > 0 for v in rep["ms_per_step"].values())
     ens.step(3)
-    done = 1 + 4 * 3 + 3
+    done = 1 + cf.ENS_TUNE_CANDIDATES * 3 + 3
     for m, case in zip(members, cases):
         ref = make(case)
         ref.time_step_rk3(done)
