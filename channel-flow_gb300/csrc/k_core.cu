@@ -507,11 +507,13 @@ struct NutSrc {
 
 // planes per z chunk of the fused RHS (its z spacings sit in shared memory)
 constexpr int RHS_ZMAX = RHS_ZMAX_HOST;
-// resident blocks per SM the fused RHS is compiled for: two (128 registers).
-// With u, v and w computed before any store, the shared-memory reads common
-// to them are issued once but more values stay live: at three blocks (80
-// registers) the FP32 kernel spills and runs 25 % slower.
-template <typename T> struct RhsMinB { static constexpr int v = 2; };
+// resident blocks per SM the fused RHS is compiled for.  With u, v and w
+// computed before any store, the shared-memory reads common to them are
+// issued once but more values stay live; with the per-thread index and mask
+// set-up hoisted out of the march and the substep and low words compile-time,
+// the FP32 kernel fits three blocks of 256 threads (85 registers): 24 warps
+// per SM instead of 16, 133 -> 105 us per launch at Re_tau 550.  FP64 keeps two.
+template <typename T> struct RhsMinB { static constexpr int v = sizeof(T) == 4 ? 3 : 2; };
 
 // Everything one launch of the fused right-hand side needs for one channel
 // (the grid of blocks is ntx x nty x nkc).
@@ -527,9 +529,40 @@ struct Rhs3Args {
     Trio<T> out, F1, Uo, Uolo, Unlo;
 };
 
+// The RK update of one point for substep S (time_integration.f90:108-145):
+// S = 1 stores the right-hand side as F1; LO: the split path's low words
+// (u^n = hi + lo; substep 3 stores the new state as hi + lo, the others the
+// rounded sum).  o: the point's index, the same in every field of its
+// component.
+template <typename T, int S, bool LO>
+__device__ __forceinline__ void rk_apply_at(T r, T f1, T uo, T uolo, int o, T *out, T *F1, T *Unlo, T ca, T cb, T dt) {
+    T inc;
+    if constexpr (S == 1) {
+        F1[o] = r;
+        inc = dt * ca * r;
+    } else {
+        inc = dt * (ca * f1 + cb * r);
+    }
+    if constexpr (sizeof(T) == 4 && LO) {
+        float hi = uo, lo = uolo;
+        if constexpr (S == 3) {
+            ff_add(hi, lo, inc);
+            out[o] = hi;
+            Unlo[o] = lo;
+        } else {
+            out[o] = hi + (lo + inc);
+        }
+    } else {
+        out[o] = uo + inc;
+    }
+}
+
 // The tile (bx, by, bz) of one channel: a block of the single-channel launch
-// or of the ensemble launch (k_rhs3_batch below).
-template <typename T, int TX, int TY>
+// or of the ensemble launch (k_rhs3_batch below), for substep S (LO: low
+// words of u^n present).  Every per-point index is formed once per thread
+// (the (i, j) part, planes follow by adding the plane stride), the ring's
+// loads are predicated by masks fixed for the march.
+template <typename T, int TX, int TY, int S, bool LO>
 __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int by, int bz) {
     const GeoT<T> g = args.g;
     const RcpT<T> rc = args.rc;
@@ -537,7 +570,7 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
     const NutSrc<T> ns = args.ns;
     const DevScal *const ds = args.ds;
     const T nu = args.nu, Om = args.Om, ca = args.ca, cb = args.cb;
-    const int rot = args.rot, s = args.s, kc_len = args.kc_len, ilim = args.ilim, klim = args.klim;
+    const int rot = args.rot, kc_len = args.kc_len, ilim = args.ilim, klim = args.klim;
     const Trio<T> out = args.out, F1 = args.F1, Uo = args.Uo, Uolo = args.Uolo, Unlo = args.Unlo;
     constexpr int SX = TX + 2, SY = TY + 2, NP = SX * SY, NT = TX * TY, NL = (NP + NT - 1) / NT;
     __shared__ T ring[3][4][NP];  // [plane slot][field U V W nu_t][tile]
@@ -579,7 +612,6 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
     rcs.dz = gzs[0] - kb;
     rcs.dzg = gzs[1] - kb;
     const bool du = i <= nx - 1 && j <= nyg - 1, dv = i <= ilim && j <= ny - 1, dw = i <= ilim && j <= nyg - 1;
-    const bool lo = Uolo.u.p != nullptr;
     // this thread's tile elements (same for every plane and field)
     int eia[NL], eja[NL], erem[NL];
 #pragma unroll
@@ -607,19 +639,34 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
             nbase[q] = ok ? (wrapn(ia, ns.nxp) - 2) + ns.nxp * (jj - 2) : 0;
         }
     }
-    // all loads of one plane are issued before any of them is used
+    // all loads of one plane are issued before any of them is used; the
+    // (i, j) part of every element's index and its in-field mask are fixed
+    int oU[NL], oV[NL], oW[NL], oN[NL];
+    bool mU[NL], mV[NL], mW[NL], mN[NL];
+#pragma unroll
+    for (int q = 0; q < NL; q++) {
+        const int ia = eia[q], ja = eja[q];
+        const bool in = erem[q] < NP;
+        mU[q] = in && ia <= nx && ja <= nyg;
+        mV[q] = in && ia <= nxg && ja <= ny;
+        mW[q] = in && ia <= nxg && ja <= nyg;
+        mN[q] = ns.S ? nsg[q] != T(0) : mW[q];
+        oU[q] = mU[q] ? U.idx(ia, ja, 0) : 0;
+        oV[q] = mV[q] ? V.idx(ia, ja, 0) : 0;
+        oW[q] = mW[q] ? W.idx(ia, ja, 0) : 0;
+        oN[q] = ns.S ? nbase[q] : (mW[q] ? nt.idx(ia, ja, 0) : 0);
+    }
     T pre[4][NL];
     auto fetch = [&](int k) {
-        const long koff = nplane * (wrapn(k, ns.nzp) - 2);
+        const bool kz = k <= nzg, kw = k <= nz;
+        const int koff = ns.S ? (int)(nplane * (wrapn(k, ns.nzp) - 2)) : k * nt.sz;
+        const T *Np = ns.S ? ns.S : nt.p;
 #pragma unroll
         for (int q = 0; q < NL; q++) {
-            const int ia = eia[q], ja = eja[q];
-            const bool in = erem[q] < NP;
-            pre[0][q] = (in && ia <= nx && ja <= nyg && k <= nzg) ? U(ia, ja, k) : T(0);
-            pre[1][q] = (in && ia <= nxg && ja <= ny && k <= nzg) ? V(ia, ja, k) : T(0);
-            pre[2][q] = (in && ia <= nxg && ja <= nyg && k <= nz) ? W(ia, ja, k) : T(0);
-            if (ns.S) pre[3][q] = (nsg[q] != T(0) && k <= nzg) ? ns.S[nbase[q] + koff] : T(0);  // |S|, formed at commit
-            else pre[3][q] = (in && ia <= nxg && ja <= nyg && k <= nzg) ? nt(ia, ja, k) : T(0);
+            pre[0][q] = (mU[q] && kz) ? U.p[oU[q] + k * U.sz] : T(0);
+            pre[1][q] = (mV[q] && kz) ? V.p[oV[q] + k * V.sz] : T(0);
+            pre[2][q] = (mW[q] && kw) ? W.p[oW[q] + k * W.sz] : T(0);
+            pre[3][q] = (mN[q] && kz) ? Np[oN[q] + koff] : T(0);  // |S| (formed at commit) or nu_t
         }
     };
     auto commit = [&](int slot) {
@@ -647,15 +694,19 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
     // the ring slots of planes k-1, k, k+1 rotate at run time: one copy of
     // the plane's code (a march unrolled by three, with compile-time slots,
     // triples the code of this large loop body and ran 5 % slower)
+    const int bu = out.u.idx(i, j, 0), bv = out.v.idx(i, j, 0), bw = out.w.idx(i, j, 0);
+    const int szu = out.u.sz, szv = out.v.sz, szw = out.w.sz;
     int sm1 = 0, s0 = 1, sp1 = 2;
     for (int k = kb; k <= ke; k++) {
         if (k + 1 <= ke) fetch(k + 2);  // in flight during this plane's work
-        // RK operands of this plane, loaded before the stencil work
+        // RK operands of this plane, loaded before the stencil work; every
+        // field of a component has that component's shape
         const bool cu = du && k <= klim, cv = dv && k <= klim, cw = dw && k <= nz - 1;
+        const int iu = bu + k * szu, iv = bv + k * szv, iw = bw + k * szw;
         T fu = T(0), fv = T(0), fw = T(0), ou = T(0), ov = T(0), ow = T(0), lu = T(0), lv = T(0), lw = T(0);
-        if (cu) { ou = Uo.u(i, j, k); if (lo) lu = Uolo.u(i, j, k); if (s > 1) fu = F1.u(i, j, k); }
-        if (cv) { ov = Uo.v(i, j, k); if (lo) lv = Uolo.v(i, j, k); if (s > 1) fv = F1.v(i, j, k); }
-        if (cw) { ow = Uo.w(i, j, k); if (lo) lw = Uolo.w(i, j, k); if (s > 1) fw = F1.w(i, j, k); }
+        if (cu) { ou = Uo.u.p[iu]; if constexpr (LO) lu = Uolo.u.p[iu]; if constexpr (S > 1) fu = F1.u.p[iu]; }
+        if (cv) { ov = Uo.v.p[iv]; if constexpr (LO) lv = Uolo.v.p[iv]; if constexpr (S > 1) fv = F1.v.p[iv]; }
+        if (cw) { ow = Uo.w.p[iw]; if constexpr (LO) lw = Uolo.w.p[iw]; if constexpr (S > 1) fw = F1.w.p[iw]; }
         RingAcc<T, TX, TY> aU, aV, aW, aN;
         aU.b[0] = ring[sm1][0]; aU.b[1] = ring[s0][0]; aU.b[2] = ring[sp1][0];
         aV.b[0] = ring[sm1][1]; aV.b[1] = ring[s0][1]; aV.b[2] = ring[sp1][1];
@@ -671,9 +722,9 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
         const T ru = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, rot, i, j, k);
         const T rv = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, rot, i, j, k);
         const T rw = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k);
-        if (cu) rk_apply<T>(ru, fu, ou, lu, lo, i, j, k, out.u, F1.u, Unlo.u, s, ca, cb, dt);
-        if (cv) rk_apply<T>(rv, fv, ov, lv, lo, i, j, k, out.v, F1.v, Unlo.v, s, ca, cb, dt);
-        if (cw) rk_apply<T>(rw, fw, ow, lw, lo, i, j, k, out.w, F1.w, Unlo.w, s, ca, cb, dt);
+        if (cu) rk_apply_at<T, S, LO>(ru, fu, ou, lu, iu, out.u.p, F1.u.p, Unlo.u.p, ca, cb, dt);
+        if (cv) rk_apply_at<T, S, LO>(rv, fv, ov, lv, iv, out.v.p, F1.v.p, Unlo.v.p, ca, cb, dt);
+        if (cw) rk_apply_at<T, S, LO>(rw, fw, ow, lw, iw, out.w.p, F1.w.p, Unlo.w.p, ca, cb, dt);
         __syncthreads();            // plane k-1 no longer read
         if (k + 1 <= ke) commit(sm1);  // plane k+2 into the freed slot
         __syncthreads();
@@ -684,9 +735,9 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
     }
 }
 
-template <typename T, int TX, int TY>
+template <typename T, int TX, int TY, int S, bool LO>
 __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3(const __grid_constant__ Rhs3Args<T> a) {
-    rhs3_tile<T, TX, TY>(a, blockIdx.x, blockIdx.y, blockIdx.z);
+    rhs3_tile<T, TX, TY, S, LO>(a, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // One launch over the tiles of several channels (an ensemble): member m owns
@@ -698,13 +749,13 @@ struct Rhs3Batch {
     Rhs3Args<T> a[CF_ENS_MAXM];
 };
 
-template <typename T, int TX, int TY>
+template <typename T, int TX, int TY, int S, bool LO>
 __global__ void __launch_bounds__(TX *TY, RhsMinB<T>::v) k_rhs3_batch(const __grid_constant__ Rhs3Batch<T> B) {
     const int bid = blockIdx.x;
     int m = 0;
     while (m + 1 < B.n && bid >= B.first[m + 1]) m++;
     const int l = bid - B.first[m], ntx = B.a[m].ntx, nty = B.a[m].nty;
-    rhs3_tile<T, TX, TY>(B.a[m], l % ntx, (l / ntx) % nty, l / (ntx * nty));
+    rhs3_tile<T, TX, TY, S, LO>(B.a[m], l % ntx, (l / ntx) % nty, l / (ntx * nty));
 }
 
 template <typename T>
@@ -772,7 +823,18 @@ template <typename T>
 int launch_rhs3(cf_ctx *ctx, int s, int src, int dst) {
     constexpr int TX = 32, TY = 8;
     const Rhs3Args<T> A = rhs3_args<T>(ctx, s, src, dst);
-    k_rhs3<T, TX, TY><<<dim3(A.ntx, A.nty, A.nkc), TX * TY, 0, ctx->st>>>(A);
+    const dim3 grd(A.ntx, A.nty, A.nkc);
+    const bool lo = sizeof(T) == 4 && A.Uolo.u.p != nullptr;
+#define CF_RHS3(SS, LL) k_rhs3<T, TX, TY, SS, LL><<<grd, TX * TY, 0, ctx->st>>>(A)
+    if constexpr (sizeof(T) == 4) {
+        if (lo) {
+            if (s == 1) CF_RHS3(1, true); else if (s == 2) CF_RHS3(2, true); else CF_RHS3(3, true);
+        }
+    }
+    if (!lo) {
+        if (s == 1) CF_RHS3(1, false); else if (s == 2) CF_RHS3(2, false); else CF_RHS3(3, false);
+    }
+#undef CF_RHS3
     count_launch(ctx, "k_rhs3");
     CF_CUDA(cudaGetLastError());
     return 0;
@@ -792,15 +854,29 @@ int launch_rhs3_batch(cudaStream_t st, cf_ctx *const *m, int s, const int *src, 
         B.a[q] = rhs3_args<T>(m[q], s, src[q], dst[q]);
         B.first[q + 1] = B.first[q] + B.a[q].ntx * B.a[q].nty * B.a[q].nkc;
     }
-    k_rhs3_batch<T, TX, TY><<<B.first[n], TX * TY, 0, st>>>(B);
+    // one variant for all members: the substep is common, the low words
+    // must be too
+    const bool lo = sizeof(T) == 4 && B.a[0].Uolo.u.p != nullptr;
+    for (int q = 1; q < n; q++)
+        if ((sizeof(T) == 4 && B.a[q].Uolo.u.p != nullptr) != lo) return CF_ERR_INVALID;
+#define CF_RHS3B(SS, LL) k_rhs3_batch<T, TX, TY, SS, LL><<<B.first[n], TX * TY, 0, st>>>(B)
+    if constexpr (sizeof(T) == 4) {
+        if (lo) {
+            if (s == 1) CF_RHS3B(1, true); else if (s == 2) CF_RHS3B(2, true); else CF_RHS3B(3, true);
+        }
+    }
+    if (!lo) {
+        if (s == 1) CF_RHS3B(1, false); else if (s == 2) CF_RHS3B(2, false); else CF_RHS3B(3, false);
+    }
+#undef CF_RHS3B
     return cudaGetLastError() == cudaSuccess ? 0 : CF_ERR_CUDA;
 }
 
 // resident fused-RHS blocks per SM (for the z-chunk plan)
 int rhs3_blocks_per_sm(int esz) {
     int n = 1;
-    if (esz == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rhs3<float, 32, 8>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rhs3<double, 32, 8>, 256, 0);
+    if (esz == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rhs3<float, 32, 8, 2, true>, 256, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_rhs3<double, 32, 8, 2, false>, 256, 0);
     return n < 1 ? 1 : n;
 }
 
