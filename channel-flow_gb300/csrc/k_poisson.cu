@@ -1336,51 +1336,63 @@ struct PhiView {
     }
 };
 
-// The three components in one pass: phi(i,j,k) is read once for the three
-// gradients (one thread per cell of the union of the three interior ranges).
+// reciprocal spacings of the split path's projection
 struct RSpG {
     const float *rxg, *ryg, *rzg;  // 1/(xg(i)-xg(i-1)) etc., 1-based
 };
 
-// KP consecutive planes per thread: every load of the thread is issued
-// before the first store (the fields may alias as far as the compiler knows).
+// planes per thread of the pressure store: every load of the thread is
+// issued before the first store
 constexpr int PROJ_KP = 2;
 
-// The ghost copies apply_boundary_conditions (boundary_conditions.f90:20-75)
-// makes of a canonical cell with no-slip walls: its periodic images in x and
-// z (update of the duplicate columns and planes, :87-244) and, on the rows
-// next to a wall, the wall ghost of the cell and of each image (:257-272):
-// -value at y centres, 0 at y faces.  xc/zc: the field sits at x/z centres
-// (extent np + 3, images of 2, 3 and np + 1) rather than faces (extent
-// np + 2, images of 2 and np + 1); yf: the field sits at y faces.
-struct ImgAxes {
-    int n1, n2, n3;
-    bool xc, zc, yf;
+// Everything the projection kernel reads: fields as plain pointers (low
+// words null unless the update is compensated), phi, reciprocal spacings
+// (split path) or coordinates (FP64 path, 1-based), extents.
+template <typename T>
+struct ProjArgs {
+    T *u, *v, *w, *ul, *vl, *wl;
+    const T *phi;
+    const float *rxg, *ryg, *rzg;
+    const T *xg, *yg, *zg;
+    int nx, ny, nz, nxg, nyg, nzg, nxp, nym, nzp, ilim, klim;
 };
 
-// the periodic image of canonical index i on an axis of extent n (0: none);
-// at most one per cell when np >= 4 (checked on the host)
+// planes per thread of the projection kernel
+constexpr int PROJ3_KP = 4;
+
+// The periodic image of canonical index i on an axis of extent n (0: none):
+// at centres (extent np + 3) images of 2, 3 and np + 1, at faces (extent
+// np + 2) images of 2 and np + 1; at most one per cell when np >= 4 (checked
+// on the host).
 __device__ __forceinline__ int img_of(int i, int n, bool centre) {
     if (centre) return i == 2 ? n - 1 : (i == 3 ? n : (i == n - 2 ? 1 : 0));
     return i == 2 ? n : (i == n - 1 ? 1 : 0);
 }
 
-template <typename T>
-__device__ __forceinline__ void put_images(const Fld<T> &F, const Fld<T> &Flo, bool lo, const ImgAxes &a, int i, int j,
-                                           int k, T v, T vl) {
-    const int xi = img_of(i, a.n1, a.xc), zi = img_of(k, a.n3, a.zc);
-    const bool yw = j == 2 || j == a.n2 - 1;
+// The ghost copies apply_boundary_conditions (boundary_conditions.f90:20-75)
+// makes of a canonical cell (i, j, k) of one field with no-slip walls: its
+// periodic images in x and z (update of the duplicate columns and planes,
+// :87-244) and, on the rows next to a wall, the wall ghost of the cell and of
+// each image (:257-272): -value at y centres, 0 at y faces.  F: the field
+// with row stride sy and plane stride sz (1-based indices), extents n1 x n2
+// x n3; xc / zc: x / z centres, yf: y faces.
+template <typename T, bool LO>
+__device__ __forceinline__ void put_images(T *F, T *Fl, int sy, int sz, int n1, int n2, int n3, bool xc, bool zc,
+                                           bool yf, int i, int j, int k, T v, T vl) {
+    const int xi = img_of(i, n1, xc), zi = img_of(k, n3, zc);
+    const bool yw = j == 2 || j == n2 - 1;
     if (!(xi | zi) && !yw) return;
     auto put = [&](int ii, int jj, int kk, T x, T xl) {
-        F(ii, jj, kk) = x;
-        if (lo) Flo(ii, jj, kk) = xl;
+        const int o = (ii - 1) + sy * (jj - 1) + sz * (kk - 1);
+        F[o] = x;
+        if constexpr (LO) Fl[o] = xl;
     };
     if (xi) put(xi, j, k, v, vl);
     if (zi) put(i, j, zi, v, vl);
     if (xi && zi) put(xi, j, zi, v, vl);
     if (yw) {
-        const int jg = j == 2 ? 1 : a.n2;
-        const T gv = a.yf ? T(0) : -v, gl = a.yf ? T(0) : -vl;
+        const int jg = j == 2 ? 1 : n2;
+        const T gv = yf ? T(0) : -v, gl = yf ? T(0) : -vl;
         put(i, jg, k, gv, gl);
         if (xi) put(xi, jg, k, gv, gl);
         if (zi) put(i, jg, zi, gv, gl);
@@ -1388,58 +1400,73 @@ __device__ __forceinline__ void put_images(const Fld<T> &F, const Fld<T> &Flo, b
     }
 }
 
-// ilim, klim: last x and z index projected (nxg-1 and nzg-1 for the full
-// interior; nxp+1 and nzp+1 for the canonical cells only).  IMG (canonical
-// cells, no-slip walls): every ghost copy of the new values is written as
-// well, which is what apply_boundary_conditions after the projection would
-// do.  Index arithmetic: the (i, j) offsets of the thread are formed once,
-// planes follow by adding the plane strides.
-template <typename T, bool IMG>
-__global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ulo, Fld<T> V, Fld<T> Vlo, Fld<T> W,
-                                                  Fld<T> Wlo, const T *__restrict__ phi, PhiView pv, RSpG rs, int ilim,
-                                                  int klim) {
-    constexpr int KP = PROJ_KP;
+// project_velocity (projection.f90:203-225) of the three components, one
+// thread per (i, j) column and PROJ3_KP planes; ilim, klim: last x and z
+// index projected (nxg-1 and nzg-1 for the full interior; nxp+1 and nzp+1
+// for the canonical cells only).  LO: the compensated update of the split
+// path's last substep (hi + lo).  IMG (canonical cells, no-slip walls):
+// every ghost copy of the new values is written as well, which is what
+// apply_boundary_conditions after the projection would do -- by the few
+// threads whose cells have any, after the main stores, from the values they
+// have just stored.  phi is read through the periodic wrap, which reproduces
+// apply_periodic_xz_pressure (projection.f90:144-162).  Every index is formed
+// once per thread; planes follow by adding the plane strides.
+template <typename T, bool IMG, bool LO>
+__global__ void __launch_bounds__(128) k_project3(const __grid_constant__ ProjArgs<T> a) {
+    constexpr int KP = PROJ3_KP;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 2;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 2;
     const int k0 = blockIdx.z * KP + 2;
-    if (i > ilim || j > g.nyg - 1) return;
-    const bool du = i <= g.nx - 1, dv = j <= g.ny - 1;
-    const bool lo = Ulo.p != nullptr;
+    const int nx = a.nx, ny = a.ny, nz = a.nz, nxg = a.nxg, nyg = a.nyg, nzg = a.nzg, klim = a.klim;
+    if (i > a.ilim || j > nyg - 1) return;
+    const bool du = i <= nx - 1, dv = j <= ny - 1;
     // phi offsets: canonical x of i and i+1, rows j and j+1, planes
-    const int nxp = pv.nxp, pls = nxp * pv.nym;
-    const int ic0 = wrapf(i, nxp) - 2, ic1 = wrapf(i + 1, nxp) - 2;
-    const int r0 = nxp * (j - 2), r1 = r0 + nxp;
+    const int nxp = a.nxp, pls = nxp * a.nym;
+    const int ic0 = wrapf(i, nxp) - 2 + nxp * (j - 2), ic1 = wrapf(i + 1, nxp) - 2 + nxp * (j - 2), jc1 = ic0 + nxp;
     int kof[KP + 1];
 #pragma unroll
-    for (int q = 0; q <= KP; q++) kof[q] = pls * (wrapf(k0 + q, pv.nzp) - 2);
-    const int iu = U.idx(i, j, k0), iv = V.idx(i, j, k0), iw = W.idx(i, j, k0);
-    T p0[KP + 1], px[KP], py[KP];
-    T u[KP], v[KP], w[KP], ul[KP], vl[KP], wl[KP];
+    for (int q = 0; q <= KP; q++) kof[q] = pls * (wrapf(k0 + q, a.nzp) - 2);
+    // field indices (1-based, the reference's extents) of plane k0
+    const int suy = nx, suz = nx * nyg, svy = nxg, svz = nxg * ny, swy = nxg, swz = nxg * nyg;
+    const int iu = (i - 1) + suy * (j - 1) + suz * (k0 - 1), iv = (i - 1) + svy * (j - 1) + svz * (k0 - 1),
+              iw = (i - 1) + swy * (j - 1) + swz * (k0 - 1);
+    const T *__restrict__ phi = a.phi;
+    T p0[KP + 1], px[KP], py[KP], u[KP], v[KP], w[KP], ul[KP], vl[KP], wl[KP];
 #pragma unroll
-    for (int q = 0; q <= KP; q++) p0[q] = k0 + q <= g.nzg - 1 ? phi[ic0 + r0 + kof[q]] : T(0);
+    for (int q = 0; q <= KP; q++) p0[q] = k0 + q <= nzg - 1 ? phi[ic0 + kof[q]] : T(0);
 #pragma unroll
     for (int q = 0; q < KP; q++) {
         const int k = k0 + q;
-        const bool kin = k <= klim, dw = k <= g.nz - 1;
-        px[q] = du && kin ? phi[ic1 + r0 + kof[q]] : T(0);
-        py[q] = dv && kin ? phi[ic0 + r1 + kof[q]] : T(0);
-        u[q] = du && kin ? U.p[iu + q * U.sz] : T(0);
-        v[q] = dv && kin ? V.p[iv + q * V.sz] : T(0);
-        w[q] = dw ? W.p[iw + q * W.sz] : T(0);
-        if (lo) {
-            ul[q] = du && kin ? Ulo.p[iu + q * U.sz] : T(0);
-            vl[q] = dv && kin ? Vlo.p[iv + q * V.sz] : T(0);
-            wl[q] = dw ? Wlo.p[iw + q * W.sz] : T(0);
+        const bool kin = k <= klim, dw = k <= nz - 1;
+        px[q] = du && kin ? phi[ic1 + kof[q]] : T(0);
+        py[q] = dv && kin ? phi[jc1 + kof[q]] : T(0);
+        u[q] = du && kin ? a.u[iu + q * suz] : T(0);
+        v[q] = dv && kin ? a.v[iv + q * svz] : T(0);
+        w[q] = dw && kin ? a.w[iw + q * swz] : T(0);
+        if constexpr (LO) {
+            ul[q] = du && kin ? a.ul[iu + q * suz] : T(0);
+            vl[q] = dv && kin ? a.vl[iv + q * svz] : T(0);
+            wl[q] = dw && kin ? a.wl[iw + q * swz] : T(0);
         }
     }
     T rx, ry;
     if constexpr (sizeof(T) == 4) {
-        rx = du ? rs.rxg[i + 1] : T(0);
-        ry = dv ? rs.ryg[j + 1] : T(0);
+        rx = du ? a.rxg[i + 1] : T(0);
+        ry = dv ? a.ryg[j + 1] : T(0);
     } else {
-        rx = du ? T(1) / (g.xg[i + 1] - g.xg[i]) : T(0);
-        ry = dv ? T(1) / (g.yg[j + 1] - g.yg[j]) : T(0);
+        rx = du ? T(1) / (a.xg[i + 1] - a.xg[i]) : T(0);
+        ry = dv ? T(1) / (a.yg[j + 1] - a.yg[j]) : T(0);
     }
+    auto upd = [&](T *F, T *Fl, int o, T f, T fl, T gr) {
+        if constexpr (sizeof(T) == 4 && LO) {
+            float hi = f, l = fl;
+            ff_add(hi, l, -gr);
+            F[o] = hi;
+            Fl[o] = l;
+        } else {
+            F[o] = f - gr;
+        }
+    };
 #pragma unroll
     for (int q = 0; q < KP; q++) {
         const int k = k0 + q;
@@ -1448,46 +1475,41 @@ __global__ void __launch_bounds__(128) k_project3(GeoT<T> g, Fld<T> U, Fld<T> Ul
         if constexpr (sizeof(T) == 4) {
             gx = (px[q] - p0[q]) * rx;
             gy = (py[q] - p0[q]) * ry;
-            gz = k <= g.nz - 1 ? (p0[q + 1] - p0[q]) * rs.rzg[k + 1] : T(0);
+            gz = k <= nz - 1 ? (p0[q + 1] - p0[q]) * a.rzg[k + 1] : T(0);
         } else {
             // projection.f90:209-223 divides by the spacings
-            gx = du ? (px[q] - p0[q]) / (g.xg[i + 1] - g.xg[i]) : T(0);
-            gy = dv ? (py[q] - p0[q]) / (g.yg[j + 1] - g.yg[j]) : T(0);
-            gz = k <= g.nz - 1 ? (p0[q + 1] - p0[q]) / (g.zg[k + 1] - g.zg[k]) : T(0);
+            gx = du ? (px[q] - p0[q]) / (a.xg[i + 1] - a.xg[i]) : T(0);
+            gy = dv ? (py[q] - p0[q]) / (a.yg[j + 1] - a.yg[j]) : T(0);
+            gz = k <= nz - 1 ? (p0[q + 1] - p0[q]) / (a.zg[k + 1] - a.zg[k]) : T(0);
         }
         (void)rx;
         (void)ry;
-        auto upd = [&](const Fld<T> &F, const Fld<T> &Flo, int o, T f, T fl, T gr) {
-            T hi = f - gr;
-            if constexpr (sizeof(T) == 4) {
-                if (lo) {
-                    float l = fl;
-                    hi = f;
-                    ff_add(hi, l, -gr);
-                    Flo.p[o] = l;
-                }
-            }
-            F.p[o] = hi;
-        };
-        if (du) upd(U, Ulo, iu + q * U.sz, u[q], ul[q], gx);
-        if (dv) upd(V, Vlo, iv + q * V.sz, v[q], vl[q], gy);
-        if (k <= g.nz - 1) upd(W, Wlo, iw + q * W.sz, w[q], wl[q], gz);
+        if (du) upd(a.u, a.ul, iu + q * suz, u[q], ul[q], gx);
+        if (dv) upd(a.v, a.vl, iv + q * svz, v[q], vl[q], gy);
+        if (k <= nz - 1) upd(a.w, a.wl, iw + q * swz, w[q], wl[q], gz);
     }
     if constexpr (IMG) {
-        // the ghost copies, from the values just stored (read back by the
-        // thread that stored them), on the few threads whose cells have any
-        const bool ex = i <= 3 || i >= g.nxg - 2, ey = j == 2 || j >= g.ny - 1, ez = k0 <= 3 || k0 + KP - 1 >= g.nzg - 2;
+        const bool ex = i <= 3 || i >= nxg - 2, ey = j == 2 || j >= ny - 1, ez = k0 <= 3 || k0 + KP - 1 >= nzg - 2;
         if (ex || ey || ez) {
-            const ImgAxes au = {g.nx, g.nyg, g.nzg, false, true, false}, av = {g.nxg, g.ny, g.nzg, true, true, true},
-                          aw = {g.nxg, g.nyg, g.nz, true, false, false};
 #pragma unroll 1
             for (int q = 0; q < KP; q++) {
                 const int k = k0 + q;
                 if (k > klim) break;
-                if (du) put_images<T>(U, Ulo, lo, au, i, j, k, U.p[iu + q * U.sz], lo ? Ulo.p[iu + q * U.sz] : T(0));
-                if (dv) put_images<T>(V, Vlo, lo, av, i, j, k, V.p[iv + q * V.sz], lo ? Vlo.p[iv + q * V.sz] : T(0));
-                if (k <= g.nz - 1)
-                    put_images<T>(W, Wlo, lo, aw, i, j, k, W.p[iw + q * W.sz], lo ? Wlo.p[iw + q * W.sz] : T(0));
+                if (du) {
+                    const int o = iu + q * suz;
+                    put_images<T, LO>(a.u, a.ul, suy, suz, nx, nyg, nzg, false, true, false, i, j, k, a.u[o],
+                                      LO ? a.ul[o] : T(0));
+                }
+                if (dv) {
+                    const int o = iv + q * svz;
+                    put_images<T, LO>(a.v, a.vl, svy, svz, nxg, ny, nzg, true, true, true, i, j, k, a.v[o],
+                                      LO ? a.vl[o] : T(0));
+                }
+                if (k <= nz - 1) {
+                    const int o = iw + q * swz;
+                    put_images<T, LO>(a.w, a.wl, swy, swz, nxg, nyg, nz, true, false, false, i, j, k, a.w[o],
+                                      LO ? a.wl[o] : T(0));
+                }
             }
         }
     }
@@ -1673,12 +1695,30 @@ int launch_projection(cf_ctx *ctx, int b, bool store_p, bool lo, bool canon, int
         // the boundary conditions as ghost copies written by the projection
         // itself: canonical cells, no-slip walls
         const bool img = bc && canon && ctx->prm.iwall_model == 0 && ctx->nxp >= 4 && ctx->nzp >= 4;
-        const dim3 grd(cdiv(ilim - 1, 32), cdiv(ctx->nyg - 2, 4), cdiv(klim - 1, PROJ_KP));
-        const Fld<T> Ul = make_fld<T>(lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg),
-                     Vl = make_fld<T>(lo ? ctx->Vlo[b] : nullptr, ctx->nxg, ctx->ny),
-                     Wl = make_fld<T>(lo ? ctx->Wlo[b] : nullptr, ctx->nxg, ctx->nyg);
-        if (img) k_project3<T, true><<<grd, blk, 0, ctx->st>>>(g, U, Ul, V, Vl, W, Wl, phi, pv, rg, ilim, klim);
-        else k_project3<T, false><<<grd, blk, 0, ctx->st>>>(g, U, Ul, V, Vl, W, Wl, phi, pv, rg, ilim, klim);
+        ProjArgs<T> pa;
+        pa.u = (T *)ctx->U[b]; pa.v = (T *)ctx->V[b]; pa.w = (T *)ctx->W[b];
+        pa.ul = lo ? (T *)ctx->Ulo[b] : nullptr;
+        pa.vl = lo ? (T *)ctx->Vlo[b] : nullptr;
+        pa.wl = lo ? (T *)ctx->Wlo[b] : nullptr;
+        pa.phi = phi;
+        pa.rxg = rg.rxg; pa.ryg = rg.ryg; pa.rzg = rg.rzg;
+        pa.xg = g.xg; pa.yg = g.yg; pa.zg = g.zg;
+        pa.nx = ctx->nx; pa.ny = ctx->ny; pa.nz = ctx->nz;
+        pa.nxg = ctx->nxg; pa.nyg = ctx->nyg; pa.nzg = ctx->nzg;
+        pa.nxp = nxp; pa.nym = nym; pa.nzp = nzp;
+        pa.ilim = ilim; pa.klim = klim;
+        const bool plo = sizeof(T) == 4 && pa.ul != nullptr;
+        const dim3 grd(cdiv(ilim - 1, 32), cdiv(ctx->nyg - 2, 4), cdiv(klim - 1, PROJ3_KP));
+        if constexpr (sizeof(T) == 4) {
+            if (plo) {
+                if (img) k_project3<T, true, true><<<grd, blk, 0, ctx->st>>>(pa);
+                else k_project3<T, false, true><<<grd, blk, 0, ctx->st>>>(pa);
+            }
+        }
+        if (!plo) {
+            if (img) k_project3<T, true, false><<<grd, blk, 0, ctx->st>>>(pa);
+            else k_project3<T, false, false><<<grd, blk, 0, ctx->st>>>(pa);
+        }
         count_launch(ctx, "k_project3");
         if (img) ctx->state_periodic = true;  // as launch_bc: holds for every later launch on the stream
         else if (bc) {
