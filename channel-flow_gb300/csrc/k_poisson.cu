@@ -505,6 +505,105 @@ __global__ void __launch_bounds__(ZR_T) k_fft_zr(typename C2<T>::t *__restrict__
     }
 }
 
+// z transforms of 384 and 512 points: three Stockham stages of radix 8, 8
+// and 6 or 8 (register DFTs), the first loading and the last storing the
+// spectrum directly; the middle stage works in place (every thread reads its
+// butterflies' inputs, a barrier, then the writes).
+constexpr int zr3_r(int n, int s) { return n == 384 ? (s < 2 ? 8 : 6) : (n == 512 ? 8 : 0); }
+constexpr int ZR3_G = 32;  // threads per line (two or fewer butterflies of each stage per thread)
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ZR_T) k_fft_zr3(typename C2<T>::t *__restrict__ spec,
+                                                  const typename C2<T>::t *__restrict__ tw_g, int nlines, int nh) {
+    typedef typename C2<T>::t C;
+    constexpr int R0 = zr3_r(N, 0), R1 = zr3_r(N, 1), R2 = zr3_r(N, 2), G = ZR3_G, LB = ZR_T / G;
+    constexpr int NB0 = N / R0, NB1 = N / R1, NB2 = N / R2, NS1 = R0, NS2 = R0 * R1, ST1 = N / (R0 * R1);
+    constexpr int I0 = (NB0 + G - 1) / G, I1 = (NB1 + G - 1) / G, I2 = (NB2 + G - 1) / G, LS = N + 1;
+    static_assert(R0 * R1 * R2 == N && NB2 == NS2, "z transform plan");
+    __shared__ C stw[N];
+    extern __shared__ unsigned char smraw[];
+    // lines fastest across the threads: a half-warp reads 16 adjacent kx
+    const int l = threadIdx.x % LB, t = threadIdx.x / LB;
+    const long L = (long)blockIdx.x * LB + l;
+    const bool act = L < nlines;
+    long gb = 0;
+    if (act) {
+        const long j = L / nh, kx = L - j * nh;
+        gb = j * N * nh + kx;
+    }
+    C *bl = (C *)smraw + l * LS;
+    {
+        C v[I0][R0];
+#pragma unroll
+        for (int it = 0; it < I0; it++) {
+            const int j = t + it * G;
+#pragma unroll
+            for (int r = 0; r < R0; r++)
+                v[it][r] = (act && j < NB0) ? spec[gb + (long)(j + r * NB0) * nh] : cmk<C>(0.0, 0.0);
+        }
+        for (int e = threadIdx.x; e < N; e += ZR_T) stw[e] = tw_g[e];
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < I0; it++) {
+            const int j = t + it * G;
+            if (j < NB0) {
+                reg_dft<R0, N>(v[it], stw);
+#pragma unroll
+                for (int r = 0; r < R0; r++) bl[j * R0 + r] = v[it][r];
+            }
+        }
+    }
+    __syncthreads();
+    {
+        C w[I1][R1];
+#pragma unroll
+        for (int it = 0; it < I1; it++) {
+            const int j = t + it * G, k = j % NS1;
+            if (j < NB1) {
+#pragma unroll
+                for (int r = 0; r < R1; r++) w[it][r] = bl[j + r * NB1];
+#pragma unroll
+                for (int r = 1; r < R1; r++) w[it][r] = cmul(w[it][r], stw[r * k * ST1]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < I1; it++) {
+            const int j = t + it * G, k = j % NS1;
+            if (j < NB1) {
+                reg_dft<R1, N>(w[it], stw);
+                const int d = (j / NS1) * NS1 * R1 + k;
+#pragma unroll
+                for (int r = 0; r < R1; r++) bl[d + r * NS1] = w[it][r];
+            }
+        }
+    }
+    __syncthreads();
+    // last stage: Ns = NB2, so k = j, the twiddle step is 1 and output r of
+    // butterfly j goes to j + r NS2
+#pragma unroll
+    for (int it = 0; it < I2; it++) {
+        const int j = t + it * G;
+        if (j < NB2) {
+            C w[R2];
+#pragma unroll
+            for (int r = 0; r < R2; r++) w[r] = bl[j + r * NB2];
+#pragma unroll
+            for (int r = 1; r < R2; r++) w[r] = cmul(w[r], stw[r * j]);
+            reg_dft<R2, N>(w, stw);
+            if (act) {
+#pragma unroll
+                for (int r = 0; r < R2; r++) spec[gb + (long)(j + r * NS2) * nh] = w[r];
+            }
+        }
+    }
+}
+
+template <typename T, int N>
+static size_t zr3_smem() {
+    return (size_t)(ZR_T / ZR3_G) * (N + 1) * sizeof(typename C2<T>::t);
+}
+
 template <typename T, int N>
 static size_t zr_smem() {
     return zr_r1(N) > 1 ? (size_t)(ZR_T / zr_threads(N)) * (N + 1) * sizeof(typename C2<T>::t) : 0;
@@ -1586,6 +1685,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
     break;
 #define CF_FFTZ(N, TW) case N: \
     if constexpr (zr_r0(N) > 0) k_fft_zr<T, N><<<cdiv(nlines, ZR_T / zr_threads(N)), ZR_T, zr_smem<T, N>(), ctx->st>>>(spec, TW, (int)nlines, nh); \
+    else if constexpr (zr3_r(N, 0) > 0) k_fft_zr3<T, N><<<cdiv(nlines, ZR_T / ZR3_G), ZR_T, zr3_smem<T, N>(), ctx->st>>>(spec, TW, (int)nlines, nh); \
     else k_fft_z<T, N><<<cdiv(nlines, LB), LB * Gz, shz, ctx->st>>>(spec, pz, TW, (int)nlines, nh, LB); \
     break;
 #define CF_FFTZF(N) CF_FFTZ(N, twzf)
@@ -1849,6 +1949,8 @@ static void fft_attrs_one() {
     cudaFuncSetAttribute(k_fwd_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_inv_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_fft_z<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+    if constexpr (zr3_r(N, 0) > 0)
+        cudaFuncSetAttribute(k_fft_zr3<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zr3_smem<T, N>());
     if constexpr (zr_r0(N) > 0) {
         // exactly what the launches request (up to 110 KB: FP64, length 96)
         cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zr_smem<T, N>());

@@ -273,9 +273,10 @@ def test_split_precision_short_horizon():
         assert e < 1e-4, (n, e)
 
 
-@pytest.mark.parametrize("dims", [(66, 65, 66), (98, 65, 98), (34, 33, 130), (194, 129, 194), (18, 17, 258)])
+@pytest.mark.parametrize("dims", [(66, 65, 66), (98, 65, 98), (34, 33, 130), (194, 129, 194), (18, 17, 258),
+                                  (34, 33, 386), (18, 17, 514)])
 def test_split_projection_matches_fp64(dims):
-    """The split-path projection (FP32 transforms, FP32 tridiagonal replays,
+    """The split-path projection (FP32 transforms of 16-512 points, FP32 tridiagonal replays,
     the pivoting modes refined against the FP64 residual) against the FP64
     projection of the same fields: U, V, W within 1e-5 normwise relative,
     P within 1e-3, and the split result divergence-free to 1e-4 max|U|/dx."""
