@@ -619,8 +619,45 @@ static size_t zr_smem() {
 // stage's butterflies store R0 adjacent elements each, and with the padding
 // both stages' accesses fall in distinct banks.
 // ---------------------------------------------------------------------------
-template <int N> __device__ __forceinline__ int xr_pos(int x) { return x + x / zr_r0(N); }
-template <int N> constexpr int xr_ls() { return N + N / zr_r0(N); }
+// radix of stage s of the x transforms' plan (1: no such stage): the two
+// stages of the z plans up to 256 points, three for 384 and 512
+constexpr int xr_r(int n, int s) {
+    return zr_r0(n) > 0 ? (s == 0 ? zr_r0(n) : (s == 1 ? zr_r1(n) : 1)) : (zr3_r(n, 0) > 0 ? zr3_r(n, s) : 0);
+}
+// threads per line of the inverse x transform
+constexpr int xr_threads(int n) { return zr_r0(n) > 0 ? zr_threads(n) : 32; }
+template <int N> __device__ __forceinline__ int xr_pos(int x) { return x + x / xr_r(N, 0); }
+template <int N> constexpr int xr_ls() { return N + N / xr_r(N, 0); }
+
+// A middle Stockham stage (span NS, radix R) of a padded line in place:
+// every thread reads its butterflies' inputs and applies the twiddles, a
+// barrier, then the DFTs and the writes (G threads per line, thread t).
+template <int N, int R, int NS, int G, typename C>
+__device__ __forceinline__ void xr_mid_stage(C *bl, const C *stw, int t) {
+    constexpr int NB = N / R, I = (NB + G - 1) / G, ST = N / (NS * R);
+    C w[I][R];
+#pragma unroll
+    for (int it = 0; it < I; it++) {
+        const int j = t + it * G, k = j % NS;
+        if (j < NB) {
+#pragma unroll
+            for (int r = 0; r < R; r++) w[it][r] = bl[xr_pos<N>(j + r * NB)];
+#pragma unroll
+            for (int r = 1; r < R; r++) w[it][r] = cmul(w[it][r], stw[r * k * ST]);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < I; it++) {
+        const int j = t + it * G, k = j % NS;
+        if (j < NB) {
+            reg_dft<R, N>(w[it], stw);
+            const int d = (j / NS) * NS * R + k;
+#pragma unroll
+            for (int r = 0; r < R; r++) bl[xr_pos<N>(d + r * NS)] = w[it][r];
+        }
+    }
+}
 
 // Forward: the divergence of the packed line pair is formed by 32 threads
 // per pair (x positions t + 32 e, every load of a thread issued before the
@@ -633,8 +670,9 @@ template <typename T, int N>
 __global__ void __launch_bounds__(ZR_T) k_fwd_xr(GeoT<T> g, Fld<T> U, Fld<T> V, Fld<T> W, typename C2<T>::t *spec,
                                                  const typename C2<T>::t *__restrict__ tw_g, RSp rs) {
     typedef typename C2<T>::t C;
-    constexpr int R0 = zr_r0(N), R1 = zr_r1(N), G = XR_FT, LP = ZR_T / G, NB0 = N / R0, NB1 = N / R1;
-    constexpr int I0 = (NB0 + G - 1) / G, I1 = (NB1 + G - 1) / G, LS = xr_ls<N>(), NH = N / 2 + 1;
+    constexpr int R0 = xr_r(N, 0), R1 = xr_r(N, 1), R2 = xr_r(N, 2), G = XR_FT, LP = ZR_T / G, NB0 = N / R0;
+    constexpr int RL = R2 > 1 ? R2 : R1, NSL = N / RL, NBL = N / RL;  // the last stage (span NSL)
+    constexpr int I0 = (NB0 + G - 1) / G, IL = (NBL + G - 1) / G, LS = xr_ls<N>(), NH = N / 2 + 1;
     constexpr int NPT = (N + G - 1) / G, XB = NPT < 3 ? NPT : 3;
     __shared__ C stw[N];
     extern __shared__ unsigned char smraw[];
@@ -713,21 +751,26 @@ __global__ void __launch_bounds__(ZR_T) k_fwd_xr(GeoT<T> g, Fld<T> U, Fld<T> V, 
             for (int r = 0; r < R0; r++) bl[xr_pos<N>(jb * R0 + r)] = v[it][r];
         }
     }
+    if constexpr (R2 > 1) {
+        __syncthreads();
+        xr_mid_stage<N, R1, R0, G>(bl, stw, t);
+    }
     if constexpr (R1 > 1) {
         __syncthreads();
-        // second stage in place: butterfly jb reads and writes jb + r R0
+        // last stage in place (span NSL = NBL, twiddle step 1): butterfly
+        // jb reads and writes jb + r NSL
 #pragma unroll
-        for (int it = 0; it < I1; it++) {
+        for (int it = 0; it < IL; it++) {
             const int jb = t + it * G;
-            if (jb < NB1) {
-                C w[R1];
+            if (jb < NBL) {
+                C w[RL];
 #pragma unroll
-                for (int r = 0; r < R1; r++) w[r] = bl[xr_pos<N>(jb + r * R0)];
+                for (int r = 0; r < RL; r++) w[r] = bl[xr_pos<N>(jb + r * NSL)];
 #pragma unroll
-                for (int r = 1; r < R1; r++) w[r] = cmul(w[r], stw[r * jb]);
-                reg_dft<R1, N>(w, stw);
+                for (int r = 1; r < RL; r++) w[r] = cmul(w[r], stw[r * jb]);
+                reg_dft<RL, N>(w, stw);
 #pragma unroll
-                for (int r = 0; r < R1; r++) bl[xr_pos<N>(jb + r * R0)] = w[r];
+                for (int r = 0; r < RL; r++) bl[xr_pos<N>(jb + r * NSL)] = w[r];
             }
         }
     }
@@ -751,8 +794,9 @@ template <typename T, int N>
 __global__ void __launch_bounds__(ZR_T) k_inv_xr(const typename C2<T>::t *__restrict__ spec, T *__restrict__ phi,
                                                  const typename C2<T>::t *__restrict__ tw_g, int nym, int nzp, T scale) {
     typedef typename C2<T>::t C;
-    constexpr int R0 = zr_r0(N), R1 = zr_r1(N), G = zr_threads(N), LP = ZR_T / G, NB0 = N / R0, NB1 = N / R1;
-    constexpr int I0 = (NB0 + G - 1) / G, I1 = (NB1 + G - 1) / G, LS = xr_ls<N>(), NH = N / 2 + 1;
+    constexpr int R0 = xr_r(N, 0), R1 = xr_r(N, 1), R2 = xr_r(N, 2), G = xr_threads(N), LP = ZR_T / G, NB0 = N / R0;
+    constexpr int RL = R2 > 1 ? R2 : R1, NSL = N / RL, NBL = N / RL;  // the last stage (span NSL)
+    constexpr int I0 = (NB0 + G - 1) / G, IL = (NBL + G - 1) / G, LS = xr_ls<N>(), NH = N / 2 + 1;
     __shared__ C stw[N];
     extern __shared__ unsigned char smraw[];
     const int lp = threadIdx.x / G, t = threadIdx.x % G;
@@ -812,21 +856,26 @@ __global__ void __launch_bounds__(ZR_T) k_inv_xr(const typename C2<T>::t *__rest
             }
         }
         __syncthreads();
+        if constexpr (R2 > 1) {
+            xr_mid_stage<N, R1, R0, G>(bl, stw, t);
+            __syncthreads();
+        }
+        // last stage (span NSL = NBL, twiddle step 1): phi stored directly
 #pragma unroll
-        for (int it = 0; it < I1; it++) {
+        for (int it = 0; it < IL; it++) {
             const int jb = t + it * G;
-            if (jb < NB1) {
-                C w[R1];
+            if (jb < NBL) {
+                C w[RL];
 #pragma unroll
-                for (int r = 0; r < R1; r++) w[r] = bl[xr_pos<N>(jb + r * R0)];
+                for (int r = 0; r < RL; r++) w[r] = bl[xr_pos<N>(jb + r * NSL)];
 #pragma unroll
-                for (int r = 1; r < R1; r++) w[r] = cmul(w[r], stw[r * jb]);
-                reg_dft<R1, N>(w, stw);
+                for (int r = 1; r < RL; r++) w[r] = cmul(w[r], stw[r * jb]);
+                reg_dft<RL, N>(w, stw);
                 if (act) {
 #pragma unroll
-                    for (int r = 0; r < R1; r++) {
-                        p0[jb + r * R0] = w[r].x * scale;
-                        p1[jb + r * R0] = w[r].y * scale;
+                    for (int r = 0; r < RL; r++) {
+                        p0[jb + r * NSL] = w[r].x * scale;
+                        p1[jb + r * NSL] = w[r].y * scale;
                     }
                 }
             }
@@ -836,7 +885,7 @@ __global__ void __launch_bounds__(ZR_T) k_inv_xr(const typename C2<T>::t *__rest
 
 template <typename T, int N>
 static size_t xr_smem() {
-    return zr_r1(N) > 1 ? (size_t)(ZR_T / zr_threads(N)) * xr_ls<N>() * sizeof(typename C2<T>::t) : 0;
+    return xr_r(N, 1) > 1 ? (size_t)(ZR_T / xr_threads(N)) * xr_ls<N>() * sizeof(typename C2<T>::t) : 0;
 }
 template <typename T, int N>
 static size_t xr_fwd_smem() {
@@ -1680,7 +1729,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
     rs.rz = ctx->d_rgeo_f + ctx->rgeo_off[4];
 #define CF_FFT_SIZES(X) X(16) X(32) X(64) X(96) X(128) X(192) X(256) X(384) X(512)
 #define CF_FWDX(N) case N: \
-    if constexpr (zr_r0(N) > 0) k_fwd_xr<T, N><<<cdiv(npairs, ZR_T / XR_FT), ZR_T, xr_fwd_smem<T, N>(), ctx->st>>>(g, U, V, W, spec, twxf, rs); \
+    if constexpr (xr_r(N, 0) > 0) k_fwd_xr<T, N><<<cdiv(npairs, ZR_T / XR_FT), ZR_T, xr_fwd_smem<T, N>(), ctx->st>>>(g, U, V, W, spec, twxf, rs); \
     else k_fwd_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(g, U, V, W, spec, px, twxf, LP, rs); \
     break;
 #define CF_FFTZ(N, TW) case N: \
@@ -1691,7 +1740,7 @@ static int poisson_solve(cf_ctx *ctx, Fld<T> U, Fld<T> V, Fld<T> W, int phases) 
 #define CF_FFTZF(N) CF_FFTZ(N, twzf)
 #define CF_FFTZB(N) CF_FFTZ(N, twzb)
 #define CF_INVX(N) case N: \
-    if constexpr (zr_r0(N) > 0) k_inv_xr<T, N><<<cdiv(npairs, ZR_T / zr_threads(N)), ZR_T, xr_smem<T, N>(), ctx->st>>>(spec, phi, twxb, nym, nzp, scale); \
+    if constexpr (xr_r(N, 0) > 0) k_inv_xr<T, N><<<cdiv(npairs, ZR_T / xr_threads(N)), ZR_T, xr_smem<T, N>(), ctx->st>>>(spec, phi, twxb, nym, nzp, scale); \
     else k_inv_x<T, N><<<cdiv(npairs, LP), LP * Gx, shx, ctx->st>>>(spec, phi, px, twxb, nym, nzp, LP, scale); \
     break;
     if (phases & POISSON_FWD) {
@@ -1949,8 +1998,11 @@ static void fft_attrs_one() {
     cudaFuncSetAttribute(k_fwd_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_inv_x<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
     cudaFuncSetAttribute(k_fft_z<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
-    if constexpr (zr3_r(N, 0) > 0)
+    if constexpr (zr3_r(N, 0) > 0) {
         cudaFuncSetAttribute(k_fft_zr3<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zr3_smem<T, N>());
+        cudaFuncSetAttribute(k_fwd_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xr_fwd_smem<T, N>());
+        cudaFuncSetAttribute(k_inv_xr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xr_smem<T, N>());
+    }
     if constexpr (zr_r0(N) > 0) {
         // exactly what the launches request (up to 110 KB: FP64, length 96)
         cudaFuncSetAttribute(k_fft_zr<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)zr_smem<T, N>());

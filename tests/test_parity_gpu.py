@@ -274,7 +274,7 @@ def test_split_precision_short_horizon():
 
 
 @pytest.mark.parametrize("dims", [(66, 65, 66), (98, 65, 98), (34, 33, 130), (194, 129, 194), (18, 17, 258),
-                                  (34, 33, 386), (18, 17, 514)])
+                                  (34, 33, 386), (18, 17, 514), (386, 17, 18), (514, 17, 34)])
 def test_split_projection_matches_fp64(dims):
     """The split-path projection (FP32 transforms of 16-512 points, FP32 tridiagonal replays,
     the pivoting modes refined against the FP64 residual) against the FP64
