@@ -97,6 +97,8 @@ def load(build_if_missing: bool = True):
     L.cf_download_rhs.argtypes = [vp, C.c_int, C.c_int, dp]
     L.cf_download_avg_nu_t.argtypes = [vp, dp]
     L.cf_get_eqwm_counters.argtypes = [vp, ip, ip]
+    L.cf_copy_wait_expired.argtypes = [vp, ip]
+    L.cf_test_skip_plane_copy.argtypes = [vp, C.c_int]
     L.cf_time_step_rk3.argtypes = [vp, C.c_int, C.c_int]
     L.cf_get_stream.argtypes = [vp]
     L.cf_get_stream.restype = vp
@@ -288,6 +290,17 @@ class Channel:
         a, b = C.c_int(), C.c_int()
         self._check(self.L.cf_get_eqwm_counters(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def copy_wait_expired(self):
+        """Blocks of the FP32 multi-pass filter kernel whose plane-copy wait
+        expired since the last query (the count is cleared)."""
+        a = C.c_int()
+        self._check(self.L.cf_copy_wait_expired(self.h, C.byref(a)))
+        return a.value
+
+    def test_skip_plane_copy(self, on):
+        """Test hook: leave out the first plane copy of every filter block."""
+        self._check(self.L.cf_test_skip_plane_copy(self.h, 1 if on else 0))
 
     def statistics(self):
         out = np.zeros(9 * self.ny + 8)

@@ -856,12 +856,44 @@ static int eddy(cf_ctx *ctx, int b) {
     return DISPATCH(launch_nut_zero<double>(ctx), launch_nut_zero<float>(ctx));
 }
 
+// Reads and clears the count of plane copies of the filter kernel whose
+// bounded wait expired (only the tensor-copy gather waits on copies).
+static int take_copy_waits(cf_ctx *ctx, int *n) {
+    *n = 0;
+    if (ctx->dsmb_map_state != 1) return 0;
+    CF_CUDA(cudaMemcpyAsync(n, &ctx->ds->n_wait, sizeof(int), cudaMemcpyDeviceToHost, ctx->st));
+    CF_CUDA(cudaMemsetAsync(&ctx->ds->n_wait, 0, sizeof(int), ctx->st));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    return 0;
+}
+
+static int check_copy_waits(cf_ctx *ctx) {
+    int n;
+    TRY(take_copy_waits(ctx, &n));
+    if (n) return cf_fail(ctx, CF_ERR_CUDA, "a plane copy of the eddy-viscosity filter did not complete in time (" +
+                                                std::to_string(n) + " blocks stopped); nu_t is not valid");
+    return 0;
+}
+
+extern "C" int cf_copy_wait_expired(cf_ctx *ctx, int *expired) {
+    if (!ctx || !expired) return cf_fail(ctx, CF_ERR_INVALID, "null argument");
+    CF_CUDA(cudaSetDevice(ctx->dev));
+    CF_CUDA(cudaStreamSynchronize(ctx->st));
+    return take_copy_waits(ctx, expired);
+}
+
+extern "C" int cf_test_skip_plane_copy(cf_ctx *ctx, int on) {
+    if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
+    ctx->dsmb_skip_first = on ? 1 : 0;
+    return CF_OK;
+}
+
 extern "C" int cf_compute_eddy_viscosity(cf_ctx *ctx) {
     if (!ctx) return cf_fail(ctx, CF_ERR_INVALID, "null context");
     CF_CUDA(cudaSetDevice(ctx->dev));
     TRY(eddy(ctx, ctx->cur));
     CF_CUDA(cudaStreamSynchronize(ctx->st));
-    return CF_OK;
+    return check_copy_waits(ctx);
 }
 
 static int wall_model(cf_ctx *ctx, int b) {
@@ -1230,7 +1262,10 @@ extern "C" int cf_time_step_rk3(cf_ctx *ctx, int nsteps, int sync) {
         ctx->cur = ctx->next_buf[X];
         ctx->old = ctx->cur;
     }
-    if (sync) CF_CUDA(cudaStreamSynchronize(ctx->st));
+    if (sync) {
+        CF_CUDA(cudaStreamSynchronize(ctx->st));
+        TRY(check_copy_waits(ctx));
+    }
     return CF_OK;
 }
 

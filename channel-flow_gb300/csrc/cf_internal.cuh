@@ -69,7 +69,8 @@ struct DevScal {
     double lmax[3];        // compute_dt maxima (bit patterns ordered as int64)
     double mass_sum;       // mass-flow integral
     double fixed_dt;       // > 0: dt forced (CFL < 0 rule)
-    int rk_step, n_nan, n_iter, pad;
+    int rk_step, n_nan, n_iter;
+    int n_wait;            // plane copies whose bounded wait expired (filter kernel)
     // FP32 copies for the split path (written next to their FP64 values)
     float dtf, dPdxf, dPdzf, corrf;
 };
@@ -199,6 +200,13 @@ struct cf_ctx {
     int dsm_nchunk_fused = 0;
     bool use_fused_dsm = true;
     int dsmb_nkc = 0;                  // z chunks of the multi-pass DSM filter kernel
+    // tensor map (a CUtensorMap) of the 15 filter quantities of dsm_q for the
+    // filter kernel's tensor-copy gather; state 0 not tried, 1 encoded, -1 not
+    // applicable.  dsmb_skip_first: test hook, the first plane copy of every
+    // block is left out so that its bounded wait expires.
+    alignas(64) unsigned char dsmb_map[128] = {};
+    int dsmb_map_state = 0;
+    int dsmb_skip_first = 0;
     bool use_rhs3 = true;              // one fused RHS + update launch per substep
     int rhs_nkc = 1;                   // z chunks of the fused RHS
     int amd_nkc = 1;                   // z chunks of the AMD pass

@@ -8,7 +8,11 @@
 // i = 2..nxg-1, k = 2..nzg-1 like the reference, i.e. the duplicate column
 // i = nxg-1 and row k = nzg-1 (copies of i = 2, k = 2) are counted twice;
 // here that is a weight 2 on the canonical column/row 2.
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
+
 #include <algorithm>
+#include <cstring>
+#include <mutex>
 
 #include "cf_internal.cuh"
 
@@ -84,16 +88,35 @@ __device__ __forceinline__ T filt_can(const T *q, const Can &c, int nyg, int i, 
 // (subgrid.f90:429-513).  A block owns a DB_X x DB_Y tile of (i, j) and
 // marches along z over a chunk of planes: each plane of the 15 quantities
 // (tile plus one halo cell, periodic in x, rows clamped to the interior) is
-// gathered into one of two shared-memory buffers with cp.async while the
-// other is filtered; the FP32 kernel filters it in y by a column pass and in
-// x at its point (the FP64 kernel with a 9-point stencil at its point) and
-// spreads the result over the z accumulators of planes r-1, r, r+1 (weights
-// 1/6, 2/3, 1/6), so that plane r-1 is complete once plane r is in.  The
-// filtered velocities Uf, Vf, Wf (stage C) are read at their actual indices,
-// while the next plane's copies are in flight.  The plane sums (float-float
-// in the FP32 kernel) count the duplicate column and plane as weight 2 on
-// i = 2 and k = 2 (the reference's loops run over i = 2..nxg-1, k = 2..nzg-1).
+// gathered into a shared-memory buffer while an earlier one is filtered; the
+// FP32 kernel filters it in y by a column pass and in x at its point (the
+// FP64 kernel with a 9-point stencil at its point) and spreads the result
+// over the z accumulators of planes r-1, r, r+1 (weights 1/6, 2/3, 1/6), so
+// that plane r-1 is complete once plane r is in.  The filtered velocities
+// Uf, Vf, Wf (stage C) are read at their actual indices, while the next
+// plane's copies are in flight.  The plane sums (float-float in the FP32
+// kernel) count the duplicate column and plane as weight 2 on i = 2 and
+// k = 2 (the reference's loops run over i = 2..nxg-1, k = 2..nzg-1).
+//
+// Two gathers: per-element cp.async copies into two buffers (any nxp, FP64
+// and FP32), and for FP32 with nxp a multiple of 4 one tensor copy (TMA) per
+// plane into three buffers, two planes in flight.  The tensor copy is a 4D
+// box of x 40, y 10, z 1 and all 15 quantities; its x origin is 4 columns
+// before the tile's halo column (16-byte aligned), its y origin the row
+// before the tile.  Rows outside 0..nym-1 arrive as zeros and meet only the
+// zero weights of the one-sided y filter (the cp.async gather clamps them
+// instead: the products are 0 either way); the periodic halo columns
+// (canonical -1 -> nxp-1 at the first tile, nxp -> 0 at the last) arrive as
+// zeros too and are overwritten from registers loaded before the wait.
 constexpr int DB_X = 32, DB_Y = 8, DB_NQ = 15;
+constexpr int DBT_BX = DB_X + 8, DBT_BY = DB_Y + 2, DBT_OX = 3;  // box extents; column of halo column 0
+constexpr int DBT_PLANE = DBT_BX * DBT_BY;                        // floats per quantity in a buffer
+constexpr unsigned DBT_BYTES = DB_NQ * DBT_PLANE * 4;             // 24000 bytes per plane
+constexpr int DBT_STRIDE = (int)((DBT_BYTES + 127) / 128 * 128);  // buffer stride: 128-byte aligned
+constexpr int DBT_NB = 3;                                         // buffers: the plane filtered + 2 in flight
+constexpr int DBT_NFIX = 2 * DB_NQ * DBT_BY;                      // periodic halo values of a plane
+// a plane copy is given up after this long (it completes within microseconds)
+constexpr uint64_t DBT_WAIT_NS = 200000000ull;
 
 // asynchronous global -> shared copies of single elements (the plane gather
 // of the next z plane runs while the current one is filtered)
@@ -105,17 +128,56 @@ __device__ __forceinline__ void cp_async_elem(void *smem, const void *gmem) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
-// dynamic shared memory of k_dsm_b: two planes of the 15 quantities
-template <typename T>
-constexpr size_t dsm_b_smem() { return (size_t)2 * DB_NQ * (DB_X + 2) * (DB_Y + 2) * sizeof(T); }
+__device__ __forceinline__ uint32_t sh_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint64_t dbt_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+// wait for phase `parity` of the mbarrier at shared address `mb`; false when
+// DBT_WAIT_NS passed first
+__device__ __forceinline__ bool dbt_wait(uint32_t mb, uint32_t parity) {
+    const uint64_t t0 = dbt_ns();
+    for (long it = 0; it < (1L << 24); it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(ok)
+            : "r"(mb), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if ((it & 31) == 31 && dbt_ns() - t0 > DBT_WAIT_NS) return false;
+    }
+    return false;
+}
+// dynamic shared memory of k_dsm_b: the plane buffers of the 15 quantities
+template <typename T, bool TMA>
+constexpr size_t dsm_b_smem() {
+    return TMA ? (size_t)DBT_NB * DBT_STRIDE + 128 : (size_t)2 * DB_NQ * (DB_X + 2) * (DB_Y + 2) * sizeof(T);
+}
 
-template <typename T>
-__global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, GeoT<T> g, RcpT<T> rc, Fld<T> Uf,
-                                                      Fld<T> Vf, Fld<T> Wf, Can c, int nyg, int kc_len, double *part,
-                                                      int nchunk) {
+// TMA: the tensor-copy gather (FP32, nxp a multiple of 4; tm maps the 15
+// quantities of q as x nxp, y nym, z nzp, quantity 15).  skip_first (a test
+// hook): plane kb-1 is not copied, so its wait expires and the block stops.
+// A wait that expired is counted in ds->n_wait; the block's copies still in
+// flight are waited for (with the same limit) before it returns.
+template <typename T, bool TMA>
+__global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const __grid_constant__ CUtensorMap tm, const T *__restrict__ q,
+                                                      GeoT<T> g, RcpT<T> rc, Fld<T> Uf, Fld<T> Vf, Fld<T> Wf, Can c,
+                                                      int nyg, int kc_len, double *part, int nchunk, DevScal *ds,
+                                                      int skip_first) {
+    static_assert(!TMA || sizeof(T) == 4, "the tensor-copy gather is the FP32 kernel's");
     constexpr int SX = DB_X + 2, SY = DB_Y + 2, NP = SX * SY;
+    // a buffer: DB_NQ quantities of PQ elements, rows of pitch PX, halo
+    // column 0 at column OX
+    constexpr int PX = TMA ? DBT_BX : SX, PQ = TMA ? DBT_PLANE : NP, OX = TMA ? DBT_OX : 0;
+    constexpr int NB = TMA ? DBT_NB : 2, BS = TMA ? DBT_STRIDE / (int)sizeof(T) : DB_NQ * NP;
     extern __shared__ __align__(16) unsigned char dsmb_raw[];
-    T *plb = (T *)dsmb_raw;  // [2 planes][DB_NQ][NP]
+    // tensor-copy destinations are 128-byte aligned
+    T *plb = (T *)(dsmb_raw + (TMA ? (128 - (sh_u32(dsmb_raw) & 127)) & 127 : 0));  // [NB][DB_NQ][PQ]
+    __shared__ __align__(8) uint64_t bar[NB];
     // the plane filtered in y, rows of the tile (FP32: within 48 KB of static
     // shared memory with the plane; the FP64 kernel filters from the plane)
     constexpr bool COLS = sizeof(T) == 4;
@@ -136,26 +198,83 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
     // split path (an FP64 instruction per cell costs dozens of FP32 ones here)
     double sl = 0.0, smm = 0.0;
     float slh = 0.f, sll = 0.f, smh = 0.f, sml = 0.f;
-    // gather of plane r (tile plus one halo cell, periodic in x, rows clamped
-    // to the interior) into buffer b, as one group of asynchronous copies
+    // gather of plane r into buffer b: one tensor copy issued by thread 0
+    // (TMA), or one group of per-element asynchronous copies (tile plus one
+    // halo cell, periodic in x, rows clamped to the interior)
     auto issue = [&](int r, int b) {
         const int rc_ = wrapn(r, c.nzp);
-        for (int e = threadIdx.x; e < NP; e += DB_X * DB_Y) {
-            const int sy = e / SX, sx = e - sy * SX;
-            // columns past the domain's last halo are never read: clamp them in range
-            const int ii = wrapn(min(i0 + sx - 1, c.nxp + 2), c.nxp), jj = min(max(j0 + sy - 1, 2), nyg - 1);
-            const long o = c(ii, jj, rc_);
+        if constexpr (TMA) {
+            if (threadIdx.x == 0) {
+                const uint32_t mb = sh_u32(&bar[b]);
+                const int x0 = blockIdx.x * DB_X - 4, y0 = blockIdx.y * DB_Y - 1, z0 = rc_ - 2;
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(mb), "r"(DBT_BYTES)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                    "[%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(sh_u32(plb + b * BS)),
+                    "l"(reinterpret_cast<uint64_t>(&tm)), "r"(x0), "r"(y0), "r"(z0), "r"(0), "r"(mb)
+                    : "memory");
+            }
+        } else {
+            for (int e = threadIdx.x; e < NP; e += DB_X * DB_Y) {
+                const int sy = e / SX, sx = e - sy * SX;
+                // columns past the domain's last halo are never read: clamp them in range
+                const int ii = wrapn(min(i0 + sx - 1, c.nxp + 2), c.nxp), jj = min(max(j0 + sy - 1, 2), nyg - 1);
+                const long o = c(ii, jj, rc_);
 #pragma unroll
-            for (int qq = 0; qq < DB_NQ; qq++) cp_async_elem<sizeof(T)>(plb + (b * DB_NQ + qq) * NP + e, q + o + qq * n);
+                for (int qq = 0; qq < DB_NQ; qq++) cp_async_elem<sizeof(T)>(plb + (b * DB_NQ + qq) * NP + e, q + o + qq * n);
+            }
+            cp_async_commit();
         }
-        cp_async_commit();
     };
-    issue(kb - 1, 0);
+    // periodic halo columns of the tensor-copy gather: column 0 of the first
+    // tile holds canonical nxp-1, column sxr = nxp - 32 bx + 1 (when inside
+    // the tile's 34 columns) canonical 0.  Task t < DBT_NFIX: side t / 150,
+    // quantity (t % 150) / 10, row t % 10; rows outside 0..nym-1 stay 0.
+    const int sxr = c.nxp - (int)blockIdx.x * DB_X + 1;
+    const bool fixl = TMA && blockIdx.x == 0, fixr = TMA && sxr >= 1 && sxr <= SX - 1;
+    const bool fixb = fixl || fixr;  // block-uniform
+    constexpr int NFT = (DBT_NFIX + DB_X * DB_Y - 1) / (DB_X * DB_Y);
+    if constexpr (TMA) {
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int b = 0; b < NB; b++) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(sh_u32(&bar[b])));
+            asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        }
+        __syncthreads();
+        for (int p = 0; p < NB - 1 && kb - 1 + p <= ke + 1; p++)
+            if (!(skip_first && p == 0)) issue(kb - 1 + p, p);
+    } else {
+        issue(kb - 1, 0);
+    }
+    int rfail = 0;
     for (int r = kb - 1; r <= ke + 1; r++) {
-        const int cur = (r - (kb - 1)) & 1;
-        T(*pl)[NP] = (T(*)[NP])(plb + cur * DB_NQ * NP);
-        __syncthreads();  // plane r-1 (the other buffer) is no longer read
-        if (r + 1 <= ke + 1) issue(r + 1, cur ^ 1);
+        const int u = r - (kb - 1), cur = u % NB;
+        T(*pl)[PQ] = (T(*)[PQ])(plb + cur * BS);
+        __syncthreads();  // plane r-1 (the buffer refilled next) is no longer read
+        if constexpr (TMA) {
+            if (r + NB - 1 <= ke + 1) issue(r + NB - 1, (u + NB - 1) % NB);
+        } else {
+            if (r + 1 <= ke + 1) issue(r + 1, cur ^ 1);
+        }
+        // the periodic halo values of plane r, loaded before the wait
+        float fxv[NFT];
+        int fxo[NFT];
+        if constexpr (TMA) {
+            if (fixb) {
+                const int z = wrapn(r, c.nzp) - 2;
+#pragma unroll
+                for (int f = 0; f < NFT; f++) {
+                    const int t = threadIdx.x + f * DB_X * DB_Y, side = t / (DB_NQ * DBT_BY);
+                    const int qq = (t % (DB_NQ * DBT_BY)) / DBT_BY, sy = t % DBT_BY, y = (int)blockIdx.y * DB_Y - 1 + sy;
+                    const bool on = t < DBT_NFIX && (side == 0 ? fixl : fixr) && y >= 0 && y < c.nym;
+                    fxo[f] = on ? qq * PQ + sy * PX + OX + (side == 0 ? 0 : sxr) : -1;
+                    fxv[f] = on ? (float)q[(long)qq * n + (side == 0 ? c.nxp - 1 : 0) + (long)c.nxp * (y + (long)c.nym * z)]
+                                : 0.f;
+                }
+            }
+        }
         // S_ij of the filtered velocities at the output plane k = r-1
         // (fil_size**2 = 4 in M, subgrid.f90:156, 463), read from global
         // memory while the plane copies are in flight
@@ -163,9 +282,27 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
         const bool outp = own && k >= kb;
         T sf[6], Sf = T(0);
         if (outp) sij_point<T>(g, rc, Uf, Vf, Wf, i, j, k, sf, Sf);
-        if (r + 1 <= ke + 1) cp_async_wait<1>();  // this thread's copies of plane r are done
-        else cp_async_wait<0>();
-        __syncthreads();  // and every thread's
+        if constexpr (TMA) {
+            // plane r has landed (every thread observes the phase; the block
+            // agrees on the outcome)
+            const bool ok = dbt_wait(sh_u32(&bar[cur]), (u / NB) & 1);
+            if (!__syncthreads_and(ok)) {
+                rfail = r;
+                break;
+            }
+            if (fixb) {
+#pragma unroll
+                for (int f = 0; f < NFT; f++)
+                    if (fxo[f] >= 0) ((float *)pl[0])[fxo[f]] = fxv[f];
+                // these generic writes precede the tensor copy that refills the buffer
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                __syncthreads();
+            }
+        } else {
+            if (r + 1 <= ke + 1) cp_async_wait<1>();  // this thread's copies of plane r are done
+            else cp_async_wait<0>();
+            __syncthreads();  // and every thread's
+        }
         // y filter, one (quantity, column) per task: the column's SY values
         // give the DB_Y filtered rows (one-sided at rows 2 and nyg-1)
         if constexpr (COLS) {
@@ -173,7 +310,7 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
             const int qq = t / SX, sx = t - qq * SX;
             T col[SY];
 #pragma unroll
-            for (int sy = 0; sy < SY; sy++) col[sy] = pl[qq][sy * SX + sx];
+            for (int sy = 0; sy < SY; sy++) col[sy] = pl[qq][sy * PX + sx + OX];
 #pragma unroll
             for (int oy = 0; oy < DB_Y; oy++) {
                 const int jr = j0 + oy;
@@ -186,7 +323,7 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
         if (!own) continue;
         // y weights of this row for the FP64 kernel (one-sided at rows 2 and nyg-1)
         const T wm = j == 2 ? T(0) : (j == nyg - 1 ? f13 : f6), wp = j == 2 ? f13 : (j == nyg - 1 ? T(0) : f6);
-        const int e = (ty + 1) * SX + tx + 1;
+        const int e = (ty + 1) * PX + tx + 1 + OX;
         T fq[DB_NQ];
 #pragma unroll
         for (int qq = 0; qq < DB_NQ; qq++) {
@@ -194,7 +331,7 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
 #pragma unroll
             for (int d = -1; d <= 1; d++) {
                 if constexpr (COLS) a += fw[d + 1] * cl[qq][ty][tx + 1 + d];
-                else a += fw[d + 1] * (wm * pl[qq][e + d - SX] + f23 * pl[qq][e + d] + wp * pl[qq][e + d + SX]);
+                else a += fw[d + 1] * (wm * pl[qq][e + d - PX] + f23 * pl[qq][e + d] + wp * pl[qq][e + d + PX]);
             }
             fq[qq] = accp[qq] + f6 * a;  // plane r-1, complete
             accp[qq] = accc[qq] + f23 * a;
@@ -219,6 +356,20 @@ __global__ void __launch_bounds__(DB_X *DB_Y) k_dsm_b(const T *__restrict__ q, G
             const double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
             sl += wgt * (double)lm;
             smm += wgt * (double)mm;
+        }
+    }
+    if constexpr (TMA) {
+        if (rfail) {
+            // a plane copy did not arrive in time: count it, wait for the
+            // copies still in flight (planes rfail .. rfail + NB - 1) and stop
+            if (threadIdx.x == 0) {
+                atomicAdd(&ds->n_wait, 1);
+                for (int p = rfail; p <= min(rfail + NB - 1, ke + 1); p++) {
+                    const int u = p - (kb - 1);
+                    if (!(skip_first && u == 0)) dbt_wait(sh_u32(&bar[u % NB]), (u / NB) & 1);
+                }
+            }
+            return;
         }
     }
     if constexpr (sizeof(T) == 4) {
@@ -448,6 +599,51 @@ int launch_nut_zero(cf_ctx *ctx) {
     return 0;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult qr = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &qr) ==
+                cudaSuccess &&
+            qr == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    });
+    return fn;
+}
+
+// Whether the multi-pass filter kernel gathers its planes with tensor copies:
+// FP32, nxp a multiple of 4 (16-byte strides and x origins), at least 40 x 10
+// canonical cells per plane (the box), not switched off (dsm_unfused 2).  The
+// tensor map of the 15 quantities of dsm_q is encoded on the first call.
+bool dsmb_tma(cf_ctx *ctx) {
+    if (ctx->dsmb_map_state == 0) {
+        ctx->dsmb_map_state = -1;
+        EncodeTiledFn fn = encode_tiled();
+        if (ctx->esz == 4 && ctx->nxp % 4 == 0 && ctx->nxp >= DBT_BX && ctx->nym >= DBT_BY && fn) {
+            CUtensorMap m;
+            const cuuint64_t dims[4] = {(cuuint64_t)ctx->nxp, (cuuint64_t)ctx->nym, (cuuint64_t)ctx->nzp, DB_NQ};
+            const cuuint64_t strides[3] = {(cuuint64_t)ctx->nxp * 4, (cuuint64_t)ctx->nxp * ctx->nym * 4,
+                                           (cuuint64_t)ctx->nCan * 4};
+            const cuuint32_t box[4] = {DBT_BX, DBT_BY, 1, DB_NQ}, es[4] = {1, 1, 1, 1};
+            if (fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, ctx->dsm_q, dims, strides, box, es,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS) {
+                static_assert(sizeof(m) == sizeof(ctx->dsmb_map), "tensor map storage");
+                std::memcpy(ctx->dsmb_map, &m, sizeof(m));
+                ctx->dsmb_map_state = 1;
+            }
+        }
+    }
+    return ctx->dsmb_map_state == 1 && ctx->prm.dsm_unfused != 2;
+}
+
 template <typename T>
 int launch_dsm(cf_ctx *ctx, int b) {
     int dir = ctx->prm.Dirichlet_nu_t == 1;
@@ -498,8 +694,19 @@ int launch_dsm(cf_ctx *ctx, int b) {
         const int kc_len = cdiv(ctx->nzp, nkc);
         const int nz_chunks = cdiv(ctx->nzp, kc_len);
         nchunk = ntx * nz_chunks;
-        k_dsm_b<T><<<dim3(ntx, cdiv(ctx->nym, DB_Y), nz_chunks), DB_X * DB_Y, dsm_b_smem<T>(), ctx->st>>>(
-            q, g, rc, Uf, Vf, Wf, c, ctx->nyg, kc_len, ctx->dsm_part, nchunk);
+        const dim3 grd(ntx, cdiv(ctx->nym, DB_Y), nz_chunks);
+        CUtensorMap tm;
+        if (dsmb_tma(ctx)) {
+            std::memcpy(&tm, ctx->dsmb_map, sizeof(tm));
+            k_dsm_b<float, true><<<grd, DB_X * DB_Y, dsm_b_smem<float, true>(), ctx->st>>>(
+                tm, (const float *)q, geo_of<float>(ctx), rcp_of<float>(ctx), make_fld<float>(ctx->Uf, ctx->nx, ctx->nyg),
+                make_fld<float>(ctx->Vf, ctx->nxg, ctx->ny), make_fld<float>(ctx->Wf, ctx->nxg, ctx->nyg), c, ctx->nyg,
+                kc_len, ctx->dsm_part, nchunk, ctx->ds, ctx->dsmb_skip_first);
+        } else {
+            std::memset(&tm, 0, sizeof(tm));  // not read by the per-element gather
+            k_dsm_b<T, false><<<grd, DB_X * DB_Y, dsm_b_smem<T, false>(), ctx->st>>>(
+                tm, q, g, rc, Uf, Vf, Wf, c, ctx->nyg, kc_len, ctx->dsm_part, nchunk, ctx->ds, 0);
+        }
         count_launch(ctx, "k_dsm_b");
     }
     if (sizeof(T) == 4)  // float-float partials of the FP32 kernel
@@ -529,8 +736,11 @@ template int launch_nut_zero<float>(cf_ctx *);
 // again); its plane partials take ceil(nxp / 32) x nkc slots per row
 int dsm_b_plan(int esz, int nxp, int nym, int nzp, int sms) {
     int per = 1;
-    if (esz == 4) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dsm_b<float>, DB_X * DB_Y, dsm_b_smem<float>());
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dsm_b<double>, DB_X * DB_Y, dsm_b_smem<double>());
+    if (esz == 4)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dsm_b<float, true>, DB_X * DB_Y, dsm_b_smem<float, true>());
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_dsm_b<double, false>, DB_X * DB_Y,
+                                                      dsm_b_smem<double, false>());
     const long tiles = (long)cdiv(nxp, DB_X) * cdiv(nym, DB_Y), res = (long)(per < 1 ? 1 : per) * sms;
     long best = 1;
     double best_cost = 1e300;
@@ -548,7 +758,11 @@ int dsm_b_plan(int esz, int nxp, int nym, int nzp, int sms) {
 // shared-memory opt-in of the multi-pass filter kernel (two planes in dynamic
 // shared memory; called at context creation)
 int dsm_b_setup() {
-    cudaFuncSetAttribute(k_dsm_b<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm_b_smem<float>());
-    cudaFuncSetAttribute(k_dsm_b<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm_b_smem<double>());
+    cudaFuncSetAttribute(k_dsm_b<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)dsm_b_smem<float, true>());
+    cudaFuncSetAttribute(k_dsm_b<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)dsm_b_smem<float, false>());
+    cudaFuncSetAttribute(k_dsm_b<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)dsm_b_smem<double, false>());
     return 0;
 }

@@ -258,6 +258,18 @@ Module channel_gpu
        Integer(c_int)     :: n_nan, n_iter
      End Function cf_get_eqwm_counters
 
+     Integer(c_int) Function cf_copy_wait_expired(ctx, expired) Bind(C, name="cf_copy_wait_expired")
+       Import :: c_int, c_ptr
+       Type(c_ptr), Value :: ctx
+       Integer(c_int)     :: expired
+     End Function cf_copy_wait_expired
+
+     Integer(c_int) Function cf_test_skip_plane_copy(ctx, on) Bind(C, name="cf_test_skip_plane_copy")
+       Import :: c_int, c_ptr
+       Type(c_ptr), Value    :: ctx
+       Integer(c_int), Value :: on
+     End Function cf_test_skip_plane_copy
+
      !-------------------------------------------------------------- fast path
      Integer(c_int) Function cf_time_step_rk3(ctx, nsteps, sync) Bind(C, name="cf_time_step_rk3")
        Import :: c_int, c_ptr

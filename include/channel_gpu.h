@@ -59,7 +59,9 @@ typedef struct {
                               (time_integration.f90:103) inside cf_time_step_rk3;
                               0: reuse the first one (bit-identical inputs)      */
     int dsm_unfused;       /* 1: evaluate the dynamic Smagorinsky model with the
-                              multi-pass kernels even where the fused pass applies */
+                              multi-pass kernels even where the fused pass applies;
+                              2: the same with the filter kernel's per-element
+                              plane gather instead of tensor copies             */
     int cfl_corrected;     /* 1: convective limit of compute_dt with the minimum
                               over cells of spacing/|u| (the reference takes the
                               maximum, time_integration.f90:191-201, which leaves
@@ -139,6 +141,16 @@ int cf_download_rhs(cf_ctx *ctx, int comp, int slot, double *out);
 int cf_download_avg_nu_t(cf_ctx *ctx, double *out);
 /* eqwm counters of the last wall-model call (wallmodel.f90:623-653). */
 int cf_get_eqwm_counters(cf_ctx *ctx, int *n_nan, int *n_iter);
+/* The multi-pass dynamic Smagorinsky filter kernel of the FP32 path gathers
+ * its planes with tensor copies and waits for each with a time limit (0.2 s);
+ * a block whose wait expired stops and is counted.  cf_copy_wait_expired
+ * synchronises, returns that count since the last query in *expired and
+ * clears it; cf_compute_eddy_viscosity and cf_time_step_rk3 (sync != 0)
+ * return CF_ERR_CUDA when it is nonzero.  cf_test_skip_plane_copy (a test
+ * hook) leaves out the first plane copy of every block so that its wait
+ * expires. */
+int cf_copy_wait_expired(cf_ctx *ctx, int *expired);
+int cf_test_skip_plane_copy(cf_ctx *ctx, int on);
 /* The inputs the equilibrium wall model hands to its ODE solve for the
  * current fields (wallmodel.f90:597-621): *npts = nx * 2 * (nz+1) wall
  * points, u_les (device array of cap >= *npts doubles, wall-point order

@@ -318,6 +318,61 @@ def test_dsm_fused_matches_multipass(precision, tol):
     assert_close(out[0][1][1:-1], out[1][1][1:-1], tol, "avg_nu_t")
 
 
+@pytest.mark.parametrize("dims,wall", [((66, 65, 66), 0), ((50, 33, 34), 0), ((42, 11, 18), 0), ((102, 17, 42), 3),
+                                       ((194, 129, 194), 3)])
+def test_dsm_tensor_copy_gather_matches_element_gather(dims, wall):
+    """The FP32 multi-pass filter kernel with its tensor-copy (TMA) plane
+    gather against the per-element gather (dsm_unfused 2), bit for bit in
+    nu_t and avg_nu_t: nxp a multiple of 32 (64, 192), of 4 only (48, 100),
+    the smallest box-sized plane (40 x 10), and the wall model's
+    non-periodic ghost rows (after one wall-model call)."""
+    import channelflow as cf
+    extra = dict(stretch=0.0, wall=3, retau=2000.0, profile="plug") if wall else {}
+    case = channel_case(*dims, seed=7, **extra)
+    out = []
+    for mode in (1, 2):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_SPLIT, dsm_unfused=mode, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.apply_boundary_conditions()
+        ch.compute_eddy_viscosity()
+        if wall:
+            ch.compute_wall_model()
+            ch.apply_boundary_conditions()
+            ch.compute_eddy_viscosity()
+        assert ch.copy_wait_expired() == 0
+        out.append((ch.download()["nu_t"], ch.avg_nu_t()))
+        ch.close()
+    assert np.array_equal(out[0][0], out[1][0]), rel_err(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1]), rel_err(out[0][1], out[1][1])
+
+
+def test_dsm_plane_copy_wait_expires():
+    """A plane copy that never arrives (test hook: the first copy of every
+    block is left out): the blocks' bounded waits expire, the eddy viscosity
+    call reports it (CF_ERR_CUDA) and clears the count, and with the hook off
+    the same context gives the nu_t of a clean one."""
+    import channelflow as cf
+    case = channel_case(66, 65, 66, seed=3)
+    ref = None
+    for hook in (False, True):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_SPLIT, dsm_unfused=1, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.apply_boundary_conditions()
+        if hook:
+            ch.test_skip_plane_copy(True)
+            with pytest.raises(cf.CfError, match="plane copy"):
+                ch.compute_eddy_viscosity()
+            assert ch.copy_wait_expired() == 0  # cleared by the failed call
+            ch.test_skip_plane_copy(False)
+        ch.compute_eddy_viscosity()
+        nut = ch.download()["nu_t"]
+        ch.close()
+        if ref is None:
+            ref = nut
+        else:
+            assert np.array_equal(nut, ref)
+
+
 def test_pinned_host_buffers_match_pageable():
     """Uploads and downloads through page-locked host arrays (converted by the
     kernels over the host link) give the same bits as pageable arrays
