@@ -86,6 +86,14 @@ struct WmState {
     double *tau_eq;
 };
 
+// Largest ncv for which the split path keeps each point's exponentials of
+// the last FP64 pass in shared memory (128 threads x (ncv-1) doubles: 45 KB).
+constexpr int EQ_EXP_NCV = 45;
+// offset (in doubles) of the kept exponentials: past the grid arrays
+__host__ __device__ __forceinline__ int eq_exp_off(int ncv) {
+    return (2 * ncv + 3) + ((2 * ncv + 4) * (int)sizeof(float) + 7) / 8;
+}
+
 // solve_u_eqwm (eqwm.f90:90-223) inline, grid in shared memory:
 // yfa[1..ncv+1], idcv[i] = 1/(y_cv(i+1)-y_cv(i)) (i = 1..ncv-1),
 // rw = 1/(y_cv(1)-y_fa(1)); grid[1..ncv] = y_cv, grid[ncv+1..2ncv+1] = y_fa.
@@ -97,9 +105,14 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
                            int nut_f32, double *tau0, double *alpha_x, double *alpha_zt, int *counters, WmState wm) {
     extern __shared__ double sg[];
     const int ncv = ep.ncv;
-    // grid: yfa[1..ncv+1], idcv[1..ncv-1], rw; FP32 copies after them
+    // grid: yfa[1..ncv+1], idcv[1..ncv-1], rw; FP32 copies after them; then
+    // (split path, ncv <= EQ_EXP_NCV) this thread's exponentials of the
+    // last FP64 pass, Ex[(q - 2) * blockDim.x + threadIdx.x] for q = 2..ncv
     double *yfa = sg, *idcv = sg + ncv + 2;
     float *yfa32 = (float *)(idcv + ncv + 1), *idcv32 = yfa32 + ncv + 2;
+    double *Ex = sg + eq_exp_off(ncv) + threadIdx.x;
+    const int exs = blockDim.x;
+    const bool keep_ex = ep.mixed && ncv <= EQ_EXP_NCV;
     for (int q = threadIdx.x; q < ncv + 2; q += blockDim.x) {
         yfa[q] = q >= 1 && q <= ncv + 1 ? grid[ncv + q] : 0.0;
         yfa32[q] = (float)yfa[q];
@@ -170,7 +183,16 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
             }
         }
         // one FP64 Picard pass of solve_u_eqwm (eqwm.f90:121-205): tau from
-        // the mixing-length viscosity of the previous tau
+        // the mixing-length viscosity of the previous tau.  In the split path
+        // (keep_ex) a pass whose factor cd differs from the last pass's by
+        // |dcd| yfa[ncv] <= 1e-3 takes exp(-(y cd)) as the last pass's value
+        // times exp(-(y dcd)), the latter as its degree-4 Taylor polynomial
+        // (truncation below 1e-17 relative), instead of evaluating exp; and
+        // the elimination runs in continuant form (below), as accurate as the
+        // division per cell of the reference's Thomas sweep (both within a
+        // few 1e-14 of exact rational elimination on the same coefficients
+        // at ncv 30).
+        double cd_last = -1.0;  // no exponentials kept yet
         auto pass64 = [&](double tau) -> double {
             double nu_eq = mu_lam / rho;
             double utau = sqrt(tau / rho);
@@ -178,26 +200,81 @@ __global__ void k_eq_solve(const Fld<double> Ud, const float *Uf32, int use_f32,
             // y utau / nu / A+ of eqwm.f90:134-136 with the per-pass factor
             // formed once (two FP64 divisions less per cell)
             const double cd = utau / nu_eq / Aplus;
-            double al = u_les, be = 0.0;
+            const double dcd = cd - cd_last;
+            const double xmax = fabs(dcd) * yfa[ncv];
+            const bool upd = keep_ex && cd_last >= 0.0 && xmax <= 1e-3, low = xmax <= 1e-6;
+            if (keep_ex) cd_last = cd;
+            auto ex = [&](int q, double yf) -> double {
+                double e;
+                if (upd) {
+                    // |x| <= 1e-6: degree 2 (truncation x^3/6 < 2e-19)
+                    const double x = -(yf * dcd);
+                    const double p = low ? 1.0 + x * (1.0 + 0.5 * x)
+                                         : 1.0 + x * (1.0 + x * (0.5 + x * (1.0 / 6.0 + x * (1.0 / 24.0))));
+                    e = Ex[(q - 2) * exs] * p;
+                } else {
+                    e = exp(-(yf * cd));
+                }
+                if (keep_ex) Ex[(q - 2) * exs] = e;
+                return e;
+            };
             double yf = yfa[ncv];
-            double D = 1.0 - exp(-(yf * cd));
+            double D = 1.0 - ex(ncv, yf);
             double mu_up = mu_lam + c1 * yf * (D * D);
+            if (!ep.mixed) {
+                double al = u_les, be = 0.0;
+                for (int q = ncv - 1; q >= 2; q--) {
+                    yf = yfa[q];
+                    D = 1.0 - ex(q, yf);
+                    double mu_q = mu_lam + c1 * yf * (D * D);
+                    double sup = mu_up * idcv[q];
+                    double sub = mu_q * idcv[q - 1];
+                    double m = -1.0 * (sup + sub) + sup * be;
+                    double rm = 1.0 / m;
+                    al = -sup * al * rm;
+                    be = -sub * rm;
+                    mu_up = mu_q;
+                }
+                double sup = mu_up * idcv[1];
+                double diag = -1.0 * (sup + mu_lam * rw);
+                double x1 = -sup * al / (diag + sup * be);
+                return mu_lam * (x1 - 0.0) * rw;
+            }
+            // Split path: the same elimination without a division per cell.
+            // With the pivots m_q = Dn_q / Dn_{q+1} (Dn_ncv = 1) the
+            // continuants follow Dn_q = -(sup_q + sub_q) Dn_{q+1} -
+            // sup_q sub_{q+1} Dn_{q+2}, and A_q = al_q Dn_q = -sup_q A_{q+1};
+            // be_2 = -sub_2 Dn_3 / Dn_2, al_2 = A_2 / Dn_2, so the first cell's
+            // unknown is one quotient.  sup_q = sub_{q+1} (both mu_{q+1} /
+            // (y_cv(q+1) - y_cv(q))).  Dn, A are rescaled by powers of two
+            // (exact) every 8 cells to stay in range.
+            double Dn1 = 1.0, Dn2 = 0.0, A = u_les, subp = 0.0;
+            double sup = mu_up * idcv[ncv - 1];
             for (int q = ncv - 1; q >= 2; q--) {
                 yf = yfa[q];
-                D = 1.0 - exp(-(yf * cd));
-                double mu_q = mu_lam + c1 * yf * (D * D);
-                double sup = mu_up * idcv[q];
-                double sub = mu_q * idcv[q - 1];
-                double m = -1.0 * (sup + sub) + sup * be;
-                double rm = 1.0 / m;
-                al = -sup * al * rm;
-                be = -sub * rm;
-                mu_up = mu_q;
+                D = 1.0 - ex(q, yf);
+                const double mu_q = mu_lam + c1 * yf * (D * D);
+                const double sub = mu_q * idcv[q - 1];
+                const double Dn = fma(-(sup + sub), Dn1, -(sup * subp) * Dn2);
+                A = -sup * A;
+                Dn2 = Dn1;
+                Dn1 = Dn;
+                subp = sub;
+                sup = sub;
+                if ((q & 7) == 0) {
+                    const int e = ((__double2hiint(Dn1) >> 20) & 0x7ff) - 1023;
+                    if (e > 512 || e < -512) {
+                        const double sc = __hiloint2double((1023 - e) << 20, 0);  // 2^-e
+                        Dn1 *= sc;
+                        Dn2 *= sc;
+                        A *= sc;
+                    }
+                }
             }
-            double sup = mu_up * idcv[1];
-            double diag = -1.0 * (sup + mu_lam * rw);
-            double x1 = -sup * al / (diag + sup * be);
-            return mu_lam * (x1 - 0.0) * rw;
+            // sup = mu_2 / (y_cv(2) - y_cv(1)) of the first cell
+            const double diag = -1.0 * (sup + mu_lam * rw);
+            const double x1 = -sup * A / (diag * Dn1 - sup * subp * Dn2);
+            return mu_lam * x1 * rw;
         };
         bool fin = false;
         if (ep.mixed && mixed_ok) {
@@ -335,7 +412,8 @@ int launch_eqwm(cf_ctx *ctx, int b) {
     ep.mixed = sizeof(T) == 4;
     CF_CUDA(cudaMemsetAsync(ctx->d_red, 0, 2 * sizeof(int), ctx->st));
     long npts = (long)nx * nzg * 2;
-    size_t sh = (size_t)(2 * ep.ncv + 4) * (sizeof(double) + sizeof(float));
+    size_t sh = (size_t)eq_exp_off(ep.ncv) * sizeof(double);
+    if (ep.mixed && ep.ncv <= EQ_EXP_NCV) sh += (size_t)(ep.ncv - 1) * 128 * sizeof(double);
     Fld<double> Ud = make_fld<double>(ctx->U[b], nx, nyg);
     WmState wm = {};
     if (ctx->wmlp) {

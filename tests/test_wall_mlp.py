@@ -308,6 +308,36 @@ def test_wall_model_inputs_are_the_solver_inputs():
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("ncv", [30, 45, 60])
+def test_split_eqwm_stress_matches_oracle_solve(ncv):
+    """The split path's eqwm solve (FP32 Picard passes, then FP64 passes;
+    for ncv <= 45 the later FP64 passes update the previous pass's
+    exponentials by a Taylor factor instead of evaluating exp) against the
+    oracle's solve_u_eqwm (eqwm.f90:90-223) of every wall point on the same
+    inputs and warm start: both stop at the reference's criterion
+    |d tau / tau_lam| < 1e-7, so they agree to a few 1e-7 of tau_lam."""
+    from oracle import solve_u_eqwm
+    import channelflow as cf
+    from channelflow import wallmlp
+    from conftest import channel_case
+    case = channel_case(18, 17, 18, stretch=0.0, wall=3, retau=2000.0, profile="plug", jref=3, ncv=ncv)
+    ch = cf.Channel(case["x"], case["y"], case["z"], precision=cf.PREC_SPLIT, **case["prm"])
+    ch.upload(case["U"], case["V"], case["W"])
+    ch.apply_boundary_conditions()
+    ch.compute_eddy_viscosity()
+    tau_in = np.ravel(ch.download_wall()["tau_eqwm_initial"], order="F")
+    u, h, nu = wallmlp.wall_model_inputs(ch)
+    u = u.cpu().numpy()
+    ch.compute_wall_model()
+    tau = np.ravel(ch.download_wall()["tau_eqwm_initial"], order="F")
+    ch.close()
+    ref = np.array([solve_u_eqwm(u[q], nu, h, ncv, 1.10, tau_in[q])[0] for q in range(u.size)])
+    tau_lam = nu * u / h
+    err = np.abs(tau - ref) / tau_lam
+    assert np.all(np.isfinite(tau)) and err.max() < 2e-6, err.max()
+
+
+@pytest.mark.gpu
 def test_harvested_solver_samples():
     """Samples drawn from the solver's own wall-modelled runs across the
     operating range: finite, positive, labelled by eqwm, and mixed into a
