@@ -55,33 +55,6 @@ __global__ void k_dsm_a(GeoT<T> g, RcpT<T> rc, Fld<T> U, Fld<T> V, Fld<T> W, T *
     q[o + Q_S * n] = S;
 }
 
-// filter_xzy (subgrid.f90:140-187) of a canonical array at a canonical centre;
-// the y direction is restricted to rows 2..nyg-1 (one-sided at both ends).
-template <typename T>
-__device__ __forceinline__ T filt_can(const T *q, const Can &c, int nyg, int i, int j, int k) {
-    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
-    T wm, w0, wp;
-    if (j == 2) { wm = T(0); w0 = f23; wp = f13; }
-    else if (j == nyg - 1) { wm = f13; w0 = f23; wp = T(0); }
-    else { wm = f6; w0 = f23; wp = f6; }
-    int jm = j > 2 ? j - 1 : j, jp = j < nyg - 1 ? j + 1 : j;
-    const T fw[3] = {f6, f23, f6};
-    T acc = T(0);
-#pragma unroll
-    for (int a = -1; a <= 1; a++) {
-        int ii = wrapc(i + a, c.nxp);
-        T sz = T(0);
-#pragma unroll
-        for (int b = -1; b <= 1; b++) {
-            int kk = wrapc(k + b, c.nzp);
-            T yv = wm * q[c(ii, jm, kk)] + w0 * q[c(ii, j, kk)] + wp * q[c(ii, jp, kk)];
-            sz += fw[b + 1] * yv;
-        }
-        acc += fw[a + 1] * sz;
-    }
-    return acc;
-}
-
 // Stages B and D: L_ij = hat(ui uj) - hat(ui) hat(uj) and hat(|S| S_ij)
 // (the filter of 15 canonical quantities), then M_ij = 4 |S(Uf)| S_ij(Uf) -
 // hat(|S| S_ij) and the plane partial sums of L.M and M.M
