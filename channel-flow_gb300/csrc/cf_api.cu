@@ -514,8 +514,9 @@ extern "C" int cf_create(int nx, int ny, int nz, const double *x, const double *
         if (p->LES_model == 3) amd_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms, &ctx->amd_nkc, &amd_parts);
         ctx->dsmb_nkc = dsm_b_plan(p->precision == CF_PREC_SPLIT ? 4 : 8, nxp, ctx->nym, nzp, dev_sms);
     }
-    size_t nch = std::max({(size_t)ctx->dsm_nblk, nch_fused, (size_t)cdiv(amd_parts, 2),
-                           (size_t)cdiv(nxp, 32) * (size_t)ctx->dsmb_nkc});
+    // (with the wall model the one-pass kernel's slots are followed by the seam band's)
+    size_t nch = std::max({(size_t)ctx->dsm_nblk, nch_fused + (p->iwall_model == 3 ? dsm_seam_slots_max() : 0),
+                           (size_t)cdiv(amd_parts, 2), (size_t)cdiv(nxp, 32) * (size_t)ctx->dsmb_nkc});
     CF_CUDA(cudaMalloc(&ctx->dsm_part, (size_t)2 * ctx->nym * nch * sizeof(double)));
     ctx->dsm_part_nch = nch;
     // avg_nu_t (1..nyg) in FP64, followed by an FP32 copy
@@ -1224,7 +1225,7 @@ extern "C" int cf_time_step_rk3(cf_ctx *ctx, int nsteps, int sync) {
     CF_CUDA(cudaSetDevice(ctx->dev));
     for (int s = 0; s < nsteps; s++) {
         int X = ctx->cur;
-        if (!ctx->state_periodic && ctx->prm.iwall_model == 0) {
+        if (!ctx->state_periodic) {
             // ghosts not yet filled by apply_boundary_conditions: run this
             // step without a graph (its first eddy viscosity takes the
             // multi-pass route), later steps are captured
@@ -1686,7 +1687,7 @@ extern "C" int cf_ensemble_step(cf_ensemble *e, int nsteps, int sync) {
         // (as cf_time_step_rk3 does), ordered after the ensemble's work
         bool eager = false;
         for (cf_ctx *c : e->m)
-            if (!c->state_periodic && c->prm.iwall_model == 0) eager = true;
+            if (!c->state_periodic) eager = true;
         if (eager) {
             ENS_CUDA(cudaEventRecord(e->fork, e->st));
             for (int q = 0; q < n; q++) {

@@ -122,12 +122,27 @@ __host__ __device__ __forceinline__ int wrapc(int i, int np) {
 
 static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 
+// The seam band of the wall-model configurations.  With the equilibrium wall
+// model the wall ghost rows of U and W (j = 1, nyg) are not periodic copies at
+// the seam columns and planes (their Neumann values use alpha at the ghost's
+// own position).  The reference reads those entries themselves in the
+// stencils of the canonical centres next to a seam and the canonical twin's
+// values where it fills ghost points (subgrid.f90:448-458), while this pass
+// reads every halo through the periodic wrap.  The centres whose result can
+// depend on the difference -- rows 2, 3, nyg-2, nyg-1 (two cells from a
+// ghost row) at columns 2..4, nxp-1..nxp+1 or planes 2..4, nzp-1..nzp+1 --
+// are computed by k_dsm_seam with the reference's readings.
+__host__ __device__ __forceinline__ bool seam_row(int j, int nyg) { return j <= 3 || j >= nyg - 2; }
+__host__ __device__ __forceinline__ bool seam_line(int i, int np) { return i <= 4 || i >= np - 1; }
+
+
 // compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual
-// indices.  FP64 divides by the spacings as the reference does; FP32 (the
-// split path) multiplies by the stored reciprocal spacings rc.
-template <typename T>
-__device__ __forceinline__ void sij_point(const GeoT<T> &g, const RcpT<T> &rc, const Fld<T> &U, const Fld<T> &V,
-                                          const Fld<T> &W, int i, int j, int k, T s[6], T &S) {
+// indices (any accessor with operator()(i, j, k)).  FP64 divides by the
+// spacings as the reference does; FP32 (the split path) multiplies by the
+// stored reciprocal spacings rc.
+template <typename T, typename A>
+__device__ __forceinline__ void sij_point_a(const GeoT<T> &g, const RcpT<T> &rc, const A &U, const A &V, const A &W,
+                                            int i, int j, int k, T s[6], T &S) {
     const T *x = g.x, *y = g.y, *z = g.z, *xg = g.xg, *yg = g.yg, *zg = g.zg;
     const T h = T(0.5), q = T(0.25);
     auto quo = [&](T a, const T *c, const T *r, int e) -> T {
@@ -159,6 +174,11 @@ __device__ __forceinline__ void sij_point(const GeoT<T> &g, const RcpT<T> &rc, c
 #pragma unroll
     for (int c = 0; c < 6; c++) a2 += (c < 3 ? T(2) : T(4)) * s[c] * s[c];
     S = sqrt(a2);
+}
+template <typename T>
+__device__ __forceinline__ void sij_point(const GeoT<T> &g, const RcpT<T> &rc, const Fld<T> &U, const Fld<T> &V,
+                                          const Fld<T> &W, int i, int j, int k, T s[6], T &S) {
+    sij_point_a<T, Fld<T>>(g, rc, U, V, W, i, j, k, s, S);
 }
 
 
@@ -197,7 +217,8 @@ struct cf_ctx {
     double *avg_nu_t = nullptr;        // (nyg) device
     int dsm_nblk = 0;
     int dsm_kc = 0;                    // z-chunk length of the fused pass
-    int dsm_nchunk_fused = 0;
+    int dsm_nchunk_fused = 0;          // plane-partial slots per row of the last one-pass launch
+    int dsm_nchunk_base = 0;           // of them, the one-pass kernel's (the seam band's follow)
     bool use_fused_dsm = true;
     int dsmb_nkc = 0;                  // z chunks of the multi-pass DSM filter kernel
     // tensor map (a CUtensorMap) of the 15 filter quantities of dsm_q for the
@@ -214,7 +235,10 @@ struct cf_ctx {
     size_t dsm_part_nch = 0;           // plane-partial slots per row allocated in dsm_part
     int amd_nparts = 0;                // partial sums per row of the last AMD pass
     bool amd_avg_pending = false;      // avg_nu_t not yet formed from them
-    bool state_periodic = false;       // U, V, W satisfy the periodic/no-slip ghost identities
+    // U, V, W hold the ghosts apply_boundary_conditions gives them: periodic
+    // copies in x and z (with the wall model: except the wall ghost rows of U
+    // and W at the seams) and the wall rule
+    bool state_periodic = false;
     // After the one-pass eddy viscosity, nu_t is held as |S| (canonical) and
     // the plane coefficient <LM>/<MM>: the fused RHS forms nu_t on the fly and
     // the nut buffer is filled only when another reader needs it.
@@ -284,6 +308,8 @@ template <typename T> int launch_rhs_update(cf_ctx *ctx, int s, int src, int dst
 template <typename T> int launch_rk_update(cf_ctx *ctx, int s);            // from stored F slots
 template <typename T> int launch_dsm(cf_ctx *ctx, int buf);                // eddy viscosity
 template <typename T> int launch_dsm_fused(cf_ctx *ctx, int buf);          // fused pass (periodic state)
+template <typename T> int launch_dsm_fused_wm(cf_ctx *ctx, int buf);       // fused pass + seam band (wall model)
+int dsm_seam_slots_max();                                                  // partial slots the seam band may take
 constexpr int CF_ENS_MAXM = 32;  // channels per batched ensemble launch at most
 // fused pass + <LM>/<MM> rows of n channels in two launches (ensembles)
 template <typename T> int launch_dsm_batch(cudaStream_t st, cf_ctx *const *m, const int *buf, int n);

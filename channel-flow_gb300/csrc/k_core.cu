@@ -169,7 +169,7 @@ static BcField bc_field(void *p, void *plo, int n1, int n2, int n3, int xc, int 
 template <typename T>
 int launch_bc(cf_ctx *ctx, int b, bool lo) {
     int wm = ctx->prm.iwall_model;
-    if (wm == 0) ctx->state_periodic = true;  // holds for every later launch on the stream
+    ctx->state_periodic = true;  // holds for every later launch on the stream
     BcSet s;
     // U: x faces, y centres, z centres
     s.f[0] = bc_field(ctx->U[b], lo ? ctx->Ulo[b] : nullptr, ctx->nx, ctx->nyg, ctx->nzg, 0, 1, wm == 3 ? 2 : 0, ctx->alpha_x);

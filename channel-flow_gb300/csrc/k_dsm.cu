@@ -458,12 +458,16 @@ __global__ void __launch_bounds__(256) k_dsm_c_t(Fld<T> A, Fld<T> Af, int n1, in
 // Stage E: avg_nu_t(j) = <LM>/<MM> (subgrid.f90:516-518) and its ghosts.
 // <LM>/<MM> per row from the block partial sums: one warp per row, lanes
 // over chunks in a fixed order, then the ghost rows (subgrid.f90:515-519).
-__global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, int dirichlet) {
+// nbase: the slots of a row outside the wall-model seam band (the seam
+// kernel's slots follow them only in the band's rows; nbase = nchunk when
+// there are none)
+__global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, int dirichlet, int nbase) {
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) + 2;
     if (j > nyg - 1) return;
+    const int nread = seam_row(j, nyg) ? nchunk : nbase;
     double a = 0.0, b = 0.0;
-    for (int q = lane; q < nchunk; q += 32) {
+    for (int q = lane; q < nread; q += 32) {
         a += part[((long)(j - 2) * nchunk + q) * 2];
         b += part[((long)(j - 2) * nchunk + q) * 2 + 1];
     }
@@ -488,12 +492,13 @@ __global__ void k_dsm_e(const double *part, int nchunk, int nyg, double *avg, in
 }
 // The same from float-float partials (L.M hi, lo, M.M hi, lo) of the one-pass
 // FP32 kernel: the sums in float-float, FP64 only for lane 0's quotient.
-__global__ void k_dsm_e_ff(const float4 *part, int nchunk, int nyg, double *avg, int dirichlet) {
+__global__ void k_dsm_e_ff(const float4 *part, int nchunk, int nyg, double *avg, int dirichlet, int nbase) {
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5) + 2;
     if (j > nyg - 1) return;
+    const int nread = seam_row(j, nyg) ? nchunk : nbase;
     float ah = 0.f, al = 0.f, bh = 0.f, bl = 0.f;
-    for (int q = lane; q < nchunk; q += 32) {
+    for (int q = lane; q < nread; q += 32) {
         const float4 v = part[(long)(j - 2) * nchunk + q];
         ff_add2(ah, al, v.x, v.y);
         ff_add2(bh, bl, v.z, v.w);
@@ -623,16 +628,17 @@ int launch_dsm(cf_ctx *ctx, int b) {
     Can c;
     c.nxp = ctx->nxp; c.nym = ctx->nym; c.nzp = ctx->nzp; c.n = (long)ctx->nCan;
     dim3 blk(32, 4, 1);
-    if (ctx->use_fused_dsm && ctx->prm.iwall_model == 0 && ctx->state_periodic) {
-        // one pass: |S| and the plane partial sums (k_dsm_fused.cu)
-        int rc = launch_dsm_fused<T>(ctx, b);
+    if (ctx->use_fused_dsm && ctx->state_periodic && (ctx->prm.iwall_model == 0 || ctx->prm.iwall_model == 3)) {
+        // one pass: |S| and the plane partial sums (k_dsm_fused.cu); with the
+        // wall model the seam band is computed by k_dsm_seam
+        int rc = ctx->prm.iwall_model == 0 ? launch_dsm_fused<T>(ctx, b) : launch_dsm_fused_wm<T>(ctx, b);
         if (rc) return rc;
-        int nch = ctx->dsm_nchunk_fused;
+        const int nch = ctx->dsm_nchunk_fused, nb = ctx->dsm_nchunk_base;
         if (sizeof(T) == 4)  // float-float partials of the FP32 kernel
             k_dsm_e_ff<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>((const float4 *)ctx->dsm_part, nch, ctx->nyg,
-                                                                ctx->avg_nu_t, dir);
+                                                                ctx->avg_nu_t, dir, nb);
         else
-            k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir);
+            k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nch, ctx->nyg, ctx->avg_nu_t, dir, nb);
         count_launch(ctx, "k_dsm_e");
         ctx->nut_lazy = true;  // nu_t = max(-C(j)|S|/2, 0) is formed by its readers
         CF_CUDA(cudaGetLastError());
@@ -684,9 +690,9 @@ int launch_dsm(cf_ctx *ctx, int b) {
     }
     if (sizeof(T) == 4)  // float-float partials of the FP32 kernel
         k_dsm_e_ff<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>((const float4 *)ctx->dsm_part, nchunk, ctx->nyg,
-                                                            ctx->avg_nu_t, dir);
+                                                            ctx->avg_nu_t, dir, nchunk);
     else
-        k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir);
+        k_dsm_e<<<cdiv(ctx->nym, 8), 256, 0, ctx->st>>>(ctx->dsm_part, nchunk, ctx->nyg, ctx->avg_nu_t, dir, nchunk);
     count_launch(ctx, "k_dsm_e");
     // stage F (nu_t = max(-C(j)|S|/2, 0) everywhere) is left to the readers,
     // as after the one-pass kernel: |S| sits in the same canonical slot, the

@@ -94,6 +94,7 @@ struct DsmArgs {
     Fld<T> U, V, W;
     RGeo rg;
     int nx, ny, nyg, nz, nxp, nzp, kc_len, nchunk, ntx, nty, nkc;
+    int seam;  // wall-model state: the centres of seam_centre() are left to k_dsm_seam
     T *Sout;
     double *part;
 };
@@ -176,6 +177,10 @@ __device__ __forceinline__ void dsm_tile(const DsmArgs<T> &args, int bx, int by,
         for (int q = 0; q < 8; q++) acc[s][q] = psplat(T(0));
     T S_m2 = T(0), S_m3 = T(0);  // |S| of Q(r-2), Q(r-3) at the own point
     T sl = T(0), smm = T(0);
+    // wall-model state: this thread's column and row in the seam band
+    // (its output planes in the band are added by k_dsm_seam instead)
+    const bool seam_rc = args.seam && seam_row(jo, nyg);
+    const bool seam_col = seam_rc && seam_line(io, nxp);
 
     // halo points of phase B: the first TX points of the rows below and
     // above the tile on one warp each, then the four points past them and
@@ -406,8 +411,10 @@ __device__ __forceinline__ void dsm_tile(const DsmArgs<T> &args, int bx, int by,
                     mm += wq * M * M;
                 }
                 T wgt = (io == 2 ? T(2) : T(1)) * (kcn == 2 ? T(2) : T(1));
-                sl += wgt * lm;
-                smm += wgt * mm;
+                if (!(seam_col || (seam_rc && seam_line(kcn, nzp)))) {
+                    sl += wgt * lm;
+                    smm += wgt * mm;
+                }
                 Sout[(long)(io - 2) + (long)nxp * ((jo - 2) + (long)(nyg - 2) * (kcn - 2))] = S_m3;
             }
         }
@@ -514,6 +521,7 @@ static DsmArgs<T> fused_args(cf_ctx *ctx, int b, int kc_len) {
     a.nty = cdiv(ctx->nym, TY);
     a.nkc = cdiv(ctx->nzp, kc_len);
     a.nchunk = a.ntx * a.nkc;
+    a.seam = 0;
     a.Sout = (T *)ctx->dsm_q + 15 * ctx->nCan;  // |S| slot of the canonical scratch
     a.part = ctx->dsm_part;
     return a;
@@ -525,7 +533,7 @@ static int launch_fused_cfg(cf_ctx *ctx, int b, int kc_len) {
     size_t sm = DsmSmem<T, TX, TY>::bytes;
     k_dsm_fused<T, TX, TY><<<dim3(a.ntx, a.nty, a.nkc), TX * TY, sm, ctx->st>>>(a);
     count_launch(ctx, "k_dsm_fused");
-    ctx->dsm_nchunk_fused = a.nchunk;
+    ctx->dsm_nchunk_fused = ctx->dsm_nchunk_base = a.nchunk;
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -584,6 +592,262 @@ int launch_dsm_fused(cf_ctx *ctx, int b) {
 
 template int launch_dsm_fused<double>(cf_ctx *, int);
 template int launch_dsm_fused<float>(cf_ctx *, int);
+
+// ---------------------------------------------------------------------------
+// k_dsm_seam: the centres of the seam band (seam_row, seam_line) of the
+// wall-model state, computed as the multi-pass route computes them
+// (subgrid.f90:376-513 with the periodic fills of :448-458): the quantities
+// of stage A at a canonical centre from U, V, W at actual indices, at a
+// ghost centre the canonical twin's; Uf, Vf, Wf at a canonical element from
+// U, V, W at actual indices (y one-sided at rows 1 and n2), at a ghost
+// element the twin's; the 27-point filter of the quantities (y one-sided at
+// rows 2 and nyg-1), L, M from S_ij(Uf), L.M and M.M with the plane-sum
+// weights.  |S| of the centre is written over the one-pass value.  One warp
+// per centre: lanes 0..26 the filter's neighbours, lanes 0..29 the 30
+// filtered-velocity elements that S_ij(Uf) reads.  Block (b, row j): its
+// warps take the row's band centres in turn and the block's sums go to
+// partial slot chunk0 + b of row j (the band's rows only: k_dsm_e and
+// k_dsm_e_ff read a row's seam slots only in those rows).
+// ---------------------------------------------------------------------------
+template <typename T>
+struct SeamArgs {
+    Fld<T> U, V, W;
+    GeoT<T> g;
+    RcpT<T> rc;
+    int nxp, nzp, nyg, ny;
+    int rows[4];                 // the band's rows (blockIdx.y)
+    int xs[6], nxs, zs[6], nzs;  // band columns and planes, distinct
+    int nchunk, chunk0;          // partial-slot stride and the first seam slot
+    T *Sout;
+    double *part;
+};
+
+// 27 values of one field around a centre (ci, cj, ck), as an accessor
+template <typename T>
+struct CubeAcc {
+    const T *c;
+    int ci, cj, ck;
+    __device__ __forceinline__ T operator()(int i, int j, int k) const {
+        return c[(i - ci + 1) + 3 * (j - cj + 1) + 9 * (k - ck + 1)];
+    }
+};
+
+// stage C at element (i, j, k) of a field with n2 rows (k_dsm_c_t's order:
+// y inside x per plane, then z); a ghost or duplicate element takes the
+// canonical twin's value
+template <typename T>
+__device__ T seam_filt_elem(const Fld<T> &F, int n2, int nxp, int nzp, int i, int j, int k) {
+    i = wrapc(i, nxp);
+    k = wrapc(k, nzp);
+    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0);
+    T wm, w0, wp;
+    if (j == 1) { wm = T(0); w0 = f23; wp = f13; }
+    else if (j == n2) { wm = f13; w0 = f23; wp = T(0); }
+    else { wm = f6; w0 = f23; wp = f6; }
+    const int jm = max(j - 1, 1), jp = min(j + 1, n2);  // weight 0 where clamped
+    T gz[3];
+#pragma unroll
+    for (int dk = -1; dk <= 1; dk++) {
+        T g = T(0);
+#pragma unroll
+        for (int a = -1; a <= 1; a++) {
+            const T fa = a == 0 ? f23 : f6;
+            g += fa * (wm * F(i + a, jm, k + dk) + w0 * F(i + a, j, k + dk) + wp * F(i + a, jp, k + dk));
+        }
+        gz[dk + 1] = g;
+    }
+    return f6 * gz[0] + f23 * gz[1] + f6 * gz[2];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dsm_seam(const __grid_constant__ SeamArgs<T> a) {
+    const int j = a.rows[blockIdx.y], nyg = a.nyg, nxp = a.nxp, nzp = a.nzp;
+    const long slot = ((long)(j - 2) * a.nchunk + a.chunk0 + blockIdx.x);
+    __shared__ double red[8][2];
+    __shared__ T cube[8][3][27];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    auto put = [&](double lm, double mm) {
+        if constexpr (sizeof(T) == 4) {
+            const float lh = (float)lm, mh = (float)mm;
+            ((float4 *)a.part)[slot] = make_float4(lh, (float)(lm - (double)lh), mh, (float)(mm - (double)mh));
+        } else {
+            a.part[slot * 2] = lm;
+            a.part[slot * 2 + 1] = mm;
+        }
+    };
+    const T f6 = T(1.0 / 6.0), f23 = T(2.0 / 3.0), f13 = T(1.0 / 3.0), h = T(0.5);
+    const T fw[3] = {f6, f23, f6};
+    // this lane's filter neighbour and its weight (y one-sided at rows 2 and nyg-1)
+    const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+    T wy = dy == 0 ? f23 : f6;
+    if (j == 2) wy = dy < 0 ? T(0) : (dy > 0 ? f13 : f23);
+    else if (j == nyg - 1) wy = dy > 0 ? T(0) : (dy < 0 ? f13 : f23);
+    const T wq = lane < 27 ? fw[dx + 1] * wy * fw[dz + 1] : T(0);
+    // this lane's filtered-velocity element (field ef, offsets ex, ey, ez)
+    int ef = 0, ex = 0, ey = 0, ez = 0;
+    if (lane < 10) {
+        ef = 0; ex = (lane & 1) - 1;
+        const int m = lane >> 1;
+        ey = m < 3 ? m - 1 : 0;
+        ez = m < 3 ? 0 : (m == 3 ? -1 : 1);
+    } else if (lane < 20) {
+        const int l = lane - 10;
+        ef = 1;
+        if (l < 6) { ex = l % 3 - 1; ey = l / 3 - 1; ez = 0; }
+        else { const int m = l - 6; ex = 0; ey = (m & 1) - 1; ez = (m >> 1) ? 1 : -1; }
+    } else if (lane < 30) {
+        const int l = lane - 20;
+        ef = 2;
+        if (l < 6) { ex = l % 3 - 1; ey = 0; ez = l / 3 - 1; }
+        else { const int m = l - 6; ex = 0; ey = (m & 1) ? 1 : -1; ez = (m >> 1) - 1; }
+    }
+    const int nxr = max(0, nxp - 6);  // columns 5..nxp-2 (outside the band's columns)
+    const long npts = (long)a.nxs * nzp + (long)a.nzs * nxr;
+    double slm = 0.0, smm = 0.0;
+    for (long p = (long)blockIdx.x * 8 + w; p < npts; p += (long)gridDim.x * 8) {
+        int i, k;
+        if (p < (long)a.nxs * nzp) {
+            i = a.xs[p / nzp];
+            k = 2 + (int)(p % nzp);
+        } else {
+            const long q = p - (long)a.nxs * nzp;
+            k = a.zs[q / nxr];
+            i = 5 + (int)(q % nxr);
+        }
+        // the stage-A quantities of this lane's neighbour, weighted
+        T qv[16];
+#pragma unroll
+        for (int c = 0; c < 16; c++) qv[c] = T(0);
+        if (wq != T(0)) {
+            const int ci = wrapc(i + dx, nxp), cj = j + dy, ck = wrapc(k + dz, nzp);
+            const T uc = h * (a.U(ci - 1, cj, ck) + a.U(ci, cj, ck));
+            const T vc = h * (a.V(ci, cj - 1, ck) + a.V(ci, cj, ck));
+            const T wc = h * (a.W(ci, cj, ck - 1) + a.W(ci, cj, ck));
+            T sq[6], S;
+            sij_point<T>(a.g, a.rc, a.U, a.V, a.W, ci, cj, ck, sq, S);
+            const T qa[15] = {uc, vc, wc, uc * uc, vc * vc, wc * wc, uc * vc, uc * wc, vc * wc,
+                              S * sq[0], S * sq[1], S * sq[2], S * sq[3], S * sq[4], S * sq[5]};
+#pragma unroll
+            for (int c = 0; c < 15; c++) qv[c] = wq * qa[c];
+            qv[15] = S;
+        }
+        // |S| of the centre (lane 13: no offset)
+        const T Sc = __shfl_sync(0xffffffffu, qv[15], 13);
+        if (lane == 13) a.Sout[(long)(i - 2) + (long)nxp * ((j - 2) + (long)(nyg - 2) * (k - 2))] = Sc;
+#pragma unroll
+        for (int c = 0; c < 15; c++)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) qv[c] += __shfl_xor_sync(0xffffffffu, qv[c], o);
+        // the filtered velocities S_ij(Uf) reads
+        if (lane < 30) {
+            const Fld<T> &F = ef == 0 ? a.U : (ef == 1 ? a.V : a.W);
+            cube[w][ef][(ex + 1) + 3 * (ey + 1) + 9 * (ez + 1)] =
+                seam_filt_elem<T>(F, ef == 1 ? a.ny : nyg, nxp, nzp, i + ex, j + ey, k + ez);
+        }
+        __syncwarp();
+        if (lane == 0) {
+            CubeAcc<T> cu{cube[w][0], i, j, k}, cv{cube[w][1], i, j, k}, cw{cube[w][2], i, j, k};
+            T sf[6], Sf;
+            sij_point_a<T, CubeAcc<T>>(a.g, a.rc, cu, cv, cw, i, j, k, sf, Sf);
+            const T fu = qv[0], fv = qv[1], fwv = qv[2];
+            const T pa[6] = {fu, fv, fwv, fu, fu, fv}, pb[6] = {fu, fv, fwv, fv, fwv, fwv};
+            T L[6], M[6];
+#pragma unroll
+            for (int c = 0; c < 6; c++) {
+                L[c] = qv[3 + c] - pa[c] * pb[c];
+                M[c] = T(4) * Sf * sf[c] - qv[9 + c];  // fil_size**2 = 4 (subgrid.f90:156, 463)
+            }
+            const T lm = L[0] * M[0] + L[1] * M[1] + L[2] * M[2] + T(2) * (L[3] * M[3] + L[4] * M[4] + L[5] * M[5]);
+            const T mm = M[0] * M[0] + M[1] * M[1] + M[2] * M[2] + T(2) * (M[3] * M[3] + M[4] * M[4] + M[5] * M[5]);
+            const double wgt = (i == 2 ? 2.0 : 1.0) * (k == 2 ? 2.0 : 1.0);
+            slm += wgt * (double)lm;
+            smm += wgt * (double)mm;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        red[w][0] = slm;
+        red[w][1] = smm;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int q = 0; q < 8; q++) {
+            s0 += red[q][0];
+            s1 += red[q][1];
+        }
+        put(s0, s1);
+    }
+}
+
+// partial slots per row the seam kernel takes (after the one-pass kernel's):
+// a block of 8 warps per 16 band centres of a row (two per warp)
+static int seam_slots(int nxp, int nzp) {
+    const long npts = 6L * nzp + 6L * std::max(0, nxp - 6);
+    return std::max(1, std::min(256, cdiv(npts, 16)));
+}
+int dsm_seam_slots_max() { return 256; }
+
+template <typename T>
+static int launch_seam(cf_ctx *ctx, int b, int chunk0, int nchunk) {
+    SeamArgs<T> a;
+    a.U = make_fld<T>(ctx->U[b], ctx->nx, ctx->nyg);
+    a.V = make_fld<T>(ctx->V[b], ctx->nxg, ctx->ny);
+    a.W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
+    a.g = geo_of<T>(ctx);
+    a.rc = rcp_of<T>(ctx);
+    a.nxp = ctx->nxp; a.nzp = ctx->nzp; a.nyg = ctx->nyg; a.ny = ctx->ny;
+    auto band = [](int np, int *out) {
+        int n = 0;
+        const int c[6] = {2, 3, 4, np - 1, np, np + 1};
+        for (int q = 0; q < 6; q++) {
+            bool dup = c[q] < 2 || c[q] > np + 1;
+            for (int r = 0; r < n; r++) dup = dup || out[r] == c[q];
+            if (!dup) out[n++] = c[q];
+        }
+        return n;
+    };
+    a.nxs = band(ctx->nxp, a.xs);
+    a.nzs = band(ctx->nzp, a.zs);
+    a.nchunk = nchunk;
+    a.chunk0 = chunk0;
+    a.Sout = (T *)ctx->dsm_q + 15 * ctx->nCan;
+    a.part = ctx->dsm_part;
+    int nr = 0;
+    for (int j : {2, 3, ctx->nyg - 2, ctx->nyg - 1}) {
+        bool dup = j < 2 || j > ctx->nyg - 1;
+        for (int r = 0; r < nr; r++) dup = dup || a.rows[r] == j;
+        if (!dup) a.rows[nr++] = j;
+    }
+    const int ns = nchunk - chunk0;
+    k_dsm_seam<T><<<dim3(ns, nr), 256, 0, ctx->st>>>(a);
+    count_launch(ctx, "k_dsm_seam");
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// The one-pass kernel on a wall-model state (ghosts filled by the boundary
+// conditions): the seam band left to k_dsm_seam, whose partial slots follow
+// the one-pass kernel's in every row.
+template <typename T>
+int launch_dsm_fused_wm(cf_ctx *ctx, int b) {
+    constexpr int TX = DsmCfg<T>::TX, TY = DsmCfg<T>::TY;
+    DsmArgs<T> a = fused_args<T, TX, TY>(ctx, b, ctx->dsm_kc);
+    const int chunk0 = a.nchunk, ns = seam_slots(ctx->nxp, ctx->nzp);
+    if ((size_t)(chunk0 + ns) > ctx->dsm_part_nch) return cf_fail(ctx, CF_ERR_INVALID, "plane-partial slots");
+    a.nchunk = chunk0 + ns;
+    a.seam = 1;
+    ctx->dsm_nchunk_base = chunk0;
+    size_t sm = DsmSmem<T, TX, TY>::bytes;
+    k_dsm_fused<T, TX, TY><<<dim3(a.ntx, a.nty, a.nkc), TX * TY, sm, ctx->st>>>(a);
+    count_launch(ctx, "k_dsm_fused");
+    CF_CUDA(cudaGetLastError());
+    ctx->dsm_nchunk_fused = a.nchunk;
+    return launch_seam<T>(ctx, b, chunk0, a.nchunk);
+}
+
+template int launch_dsm_fused_wm<double>(cf_ctx *, int);
+template int launch_dsm_fused_wm<float>(cf_ctx *, int);
 
 __global__ void __launch_bounds__(256) k_dsm_e_batch(const __grid_constant__ DsmEBatch B) {
     const int bid = blockIdx.x;
@@ -653,7 +917,7 @@ int launch_dsm_batch(cudaStream_t st, cf_ctx *const *m, const int *buf, int n) {
         cf_ctx *c = m[q];
         B.a[q] = fused_args<T, TX, TY>(c, buf[q], c->dsm_kc);
         B.first[q + 1] = B.first[q] + B.a[q].ntx * B.a[q].nty * B.a[q].nkc;
-        c->dsm_nchunk_fused = B.a[q].nchunk;
+        c->dsm_nchunk_fused = c->dsm_nchunk_base = B.a[q].nchunk;
         E.a[q].part = c->dsm_part;
         E.a[q].avg = c->avg_nu_t;
         E.a[q].nchunk = B.a[q].nchunk;

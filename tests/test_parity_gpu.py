@@ -157,8 +157,11 @@ def test_dt_and_mass_flow():
     assert abs(ch.compute_dPx_for_constant_mass_flow() - o.compute_dPx_for_constant_mass_flow()) <= 1e-15
 
 
-@pytest.mark.parametrize("which", ["small"])
+@pytest.mark.parametrize("which", ["small", "config1"])
 def test_wall_model_eqwm(which):
+    """eqwm alphas, stress and counters, the boundary conditions they give,
+    and then the eddy viscosity of that state, whose wall ghost rows are not
+    periodic at the seams (the one-pass kernel with the seam band)."""
     case = channel_case(*CASES[which], stretch=0.0, wall=3, retau=2000.0, profile="plug", jref=3)
     o, ch = make_pair(case)
     for a in (o, ch):
@@ -172,6 +175,9 @@ def test_wall_model_eqwm(which):
     assert ch.eqwm_counters() == (int(o.scalar("n_nan_eqwm")), int(o.scalar("n_iter_eqwm")))
     o.apply_boundary_conditions(); ch.apply_boundary_conditions()
     compare_fields(o, ch, 1e-12, what="eqwm BC")
+    o.compute_eddy_viscosity(); ch.compute_eddy_viscosity()
+    assert_close(ch.download()["nu_t"], o.fields()["nu_t"], 1e-12, "nu_t after the eqwm BC")
+    assert_close(ch.avg_nu_t()[1:-1], o.array("avg_nu_t").ravel()[1:-1], 1e-12, "avg_nu_t after the eqwm BC")
 
 
 @pytest.mark.parametrize("which,wall", [("small", 0), ("config1", 0), ("small", 3)])
@@ -314,6 +320,36 @@ def test_dsm_fused_matches_multipass(precision, tol):
         ch.apply_boundary_conditions()
         ch.compute_eddy_viscosity()
         out.append((ch.download()["nu_t"], ch.avg_nu_t()))
+    assert_close(out[0][0], out[1][0], tol, "nu_t")
+    assert_close(out[0][1][1:-1], out[1][1][1:-1], tol, "avg_nu_t")
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (1, 2e-4)])
+@pytest.mark.parametrize("dims", [(18, 17, 18), (34, 33, 34), (102, 25, 74), (66, 65, 66)])
+def test_dsm_fused_wall_model_matches_multipass(dims, precision, tol):
+    """The one-pass dynamic Smagorinsky kernel on a wall-model state (the
+    seam band computed by k_dsm_seam with the reference's readings of the
+    non-periodic wall ghosts) against the multi-pass kernels, after an eqwm
+    call and the boundary conditions it implies; the state's wall ghost rows
+    are checked to differ from their periodic twins at the seams."""
+    import channelflow as cf
+    case = channel_case(*dims, seed=11, stretch=0.0, wall=3, retau=2000.0, profile="plug")
+    out = []
+    for unfused in (0, 1):
+        ch = cf.Channel(case["x"], case["y"], case["z"], precision=precision, dsm_unfused=unfused, **case["prm"])
+        ch.upload(case["U"], case["V"], case["W"])
+        ch.apply_boundary_conditions()
+        ch.compute_eddy_viscosity()
+        ch.compute_wall_model()
+        ch.apply_boundary_conditions()
+        f = ch.download()
+        # U's ghost column 1 and ghost plane 1 against their periodic twins, in the wall rows
+        gap = max(np.abs(f["U"][0, [0, -1], :] - f["U"][-2, [0, -1], :]).max(),
+                  np.abs(f["U"][:, [0, -1], 0] - f["U"][:, [0, -1], -3]).max())
+        assert gap > 1e-12 * np.abs(f["U"]).max(), gap
+        ch.compute_eddy_viscosity()
+        out.append((ch.download()["nu_t"], ch.avg_nu_t()))
+        ch.close()
     assert_close(out[0][0], out[1][0], tol, "nu_t")
     assert_close(out[0][1][1:-1], out[1][1][1:-1], tol, "avg_nu_t")
 
