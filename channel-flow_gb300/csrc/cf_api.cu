@@ -1891,14 +1891,16 @@ static int tune_t(cf_ctx *ctx, int reps, double *rep) {
         rep[1] = best;
     }
     // the eddy-viscosity pass
-    if (!rc && ctx->prm.LES_model == 2 && ctx->use_fused_dsm && ctx->prm.iwall_model == 0 && ctx->state_periodic) {
+    if (!rc && ctx->prm.LES_model == 2 && ctx->use_fused_dsm && ctx->state_periodic &&
+        (ctx->prm.iwall_model == 0 || ctx->prm.iwall_model == 3)) {
         const int keep = ctx->dsm_kc;
         const int ntx = cdiv(ctx->nxp, sizeof(T) == 4 ? 32 : 16);
+        const size_t nseam = ctx->prm.iwall_model == 3 ? (size_t)dsm_seam_slots_max() : 0;
         double best = 1e300;
         int best_kc = keep, last_len = -1;
         for (int nn = cdiv(nzp, DSM_ZMAX_HOST); nn <= std::max(1, nzp / 4) && !rc; nn++) {
             const int len = cdiv(nzp, nn);
-            if (len == last_len || (size_t)ntx * cdiv(nzp, len) > ctx->dsm_part_nch) continue;
+            if (len == last_len || (size_t)ntx * cdiv(nzp, len) + nseam > ctx->dsm_part_nch) continue;
             last_len = len;
             ctx->dsm_kc = len;
             double us = 0;

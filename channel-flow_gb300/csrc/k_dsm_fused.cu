@@ -35,8 +35,11 @@
 // The halo is read through the periodic wrap, which reproduces the
 // reference's periodic copies whenever U, V, W are themselves periodic in x
 // and z -- true after apply_boundary_conditions with no-slip walls
-// (iwall_model 0).  The plane sums count the duplicate column i = nxg-1 and
-// plane k = nzg-1 of the reference's loops as weight 2 on i = 2, k = 2.
+// (iwall_model 0).  With the equilibrium wall model it holds except in the
+// wall ghost rows at the seams; the centres that can see those entries (the
+// seam band, seam_row / seam_line) are then left to k_dsm_seam.  The plane
+// sums count the duplicate column i = nxg-1 and plane k = nzg-1 of the
+// reference's loops as weight 2 on i = 2, k = 2.
 #include <type_traits>
 
 #include "cf_internal.cuh"
