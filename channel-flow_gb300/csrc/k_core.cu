@@ -197,9 +197,19 @@ struct RkCoef {
 
 // The spacings enter as reciprocals (rc): 1/(xg(i+1)-xg(i)) = rc.dxg[i+1],
 // 1/(x(i)-x(i-1)) = rc.dx[i], and so on.
-template <typename T, typename A, typename RC>
+//
+// ZC (the z-marching fused kernel): the z-face terms of a cell -- its
+// advective and viscous fluxes through the faces k-1/2 and k+1/2 -- are
+// taken as rdz3 * (F(k+1/2) - F(k-1/2)) with F = viscous flux less advective
+// flux; *fz holds F(k-1/2) on entry (carried from the cell below, or formed
+// by rhs_*_zflux_dn for the first plane of a chunk) and F(k+1/2) as the
+// next cell's F(k-1/2) on return (for u with the spacing 1/(x(i)-x(i-1))
+// that the reference's lower face uses, rdx1; the cell's own upper face
+// uses rdx2).
+template <typename T, typename A, typename RC, bool ZC = false>
 __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
-                                         const A &nt, T nu, T dPdx, T Om, bool rot, int i, int j, int k) {
+                                         const A &nt, T nu, T dPdx, T Om, bool rot, int i, int j, int k,
+                                         T *fz = nullptr) {
     const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
     const T rdx1 = rc.dx[i], rdx2 = rc.dx[i + 1], rdx3 = rc.dxg[i + 1];
@@ -217,10 +227,12 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A
     r += -(uy1 * vx1 - uy0 * vx0) * rdy3;
     // 3) -duw/dz   (:84-101)
     T uz1 = h * (U(i, j, k) + U(i, j, k + 1));
-    T uz0 = h * (U(i, j, k - 1) + U(i, j, k));
     T wx1 = h * (W(i, j, k) + W(i + 1, j, k));
-    T wx0 = h * (W(i, j, k - 1) + W(i + 1, j, k - 1));
-    r += -(uz1 * wx1 - uz0 * wx0) * rdz3;
+    if constexpr (!ZC) {
+        T uz0 = h * (U(i, j, k - 1) + U(i, j, k));
+        T wx0 = h * (W(i, j, k - 1) + W(i + 1, j, k - 1));
+        r += -(uz1 * wx1 - uz0 * wx0) * rdz3;
+    }
     // 4) viscous   (:108-163)
     T t2j = (U(i, j + 1, k) - U(i, j, k)) * rc.dyg[j + 1];
     T t2jm = (U(i, j, k) - U(i, j - 1, k)) * rc.dyg[j];
@@ -229,14 +241,21 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A
     T nu_y1 = nu + h * (w0[j - 1] * nt(i, j - 1, k) + w1[j - 1] * nt(i, j, k) + w0[j - 1] * nt(i + 1, j - 1, k) +
                         w1[j - 1] * nt(i + 1, j, k));
     T nu_y2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i + 1, j, k) + w1[j] * nt(i + 1, j + 1, k));
-    T nu_z1 = nu + q * (nt(i, j, k) + nt(i, j, k - 1) + nt(i + 1, j, k) + nt(i + 1, j, k - 1));
     T nu_z2 = nu + q * (nt(i, j, k) + nt(i, j, k + 1) + nt(i + 1, j, k) + nt(i + 1, j, k + 1));
     T visc = T(2) * rdx3 * (nu_x2 * (U(i + 1, j, k) - U(i, j, k)) * rdx2 - nu_x1 * (U(i, j, k) - U(i - 1, j, k)) * rdx1) +
              rdy3 * (nu_y2 * (t2j + (V(i + 1, j, k) - V(i, j, k)) * rdx2) -
-                     nu_y1 * (t2jm + (V(i + 1, j - 1, k) - V(i, j - 1, k)) * rdx1)) +
-             rdz3 * (nu_z2 * ((U(i, j, k + 1) - U(i, j, k)) * rdz2 + (W(i + 1, j, k) - W(i, j, k)) * rdx2) -
-                     nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) * rdz1 + (W(i + 1, j, k - 1) - W(i, j, k - 1)) * rdx1));
-    r += visc;
+                     nu_y1 * (t2jm + (V(i + 1, j - 1, k) - V(i, j - 1, k)) * rdx1));
+    if constexpr (!ZC) {
+        T nu_z1 = nu + q * (nt(i, j, k) + nt(i, j, k - 1) + nt(i + 1, j, k) + nt(i + 1, j, k - 1));
+        visc += rdz3 * (nu_z2 * ((U(i, j, k + 1) - U(i, j, k)) * rdz2 + (W(i + 1, j, k) - W(i, j, k)) * rdx2) -
+                        nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) * rdz1 + (W(i + 1, j, k - 1) - W(i, j, k - 1)) * rdx1));
+        r += visc;
+    } else {
+        r += visc;
+        const T gz = (U(i, j, k + 1) - U(i, j, k)) * rdz2, dw = W(i + 1, j, k) - W(i, j, k), a = uz1 * wx1;
+        r += rdz3 * ((nu_z2 * (gz + dw * rdx2) - a) - *fz);
+        *fz = nu_z2 * (gz + dw * rdx1) - a;
+    }
     r += dPdx;  // :166
     if (rot) {  // |Om| > 1e-6, :169-177
         T tv0 = h * (V(i, j - 1, k) + V(i, j, k));
@@ -246,9 +265,9 @@ __device__ __forceinline__ T rhs_u_point(const GeoT<T> &g, const RC &rc, const A
     return r;
 }
 
-template <typename T, typename A, typename RC>
+template <typename T, typename A, typename RC, bool ZC = false>
 __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
-                                         const A &nt, T nu, T Om, bool rot, int i, int j, int k) {
+                                         const A &nt, T nu, T Om, bool rot, int i, int j, int k, T *fz = nullptr) {
     const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5);
     const T rdx1 = rc.dxg[i], rdx2 = rc.dxg[i + 1], rdx3 = rc.dx[i];
@@ -266,23 +285,32 @@ __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const RC &rc, const A
     r += -(uy1 * vx1 - uy0 * vx0) * rdx3;
     // 3) -dvw/dz (:250-267)
     T vz1 = h * (V(i, j, k) + V(i, j, k + 1));
-    T vz0 = h * (V(i, j, k - 1) + V(i, j, k));
     T wy1 = w0[j] * W(i, j, k) + w1[j] * W(i, j + 1, k);
-    T wy0 = w0[j] * W(i, j, k - 1) + w1[j] * W(i, j + 1, k - 1);
-    r += -(vz1 * wy1 - vz0 * wy0) * rdz3;
+    if constexpr (!ZC) {
+        T vz0 = h * (V(i, j, k - 1) + V(i, j, k));
+        T wy0 = w0[j] * W(i, j, k - 1) + w1[j] * W(i, j + 1, k - 1);
+        r += -(vz1 * wy1 - vz0 * wy0) * rdz3;
+    }
     // 4) viscous (:276-331)
     T nu_x1 = nu + h * (w0[j] * nt(i - 1, j, k) + w1[j] * nt(i - 1, j + 1, k) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
     T nu_x2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i + 1, j, k) + w1[j] * nt(i + 1, j + 1, k));
     T nu_y1 = nu + nt(i, j, k);
     T nu_y2 = nu + nt(i, j + 1, k);
-    T nu_z1 = nu + h * (w0[j] * nt(i, j, k - 1) + w1[j] * nt(i, j + 1, k - 1) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
     T nu_z2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i, j, k + 1) + w1[j] * nt(i, j + 1, k + 1));
     T visc = rdx3 * (nu_x2 * ((V(i + 1, j, k) - V(i, j, k)) * rdx2 + (U(i, j + 1, k) - U(i, j, k)) * rdy3) -
                      nu_x1 * ((V(i, j, k) - V(i - 1, j, k)) * rdx1 + (U(i - 1, j + 1, k) - U(i - 1, j, k)) * rdy3)) +
-             T(2) * rdy3 * (nu_y2 * (V(i, j + 1, k) - V(i, j, k)) * rdy2 - nu_y1 * (V(i, j, k) - V(i, j - 1, k)) * rdy1) +
-             rdz3 * (nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) * rdz2 + (W(i, j + 1, k) - W(i, j, k)) * rdy3) -
-                     nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) * rdz1 + (W(i, j + 1, k - 1) - W(i, j, k - 1)) * rdy3));
-    r += visc;
+             T(2) * rdy3 * (nu_y2 * (V(i, j + 1, k) - V(i, j, k)) * rdy2 - nu_y1 * (V(i, j, k) - V(i, j - 1, k)) * rdy1);
+    if constexpr (!ZC) {
+        T nu_z1 = nu + h * (w0[j] * nt(i, j, k - 1) + w1[j] * nt(i, j + 1, k - 1) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
+        visc += rdz3 * (nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) * rdz2 + (W(i, j + 1, k) - W(i, j, k)) * rdy3) -
+                        nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) * rdz1 + (W(i, j + 1, k - 1) - W(i, j, k - 1)) * rdy3));
+        r += visc;
+    } else {
+        r += visc;
+        const T f = nu_z2 * ((V(i, j, k + 1) - V(i, j, k)) * rdz2 + (W(i, j + 1, k) - W(i, j, k)) * rdy3) - vz1 * wy1;
+        r += rdz3 * (f - *fz);
+        *fz = f;
+    }
     if (rot) {  // :334-342
         T tu0 = h * (U(i - 1, j, k) + U(i, j, k));
         T tu1 = h * (U(i - 1, j + 1, k) + U(i, j + 1, k));
@@ -291,9 +319,9 @@ __device__ __forceinline__ T rhs_v_point(const GeoT<T> &g, const RC &rc, const A
     return r;
 }
 
-template <typename T, typename A, typename RC>
+template <typename T, typename A, typename RC, bool ZC = false>
 __device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
-                                         const A &nt, T nu, T dPdz, int i, int j, int k) {
+                                         const A &nt, T nu, T dPdz, int i, int j, int k, T *fz = nullptr) {
     const T *w0 = g.w0, *w1 = g.w1;
     const T h = T(0.5), q = T(0.25);
     const T rdx1 = rc.dxg[i], rdx2 = rc.dxg[i + 1], rdx3 = rc.dx[i];
@@ -301,8 +329,11 @@ __device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const RC &rc, const A
     const T rdz1 = rc.dz[k], rdz2 = rc.dz[k + 1], rdz3 = rc.dzg[k + 1];
     // 1) -dw^2/dz (equations.f90:370-384)
     T a = h * (W(i, j, k) + W(i, j, k + 1));
-    T b = h * (W(i, j, k - 1) + W(i, j, k));
-    T r = -(a * a - b * b) * rdz3;
+    T r = T(0);
+    if constexpr (!ZC) {
+        T b = h * (W(i, j, k - 1) + W(i, j, k));
+        r = -(a * a - b * b) * rdz3;
+    }
     // 2) -duw/dx (:389-406)
     T uz1 = h * (U(i, j, k) + U(i, j, k + 1));
     T uz0 = h * (U(i - 1, j, k) + U(i - 1, j, k + 1));
@@ -323,16 +354,51 @@ __device__ __forceinline__ T rhs_w_point(const GeoT<T> &g, const RC &rc, const A
     T nu_y1 = nu + h * (w0[j - 1] * nt(i, j - 1, k) + w1[j - 1] * nt(i, j, k) + w0[j - 1] * nt(i, j - 1, k + 1) +
                         w1[j - 1] * nt(i, j, k + 1));
     T nu_y2 = nu + h * (w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k) + w0[j] * nt(i, j, k + 1) + w1[j] * nt(i, j + 1, k + 1));
-    T nu_z1 = nu + nt(i, j, k);
     T nu_z2 = nu + nt(i, j, k + 1);
     T visc = rdx3 * (nu_x2 * ((W(i + 1, j, k) - W(i, j, k)) * rdx2 + (U(i, j, k + 1) - U(i, j, k)) * rdz2) -
                      nu_x1 * ((W(i, j, k) - W(i - 1, j, k)) * rdx1 + (U(i - 1, j, k + 1) - U(i - 1, j, k)) * rdz1)) +
              rdy3 * (nu_y2 * (t2j + (V(i, j, k + 1) - V(i, j, k)) * rdz2) -
-                     nu_y1 * (t2jm + (V(i, j - 1, k + 1) - V(i, j - 1, k)) * rdz1)) +
-             T(2) * rdz3 * (nu_z2 * (W(i, j, k + 1) - W(i, j, k)) * rdz2 - nu_z1 * (W(i, j, k) - W(i, j, k - 1)) * rdz1);
-    r += visc;
+                     nu_y1 * (t2jm + (V(i, j - 1, k + 1) - V(i, j - 1, k)) * rdz1));
+    if constexpr (!ZC) {
+        T nu_z1 = nu + nt(i, j, k);
+        visc += T(2) * rdz3 * (nu_z2 * (W(i, j, k + 1) - W(i, j, k)) * rdz2 - nu_z1 * (W(i, j, k) - W(i, j, k - 1)) * rdz1);
+        r += visc;
+    } else {
+        r += visc;
+        const T f = T(2) * (nu_z2 * (W(i, j, k + 1) - W(i, j, k)) * rdz2) - a * a;
+        r += rdz3 * (f - *fz);
+        *fz = f;
+    }
     r += dPdz;  // :496
     return r;
+}
+
+// F(k-1/2) of the u, v and w cells at (i, j, k) as the reference's lower
+// z faces take them (the first plane of a z-marching chunk; later planes
+// carry it from the cell below, see ZC above).
+template <typename T, typename A, typename RC>
+__device__ __forceinline__ void rhs_zflux_dn(const GeoT<T> &g, const RC &rc, const A &U, const A &V, const A &W,
+                                             const A &nt, T nu, int i, int j, int k, T &fu, T &fv, T &fw) {
+    const T *w0 = g.w0, *w1 = g.w1;
+    const T h = T(0.5), q = T(0.25);
+    {
+        const T uz0 = h * (U(i, j, k - 1) + U(i, j, k)), wx0 = h * (W(i, j, k - 1) + W(i + 1, j, k - 1));
+        const T nu_z1 = nu + q * (nt(i, j, k) + nt(i, j, k - 1) + nt(i + 1, j, k) + nt(i + 1, j, k - 1));
+        fu = nu_z1 * ((U(i, j, k) - U(i, j, k - 1)) * rc.dzg[k] + (W(i + 1, j, k - 1) - W(i, j, k - 1)) * rc.dx[i]) -
+             uz0 * wx0;
+    }
+    {
+        const T vz0 = h * (V(i, j, k - 1) + V(i, j, k)), wy0 = w0[j] * W(i, j, k - 1) + w1[j] * W(i, j + 1, k - 1);
+        const T nu_z1 =
+            nu + h * (w0[j] * nt(i, j, k - 1) + w1[j] * nt(i, j + 1, k - 1) + w0[j] * nt(i, j, k) + w1[j] * nt(i, j + 1, k));
+        fv = nu_z1 * ((V(i, j, k) - V(i, j, k - 1)) * rc.dzg[k] + (W(i, j + 1, k - 1) - W(i, j, k - 1)) * rc.dyg[j + 1]) -
+             vz0 * wy0;
+    }
+    {
+        const T b = h * (W(i, j, k - 1) + W(i, j, k));
+        const T nu_z1 = nu + nt(i, j, k);
+        fw = T(2) * (nu_z1 * (W(i, j, k) - W(i, j, k - 1)) * rc.dz[k]) - b * b;
+    }
 }
 
 // RK3 stage update of one point (time_integration.f90:108-110, 124-126,
@@ -691,6 +757,19 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
     fetch(kb + 1);
     commit(2);
     __syncthreads();
+    // the z-face fluxes below the chunk's first plane, carried up the march
+    T fzu, fzv, fzw;
+    {
+        RingAcc<T, TX, TY> aU, aV, aW, aN;
+        aU.b[0] = ring[0][0]; aU.b[1] = ring[1][0]; aU.b[2] = ring[2][0];
+        aV.b[0] = ring[0][1]; aV.b[1] = ring[1][1]; aV.b[2] = ring[2][1];
+        aW.b[0] = ring[0][2]; aW.b[1] = ring[1][2]; aW.b[2] = ring[2][2];
+        aN.b[0] = ring[0][3]; aN.b[1] = ring[1][3]; aN.b[2] = ring[2][3];
+        aU.i0 = aV.i0 = aW.i0 = aN.i0 = i0;
+        aU.j0 = aV.j0 = aW.j0 = aN.j0 = j0;
+        aU.kc = aV.kc = aW.kc = aN.kc = kb;
+        rhs_zflux_dn<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, i, j, kb, fzu, fzv, fzw);
+    }
     // the ring slots of planes k-1, k, k+1 rotate at run time: one copy of
     // the plane's code (a march unrolled by three, with compile-time slots,
     // triples the code of this large loop body and ran 5 % slower)
@@ -719,9 +798,12 @@ __device__ __forceinline__ void rhs3_tile(const Rhs3Args<T> &args, int bx, int b
         // tile and its halo, so the reads stay inside it; points outside the
         // field are not stored): with no store between them the shared-memory
         // reads common to u, v and w are issued once
-        const T ru = rhs_u_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, rot, i, j, k);
-        const T rv = rhs_v_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, Om, rot, i, j, k);
-        const T rw = rhs_w_point<T, RingAcc<T, TX, TY>>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k);
+        const T ru = rhs_u_point<T, RingAcc<T, TX, TY>, RcpT<T>, true>(gl, rcs, aU, aV, aW, aN, nu, dPdx, Om, rot, i,
+                                                                          j, k, &fzu);
+        const T rv = rhs_v_point<T, RingAcc<T, TX, TY>, RcpT<T>, true>(gl, rcs, aU, aV, aW, aN, nu, Om, rot, i, j, k,
+                                                                          &fzv);
+        const T rw = rhs_w_point<T, RingAcc<T, TX, TY>, RcpT<T>, true>(gl, rcs, aU, aV, aW, aN, nu, dPdz, i, j, k,
+                                                                          &fzw);
         if (cu) rk_apply_at<T, S, LO>(ru, fu, ou, lu, iu, out.u.p, F1.u.p, Unlo.u.p, ca, cb, dt);
         if (cv) rk_apply_at<T, S, LO>(rv, fv, ov, lv, iv, out.v.p, F1.v.p, Unlo.v.p, ca, cb, dt);
         if (cw) rk_apply_at<T, S, LO>(rw, fw, ow, lw, iw, out.w.p, F1.w.p, Unlo.w.p, ca, cb, dt);
