@@ -128,12 +128,14 @@ static inline int cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 // own position).  The reference reads those entries themselves in the
 // stencils of the canonical centres next to a seam and the canonical twin's
 // values where it fills ghost points (subgrid.f90:448-458), while this pass
-// reads every halo through the periodic wrap.  The centres whose result can
-// depend on the difference -- rows 2, 3, nyg-2, nyg-1 (two cells from a
-// ghost row) at columns 2..4, nxp-1..nxp+1 or planes 2..4, nzp-1..nzp+1 --
-// are computed by k_dsm_seam with the reference's readings.
+// reads every halo through the periodic wrap.  A centre's L.M, M.M and |S|
+// read U, V, W within two cells of it (through its neighbours' quantities and
+// the filtered velocities), so the centres that can see a wall ghost entry
+// outside the canonical columns and planes -- rows 2, 3, nyg-2, nyg-1 at
+// columns 2, 3, nxp, nxp+1 or planes 2, 3, nzp, nzp+1 -- are computed by
+// k_dsm_seam with the reference's readings.
 __host__ __device__ __forceinline__ bool seam_row(int j, int nyg) { return j <= 3 || j >= nyg - 2; }
-__host__ __device__ __forceinline__ bool seam_line(int i, int np) { return i <= 4 || i >= np - 1; }
+__host__ __device__ __forceinline__ bool seam_line(int i, int np) { return i <= 3 || i >= np; }
 
 
 // compute_Sij at one centre (subgrid.f90:891-949) from arrays at actual

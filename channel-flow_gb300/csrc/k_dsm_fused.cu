@@ -619,7 +619,7 @@ struct SeamArgs {
     RcpT<T> rc;
     int nxp, nzp, nyg, ny;
     int rows[4];                 // the band's rows (blockIdx.y)
-    int xs[6], nxs, zs[6], nzs;  // band columns and planes, distinct
+    int xs[4], nxs, zs[4], nzs;  // band columns and planes, distinct
     int nchunk, chunk0;          // partial-slot stride and the first seam slot
     T *Sout;
     double *part;
@@ -704,7 +704,7 @@ __global__ void __launch_bounds__(256) k_dsm_seam(const __grid_constant__ SeamAr
         if (l < 6) { ex = l % 3 - 1; ey = 0; ez = l / 3 - 1; }
         else { const int m = l - 6; ex = 0; ey = (m & 1) ? 1 : -1; ez = (m >> 1) - 1; }
     }
-    const int nxr = max(0, nxp - 6);  // columns 5..nxp-2 (outside the band's columns)
+    const int nxr = max(0, nxp - 4);  // columns 4..nxp-1 (outside the band's columns)
     const long npts = (long)a.nxs * nzp + (long)a.nzs * nxr;
     double slm = 0.0, smm = 0.0;
     for (long p = (long)blockIdx.x * 8 + w; p < npts; p += (long)gridDim.x * 8) {
@@ -715,7 +715,7 @@ __global__ void __launch_bounds__(256) k_dsm_seam(const __grid_constant__ SeamAr
         } else {
             const long q = p - (long)a.nxs * nzp;
             k = a.zs[q / nxr];
-            i = 5 + (int)(q % nxr);
+            i = 4 + (int)(q % nxr);
         }
         // the stage-A quantities of this lane's neighbour, weighted
         T qv[16];
@@ -786,7 +786,7 @@ __global__ void __launch_bounds__(256) k_dsm_seam(const __grid_constant__ SeamAr
 // partial slots per row the seam kernel takes (after the one-pass kernel's):
 // a block of 8 warps per 16 band centres of a row (two per warp)
 static int seam_slots(int nxp, int nzp) {
-    const long npts = 6L * nzp + 6L * std::max(0, nxp - 6);
+    const long npts = 4L * nzp + 4L * std::max(0, nxp - 4);
     return std::max(1, std::min(256, cdiv(npts, 16)));
 }
 int dsm_seam_slots_max() { return 256; }
@@ -802,8 +802,8 @@ static int launch_seam(cf_ctx *ctx, int b, int chunk0, int nchunk) {
     a.nxp = ctx->nxp; a.nzp = ctx->nzp; a.nyg = ctx->nyg; a.ny = ctx->ny;
     auto band = [](int np, int *out) {
         int n = 0;
-        const int c[6] = {2, 3, 4, np - 1, np, np + 1};
-        for (int q = 0; q < 6; q++) {
+        const int c[4] = {2, 3, np, np + 1};
+        for (int q = 0; q < 4; q++) {
             bool dup = c[q] < 2 || c[q] > np + 1;
             for (int r = 0; r < n; r++) dup = dup || out[r] == c[q];
             if (!dup) out[n++] = c[q];

@@ -83,7 +83,7 @@ def _seam_row(j, nyg):
 
 
 def _seam_line(i, n):
-    return i <= 4 or i >= n - 1
+    return i <= 3 or i >= n
 
 
 def test_seam_band_holds_every_centre_that_reads_a_nonperiodic_wall_ghost():
@@ -91,16 +91,20 @@ def test_seam_band_holds_every_centre_that_reads_a_nonperiodic_wall_ghost():
     multi-pass route forms them: the stage-A quantities of the 27 neighbours
     (compute_Sij reads U at x faces i-1..i, rows j-1..j+1, planes k-1..k+1 and
     W at centres i-1..i+1, rows j-1..j+1, faces k-1..k; a ghost neighbour
-    takes its canonical twin's) and the filtered velocities that compute_Sij of
-    Uf reads (each a 27-point filter of the field around the element, a ghost
-    element its twin's).  Non-periodic entries: the wall ghost rows of U at
-    column 1 and nx and planes 1, nzg-1, nzg, and of W at column 1 and plane 1."""
+    takes its canonical twin's) and every filtered-velocity element around the
+    centre (a 27-point filter of the field around the element, a ghost element
+    its twin's) -- more than compute_Sij of Uf reads.  Every wall ghost row
+    entry of U and W outside the canonical columns and planes is taken as
+    possibly not a periodic copy (the equilibrium wall model's Neumann values
+    use alpha at the ghost's own position; compared with the oracle, U's
+    differ at column 1, column nx and planes 1, nzg-1, nzg, W's at column 1
+    and plane 1)."""
     nxp, nzp, nyg = 12, 10, 14
-    nx, nzg, nz = nxp + 2, nzp + 3, nzp + 2
+    nx, nzg, nz, nxg = nxp + 2, nzp + 3, nzp + 2, nxp + 3
     wrap = lambda i, n: 2 + (i - 2) % n
-    bad_u = {(i, j, k) for j in (1, nyg) for i in range(1, nx + 1) for k in range(1, nzg + 1)
-             if i in (1, nx) or k in (1, nzg - 1, nzg)}
-    bad_w = {(i, j, k) for j in (1, nyg) for i in range(1, nxp + 4) for k in range(1, nz + 1) if i == 1 or k == 1}
+    canon = lambda i, k: 2 <= i <= nxp + 1 and 2 <= k <= nzp + 1
+    bad_u = {(i, j, k) for j in (1, nyg) for i in range(1, nx + 1) for k in range(1, nzg + 1) if not canon(i, k)}
+    bad_w = {(i, j, k) for j in (1, nyg) for i in range(1, nxg + 1) for k in range(1, nz + 1) if not canon(i, k)}
 
     def q_reads(i, j, k):  # stage-A quantities at a canonical centre
         i, k = wrap(i, nxp), wrap(k, nzp)
@@ -128,11 +132,11 @@ def test_seam_band_holds_every_centre_that_reads_a_nonperiodic_wall_ghost():
                     assert _seam_row(j, nyg) and (_seam_line(i, nxp) or _seam_line(k, nzp)), (i, j, k)
 
     # the enumeration of k_dsm_seam: band columns (every plane), then band
-    # planes at the columns 5..nxp-2
-    for np_x, np_z in ((12, 10), (16, 16), (7, 9), (5, 6), (4, 4)):
-        band = lambda n: sorted({c for c in (2, 3, 4, n - 1, n, n + 1) if 2 <= c <= n + 1})
-        xs, zs, nxr = band(np_x), band(np_z), max(0, np_x - 6)
-        pts = [(x, k) for x in xs for k in range(2, np_z + 2)] + [(5 + q % nxr, zs[q // nxr])
+    # planes at the columns 4..nxp-1
+    for np_x, np_z in ((12, 10), (16, 16), (7, 9), (5, 6), (4, 4), (3, 5)):
+        band = lambda n: sorted({c for c in (2, 3, n, n + 1) if 2 <= c <= n + 1})
+        xs, zs, nxr = band(np_x), band(np_z), max(0, np_x - 4)
+        pts = [(x, k) for x in xs for k in range(2, np_z + 2)] + [(4 + q % nxr, zs[q // nxr])
                                                                   for q in range(len(zs) * nxr)]
         want = [(i, k) for i in range(2, np_x + 2) for k in range(2, np_z + 2)
                 if _seam_line(i, np_x) or _seam_line(k, np_z)]
