@@ -319,6 +319,7 @@ template <typename T> int launch_dsm_batch(cudaStream_t st, cf_ctx *const *m, co
 template <typename T> int launch_rhs3_batch(cudaStream_t st, cf_ctx *const *m, int s, const int *src, const int *dst, int n);
 template <typename T> int launch_nut_zero(cf_ctx *ctx);
 template <typename T> int launch_nut_materialize(cf_ctx *ctx);       // fill nut if held lazily
+template <typename T> int launch_nut_wall_rows(cf_ctx *ctx);         // its rows 1, 2, nyg-1, nyg only (stays lazy)
 // canon: project the canonical cells only (the boundary conditions that
 // follow rewrite the periodic duplicates)
 // one channel's tridiagonal systems for the batched solve of an ensemble

@@ -528,9 +528,12 @@ __global__ void k_dsm_e_ff(const float4 *part, int nchunk, int nyg, double *avg,
 // Stage F: nu_t = max(-0.5 C(j) |S|, 0) everywhere, periodic copies and the
 // wall ghost rule (subgrid.f90:521-536).
 template <typename T>
-__global__ void k_dsm_f(Fld<T> nt, const T *Sq, const double *avg, Can c, int nxg, int nyg, int nzg, int dirichlet) {
+// walls: rows 1, 2, nyg-1, nyg only (blockDim.y = 4, one block row)
+__global__ void k_dsm_f(Fld<T> nt, const T *Sq, const double *avg, Can c, int nxg, int nyg, int nzg, int dirichlet,
+                        int walls) {
     int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    if (walls) j = threadIdx.y < 2 ? 1 + threadIdx.y : nyg - 3 + threadIdx.y;
     int k = blockIdx.z + 1;
     if (i > nxg || j > nyg) return;
     int jj = j == 1 ? 2 : (j == nyg ? nyg - 1 : j);
@@ -559,9 +562,26 @@ int launch_nut_materialize(cf_ctx *ctx) {
     Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
     T *q = (T *)ctx->dsm_q;
     k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), cdiv(ctx->nyg, 4), ctx->nzg), dim3(32, 4, 1), 0, ctx->st>>>(
-        nt, q + Q_S * c.n, ctx->avg_nu_t, c, ctx->nxg, ctx->nyg, ctx->nzg, ctx->prm.Dirichlet_nu_t == 1);
+        nt, q + Q_S * c.n, ctx->avg_nu_t, c, ctx->nxg, ctx->nyg, ctx->nzg, ctx->prm.Dirichlet_nu_t == 1, 0);
     count_launch(ctx, "k_dsm_f");
     ctx->nut_lazy = false;
+    CF_CUDA(cudaGetLastError());
+    return 0;
+}
+
+// nu_t of the wall rows and their neighbours (j = 1, 2, nyg-1, nyg), the
+// only rows the wall model reads; the rest of the field stays lazy (its
+// other readers materialise it).
+template <typename T>
+int launch_nut_wall_rows(cf_ctx *ctx) {
+    if (!ctx->nut_lazy) return 0;
+    Can c;
+    c.nxp = ctx->nxp; c.nym = ctx->nym; c.nzp = ctx->nzp; c.n = (long)ctx->nCan;
+    Fld<T> nt = make_fld<T>(ctx->nut, ctx->nxg, ctx->nyg);
+    k_dsm_f<T><<<dim3(cdiv(ctx->nxg, 32), 1, ctx->nzg), dim3(32, 4, 1), 0, ctx->st>>>(
+        nt, (T *)ctx->dsm_q + Q_S * c.n, ctx->avg_nu_t, c, ctx->nxg, ctx->nyg, ctx->nzg,
+        ctx->prm.Dirichlet_nu_t == 1, 1);
+    count_launch(ctx, "k_dsm_f");
     CF_CUDA(cudaGetLastError());
     return 0;
 }
@@ -708,6 +728,8 @@ template int launch_dsm<float>(cf_ctx *, int);
 template int launch_nut_zero<double>(cf_ctx *);
 template int launch_nut_materialize<double>(cf_ctx *);
 template int launch_nut_materialize<float>(cf_ctx *);
+template int launch_nut_wall_rows<double>(cf_ctx *);
+template int launch_nut_wall_rows<float>(cf_ctx *);
 template int launch_nut_zero<float>(cf_ctx *);
 
 // z chunks of the multi-pass filter kernel: the count that minimises (waves

@@ -396,7 +396,7 @@ __global__ void k_eq_alphaz(const double *azt, double *az, int nx, int nxg, int 
 
 template <typename T>
 int launch_eqwm(cf_ctx *ctx, int b) {
-    if (int rc = launch_nut_materialize<T>(ctx)) return rc;
+    if (int rc = launch_nut_wall_rows<T>(ctx)) return rc;  // the rows k_eq_solve reads
     int nx = ctx->nx, nxg = ctx->nxg, nyg = ctx->nyg, nz = ctx->nz, nzg = ctx->nzg;
     Fld<T> W = make_fld<T>(ctx->W[b], ctx->nxg, ctx->nyg);
     k_eq_zinterp_t<T><<<dim3(cdiv(nxg, 128), nzg, 2), 128, 0, ctx->st>>>(W, ctx->prm.jref_eqwm, nxg, nyg, nzg,
