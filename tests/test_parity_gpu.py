@@ -81,15 +81,19 @@ def test_boundary_conditions_exact(which):
 
 
 @pytest.mark.parametrize("precision", [0, 1])
-@pytest.mark.parametrize("dims", [(34, 33, 34), (18, 17, 22), (66, 65, 66)])
-def test_step_ghosts_are_the_boundary_conditions(precision, dims):
-    """After graph-captured steps (no-slip walls: the projection writes every
-    ghost copy of its canonical cells instead of a separate
-    apply_boundary_conditions), the ghosts hold exactly what
-    apply_boundary_conditions would put there: the fields do not change
-    when it is applied once more (low words included in the split path)."""
+@pytest.mark.parametrize("dims,wall", [((34, 33, 34), 0), ((18, 17, 22), 0), ((66, 65, 66), 0), ((34, 33, 34), 3),
+                                       ((26, 17, 22), 3)])
+def test_step_ghosts_are_the_boundary_conditions(precision, dims, wall):
+    """After graph-captured steps (the projection writes every ghost copy of
+    its canonical cells instead of a separate apply_boundary_conditions: the
+    no-slip rule, or with the equilibrium wall model its Neumann rule with
+    alpha at each ghost; no mass-flow forcing in the wall-model cases, so that
+    the step ends with the projection), the ghosts hold exactly what
+    apply_boundary_conditions would put there: the fields do not change when
+    it is applied once more (low words included in the split path)."""
     import channelflow as cf
-    case = channel_case(*dims, seed=11)
+    extra = dict(stretch=0.0, wall=3, retau=2000.0, profile="plug", mass=0) if wall else {}
+    case = channel_case(*dims, seed=11, **extra)
     ch = cf.Channel(case["x"], case["y"], case["z"], precision=precision, **case["prm"])
     ch.upload(case["U"], case["V"], case["W"])
     ch.init_mass_flow()
